@@ -1,0 +1,136 @@
+"""Generates the committed golden fixtures in tests/golden/ by running the
+reference SCFT code itself (compiled by oracle/Makefile into
+oracle/_ref/scft_ref, Dim=3, FFT via the oracle shim).
+
+    make -C oracle && python tests/golden/make_golden.py
+
+Each fixture <name>.npz holds
+  case_json      the bcp.input parameters (json text)
+  in_<field>     the seeded initial fields written as w*.res
+  trace          rows [iter, Re H, Im H, Re Qd, Im Qd, Re Qga, Im Qga] after
+                 0..iters update_1s() calls, at full precision
+  scalars_json   nD, phiD, Vf, np_frac, ... after initialisation
+  <array>        reference outputs (see ARRAYS), or, for the large
+                 config-0 case, per-array digests (see digest()).
+"""
+from __future__ import annotations
+
+import json
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+from ref_case import Case, run_reference  # noqa: E402
+
+ARRAYS = ["hhat", "poly_bond_fft", "gaa", "gab", "gbb", "rho_exp_nr", "expl_grafts", "smwa0", "smwb0",
+          "rhoda0", "rhodb0", "wpl", "wabp", "wabm", "wbcp", "wbcm", "wacp", "wacm", "smwa", "smwb",
+          "rhoda", "rhodb"]
+DIGEST_IDX_SEED = 7
+
+
+def seeded_fields(c: Case, seed: int, amp: float, noise: float, extra: bool) -> dict:
+    """Lamellar w_AB^- along x plus small seeded noise; imaginary w+ and w_AB^+
+    (the reference's mean-field phase convention, code/initialize.cpp:459-481)."""
+    rng = np.random.default_rng(seed)
+    x = np.arange(c.Nx[0]) * c.L[0] / c.Nx[0]
+    f = {}
+    f["wabm"] = (amp * np.cos(2 * np.pi * x / c.L[0])[None, None, :]
+                 + noise * rng.standard_normal(c.shape)).astype(np.complex128)
+    f["wpl"] = 1j * noise * rng.standard_normal(c.shape)
+    f["wabp"] = 1j * noise * rng.standard_normal(c.shape)
+    if extra:
+        f["wbcm"] = (5 * noise * rng.standard_normal(c.shape)).astype(np.complex128)
+        f["wbcp"] = 1j * noise * rng.standard_normal(c.shape)
+        f["wacm"] = (5 * noise * rng.standard_normal(c.shape)).astype(np.complex128)
+        f["wacp"] = 1j * 2 * noise * rng.standard_normal(c.shape)
+    return f
+
+
+def tiny_cases() -> dict:
+    base = dict(Nx=(8, 10, 6), L=(4.0, 5.0, 3.5), a_smear=0.2, rho0=5.0, kappa=50.0, lam_pl=0.005,
+                lam_mi=0.005, L_nr=0.6, R_nr=1.2, xi_nr=0.3)
+    cases = {}
+    c = Case(Nda=3, Ndb=5, chi_ab=0.5, n_exp_nr=1, centers=((0.4, 0.55, 0.5), (0.5, 0.5, 0.5)),
+             orients=((0.9, 0.3, 0.1), (1.0, 0.0, 0.0)), **base)
+    c.fields = seeded_fields(c, 1, 0.3, 0.01, False)
+    cases["tiny_plate"] = (c, 6, True)
+    c = Case(Nda=3, Ndb=5, chi_ab=0.5, chi_bc=-0.2, chi_ac=0.4, sigma=0.3, Ng=4, n_exp_nr=2,
+             centers=((0.3, 0.5, 0.5), (0.7, 0.5, 0.5)), orients=((0.9, 0.3, 0.1), (0.2, 1.0, 0.0)),
+             **base)
+    c.fields = seeded_fields(c, 2, 0.3, 0.01, True)
+    cases["tiny_graft"] = (c, 6, True)
+    c = Case(Nda=3, Ndb=4, chi_ab=-0.3, n_exp_nr=0, **base)
+    c.fields = seeded_fields(c, 3, 0.3, 0.01, False)
+    cases["tiny_negab_oddN"] = (c, 6, True)
+    c = Case(Nda=5, Ndb=0, chi_ab=0.5, n_exp_nr=1, centers=((0.5, 0.5, 0.5), (0.5, 0.5, 0.5)),
+             orients=((1.0, 0.0, 0.0), (1.0, 0.0, 0.0)), **base)
+    c.fields = seeded_fields(c, 4, 0.3, 0.01, False)
+    cases["tiny_single_block"] = (c, 4, True)
+    return cases
+
+
+def config0_case() -> Case:
+    """Config 0: AB diblock, N=32, f=0.5, chiN=20, C=50, 32^3 grid, box 4.0 Rg.
+    b-units with Rg^2=(N-1)/6 (code/initialize.cpp:55): chi=chiN/N,
+    rho0=C*N/Rg^3, w_AB^- = 0.5*chi*cos(2*pi*x/L) + N(0, 0.01^2) per segment."""
+    N = 32
+    Rg = np.sqrt((N - 1) / 6.0)
+    Lb = 4.0 * Rg
+    c = Case(Nda=16, Ndb=16, a_smear=0.2, rho0=50.0 * N / Rg ** 3, chi_ab=20.0 / N, kappa=50.0,
+             Nx=(32, 32, 32), L=(Lb, Lb, Lb), lam_pl=0.005, lam_mi=0.005, n_exp_nr=0)
+    rng = np.random.default_rng(20240)
+    x = np.arange(32) * Lb / 32
+    c.fields = {"wabm": (0.5 * c.chi_ab * np.cos(2 * np.pi * x / Lb)[None, None, :]
+                         + 0.01 * rng.standard_normal(c.shape)).astype(np.complex128),
+                "wpl": np.zeros(c.shape, np.complex128),
+                "wabp": np.zeros(c.shape, np.complex128)}
+    return c
+
+
+def digest(a: np.ndarray) -> np.ndarray:
+    """Size-independent summary: sum, sum of |.|^2, and 64 sampled points."""
+    a = a.ravel()
+    idx = np.random.default_rng(DIGEST_IDX_SEED).choice(a.size, 64, replace=False)
+    return np.concatenate([[a.sum(), (np.abs(a) ** 2).sum()], a[idx]])
+
+
+def case_json(c: Case) -> str:
+    d = {k: getattr(c, k) for k in c.__dataclass_fields__ if k != "fields"}
+    return json.dumps(d)
+
+
+def main():
+    tmp = tempfile.mkdtemp(prefix="golden_")
+    for name, (c, iters, hist) in tiny_cases().items():
+        out = run_reference(os.path.join(tmp, name), c, iters, hist=hist)
+        z = {"case_json": case_json(c), "trace": out["trace"], "scalars_json": json.dumps(out["scalars"])}
+        for k, v in c.fields.items():
+            z["in_" + k] = v
+        for k in ARRAYS:
+            z[k] = out[k]
+        if c.sigma > 0 and c.n_exp_nr > 0:
+            z["rhog_exp0"] = out["rhog_exp0"]
+            z["rhog_exp"] = out["rhog_exp"]
+            z["gc"] = out["gc"]
+        if hist:
+            z["qd0"], z["qddag0"] = out["qd0"], out["qddag0"]
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **z)
+        print(name, "H0", out["trace"][0, 1], "H_end", out["trace"][-1, 1])
+    c = config0_case()
+    out = run_reference(os.path.join(tmp, "config0"), c, 200, hist=False, timeout=3600)
+    z = {"case_json": case_json(c), "trace": out["trace"], "scalars_json": json.dumps(out["scalars"]),
+         "digest_idx_seed": DIGEST_IDX_SEED}
+    for k in ["rhoda0", "rhodb0", "rhoda", "rhodb", "wpl", "wabp", "wabm", "smwa", "smwb"]:
+        z["digest_" + k] = digest(out[k])
+    np.savez_compressed(os.path.join(HERE, "config0_32cubed_N32.npz"), **z)
+    print("config0 H0", out["trace"][0, 1], "H200", out["trace"][-1, 1])
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,160 @@
+"""Pins the oracle: the numpy restatement (oracle/scft_oracle.py) and the FFT
+shim used to compile the reference (oracle/fftw_shim/) against known answers
+and against the golden fixtures produced by the reference itself."""
+import ctypes
+import json
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, ROOT
+
+import scft_oracle as O
+from ref_case import Case
+import sys as _sys
+_sys.path.insert(0, GOLDEN)
+
+SHIM = os.path.join(ROOT, "oracle", "_ref", "libfftw_shim.so")
+TINY = ["tiny_plate", "tiny_graft", "tiny_negab_oddN", "tiny_single_block"]
+
+
+def load_golden(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    d = json.loads(str(z["case_json"]))
+    c = Case(**{k: (tuple(map(tuple, v)) if k in ("centers", "orients", "ic") else
+                    (tuple(v) if isinstance(v, list) else v)) for k, v in d.items()})
+    c.fields = {k[3:]: z[k] for k in z.files if k.startswith("in_")}
+    return c, z
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def shim():
+    if not os.path.exists(SHIM):
+        subprocess.run(["make", "-C", os.path.join(ROOT, "oracle"), "shim"], check=True,
+                       capture_output=True)
+    lib = ctypes.CDLL(SHIM)
+    lib.fftw_plan_dft.restype = ctypes.c_void_p
+    lib.fftw_plan_dft.argtypes = [ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_void_p,
+                                  ctypes.c_void_p, ctypes.c_int, ctypes.c_uint]
+    lib.fftw_execute.argtypes = [ctypes.c_void_p]
+    lib.fftw_destroy_plan.argtypes = [ctypes.c_void_p]
+    return lib
+
+
+def direct_dft(a, sign):
+    """Known answer: the defining O(n^2) sum along each axis."""
+    out = a.astype(np.complex128)
+    for ax in range(a.ndim):
+        n = a.shape[ax]
+        j = np.arange(n)
+        W = np.exp(sign * 2j * np.pi * (np.outer(j, j) % n) / n)
+        out = np.moveaxis(np.tensordot(W, np.moveaxis(out, ax, 0), axes=(1, 0)), 0, ax)
+    return out
+
+
+@pytest.mark.parametrize("shape", [(8, 8, 8), (12, 10, 6), (6, 16, 9), (7, 11, 5), (3, 48, 2)])
+@pytest.mark.parametrize("sign", [-1, 1])
+def test_shim_fft_known_answer(shim, shape, sign):
+    rng = np.random.default_rng(sum(shape))
+    a = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    out = np.zeros_like(a)
+    n = (ctypes.c_int * 3)(*shape)
+    p = shim.fftw_plan_dft(3, n, a.ctypes.data, out.ctypes.data, sign, 0)
+    shim.fftw_execute(p)
+    shim.fftw_destroy_plan(p)
+    assert rel(out, direct_dft(a, sign)) < 1e-14
+
+
+def test_shim_fft_in_place_and_zeroed_malloc(shim):
+    shim.fftw_malloc.restype = ctypes.c_void_p
+    shim.fftw_malloc.argtypes = [ctypes.c_size_t]
+    shim.fftw_free.argtypes = [ctypes.c_void_p]
+    p = shim.fftw_malloc(4096)
+    assert all(b == 0 for b in ctypes.string_at(p, 4096))
+    shim.fftw_free(p)
+    rng = np.random.default_rng(3)
+    a = rng.standard_normal((4, 6, 10)) + 0j
+    ref = np.fft.fftn(a)
+    n = (ctypes.c_int * 3)(4, 6, 10)
+    pl = shim.fftw_plan_dft(3, n, a.ctypes.data, a.ctypes.data, -1, 0)
+    shim.fftw_execute(pl)
+    assert rel(a, ref) < 1e-14
+
+
+def test_oracle_fft_conventions():
+    g = O.Grid((6, 4, 10), (3.0, 2.0, 5.0))
+    rng = np.random.default_rng(0)
+    a = rng.standard_normal(g.shape) + 1j * rng.standard_normal(g.shape)
+    # forward scaled by 1/M, backward unscaled (code/fft_wrappers.cpp:4-64)
+    assert rel(O.fft_fwd(g, a), direct_dft(a, -1) / g.M) < 1e-14
+    assert rel(O.fft_bck(g, O.fft_fwd(g, a)), a) < 1e-14
+
+
+@pytest.mark.parametrize("name", TINY)
+def test_restatement_matches_reference_fixture(name):
+    c, z = load_golden(name)
+    s = O.System.from_case(c)
+    st = O.State.from_fields(s.g, c.fields)
+    iters = int(z["trace"][-1, 0])
+    rows = O.run(s, st, iters)
+    tr = z["trace"]
+    # H and Q per iteration: the bar is 1e-9 relative (H), found ~1e-15
+    assert np.abs(rows[:, 1] - tr[:, 1]).max() <= 1e-12 * np.abs(tr[:, 1]).max()
+    assert np.abs(rows[:, 3] - tr[:, 3]).max() <= 1e-12 * np.abs(tr[:, 3]).max()
+    if c.sigma > 0:
+        assert np.abs(rows[:, 5] - tr[:, 5]).max() <= 1e-12 * np.abs(tr[:, 5]).max()
+    for k in ("hhat", "poly_bond_fft", "gaa", "gab", "gbb", "rho_exp_nr", "expl_grafts"):
+        if np.abs(z[k]).max() > 0:
+            assert rel(s.tables[k], z[k]) < 1e-12, k
+    for k in ("wpl", "wabp", "wabm", "wbcp", "wbcm", "wacp", "wacm"):
+        if np.abs(z[k]).max() > 0:
+            assert rel(getattr(st, k), z[k]) < 1e-12, k
+    for k in ("rhoda", "rhodb", "smwa", "smwb"):
+        assert rel(st.out[k], z[k]) < 1e-12, k
+    sc = json.loads(str(z["scalars_json"]))
+    assert abs(s.nD - sc["nD"]) <= 1e-13 * sc["nD"]
+
+
+@pytest.mark.parametrize("name", TINY)
+def test_restatement_propagators_match_reference(name):
+    c, z = load_golden(name)
+    s = O.System.from_case(c)
+    st = O.State.from_fields(s.g, c.fields)
+    O.calc_poly_density(s, st, keep_hist=True)
+    assert rel(st.out["qd"], z["qd0"]) < 1e-12
+    assert rel(st.out["qddag"], z["qddag0"]) < 1e-12
+    assert rel(st.out["rhoda"], z["rhoda0"]) < 1e-12
+
+
+def test_segment_count_invariant():
+    """code/simulate.cpp:61-72: integral(rho_A + rho_B) = nD * N."""
+    c, _ = load_golden("tiny_plate")
+    s = O.System.from_case(c)
+    st = O.State.from_fields(s.g, c.fields)
+    o = O.calc_poly_density(s, st)
+    tot = O.integ_trapPBC(s.g, o["rhoda"] + o["rhodb"]).real
+    assert abs(tot - s.nD * s.N) < 1e-10 * s.nD * s.N
+
+
+def test_restatement_config0_trace():
+    """Config 0 (32^3, N=32, 200 x update_1s): full-size H trace and digests."""
+    z = np.load(os.path.join(GOLDEN, "config0_32cubed_N32.npz"))
+    d = json.loads(str(z["case_json"]))
+    c = Case(**{k: (tuple(map(tuple, v)) if k in ("centers", "orients", "ic") else
+                    (tuple(v) if isinstance(v, list) else v)) for k, v in d.items()})
+    from make_golden import config0_case, digest
+    c.fields = config0_case().fields
+    s = O.System.from_case(c)
+    st = O.State.from_fields(s.g, c.fields)
+    rows = O.run(s, st, 200)
+    tr = z["trace"]
+    assert np.abs(rows[:, 1] - tr[:, 1]).max() <= 1e-10 * np.abs(tr[:, 1]).max()
+    for k in ("rhoda", "rhodb", "wpl", "wabm"):
+        src = st.out[k] if k.startswith("rho") else getattr(st, k)
+        assert rel(digest(src), z["digest_" + k]) < 1e-10, k
