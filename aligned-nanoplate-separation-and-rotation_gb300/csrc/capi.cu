@@ -1,0 +1,187 @@
+// capi.cu -- extern "C" entry points of libscft (declared in include/scft.h).
+// Every entry point catches exceptions and turns them into a status code; the
+// message is kept per host thread for scft_last_error().
+#include <cstring>
+#include <new>
+#include <string>
+
+#include "context.h"
+
+namespace scft {
+void ctx_create(scft_ctx *c, const scft_params *params, int n_inst);
+void ctx_destroy(scft_ctx *c);
+void ctx_poly_density(scft_ctx *c);
+void ctx_update(scft_ctx *c, int n_iter);
+int ctx_calc_H(scft_ctx *c, double *out);
+void ctx_set_fields(scft_ctx *c, int k, const double *w);
+void ctx_get_fields(scft_ctx *c, int k, double *w);
+void ctx_get_density(scft_ctx *c, int k, double *ra, double *rb, double *rg);
+void ctx_get_smeared(scft_ctx *c, int k, double *a, double *b, double *g);
+void ctx_fft3d(scft_ctx *c, int k, double *data, int count, int sign);
+void ctx_diblock_density(scft_ctx *c, int k, const double *smwa, const double *smwb, double *ra, double *rb,
+                         double *Q);
+void ctx_override_nD(scft_ctx *c, int k, double nD);
+int error_code(const std::exception &e);
+}  // namespace scft
+
+static thread_local std::string g_err;
+
+static int fail(int code, const std::string &msg) {
+  g_err = msg;
+  return code;
+}
+
+#define API_BODY(stmt)                                       \
+  try {                                                      \
+    stmt;                                                    \
+  } catch (const std::bad_alloc &) {                         \
+    return fail(SCFT_ERR_NOMEM, "host allocation failed");  \
+  } catch (const std::exception &e) {                        \
+    return fail(scft::error_code(e), e.what());              \
+  }
+
+static int check_ctx(scft_ctx *c, int inst) {
+  if (!c) return fail(SCFT_ERR_ARG, "null context");
+  if (inst < 0 || inst >= (int)c->inst.size()) return fail(SCFT_ERR_ARG, "instance index out of range");
+  return SCFT_OK;
+}
+
+extern "C" {
+
+const char *scft_last_error(void) { return g_err.c_str(); }
+
+int scft_version(void) { return 1; }
+
+int scft_create(const scft_params *params, int n_inst, scft_ctx **out) {
+  if (!out) return fail(SCFT_ERR_ARG, "null output pointer");
+  *out = nullptr;
+  if (!params || n_inst < 1) return fail(SCFT_ERR_ARG, "need at least one instance");
+  scft_ctx *c = new (std::nothrow) scft_ctx();
+  if (!c) return fail(SCFT_ERR_NOMEM, "host allocation failed");
+  try {
+    scft::ctx_create(c, params, n_inst);
+  } catch (const std::exception &e) {
+    const int code = scft::error_code(e);
+    g_err = e.what();
+    scft::ctx_destroy(c);
+    delete c;
+    return code;
+  }
+  *out = c;
+  return SCFT_OK;
+}
+
+void scft_destroy(scft_ctx *c) {
+  if (!c) return;
+  scft::ctx_destroy(c);
+  delete c;
+}
+
+int scft_get_info(scft_ctx *c, int inst, scft_info *info) {
+  if (int s = check_ctx(c, inst)) return s;
+  if (!info) return fail(SCFT_ERR_ARG, "null info");
+  *info = c->inst[inst].info;
+  return SCFT_OK;
+}
+
+int scft_set_fields(scft_ctx *c, int inst, const double *w) {
+  if (int s = check_ctx(c, inst)) return s;
+  if (!w) return fail(SCFT_ERR_ARG, "null field buffer");
+  API_BODY(scft::ctx_set_fields(c, inst, w));
+  return SCFT_OK;
+}
+
+int scft_get_fields(scft_ctx *c, int inst, double *w) {
+  if (int s = check_ctx(c, inst)) return s;
+  if (!w) return fail(SCFT_ERR_ARG, "null field buffer");
+  API_BODY(scft::ctx_get_fields(c, inst, w));
+  return SCFT_OK;
+}
+
+int scft_calc_poly_density(scft_ctx *c) {
+  if (int s = check_ctx(c, 0)) return s;
+  API_BODY(scft::ctx_poly_density(c));
+  return SCFT_OK;
+}
+
+int scft_update_1s(scft_ctx *c, int n_iter) {
+  if (int s = check_ctx(c, 0)) return s;
+  if (n_iter < 0) return fail(SCFT_ERR_ARG, "n_iter must be >= 0");
+  API_BODY(scft::ctx_update(c, n_iter));
+  return SCFT_OK;
+}
+
+int scft_calc_H(scft_ctx *c, double *out) {
+  if (int s = check_ctx(c, 0)) return s;
+  if (!out) return fail(SCFT_ERR_ARG, "null output");
+  int st = SCFT_OK;
+  API_BODY(st = scft::ctx_calc_H(c, out));
+  if (st == SCFT_ERR_NAN) return fail(st, "H is NaN");
+  if (st == SCFT_ERR_QNONPOS) return fail(st, "graft propagator q_g[Ng-1] <= 0 at 5 or more points");
+  return st;
+}
+
+int scft_get_density(scft_ctx *c, int inst, double *ra, double *rb, double *rg) {
+  if (int s = check_ctx(c, inst)) return s;
+  API_BODY(scft::ctx_get_density(c, inst, ra, rb, rg));
+  return SCFT_OK;
+}
+
+int scft_get_smeared(scft_ctx *c, int inst, double *a, double *b, double *g) {
+  if (int s = check_ctx(c, inst)) return s;
+  API_BODY(scft::ctx_get_smeared(c, inst, a, b, g));
+  return SCFT_OK;
+}
+
+int scft_diblock_density(scft_ctx *c, int inst, const double *smwa, const double *smwb, double *ra, double *rb,
+                         double *Q) {
+  if (int s = check_ctx(c, inst)) return s;
+  if (!smwa || !smwb) return fail(SCFT_ERR_ARG, "null field");
+  API_BODY(scft::ctx_diblock_density(c, inst, smwa, smwb, ra, rb, Q));
+  return SCFT_OK;
+}
+
+int scft_homopolymer_density(scft_ctx *c, int inst, const double *W, int N, double nK, double *rho, double *Q) {
+  if (int s = check_ctx(c, inst)) return s;
+  if (!W || N < 1) return fail(SCFT_ERR_ARG, "need a field and N >= 1");
+  // homopolymer_discrete is diblock_discrete with a single block (Na = N):
+  // q-dagger equals q (code/diblock_discrete.cpp:60-83 vs
+  // code/homopolymer_discrete.cpp:18-41) and every term goes to rho_A.
+  scft_params p = c->inst[inst].p;
+  p.Nda = N;
+  p.Ndb = 0;
+  p.n_exp_nr = 0;
+  p.sigma = 0.0;
+  p.Ng = 0;
+  p.precision = SCFT_PREC_FP64;
+  scft_ctx *h = nullptr;
+  int st = scft_create(&p, 1, &h);
+  if (st != SCFT_OK) return st;
+  try {
+    scft::ctx_override_nD(h, 0, nK);
+    scft::ctx_diblock_density(h, 0, W, W, rho, nullptr, Q);
+  } catch (const std::exception &e) {
+    const int code = scft::error_code(e);
+    g_err = e.what();
+    scft_destroy(h);
+    return code;
+  }
+  scft_destroy(h);
+  return SCFT_OK;
+}
+
+int scft_fft3d(scft_ctx *c, int inst, double *data, int count, int sign) {
+  if (int s = check_ctx(c, inst)) return s;
+  if (!data || count < 1 || (sign != -1 && sign != 1)) return fail(SCFT_ERR_ARG, "bad fft arguments");
+  API_BODY(scft::ctx_fft3d(c, inst, data, count, sign));
+  return SCFT_OK;
+}
+
+int scft_sync(scft_ctx *c) {
+  if (!c) return fail(SCFT_ERR_ARG, "null context");
+  cudaError_t e = cudaStreamSynchronize(c->st);
+  if (e != cudaSuccess) return fail(SCFT_ERR_CUDA, cudaGetErrorString(e));
+  return SCFT_OK;
+}
+
+}  // extern "C"

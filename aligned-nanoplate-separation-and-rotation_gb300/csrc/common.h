@@ -1,0 +1,48 @@
+// common.h -- types shared by the host side and the CUDA kernels of libscft.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace scft {
+
+constexpr int kMaxStages = 8;
+
+// Stage plan of a 1-D FFT of length n along one grid axis: radices applied in
+// order (Stockham autosort, decimation in time) and the offset of this
+// length's twiddle table exp(-2*pi*i*t/n), t = 0..n-1, in the context's
+// twiddle buffer.
+struct AxisPlan {
+  int n;
+  int nst;
+  int radix[kMaxStages];
+  int tw;
+};
+
+// Geometry of one instance's grid, as the kernels see it.
+struct DevGeom {
+  int nx, ny, nz;
+  int tx;  // x-columns per z-pass tile (divides nx)
+  long long M;
+  AxisPlan ax[3];
+};
+
+// One CTA of an xy-plane pass: array base pointer (complex, M entries),
+// geometry index, z plane.
+struct PlaneJob {
+  void *ptr;
+  int geom;
+  int z;
+};
+
+// One CTA of a z-column pass: tile of `tx` consecutive x columns at row y.
+// kern: optional real k-space multiplier table (M entries) for a fused
+// forward-multiply-inverse pass; NULL means plain transform.
+struct ColJob {
+  void *ptr;
+  const void *kern;
+  int geom;
+  int x0, y;
+};
+
+}  // namespace scft

@@ -1,0 +1,978 @@
+// context.cu -- scft_ctx: instance set-up and the per-iteration sequences.
+//
+// Set-up follows code/initialize.cpp:45-412 (grid, smearing kernel hhat, plate
+// density and graft map, volumes and chain counts, Debye functions, bond
+// kernel).  Tables that the reference computes point by point from get_k()
+// (hhat, poly_bond_fft, gaa, gab, gbb, gc) are computed here on the host in
+// FP64 with the same expressions; the plate profile and its spectral gradient
+// are computed on the device (they need FFTs).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <stdexcept>
+
+#include "context.h"
+#include "fft_core.cuh"
+#include "prop_launch.h"
+
+namespace scft {
+
+constexpr double kPI = 3.14159265358979323846263383;  // code/globals.h:31
+
+struct ScftError : std::runtime_error {
+  int code;
+  ScftError(int c, const std::string &m) : std::runtime_error(m), code(c) {}
+};
+
+#define CK(x)                                                                                   \
+  do {                                                                                          \
+    cudaError_t e_ = (x);                                                                       \
+    if (e_ != cudaSuccess)                                                                      \
+      throw ScftError(SCFT_ERR_CUDA, std::string(#x) + ": " + cudaGetErrorString(e_));          \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// FFT plans
+// ---------------------------------------------------------------------------
+static bool make_axis_plan(int n, AxisPlan &ap) {
+  ap.n = n;
+  ap.nst = 0;
+  int m = n;
+  while (m % 8 == 0 && ap.nst < kMaxStages) { ap.radix[ap.nst++] = 8; m /= 8; }
+  while (m % 4 == 0 && ap.nst < kMaxStages) { ap.radix[ap.nst++] = 4; m /= 4; }
+  while (m % 2 == 0 && ap.nst < kMaxStages) { ap.radix[ap.nst++] = 2; m /= 2; }
+  while (m % 3 == 0 && ap.nst < kMaxStages) { ap.radix[ap.nst++] = 3; m /= 3; }
+  while (m % 5 == 0 && ap.nst < kMaxStages) { ap.radix[ap.nst++] = 5; m /= 5; }
+  return m == 1;
+}
+
+static LaunchShape choose_shape(int E, size_t elem, size_t extra) {
+  LaunchShape s;
+  int maxv = 8;
+  int t = 0;
+  for (maxv = 8; maxv <= 32; maxv *= 2) {
+    t = ((E + maxv - 1) / maxv + 31) / 32 * 32;
+    if (t <= 512) break;
+  }
+  if (maxv > 32) {
+    maxv = 32;
+    t = ((E + maxv - 1) / maxv + 31) / 32 * 32;
+  }
+  if (t < 64) t = 64;
+  s.threads = t;
+  s.maxv = maxv;
+  s.smem = (int)(E * elem + extra);
+  return s;
+}
+
+// ---------------------------------------------------------------------------
+// host-side tables (code/array_utils.cpp:239-272, code/initialize.cpp:97-102,
+// :401-404, code/calc_debye.cpp:5-68)
+// ---------------------------------------------------------------------------
+static double get_k(const Instance &I, long long id, double k[3]) {
+  const int *Nx = I.p.Nx;
+  const double *L = I.p.L;
+  int n[3];
+  n[2] = (int)(id / Nx[1] / Nx[0]);
+  n[1] = (int)(id / Nx[0] - (long long)n[2] * Nx[1]);
+  n[0] = (int)(id - ((long long)n[1] + (long long)n[2] * Nx[1]) * Nx[0]);
+  double kmag = 0.0;
+  for (int d = 0; d < 3; d++) {
+    if (double(n[d]) < double(Nx[d]) / 2.)
+      k[d] = 2 * kPI * double(n[d]) / L[d];
+    else
+      k[d] = 2 * kPI * double(n[d] - Nx[d]) / L[d];
+  }
+  for (int d = 0; d < 3; d++) kmag += k[d] * k[d];
+  return kmag;
+}
+
+template <class T> static T *dalloc(scft_ctx *c, size_t n) {
+  void *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc(&p, n * sizeof(T));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    throw ScftError(SCFT_ERR_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+  }
+  c->allocs.push_back(p);
+  CK(cudaMemsetAsync(p, 0, n * sizeof(T), c->st));
+  return reinterpret_cast<T *>(p);
+}
+
+template <class T> static T *dupload(scft_ctx *c, const std::vector<T> &v) {
+  T *p = dalloc<T>(c, v.size());
+  CK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, c->st));
+  return p;
+}
+
+// ---------------------------------------------------------------------------
+// device set-up kernels: plate profile and graft map
+// ---------------------------------------------------------------------------
+struct PlateArgs {
+  int nx, ny, nz;
+  double dx[3], L[3], c[3], u[3];
+  double len, rad, xi;
+  int shape;
+};
+
+// code/initialize.cpp:578-612 (explicit_nanorod), code/array_utils.cpp:588-646
+__global__ void k_plate(double2 *out, PlateArgs a, int accumulate) {
+  const long long M = (long long)a.nx * a.ny * a.nz;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
+    const int ix = (int)(i % a.nx);
+    const int iy = (int)((i / a.nx) % a.ny);
+    const int iz = (int)(i / ((long long)a.nx * a.ny));
+    const int nn[3] = {ix, iy, iz};
+    double dr[3];
+    for (int d = 0; d < 3; d++) {
+      const double x = double(nn[d]) * a.dx[d];
+      double r = x - a.c[d];
+      if (r >= 0.5 * a.L[d]) r -= a.L[d];
+      else if (r < -0.5 * a.L[d]) r += a.L[d];
+      dr[d] = r;
+    }
+    double v;
+    if (a.shape == SCFT_PLATE_CUBOID) {
+      // slab of thickness len along u, square of side 2*rad in the plane:
+      // in-plane axes e1 = normalised (u x z) (or u x y when u is along z), e2 = u x e1
+      double e1[3];
+      if (fabs(a.u[2]) < 0.9) {
+        e1[0] = a.u[1]; e1[1] = -a.u[0]; e1[2] = 0.0;
+      } else {
+        e1[0] = 0.0; e1[1] = a.u[2]; e1[2] = -a.u[1];
+      }
+      const double n1 = sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
+      for (int d = 0; d < 3; d++) e1[d] /= n1;
+      const double e2[3] = {a.u[1] * e1[2] - a.u[2] * e1[1], a.u[2] * e1[0] - a.u[0] * e1[2],
+                            a.u[0] * e1[1] - a.u[1] * e1[0]};
+      const double p0 = a.u[0] * dr[0] + a.u[1] * dr[1] + a.u[2] * dr[2];
+      const double p1 = e1[0] * dr[0] + e1[1] * dr[1] + e1[2] * dr[2];
+      const double p2 = e2[0] * dr[0] + e2[1] * dr[1] + e2[2] * dr[2];
+      v = 0.125 * erfc((fabs(p0) - 0.5 * a.len) / a.xi) * erfc((fabs(p1) - a.rad) / a.xi) *
+          erfc((fabs(p2) - a.rad) / a.xi);
+    } else {
+      double udr = 0.0;
+      for (int d = 0; d < 3; d++) udr += a.u[d] * dr[d];
+      double mag = 0.0, dum;
+      dum = a.u[1] * dr[2] - a.u[2] * dr[1];
+      mag += dum * dum;
+      dum = a.u[2] * dr[0] - a.u[0] * dr[2];
+      mag += dum * dum;
+      dum = a.u[0] * dr[1] - a.u[1] * dr[0];
+      mag += dum * dum;
+      const double ucr = sqrt(mag);
+      v = 0.25 * erfc((fabs(udr) - 0.5 * a.len) / a.xi) * erfc((fabs(ucr) - a.rad) / a.xi);
+    }
+    if (accumulate) out[i] = make_double2(out[i].x + v, out[i].y);
+    else out[i] = make_double2(v, 0.0);
+  }
+}
+
+// multiply k-space array by I*k_alias[dir] (code/array_utils.cpp:181-235, :565-579)
+__global__ void k_mul_ik_alias(double2 *a, int nx, int ny, int nz, double Lx, double Ly, double Lz, int dir) {
+  const long long M = (long long)nx * ny * nz;
+  const int Nn[3] = {nx, ny, nz};
+  const double L[3] = {Lx, Ly, Lz};
+  const int has_nyq = (nx % 2 == 0) || (ny % 2 == 0) || (nz % 2 == 0);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
+    const int n[3] = {(int)(i % nx), (int)((i / nx) % ny), (int)(i / ((long long)nx * ny))};
+    double k[3];
+    for (int d = 0; d < 3; d++) {
+      if (Nn[d] % 2 == 0 && n[d] == Nn[d] / 2) k[d] = 0.0;
+      else if (double(n[d]) < double(Nn[d]) / 2.) k[d] = 2 * kPI * double(n[d]) / L[d];
+      else k[d] = 2 * kPI * double(n[d] - Nn[d]) / L[d];
+    }
+    if (i != 0 && has_nyq) {
+      for (int d = 0; d < 3; d++)
+        if (k[d] == 0.0) { k[0] = k[1] = k[2] = 0.0; break; }
+    }
+    const double kv = k[dir];
+    const double2 v = a[i];
+    // v * (I*kv) with (I*kv) = (0, kv)
+    a[i] = make_double2(v.x * 0.0 - v.y * kv, v.x * kv + v.y * 0.0);
+  }
+}
+
+__device__ double2 csqrt_d(double2 z) {
+  const double x = z.x, y = z.y;
+  if (x == 0.0 && y == 0.0) return make_double2(0.0, y);
+  const double r = hypot(x, y);
+  if (x >= 0.0) {
+    const double t = sqrt(0.5 * (r + x));
+    return make_double2(t, y / (2.0 * t));
+  }
+  const double t = sqrt(0.5 * (r - x));
+  return make_double2(fabs(y) / (2.0 * t), copysign(t, y));
+}
+
+// graft map += sqrt(gx^2 + gy^2 + gz^2) (complex), code/initialize.cpp:175-186
+__global__ void k_grad_mag_acc(double2 *acc, const double2 *gx, const double2 *gy, const double2 *gz, long long M) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
+    double2 t = make_double2(0.0, 0.0);
+    const double2 *g[3] = {gx, gy, gz};
+    for (int d = 0; d < 3; d++) t = cadd(t, cmul(g[d][i], g[d][i]));
+    acc[i] = cadd(acc[i], csqrt_d(t));
+  }
+}
+
+__global__ void k_scale_c(double2 *a, double2 s, long long M, int divide) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
+    if (divide) {
+      // a / s (Smith)
+      const double2 b = s, x = a[i];
+      double2 r;
+      if (fabs(b.x) < fabs(b.y)) {
+        const double q = b.x / b.y, d = b.x * q + b.y;
+        r = make_double2((x.x * q + x.y) / d, (x.y * q - x.x) / d);
+      } else {
+        const double q = b.y / b.x, d = b.y * q + b.x;
+        r = make_double2((x.y * q + x.x) / d, (x.y - x.x * q) / d);
+      }
+      a[i] = r;
+    } else {
+      a[i] = cmul(a[i], s);
+    }
+  }
+}
+
+__global__ void k_real_part(double *out, const double2 *in, long long M) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x)
+    out[i] = in[i].x;
+}
+
+// plain block partial sums of a complex array (set-up only)
+__global__ void k_sum_partials(const double2 *a, long long M, double2 *out) {
+  __shared__ double2 red[32];
+  double2 s = make_double2(0.0, 0.0);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x)
+    s = cadd(s, a[i]);
+  for (int o = 16; o > 0; o >>= 1) {
+    s.x += __shfl_down_sync(0xffffffffu, s.x, o);
+    s.y += __shfl_down_sync(0xffffffffu, s.y, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) red[w] = s;
+  __syncthreads();
+  if (w == 0) {
+    s = l < (int)(blockDim.x >> 5) ? red[l] : make_double2(0.0, 0.0);
+    for (int o = 16; o > 0; o >>= 1) {
+      s.x += __shfl_down_sync(0xffffffffu, s.x, o);
+      s.y += __shfl_down_sync(0xffffffffu, s.y, o);
+    }
+    if (l == 0) out[blockIdx.x] = s;
+  }
+}
+
+}  // namespace scft
+
+using namespace scft;
+
+// ---------------------------------------------------------------------------
+// internal helpers (host)
+// ---------------------------------------------------------------------------
+namespace {
+
+const int kSumBlocks = 128;
+
+cd integ(scft_ctx *c, const Instance &I, const double2 *a, double2 *scratch) {
+  k_sum_partials<<<kSumBlocks, 256, 0, c->st>>>(a, I.M, scratch);
+  CK(cudaGetLastError());
+  std::vector<double2> h(kSumBlocks);
+  CK(cudaMemcpyAsync(h.data(), scratch, sizeof(double2) * kSumBlocks, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  cd s(0.0, 0.0);
+  for (int b = 0; b < kSumBlocks; b++) s += cd(h[b].x, h[b].y);
+  for (int d = 0; d < 3; d++) s *= I.info.dx[d];
+  return s;
+}
+
+// Runs plane + column passes over a list of arrays of one instance.
+void fft3d_arrays(scft_ctx *c, const Instance &I, const std::vector<double2 *> &arrs, int sign) {
+  const DevGeom &g = c->geoms[I.geom];
+  std::vector<PlaneJob> pj;
+  std::vector<ColJob> cj;
+  for (double2 *a : arrs) {
+    for (int z = 0; z < g.nz; z++) pj.push_back(PlaneJob{a, I.geom, z});
+    for (int y = 0; y < g.ny; y++)
+      for (int x0 = 0; x0 < g.nx; x0 += g.tx) cj.push_back(ColJob{a, nullptr, I.geom, x0, y});
+  }
+  PlaneJob *dpj = nullptr;
+  ColJob *dcj = nullptr;
+  CK(cudaMalloc(&dpj, sizeof(PlaneJob) * pj.size()));
+  CK(cudaMalloc(&dcj, sizeof(ColJob) * cj.size()));
+  CK(cudaMemcpyAsync(dpj, pj.data(), sizeof(PlaneJob) * pj.size(), cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(dcj, cj.data(), sizeof(ColJob) * cj.size(), cudaMemcpyHostToDevice, c->st));
+  LaunchShape sp = choose_shape(g.nx * g.ny, sizeof(double2), (g.nx + g.ny + 32) * sizeof(double2));
+  LaunchShape sc = choose_shape(g.tx * g.nz, sizeof(double2), (g.nz + 32) * sizeof(double2));
+  if (sign < 0) {
+    CK(launch_plane_fft<double>(sp, dpj, (int)pj.size(), c->d_geoms, c->d_tw64, -1, 0, c->st));
+    CK(launch_col_fft<double>(sc, dcj, (int)cj.size(), c->d_geoms, c->d_tw64, 0, 1, c->st));
+  } else {
+    CK(launch_col_fft<double>(sc, dcj, (int)cj.size(), c->d_geoms, c->d_tw64, 1, 0, c->st));
+    CK(launch_plane_fft<double>(sp, dpj, (int)pj.size(), c->d_geoms, c->d_tw64, +1, 0, c->st));
+  }
+  CK(cudaStreamSynchronize(c->st));
+  cudaFree(dpj);
+  cudaFree(dcj);
+}
+
+void validate(const scft_params &p) {
+  auto bad = [](const std::string &m) { throw ScftError(SCFT_ERR_ARG, m); };
+  if (p.Nda < 0 || p.Ndb < 0 || p.Nda + p.Ndb < 1) bad("Nda + Ndb must be >= 1");
+  for (int d = 0; d < 3; d++) {
+    if (p.Nx[d] < 2) bad("Nx must be >= 2 in every direction");
+    if (!(p.L[d] > 0)) bad("L must be positive");
+    AxisPlan ap;
+    if (!make_axis_plan(p.Nx[d], ap)) throw ScftError(SCFT_ERR_UNSUPPORTED, "grid sizes must be 2^a 3^b 5^c");
+  }
+  if (!(p.kappa > 0)) bad("kappa must be > 0 (code/1s_update.cpp:72-78 leaves B unset otherwise)");
+  if (!(p.rho0 > 0)) bad("rho0 must be positive");
+  if (p.n_exp_nr < 0 || p.n_exp_nr > 2) bad("n_exp_nr must be 0, 1 or 2 (code/globals.h:57-58)");
+  if (p.n_exp_nr > 0) {
+    for (int j = 0; j < p.n_exp_nr; j++)
+      for (int d = 0; d < 3; d++)
+        if (p.center[j][d] < 0.0 || p.center[j][d] > 1.0) bad("plate centres are fractions of L in [0,1]");
+    if (!(p.xi_nr > 0)) bad("xi_nr must be positive");
+  }
+  if (p.precision != SCFT_PREC_FP64 && p.precision != SCFT_PREC_MIXED) bad("unknown precision");
+  if (p.sigma > 0 && p.Ng < 1) bad("grafted chains need Ng >= 1");
+}
+
+void setup_instance(scft_ctx *c, Instance &I, int idx) {
+  const scft_params &p = I.p;
+  I.N = p.Nda + p.Ndb;
+  I.Na = p.Nda;
+  I.Ng = p.Ng;
+  I.fD = I.N > 0 ? double(p.Nda) / double(I.N) : 0.0;
+  I.Rg2 = double(I.N - 1) / 6.0;
+  // code/read_input.cpp:53-85
+  I.neg_ab = p.chi_ab < 0.0; I.cab = fabs(p.chi_ab);
+  I.neg_bc = p.chi_bc < 0.0; I.cbc = fabs(p.chi_bc);
+  I.neg_ac = p.chi_ac < 0.0; I.cac = fabs(p.chi_ac);
+  const double sigma = (p.Ng == 0) ? 0.0 : p.sigma;  // code/read_input.cpp:200
+  I.single = (I.Na == 0 || I.Na == I.N);
+  I.hmax = (I.N - 1) / 2;
+  // code/initialize.cpp:60-67
+  I.M = 1;
+  double V = 1.0;
+  for (int d = 0; d < 3; d++) {
+    I.M *= p.Nx[d];
+    V *= p.L[d];
+    I.info.dx[d] = p.L[d] / double(p.Nx[d]);
+  }
+  I.info.M = I.M;
+  I.info.V = V;
+  I.info.N = I.N;
+  const long long M = I.M;
+
+  // geometry record
+  DevGeom g;
+  g.nx = p.Nx[0];
+  g.ny = p.Nx[1];
+  g.nz = p.Nx[2];
+  g.M = M;
+  g.tx = 16;
+  while (g.nx % g.tx) g.tx /= 2;
+  for (int d = 0; d < 3; d++) make_axis_plan(p.Nx[d], g.ax[d]);
+  I.geom = (int)c->geoms.size();
+  c->geoms.push_back(g);
+
+  // tables from get_k
+  std::vector<double> hh(M), pb(M), gaa(M), gab(M), gbb(M), gc(M, 0.0);
+  const double a2 = p.a_smear * p.a_smear;
+  const double fD = I.fD, Rg2 = I.Rg2;
+  const double alpha_c = (I.N > 1) ? double(p.Ng - 1) / double(I.N - 1) : 0.0;
+  for (long long i = 0; i < M; i++) {
+    double kv[3];
+    const double k2 = get_k(I, i, kv);
+    hh[i] = exp(-k2 * a2 / 2.0);
+    pb[i] = exp(-k2 / 6.0);
+    const double x = k2 * Rg2;
+    gaa[i] = 2.0 * (exp(-x * fD) + fD * x - 1.0) / x / x;
+    gbb[i] = 2.0 * (exp(-x * (1.0 - fD)) + (1.0 - fD) * x - 1.0) / x / x;
+    gab[i] = (1.0 - exp(-x * fD)) * (1.0 - exp(-x * (1.0 - fD))) / x / x;
+    if (sigma > 0) {
+      const double dm1 = k2 * Rg2 * alpha_c;
+      gc[i] = (dm1 == 0.0) ? 1.0 : 2.0 * (exp(-dm1) + dm1 - 1.0) / dm1 / dm1;
+    }
+  }
+  gaa[0] = fD * fD;
+  gbb[0] = (1.0 - fD) * (1.0 - fD);
+  gab[0] = fD * (1.0 - fD);
+  I.hhat = dupload(c, hh);
+  I.pbond = dupload(c, pb);
+  I.gaa = dupload(c, gaa);
+  I.gab = dupload(c, gab);
+  I.gbb = dupload(c, gbb);
+  I.gc = dupload(c, gc);
+
+  // device arrays
+  for (int f = 0; f < 7; f++) I.w[f] = dalloc<double2>(c, M);
+  for (int f = 0; f < 3; f++) {
+    I.sm[f] = dalloc<double2>(c, M);
+    I.rho[f] = dalloc<double2>(c, M);
+    I.expw[f] = dalloc<double2>(c, M);
+  }
+  for (int q = 0; q < 2; q++)
+    for (int s = 0; s < 2; s++) I.acc[q][s] = dalloc<double2>(c, M);
+  for (int q = 0; q < 2; q++) {
+    if (q == 1 && I.single) {
+      I.work[1] = I.work[0];
+      I.hist[1] = I.hist[0];
+      continue;
+    }
+    I.work[q] = dalloc<double2>(c, M);
+    I.hist[q] = dalloc<double2>(c, (size_t)M * (I.hmax + 1));
+  }
+  I.qpart = dalloc<double2>(c, g.nz);
+  I.scal = dalloc<double2>(c, kNumScalars);
+  I.exp_nrH = dalloc<double2>(c, M);
+  I.grafts = dalloc<double2>(c, M);
+  I.rho_exp_nr = dalloc<double>(c, M);
+  (void)idx;
+}
+
+// Plate profile, graft map and chain counts (code/initialize.cpp:139-386).
+void setup_plates(scft_ctx *c, Instance &I) {
+  const scft_params &p = I.p;
+  const long long M = I.M;
+  const double sigma = (p.Ng == 0) ? 0.0 : p.sigma;
+  double2 *rho_np = dalloc<double2>(c, M);
+  double2 *pd = dalloc<double2>(c, M);
+  double2 *gr[3] = {dalloc<double2>(c, M), dalloc<double2>(c, M), dalloc<double2>(c, M)};
+  double2 *scratch = dalloc<double2>(c, kSumBlocks);
+  const int blocks = 1024;
+  auto plate_args = [&](int j, double len, double rad) {
+    PlateArgs a;
+    a.nx = p.Nx[0]; a.ny = p.Nx[1]; a.nz = p.Nx[2];
+    double un = 0.0;
+    for (int d = 0; d < 3; d++) un += p.orient[j][d] * p.orient[j][d];
+    un = sqrt(un);
+    for (int d = 0; d < 3; d++) {
+      a.dx[d] = I.info.dx[d];
+      a.L[d] = p.L[d];
+      a.c[d] = p.center[j][d] * p.L[d];
+      a.u[d] = p.orient[j][d] / un;  // code/read_input.cpp:220-235
+    }
+    a.len = len; a.rad = rad; a.xi = p.xi_nr;
+    a.shape = p.plate_shape;
+    return a;
+  };
+  // graft map from the 1.05x-enlarged plates (code/initialize.cpp:160-200)
+  for (int j = 0; j < p.n_exp_nr; j++) {
+    k_plate<<<blocks, 256, 0, c->st>>>(pd, plate_args(j, p.L_nr * 1.05, p.R_nr * 1.05), 0);
+    CK(cudaGetLastError());
+    for (int d = 0; d < 3; d++) {
+      CK(cudaMemcpyAsync(gr[d], pd, sizeof(double2) * M, cudaMemcpyDeviceToDevice, c->st));
+      fft3d_arrays(c, I, {gr[d]}, -1);
+      k_mul_ik_alias<<<blocks, 256, 0, c->st>>>(gr[d], p.Nx[0], p.Nx[1], p.Nx[2], p.L[0], p.L[1], p.L[2], d);
+      CK(cudaGetLastError());
+      fft3d_arrays(c, I, {gr[d]}, +1);
+    }
+    k_grad_mag_acc<<<blocks, 256, 0, c->st>>>(I.grafts, gr[0], gr[1], gr[2], M);
+    CK(cudaGetLastError());
+    if (j == p.n_exp_nr - 1) {
+      const cd tot = integ(c, I, I.grafts, scratch);
+      k_scale_c<<<blocks, 256, 0, c->st>>>(I.grafts, make_double2(tot.real(), tot.imag()), M, 1);
+      CK(cudaGetLastError());
+    }
+  }
+  // core density (code/initialize.cpp:210-239)
+  for (int j = 0; j < p.n_exp_nr; j++) {
+    k_plate<<<blocks, 256, 0, c->st>>>(rho_np, plate_args(j, p.L_nr, p.R_nr), 1);
+    CK(cudaGetLastError());
+  }
+  k_real_part<<<blocks, 256, 0, c->st>>>(I.rho_exp_nr, rho_np, M);
+  CK(cudaGetLastError());
+  CK(cudaMemcpyAsync(I.exp_nrH, rho_np, sizeof(double2) * M, cudaMemcpyDeviceToDevice, c->st));
+  fft3d_arrays(c, I, {I.exp_nrH}, -1);
+  // volumes and counts (code/initialize.cpp:249-386), no film, no field NPs
+  const double V = I.info.V;
+  const double V_exp = integ(c, I, rho_np, scratch).real();
+  const double Vf = V - 0.0;
+  const double np_frac = V_exp / Vf;
+  const double V1 = p.n_exp_nr > 0 ? V_exp / double(p.n_exp_nr) : 0.0;
+  if (sigma > 0.0 && p.n_exp_nr > 0) {
+    const cd en = integ(c, I, I.grafts, scratch);
+    const cd inv = 1.0 / en;
+    k_scale_c<<<blocks, 256, 0, c->st>>>(I.grafts, make_double2(inv.real(), inv.imag()), M, 0);
+    CK(cudaGetLastError());
+  }
+  const double nP = (p.n_exp_nr == 0) ? 0.0 : V_exp / V1;
+  double ng_per_np = 0.0, phiG = 0.0;
+  if (sigma > 0.0) {
+    ng_per_np = sigma * 4.0 * kPI * p.R_nr * p.R_nr;
+    phiG = ng_per_np * nP * p.Ng / p.rho0 / Vf;
+  }
+  const double phiD = 1.0 - 0.0 - np_frac - phiG;
+  I.info.Vf = Vf;
+  I.info.np_frac = np_frac;
+  I.info.nP = nP;
+  I.info.ng_per_np = ng_per_np;
+  I.info.phiG = phiG;
+  I.info.phiD = phiD;
+  I.info.nD = phiD * p.rho0 * Vf / I.N;
+  I.graft = (sigma > 0.0 && p.n_exp_nr > 0 && nP > 0.0) ? 1 : 0;
+  if (I.graft) {
+    I.gwork = dalloc<double2>(c, M);
+    I.ghist = dalloc<double2>(c, (size_t)M * p.Ng);
+    I.gacc = dalloc<double2>(c, M);
+  }
+  CK(cudaStreamSynchronize(c->st));
+}
+
+// Builds the device views and job lists once all instances exist.
+void build_jobs(scft_ctx *c) {
+  const int n = (int)c->inst.size();
+  std::vector<FieldInst> fi(n);
+  std::vector<PropInst> pi(n);
+  for (int k = 0; k < n; k++) {
+    Instance &I = c->inst[k];
+    FieldInst &F = fi[k];
+    memset(&F, 0, sizeof F);
+    F.M = I.M;
+    F.geom = I.geom;
+    F.rho0 = I.p.rho0;
+    F.kappa = I.p.kappa;
+    F.cab = I.cab; F.cbc = I.cbc; F.cac = I.cac;
+    F.neg_ab = I.neg_ab; F.neg_bc = I.neg_bc; F.neg_ac = I.neg_ac;
+    F.phiD = I.info.phiD; F.phiG = I.info.phiG;
+    F.lam_pl = I.p.lam_pl; F.lam_mi = I.p.lam_mi;
+    F.nD = I.info.nD; F.V = I.info.V;
+    for (int d = 0; d < 3; d++) F.dx[d] = I.info.dx[d];
+    F.N = I.N; F.Ng = I.Ng; F.np_chem = I.p.np_chem; F.graft = I.graft; F.single = I.single;
+    F.ng_per_np = I.info.ng_per_np;
+    F.n_exp_nr = I.p.n_exp_nr;
+    for (int f = 0; f < 7; f++) F.w[f] = I.w[f];
+    for (int f = 0; f < 3; f++) { F.sm[f] = I.sm[f]; F.rho[f] = I.rho[f]; F.expw[f] = I.expw[f]; }
+    F.hhat = I.hhat; F.gaa = I.gaa; F.gab = I.gab; F.gbb = I.gbb; F.gc = I.gc;
+    F.rho_exp_nr = I.rho_exp_nr;
+    F.exp_nrH = I.exp_nrH;
+    for (int q = 0; q < 2; q++)
+      for (int s = 0; s < 2; s++) F.acc[q][s] = I.acc[q][s];
+    F.qpart = I.qpart;
+    F.nz = I.p.Nx[2];
+    F.scal = I.scal;
+    F.gacc = I.gacc;
+    F.ghist_last = I.graft ? I.ghist + (size_t)I.M * (I.Ng - 1) : nullptr;
+    F.grafts = I.grafts;
+
+    PropInst &P = pi[k];
+    memset(&P, 0, sizeof P);
+    P.geom = I.geom;
+    P.N = I.N;
+    P.Na = I.Na;
+    P.single = I.single;
+    P.hmax = I.hmax;
+    for (int q = 0; q < 2; q++) {
+      P.work[q] = I.work[q];
+      P.hist[q] = I.hist[q];
+      P.expw[q] = I.expw[q];
+      for (int s = 0; s < 2; s++) P.acc[q][s] = I.acc[q][s];
+    }
+    P.qpart = I.qpart;
+    P.graft = I.graft;
+    P.Ng = I.Ng;
+    P.gwork = I.gwork;
+    P.ghist = I.ghist;
+    P.gacc = I.gacc;
+    P.gexpw = I.expw[2];
+    P.grafts = I.grafts;
+  }
+  c->d_fi = dupload(c, fi);
+  c->d_pi = dupload(c, pi);
+
+  // field transform job lists
+  std::vector<PlaneJob> pj_upd, pj_fld, pj_sm;
+  std::vector<ColJob> cj_upd, cj_fld, cj_sm;
+  int emax_plane = 0, emax_col = 0, nxy_max = 0, nz_max = 0;
+  for (int k = 0; k < n; k++) {
+    Instance &I = c->inst[k];
+    const DevGeom &g = c->geoms[I.geom];
+    emax_plane = std::max(emax_plane, g.nx * g.ny);
+    emax_col = std::max(emax_col, g.tx * g.nz);
+    nxy_max = std::max(nxy_max, g.nx + g.ny);
+    nz_max = std::max(nz_max, g.nz);
+    std::vector<double2 *> upd = {I.rho[0], I.rho[1]};
+    if (I.graft) upd.push_back(I.rho[2]);
+    std::vector<double2 *> fld = {I.w[0]};
+    if (I.cab != 0.0) { fld.push_back(I.w[2]); fld.push_back(I.w[1]); }
+    if (I.cbc != 0.0) { fld.push_back(I.w[4]); fld.push_back(I.w[3]); }
+    if (I.cac != 0.0) { fld.push_back(I.w[6]); fld.push_back(I.w[5]); }
+    for (double2 *a : fld) upd.push_back(a);
+    std::vector<double2 *> smr = {I.sm[0], I.sm[1]};
+    if (I.graft) smr.push_back(I.sm[2]);
+    auto add = [&](std::vector<double2 *> &arrs, std::vector<PlaneJob> &pj, std::vector<ColJob> &cj,
+                   const void *kern) {
+      for (double2 *a : arrs) {
+        for (int z = 0; z < g.nz; z++) pj.push_back(PlaneJob{a, I.geom, z});
+        for (int y = 0; y < g.ny; y++)
+          for (int x0 = 0; x0 < g.nx; x0 += g.tx) cj.push_back(ColJob{a, kern, I.geom, x0, y});
+      }
+    };
+    add(upd, pj_upd, cj_upd, nullptr);
+    add(fld, pj_fld, cj_fld, nullptr);
+    add(smr, pj_sm, cj_sm, I.hhat);
+  }
+  c->shp_plane = choose_shape(emax_plane, sizeof(double2), (nxy_max + 32) * sizeof(double2));
+  c->shp_col = choose_shape(emax_col, sizeof(double2), (nz_max + 32) * sizeof(double2));
+  c->shp_prop = c->shp_plane;
+  if (c->shp_plane.smem > 227 * 1024)
+    throw ScftError(SCFT_ERR_UNSUPPORTED, "xy plane too large for the FP64 plane pass (nx*ny*16 B > 227 KB)");
+  c->d_pj_upd = dupload(c, pj_upd); c->n_pj_upd = (int)pj_upd.size();
+  c->d_pj_fld = dupload(c, pj_fld); c->n_pj_fld = (int)pj_fld.size();
+  c->d_pj_sm = dupload(c, pj_sm); c->n_pj_sm = (int)pj_sm.size();
+  c->d_cj_upd = dupload(c, cj_upd); c->n_cj_upd = (int)cj_upd.size();
+  c->d_cj_fld = dupload(c, cj_fld); c->n_cj_fld = (int)cj_fld.size();
+  c->d_cj_sm = dupload(c, cj_sm); c->n_cj_sm = (int)cj_sm.size();
+
+  // propagator job lists, instances ordered by decreasing N so that the jobs
+  // still active at step n form a prefix
+  std::vector<int> order(n);
+  for (int k = 0; k < n; k++) order[k] = k;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return c->inst[a].N > c->inst[b].N; });
+  std::vector<PropJob> ppj;
+  std::vector<ColJob> pcj;
+  std::vector<int> inst_pj_end(n), inst_cj_end(n);
+  c->nmax = 0;
+  for (int oi = 0; oi < n; oi++) {
+    const int k = order[oi];
+    Instance &I = c->inst[k];
+    const DevGeom &g = c->geoms[I.geom];
+    c->nmax = std::max(c->nmax, I.N);
+    const int np = I.single ? 1 : 2;
+    for (int q = 0; q < np; q++) {
+      for (int z = 0; z < g.nz; z++) ppj.push_back(PropJob{k, q, z});
+      for (int y = 0; y < g.ny; y++)
+        for (int x0 = 0; x0 < g.nx; x0 += g.tx) pcj.push_back(ColJob{I.work[q], I.pbond, I.geom, x0, y});
+    }
+    inst_pj_end[oi] = (int)ppj.size();
+    inst_cj_end[oi] = (int)pcj.size();
+  }
+  c->prop_pj_count.assign(c->nmax, 0);
+  c->prop_cj_count.assign(c->nmax, 0);
+  for (int s = 0; s < c->nmax; s++) {
+    for (int oi = 0; oi < n; oi++) {
+      if (c->inst[order[oi]].N > s) {
+        c->prop_pj_count[s] = inst_pj_end[oi];
+        c->prop_cj_count[s] = inst_cj_end[oi];
+      }
+    }
+  }
+  c->d_prop_pj = dupload(c, ppj);
+  c->d_prop_cj = dupload(c, pcj);
+
+  // graft sweep job lists, graft instances ordered by decreasing Ng
+  std::vector<int> gorder;
+  for (int k = 0; k < n; k++)
+    if (c->inst[k].graft) gorder.push_back(k);
+  std::stable_sort(gorder.begin(), gorder.end(), [&](int a, int b) { return c->inst[a].Ng > c->inst[b].Ng; });
+  std::vector<PropJob> gpj;
+  std::vector<ColJob> gcj;
+  std::vector<int> gp_end, gc_end;
+  c->ngmax = 0;
+  for (int k : gorder) {
+    Instance &I = c->inst[k];
+    const DevGeom &g = c->geoms[I.geom];
+    c->ngmax = std::max(c->ngmax, I.Ng);
+    for (int z = 0; z < g.nz; z++) gpj.push_back(PropJob{k, 0, z});
+    for (int y = 0; y < g.ny; y++)
+      for (int x0 = 0; x0 < g.nx; x0 += g.tx) gcj.push_back(ColJob{I.gwork, I.pbond, I.geom, x0, y});
+    gp_end.push_back((int)gpj.size());
+    gc_end.push_back((int)gcj.size());
+  }
+  c->graft_pj_count.assign(c->ngmax, 0);
+  c->graft_cj_count.assign(c->ngmax, 0);
+  for (int s2 = 0; s2 < c->ngmax; s2++)
+    for (size_t oi = 0; oi < gorder.size(); oi++)
+      if (c->inst[gorder[oi]].Ng > s2) {
+        c->graft_pj_count[s2] = gp_end[oi];
+        c->graft_cj_count[s2] = gc_end[oi];
+      }
+  if (!gpj.empty()) {
+    c->d_graft_pj = dupload(c, gpj);
+    c->d_graft_cj = dupload(c, gcj);
+  }
+  c->gblocks = 64;
+  c->d_gpart = dalloc<double2>(c, (size_t)n * c->gblocks * 2);
+  long long mmax = 0;
+  for (auto &I : c->inst) mmax = std::max(mmax, I.M);
+  c->eblocks = (int)std::min<long long>(2048, (mmax + 255) / 256);
+  c->hblocks = 64;
+  c->d_hpart = dalloc<double2>(c, (size_t)n * 4 * c->hblocks);
+}
+
+// calc_poly_density for every instance (code/calc_poly_density.cpp:37-161)
+void seq_poly_density(scft_ctx *c) {
+  const int n = (int)c->inst.size();
+  cudaStream_t st = c->st;
+  CK(launch_assemble(c->d_fi, n, c->eblocks, st));
+  // smearing: smw = IFFT[ hhat * FFT[w] / M ]  (code/calc_poly_density.cpp:93-104)
+  CK(launch_plane_fft<double>(c->shp_plane, c->d_pj_sm, c->n_pj_sm, c->d_geoms, c->d_tw64, -1, 0, st));
+  CK(launch_col_fft<double>(c->shp_col, c->d_cj_sm, c->n_cj_sm, c->d_geoms, c->d_tw64, 2, 1, st));
+  CK(launch_plane_fft<double>(c->shp_plane, c->d_pj_sm, c->n_pj_sm, c->d_geoms, c->d_tw64, +1, 0, st));
+  CK(launch_boltzmann(c->d_fi, n, c->eblocks, st));
+  for (auto &I : c->inst)
+    for (int q = 0; q < 2; q++)
+      for (int s = 0; s < 2; s++) CK(cudaMemsetAsync(I.acc[q][s], 0, sizeof(double2) * I.M, st));
+  // propagator sweep (code/diblock_discrete.cpp:18-85, code/calc_poly_density.cpp:178-190)
+  CK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[0], c->d_pi, c->d_geoms, c->d_tw64, 0, st));
+  for (int s = 1; s < c->nmax; s++) {
+    CK(launch_col_fft<double>(c->shp_col, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw64, 2, 1, st));
+    CK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[s], c->d_pi, c->d_geoms, c->d_tw64, s,
+                             st));
+  }
+  CK(launch_q_finalize(c->d_fi, n, st));
+  CK(launch_density(c->d_fi, n, c->eblocks, st));
+  // grafted chains (code/calc_poly_density.cpp:131-133,155-159)
+  if (c->ngmax > 0) {
+    for (auto &I : c->inst)
+      if (I.graft) CK(cudaMemsetAsync(I.gacc, 0, sizeof(double2) * I.M, st));
+    for (int sweep = 0; sweep < 2; sweep++) {
+      CK(launch_graft_plane_f64(c->shp_prop, c->d_graft_pj, c->graft_pj_count[0], c->d_pi, c->d_geoms, c->d_tw64,
+                                sweep, 0, st));
+      for (int s = 1; s < c->ngmax; s++) {
+        CK(launch_col_fft<double>(c->shp_col, c->d_graft_cj, c->graft_cj_count[s], c->d_geoms, c->d_tw64, 2, 1,
+                                  st));
+        CK(launch_graft_plane_f64(c->shp_prop, c->d_graft_pj, c->graft_pj_count[s], c->d_pi, c->d_geoms,
+                                  c->d_tw64, sweep, s, st));
+      }
+    }
+    CK(launch_graft_finalize(c->d_fi, n, c->gblocks, c->d_gpart, st));
+    CK(launch_qga_finalize(c->d_fi, n, c->gblocks, c->d_gpart, st));
+  }
+}
+
+// update_1s for every instance (code/1s_update.cpp:7-352)
+void seq_update_1s(scft_ctx *c) {
+  const int n = (int)c->inst.size();
+  cudaStream_t st = c->st;
+  CK(launch_plane_fft<double>(c->shp_plane, c->d_pj_upd, c->n_pj_upd, c->d_geoms, c->d_tw64, -1, 0, st));
+  CK(launch_col_fft<double>(c->shp_col, c->d_cj_upd, c->n_cj_upd, c->d_geoms, c->d_tw64, 0, 1, st));
+  CK(launch_update_1s(c->d_fi, n, c->eblocks, st));
+  CK(launch_col_fft<double>(c->shp_col, c->d_cj_fld, c->n_cj_fld, c->d_geoms, c->d_tw64, 1, 0, st));
+  CK(launch_plane_fft<double>(c->shp_plane, c->d_pj_fld, c->n_pj_fld, c->d_geoms, c->d_tw64, +1, 0, st));
+  seq_poly_density(c);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// entry points used by capi.cpp
+// ---------------------------------------------------------------------------
+namespace scft {
+
+void ctx_create(scft_ctx *c, const scft_params *params, int n_inst) {
+  CK(cudaGetDevice(&c->device));
+  CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
+  c->inst.resize(n_inst);
+  for (int k = 0; k < n_inst; k++) {
+    validate(params[k]);
+    c->inst[k].p = params[k];
+    setup_instance(c, c->inst[k], k);
+  }
+  // twiddle tables for every distinct axis length
+  std::map<int, int> off;
+  std::vector<double2> tw;
+  for (auto &g : c->geoms) {
+    for (int d = 0; d < 3; d++) {
+      const int nn = g.ax[d].n;
+      if (!off.count(nn)) {
+        off[nn] = (int)tw.size();
+        const long double two_pi = 6.283185307179586476925286766559005768L;
+        for (int t = 0; t < nn; t++) {
+          const long double a = two_pi * (long double)t / (long double)nn;
+          tw.push_back(make_double2((double)cosl(a), (double)-sinl(a)));
+        }
+      }
+      g.ax[d].tw = off[nn];
+    }
+  }
+  c->d_tw64 = dupload(c, tw);
+  c->d_geoms = dupload(c, c->geoms);
+  for (auto &I : c->inst) setup_plates(c, I);
+  build_jobs(c);
+  CK(cudaStreamSynchronize(c->st));
+}
+
+void ctx_destroy(scft_ctx *c) {
+  if (c->g_update) cudaGraphExecDestroy(c->g_update);
+  for (void *p : c->allocs) cudaFree(p);
+  if (c->st) cudaStreamDestroy(c->st);
+}
+
+void ctx_poly_density(scft_ctx *c) {
+  seq_poly_density(c);
+  CK(cudaStreamSynchronize(c->st));
+  c->dirty_density = 0;
+}
+
+void ctx_update(scft_ctx *c, int n_iter) {
+  if (n_iter <= 0) return;
+  if (c->dirty_density) ctx_poly_density(c);
+  int k = 0;
+  if (!c->g_update) {
+    // first iteration runs eagerly (kernel attributes get set), then capture
+    seq_update_1s(c);
+    CK(cudaStreamSynchronize(c->st));
+    k = 1;
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+    try {
+      seq_update_1s(c);
+    } catch (...) {
+      cudaGraph_t g2;
+      cudaStreamEndCapture(c->st, &g2);
+      throw;
+    }
+    CK(cudaStreamEndCapture(c->st, &graph));
+    CK(cudaGraphInstantiate(&c->g_update, graph, 0));
+    cudaGraphDestroy(graph);
+  }
+  for (; k < n_iter; k++) CK(cudaGraphLaunch(c->g_update, c->st));
+  CK(cudaStreamSynchronize(c->st));
+}
+
+// calc_H (code/calc_h.cpp:9-64); out per instance: Re H, Im H, Re Qd, Im Qd, Re Qga
+int ctx_calc_H(scft_ctx *c, double *out) {
+  if (c->dirty_density) ctx_poly_density(c);
+  const int n = (int)c->inst.size();
+  CK(launch_h_partials(c->d_fi, n, c->hblocks, c->d_hpart, c->st));
+  std::vector<double2> hp((size_t)n * 4 * c->hblocks);
+  CK(cudaMemcpyAsync(hp.data(), c->d_hpart, sizeof(double2) * hp.size(), cudaMemcpyDeviceToHost, c->st));
+  std::vector<double2> sc((size_t)n * kNumScalars);
+  for (int k = 0; k < n; k++)
+    CK(cudaMemcpyAsync(&sc[(size_t)k * kNumScalars], c->inst[k].scal, sizeof(double2) * kNumScalars,
+                       cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  int status = SCFT_OK;
+  for (int k = 0; k < n; k++) {
+    const Instance &I = c->inst[k];
+    cd part[4];
+    for (int j = 0; j < 4; j++) {
+      cd s(0.0, 0.0);
+      for (int b = 0; b < c->hblocks; b++) {
+        const double2 v = hp[((size_t)k * 4 + j) * c->hblocks + b];
+        s += cd(v.x, v.y);
+      }
+      for (int d = 0; d < 3; d++) s *= I.info.dx[d];
+      part[j] = s;
+    }
+    if (I.cbc == 0.0) part[1] = 0.0;
+    if (I.cac == 0.0) part[2] = 0.0;
+    if (I.cab == 0.0) part[3] = 0.0;
+    cd H = part[0] + part[1] + part[2] + part[3];
+    const cd Qd(sc[(size_t)k * kNumScalars + kQd].x, sc[(size_t)k * kNumScalars + kQd].y);
+    const cd Qga(sc[(size_t)k * kNumScalars + kQga].x, sc[(size_t)k * kNumScalars + kQga].y);
+    if (I.info.nD > 0.0) H += -I.info.nD * std::log(Qd);
+    if (I.p.n_exp_nr > 0 && I.graft) H += -double(I.p.n_exp_nr) * I.info.ng_per_np * Qga.real();
+    out[5 * k + 0] = H.real();
+    out[5 * k + 1] = H.imag();
+    out[5 * k + 2] = Qd.real();
+    out[5 * k + 3] = Qd.imag();
+    out[5 * k + 4] = Qga.real();
+    if (H != H) status = SCFT_ERR_NAN;
+    // the reference exits once 5 points have Re q_g[Ng-1] <= 0 (code/grafted_nanoparticle.cpp:313-334)
+    if (I.graft && sc[(size_t)k * kNumScalars + kQg].x >= 5.0 && status == SCFT_OK) status = SCFT_ERR_QNONPOS;
+  }
+  return status;
+}
+
+void ctx_set_fields(scft_ctx *c, int k, const double *w) {
+  Instance &I = c->inst[k];
+  for (int f = 0; f < 7; f++)
+    CK(cudaMemcpyAsync(I.w[f], w + (size_t)f * 2 * I.M, sizeof(double2) * I.M, cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  c->dirty_density = 1;
+}
+
+void ctx_get_fields(scft_ctx *c, int k, double *w) {
+  Instance &I = c->inst[k];
+  for (int f = 0; f < 7; f++)
+    CK(cudaMemcpyAsync(w + (size_t)f * 2 * I.M, I.w[f], sizeof(double2) * I.M, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+}
+
+void ctx_get_density(scft_ctx *c, int k, double *ra, double *rb, double *rg) {
+  if (c->dirty_density) ctx_poly_density(c);
+  Instance &I = c->inst[k];
+  double *outs[3] = {ra, rb, rg};
+  for (int f = 0; f < 3; f++)
+    if (outs[f]) CK(cudaMemcpyAsync(outs[f], I.rho[f], sizeof(double2) * I.M, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+}
+
+void ctx_get_smeared(scft_ctx *c, int k, double *a, double *b, double *g) {
+  if (c->dirty_density) ctx_poly_density(c);
+  Instance &I = c->inst[k];
+  double *outs[3] = {a, b, g};
+  for (int f = 0; f < 3; f++)
+    if (outs[f]) CK(cudaMemcpyAsync(outs[f], I.sm[f], sizeof(double2) * I.M, cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+}
+
+void ctx_fft3d(scft_ctx *c, int k, double *data, int count, int sign) {
+  Instance &I = c->inst[k];
+  double2 *buf = nullptr;
+  CK(cudaMalloc(&buf, sizeof(double2) * I.M * count));
+  std::vector<double2 *> arrs;
+  try {
+    CK(cudaMemcpyAsync(buf, data, sizeof(double2) * I.M * count, cudaMemcpyHostToDevice, c->st));
+    for (int j = 0; j < count; j++) arrs.push_back(buf + (size_t)j * I.M);
+    fft3d_arrays(c, I, arrs, sign);
+    CK(cudaMemcpyAsync(data, buf, sizeof(double2) * I.M * count, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+  } catch (...) {
+    cudaFree(buf);
+    throw;
+  }
+  cudaFree(buf);
+}
+
+// diblock_discrete + integrate_diblock_discrete on given smeared fields.
+void ctx_diblock_density(scft_ctx *c, int k, const double *smwa, const double *smwb, double *ra, double *rb,
+                         double *Q) {
+  Instance &I = c->inst[k];
+  CK(cudaMemcpyAsync(I.sm[0], smwa, sizeof(double2) * I.M, cudaMemcpyHostToDevice, c->st));
+  CK(cudaMemcpyAsync(I.sm[1], smwb, sizeof(double2) * I.M, cudaMemcpyHostToDevice, c->st));
+  const int n = (int)c->inst.size();
+  cudaStream_t st = c->st;
+  CK(launch_boltzmann(c->d_fi, n, c->eblocks, st));
+  for (auto &J : c->inst)
+    for (int q = 0; q < 2; q++)
+      for (int s = 0; s < 2; s++) CK(cudaMemsetAsync(J.acc[q][s], 0, sizeof(double2) * J.M, st));
+  CK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[0], c->d_pi, c->d_geoms, c->d_tw64, 0, st));
+  for (int s = 1; s < c->nmax; s++) {
+    CK(launch_col_fft<double>(c->shp_col, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw64, 2, 1, st));
+    CK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[s], c->d_pi, c->d_geoms, c->d_tw64, s,
+                             st));
+  }
+  CK(launch_q_finalize(c->d_fi, n, st));
+  CK(launch_density(c->d_fi, n, c->eblocks, st));
+  if (ra) CK(cudaMemcpyAsync(ra, I.rho[0], sizeof(double2) * I.M, cudaMemcpyDeviceToHost, st));
+  if (rb) CK(cudaMemcpyAsync(rb, I.rho[1], sizeof(double2) * I.M, cudaMemcpyDeviceToHost, st));
+  if (Q) CK(cudaMemcpyAsync(Q, I.scal + kQd, sizeof(double2), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  c->dirty_density = 1;
+}
+
+int error_code(const std::exception &e) {
+  const ScftError *se = dynamic_cast<const ScftError *>(&e);
+  return se ? se->code : SCFT_ERR_CUDA;
+}
+
+}  // namespace scft
+
+namespace scft {
+// Replaces nD of instance k (used by the homopolymer entry point, where the
+// chain count nK is an argument).
+void ctx_override_nD(scft_ctx *c, int k, double nD) {
+  c->inst[k].info.nD = nD;
+  CK(cudaMemcpyAsync(reinterpret_cast<char *>(c->d_fi + k) + offsetof(FieldInst, nD), &nD, sizeof(double),
+                     cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+}
+}  // namespace scft

@@ -1,0 +1,86 @@
+// context.h -- host-side state of an scft_ctx.
+#pragma once
+
+#include <complex>
+#include <string>
+#include <vector>
+
+#include "../../include/scft.h"
+#include "common.h"
+#include "inst.h"
+#include "launch.h"
+
+namespace scft {
+
+typedef std::complex<double> cd;
+
+struct Instance {
+  scft_params p;
+  scft_info info;
+  int N, Na, Ng;
+  double fD, Rg2, cab, cbc, cac;
+  int neg_ab, neg_bc, neg_ac;
+  int graft;   // sigma > 0, Ng > 0 and explicit plates present
+  int single;  // q-dagger equals q
+  int hmax;
+  int geom;
+  long long M;
+  // device arrays (complex FP64 unless noted)
+  double2 *w[7] = {};
+  double2 *sm[3] = {};
+  double2 *rho[3] = {};
+  double2 *expw[3] = {};
+  double2 *acc[2][2] = {};
+  double2 *work[2] = {};
+  double2 *hist[2] = {};
+  double2 *qpart = nullptr;
+  double2 *scal = nullptr;
+  double2 *exp_nrH = nullptr;
+  double2 *grafts = nullptr;  // expl_grafts (real space)
+  double *hhat = nullptr, *gaa = nullptr, *gab = nullptr, *gbb = nullptr, *gc = nullptr;
+  double *pbond = nullptr, *rho_exp_nr = nullptr;
+  double2 *gwork = nullptr, *ghist = nullptr, *gacc = nullptr;  // graft sweeps
+};
+
+struct DevBuf {
+  void *ptr = nullptr;
+  size_t bytes = 0;
+};
+
+struct scft_ctx_impl;
+
+}  // namespace scft
+
+struct scft_ctx {
+  int device = 0;
+  cudaStream_t st = nullptr;
+  std::vector<scft::Instance> inst;
+  std::vector<scft::DevGeom> geoms;
+  scft::DevGeom *d_geoms = nullptr;
+  void *d_tw64 = nullptr;
+  std::vector<void *> allocs;  // every cudaMalloc of this context
+  scft::FieldInst *d_fi = nullptr;
+  scft::PropInst *d_pi = nullptr;
+  // job lists (device) and their shapes
+  scft::PlaneJob *d_pj_upd = nullptr, *d_pj_fld = nullptr, *d_pj_sm = nullptr;
+  int n_pj_upd = 0, n_pj_fld = 0, n_pj_sm = 0;
+  scft::ColJob *d_cj_upd = nullptr, *d_cj_fld = nullptr, *d_cj_sm = nullptr;
+  int n_cj_upd = 0, n_cj_fld = 0, n_cj_sm = 0;
+  scft::PropJob *d_prop_pj = nullptr;
+  scft::ColJob *d_prop_cj = nullptr;
+  std::vector<int> prop_pj_count, prop_cj_count;  // jobs active at step n (prefix counts)
+  int nmax = 0;
+  scft::PropJob *d_graft_pj = nullptr;
+  scft::ColJob *d_graft_cj = nullptr;
+  std::vector<int> graft_pj_count, graft_cj_count;
+  int ngmax = 0;
+  double2 *d_gpart = nullptr;
+  int gblocks = 0;
+  scft::LaunchShape shp_plane{}, shp_col{}, shp_prop{};
+  int eblocks = 0;  // blocks per instance for pointwise kernels
+  double2 *d_hpart = nullptr;
+  int hblocks = 0;
+  cudaGraphExec_t g_update = nullptr;
+  int update_runs = 0;
+  int dirty_density = 1;
+};

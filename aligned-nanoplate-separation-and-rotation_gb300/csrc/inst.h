@@ -1,0 +1,69 @@
+// inst.h -- per-instance device views used by the propagator and field kernels.
+#pragma once
+
+#include "common.h"
+
+namespace scft {
+
+// Device scalars of one instance (double2 slots).
+enum ScalarSlot {
+  kQd = 0,       // Q of the diblock (code/diblock_discrete.cpp:87)
+  kFactor = 1,   // nD / Q / V (code/calc_poly_density.cpp:176)
+  kQga = 2,      // Qga_exp (code/grafted_nanoparticle.cpp:112)
+  kQg = 3,       // graft propagator check: count of points with Re q_g[Ng-1] <= 0 in .x
+  kNumScalars = 4
+};
+
+// View of one instance for the propagator sweeps.  Propagator p = 0 is q
+// (starts at the A end), p = 1 is q-dagger (starts at the B end).
+struct PropInst {
+  int geom;
+  int N, Na;
+  int single;  // q-dagger equals q (Na == 0 or Na == N, code/diblock_discrete.cpp:60-83)
+  int hmax;    // last history slot kept: (N-1)/2
+  void *work[2];
+  void *hist[2];
+  const double2 *expw[2];  // e^{-W_A}, e^{-W_B}
+  double2 *acc[2][2];      // density accumulators [p][A or B]
+  double2 *qpart;          // [nz] plane sums of q_{N-1}
+  // grafted chains on explicit plates (code/grafted_nanoparticle.cpp:15-117)
+  int graft, Ng;
+  void *gwork;             // working array of the graft sweeps
+  void *ghist;             // q_g, all Ng steps
+  double2 *gacc;           // sum_j q_g[j] qdag_g[Ng-1-j]
+  const double2 *gexpw;    // e^{-smwg}
+  const double2 *grafts;   // normalised graft map (real space)
+};
+
+struct PropJob {
+  int inst;
+  int p;
+  int z;
+};
+
+// View of one instance for the field-level kernels.
+struct FieldInst {
+  long long M;
+  int geom;
+  double rho0, kappa, cab, cbc, cac;
+  int neg_ab, neg_bc, neg_ac;
+  double phiD, phiG, lam_pl, lam_mi, nD, V, dx[3];
+  int N, Ng, np_chem, graft, single;
+  double ng_per_np;
+  int n_exp_nr;
+  double2 *w[7];       // wpl, wabp, wabm, wbcp, wbcm, wacp, wacm
+  double2 *sm[3];      // w_A, w_B, w_G, smeared in place into smwa, smwb, smwg
+  double2 *rho[3];     // rhoda, rhodb, rhog_exp
+  double2 *expw[3];    // e^{-smwa}, e^{-smwb}, e^{-smwg}
+  const double *hhat, *gaa, *gab, *gbb, *gc, *rho_exp_nr;
+  const double2 *exp_nrH;
+  double2 *acc[2][2];
+  double2 *qpart;
+  int nz;
+  double2 *scal;       // kNumScalars device scalars
+  double2 *gacc;       // graft density accumulator
+  const double2 *ghist_last;  // q_g[Ng-1]
+  const double2 *grafts;
+};
+
+}  // namespace scft

@@ -1,0 +1,150 @@
+// kernels_fft.cu -- batched 3-D complex FFTs on per-instance grids.
+//
+// A 3-D transform is two passes over the array:
+//   plane pass : one CTA per (array, z) loads the nx*ny plane into shared
+//                memory, transforms rows (x) then columns (y), stores it;
+//   column pass: one CTA per (array, y, x-tile) loads tx*nz values, transforms
+//                along z and stores them.  With a k-space multiplier table the
+//                column pass does forward-z, multiply, inverse-z in one go, which
+//                is the whole k-space half of a convolution.
+// The reference's fft_fwd_wrapper/fft_bck_wrapper (code/fft_wrappers.cpp:4-67)
+// are forward scaled by 1/M and backward unscaled; the scale is folded into
+// the last pass of a forward transform or into the multiplier.
+#include "fft_core.cuh"
+#include "launch.h"
+
+namespace scft {
+
+template <typename T, int SIGN, int MAXV>
+__global__ void __launch_bounds__(512) k_plane_fft(const PlaneJob *__restrict__ jobs, const DevGeom *__restrict__ geoms,
+                            const cx<T> *__restrict__ twbuf, int scale_by_M) {
+  typedef cx<T> C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const PlaneJob jb = jobs[blockIdx.x];
+  const DevGeom g = geoms[jb.geom];
+  const int E = g.nx * g.ny;
+  C *plane = reinterpret_cast<C *>(smem_raw);
+  C *twx = plane + E;
+  C *twy = twx + g.nx;
+  load_tw<T>(twx, twbuf, g.ax[0]);
+  load_tw<T>(twy, twbuf, g.ax[1]);
+  C *a = reinterpret_cast<C *>(jb.ptr) + (long long)jb.z * E;
+  for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = a[e];
+  __syncthreads();
+  fft_plane<T, SIGN, MAXV>(plane, g, twx, twy);
+  if (scale_by_M) {
+    const T s = (T)(1.0 / (double)g.M);
+    for (int e = threadIdx.x; e < E; e += blockDim.x) a[e] = cscale(plane[e], s);
+  } else {
+    for (int e = threadIdx.x; e < E; e += blockDim.x) a[e] = plane[e];
+  }
+}
+
+// MODE 0: forward z (sign -1); 1: inverse z (sign +1); 2: forward, multiply by
+// kern[x,y,z] * scale, inverse.
+template <typename T, int MODE, int MAXV>
+__global__ void __launch_bounds__(512) k_col_fft(const ColJob *__restrict__ jobs, const DevGeom *__restrict__ geoms,
+                          const cx<T> *__restrict__ twbuf, int scale_by_M) {
+  typedef cx<T> C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const ColJob jb = jobs[blockIdx.x];
+  const DevGeom g = geoms[jb.geom];
+  const int tx = g.tx, nz = g.nz;
+  const int E = tx * nz;
+  C *tile = reinterpret_cast<C *>(smem_raw);
+  C *twz = tile + E;
+  load_tw<T>(twz, twbuf, g.ax[2]);
+  C *a = reinterpret_cast<C *>(jb.ptr);
+  const long long plane = (long long)g.nx * g.ny;
+  const long long base = (long long)jb.y * g.nx + jb.x0;
+  for (int e = threadIdx.x; e < E; e += blockDim.x) {
+    const int z = e / tx, x = e - z * tx;
+    tile[e] = a[z * plane + base + x];
+  }
+  __syncthreads();
+  if (MODE == 1) {
+    fft_lines<T, +1, MAXV>(tile, g.ax[2], tx, 1, tx, twz);
+  } else {
+    fft_lines<T, -1, MAXV>(tile, g.ax[2], tx, 1, tx, twz);
+  }
+  if (MODE == 2) {
+    const T *kern = reinterpret_cast<const T *>(jb.kern);
+    const T s = scale_by_M ? (T)(1.0 / (double)g.M) : (T)1;
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      const int z = e / tx, x = e - z * tx;
+      const T kv = kern[z * plane + base + x];
+      tile[e] = cscale(cscale(tile[e], s), kv);
+    }
+    __syncthreads();
+    fft_lines<T, +1, MAXV>(tile, g.ax[2], tx, 1, tx, twz);
+  }
+  const T s = (MODE == 0 && scale_by_M) ? (T)(1.0 / (double)g.M) : (T)1;
+  for (int e = threadIdx.x; e < E; e += blockDim.x) {
+    const int z = e / tx, x = e - z * tx;
+    a[z * plane + base + x] = (MODE == 0 && scale_by_M) ? cscale(tile[e], s) : tile[e];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host launchers
+// ---------------------------------------------------------------------------
+template <typename T, int SIGN, int MAXV>
+static cudaError_t launch_plane_t(const LaunchShape &ls, const PlaneJob *jobs, int njobs, const DevGeom *geoms,
+                                  const void *tw, int scale, cudaStream_t st) {
+  auto kfn = k_plane_fft<T, SIGN, MAXV>;
+  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, ls.smem);
+  if (e != cudaSuccess) return e;
+  kfn<<<njobs, ls.threads, ls.smem, st>>>(jobs, geoms, reinterpret_cast<const cx<T> *>(tw), scale);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_plane_fft(const LaunchShape &ls, const PlaneJob *jobs, int njobs, const DevGeom *geoms,
+                             const void *tw, int sign, int scale, cudaStream_t st) {
+  if (njobs <= 0) return cudaSuccess;
+  if (sign < 0) {
+    if (ls.maxv <= 8) return launch_plane_t<T, -1, 8>(ls, jobs, njobs, geoms, tw, scale, st);
+    if (ls.maxv <= 16) return launch_plane_t<T, -1, 16>(ls, jobs, njobs, geoms, tw, scale, st);
+    return launch_plane_t<T, -1, 32>(ls, jobs, njobs, geoms, tw, scale, st);
+  }
+  if (ls.maxv <= 8) return launch_plane_t<T, 1, 8>(ls, jobs, njobs, geoms, tw, scale, st);
+  if (ls.maxv <= 16) return launch_plane_t<T, 1, 16>(ls, jobs, njobs, geoms, tw, scale, st);
+  return launch_plane_t<T, 1, 32>(ls, jobs, njobs, geoms, tw, scale, st);
+}
+
+template <typename T, int MODE, int MAXV>
+static cudaError_t launch_col_t(const LaunchShape &ls, const ColJob *jobs, int njobs, const DevGeom *geoms,
+                                const void *tw, int scale, cudaStream_t st) {
+  auto kfn = k_col_fft<T, MODE, MAXV>;
+  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, ls.smem);
+  if (e != cudaSuccess) return e;
+  kfn<<<njobs, ls.threads, ls.smem, st>>>(jobs, geoms, reinterpret_cast<const cx<T> *>(tw), scale);
+  return cudaGetLastError();
+}
+
+template <typename T>
+cudaError_t launch_col_fft(const LaunchShape &ls, const ColJob *jobs, int njobs, const DevGeom *geoms,
+                           const void *tw, int mode, int scale, cudaStream_t st) {
+  if (njobs <= 0) return cudaSuccess;
+#define SCFT_COL(MODE)                                                                          \
+  do {                                                                                          \
+    if (ls.maxv <= 8) return launch_col_t<T, MODE, 8>(ls, jobs, njobs, geoms, tw, scale, st);   \
+    if (ls.maxv <= 16) return launch_col_t<T, MODE, 16>(ls, jobs, njobs, geoms, tw, scale, st); \
+    return launch_col_t<T, MODE, 32>(ls, jobs, njobs, geoms, tw, scale, st);                    \
+  } while (0)
+  if (mode == 0) SCFT_COL(0);
+  if (mode == 1) SCFT_COL(1);
+  SCFT_COL(2);
+#undef SCFT_COL
+}
+
+template cudaError_t launch_plane_fft<double>(const LaunchShape &, const PlaneJob *, int, const DevGeom *,
+                                              const void *, int, int, cudaStream_t);
+template cudaError_t launch_plane_fft<float>(const LaunchShape &, const PlaneJob *, int, const DevGeom *,
+                                             const void *, int, int, cudaStream_t);
+template cudaError_t launch_col_fft<double>(const LaunchShape &, const ColJob *, int, const DevGeom *,
+                                            const void *, int, int, cudaStream_t);
+template cudaError_t launch_col_fft<float>(const LaunchShape &, const ColJob *, int, const DevGeom *,
+                                           const void *, int, int, cudaStream_t);
+
+}  // namespace scft

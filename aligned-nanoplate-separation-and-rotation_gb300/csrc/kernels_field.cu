@@ -1,0 +1,390 @@
+// kernels_field.cu -- pointwise and reduction kernels of the plain FP64 method.
+//
+// All kernels take an array of FieldInst views and a 2-D grid: blockIdx.y is
+// the instance, blockIdx.x strides over its M grid points.  Complex
+// arithmetic follows the reference's std::complex<double> expressions term by
+// term; where the reference divides by a complex number whose imaginary part
+// is exactly zero (the 1S denominators), the division is done per component,
+// which is what the complex division reduces to in that case.
+#include "fft_core.cuh"
+#include "inst.h"
+#include "launch.h"
+#include "prop_launch.h"
+
+namespace scft {
+
+__device__ __forceinline__ double2 cexp_d(double2 z) {
+  double s, c;
+  sincos(z.y, &s, &c);
+  const double e = exp(z.x);
+  return make_double2(e * c, e * s);
+}
+
+// Smith's algorithm for a / b.
+__device__ __host__ __forceinline__ double2 cdiv_d(double2 a, double2 b) {
+  if (fabs(b.x) < fabs(b.y)) {
+    const double r = b.x / b.y, d = b.x * r + b.y;
+    return make_double2((a.x * r + a.y) / d, (a.y * r - a.x) / d);
+  }
+  const double r = b.y / b.x, d = b.y * r + b.x;
+  return make_double2((a.y * r + a.x) / d, (a.y - a.x * r) / d);
+}
+
+#define FOR_POINTS(FI)                                                              \
+  const FieldInst &FI = fi[blockIdx.y];                                             \
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < FI.M; \
+       i += (long long)gridDim.x * blockDim.x)
+
+// code/calc_poly_density.cpp:42-54
+__global__ void k_assemble(const FieldInst *__restrict__ fi) {
+  FOR_POINTS(F) {
+    const double2 pl = F.w[0][i], abp = F.w[1][i], abm = F.w[2][i];
+    const double2 bcp = F.w[3][i], bcm = F.w[4][i], acp = F.w[5][i], acm = F.w[6][i];
+    // I*x = (-x.y, x.x)
+    const double2 Ipl = make_double2(-pl.y, pl.x);
+    double2 ab_a, ab_b, ac_a, bc_b, ac_g, bc_g;
+    if (F.neg_ab) {  // I*wabm - wabp ; -I*wabm - wabp
+      ab_a = make_double2(-abm.y - abp.x, abm.x - abp.y);
+      ab_b = make_double2(abm.y - abp.x, -abm.x - abp.y);
+    } else {  // I*wabp - wabm ; I*wabp + wabm
+      ab_a = make_double2(-abp.y - abm.x, abp.x - abm.y);
+      ab_b = make_double2(-abp.y + abm.x, abp.x + abm.y);
+    }
+    if (F.neg_ac) {  // I*wacm - wacp ; -I*wacm - wacp
+      ac_a = make_double2(-acm.y - acp.x, acm.x - acp.y);
+      ac_g = make_double2(acm.y - acp.x, -acm.x - acp.y);
+    } else {  // I*wacp - wacm ; I*wacp + wacm
+      ac_a = make_double2(-acp.y - acm.x, acp.x - acm.y);
+      ac_g = make_double2(-acp.y + acm.x, acp.x + acm.y);
+    }
+    if (F.neg_bc) {  // I*wbcm - wbcp ; -I*wbcm - wbcp
+      bc_b = make_double2(-bcm.y - bcp.x, bcm.x - bcp.y);
+      bc_g = make_double2(bcm.y - bcp.x, -bcm.x - bcp.y);
+    } else {  // I*wbcp - wbcm ; I*wbcp + wbcm
+      bc_b = make_double2(-bcp.y - bcm.x, bcp.x - bcm.y);
+      bc_g = make_double2(-bcp.y + bcm.x, bcp.x + bcm.y);
+    }
+    F.sm[0][i] = cadd(cadd(Ipl, ab_a), ac_a);
+    F.sm[1][i] = cadd(cadd(Ipl, ab_b), bc_b);
+    if (F.graft) F.sm[2][i] = cadd(cadd(Ipl, ac_g), bc_g);
+  }
+}
+
+// e^{-smw} for the propagators (code/diblock_discrete.cpp:21-28,54,79).
+__global__ void k_boltzmann(const FieldInst *__restrict__ fi) {
+  FOR_POINTS(F) {
+    const int nf = F.graft ? 3 : 2;
+    for (int f = 0; f < nf; f++) {
+      const double2 s = F.sm[f][i];
+      F.expw[f][i] = cexp_d(make_double2(-s.x, -s.y));
+    }
+  }
+}
+
+// Q = integ_trapPBC(q[N-1]) / V and factor = nD / Q / V, one thread per instance.
+__global__ void k_q_finalize(const FieldInst *__restrict__ fi, int ninst) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ninst) return;
+  const FieldInst &F = fi[t];
+  double2 s = make_double2(0.0, 0.0);
+  for (int z = 0; z < F.nz; z++) s = cadd(s, F.qpart[z]);
+  for (int d = 0; d < 3; d++) s = make_double2(s.x * F.dx[d], s.y * F.dx[d]);
+  const double2 Q = make_double2(s.x / F.V, s.y / F.V);
+  double2 f = cdiv_d(make_double2(F.nD, 0.0), Q);
+  f = make_double2(f.x / F.V, f.y / F.V);
+  F.scal[kQd] = Q;
+  F.scal[kFactor] = f;
+}
+
+// code/calc_poly_density.cpp:187-188: rho *= exp(w) * factor
+__global__ void k_density(const FieldInst *__restrict__ fi) {
+  FOR_POINTS(F) {
+    const double2 fac = F.scal[kFactor];
+    double2 a = F.acc[0][0][i], b = F.acc[0][1][i];
+    if (!F.single) {
+      a = cadd(a, F.acc[1][0][i]);
+      b = cadd(b, F.acc[1][1][i]);
+    }
+    F.rho[0][i] = cmul(a, cmul(cexp_d(F.sm[0][i]), fac));
+    F.rho[1][i] = cmul(b, cmul(cexp_d(F.sm[1][i]), fac));
+  }
+}
+
+__device__ __forceinline__ double2 clog_d(double2 z) {
+  return make_double2(log(hypot(z.x, z.y)), atan2(z.y, z.x));
+}
+
+// Graft density and the Qga integrand (code/grafted_nanoparticle.cpp:100-117):
+//   rhog = acc * (ng_per_np * n_exp * exp(+smwg)),
+//   tmp  = Re(grafts) <= 0 ? 0 : grafts * log(q_g[Ng-1]).
+// part[(inst*gridDim.x + blk)*2 + {0,1}] = (sum of tmp, (count of Re q <= 0, 0)).
+__global__ void k_graft_finalize(const FieldInst *__restrict__ fi, double2 *__restrict__ part) {
+  __shared__ double2 red[32];
+  __shared__ double redc[32];
+  const FieldInst &F = fi[blockIdx.y];
+  if (!F.graft) return;
+  const double s = F.ng_per_np * F.n_exp_nr;
+  double2 acc = make_double2(0.0, 0.0);
+  double cnt = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < F.M;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double2 e = cexp_d(F.sm[2][i]);
+    F.rho[2][i] = cmul(F.gacc[i], make_double2(s * e.x, s * e.y));
+    const double2 gr = F.grafts[i];
+    const double2 ql = F.ghist_last[i];
+    if (gr.x > 0.0) acc = cadd(acc, cmul(gr, clog_d(ql)));
+    if (ql.x <= 0.0) cnt += 1.0;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+    acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+    cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { red[w] = acc; redc[w] = cnt; }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    acc = l < nw ? red[l] : make_double2(0.0, 0.0);
+    cnt = l < nw ? redc[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+      cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    }
+    if (l == 0) {
+      const long long b = (long long)blockIdx.y * gridDim.x + blockIdx.x;
+      part[2 * b] = acc;
+      part[2 * b + 1] = make_double2(cnt, 0.0);
+    }
+  }
+}
+
+// Qga = integ_trapPBC(tmp) (code/grafted_nanoparticle.cpp:112), one thread per instance.
+__global__ void k_qga_finalize(const FieldInst *__restrict__ fi, int ninst, int blocks,
+                               const double2 *__restrict__ part) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ninst) return;
+  const FieldInst &F = fi[t];
+  if (!F.graft) return;
+  double2 s = make_double2(0.0, 0.0);
+  double cnt = 0.0;
+  for (int b = 0; b < blocks; b++) {
+    s = cadd(s, part[2 * ((long long)t * blocks + b)]);
+    cnt += part[2 * ((long long)t * blocks + b) + 1].x;
+  }
+  for (int d = 0; d < 3; d++) s = make_double2(s.x * F.dx[d], s.y * F.dx[d]);
+  F.scal[kQga] = s;
+  F.scal[kQg] = make_double2(cnt, 0.0);
+}
+
+// code/1s_update.cpp:58-329, k-space (mean-field: no noise, no film/channel,
+// no field nanoparticles, no homopolymer).  Arrays are the forward transforms
+// (1/M scaled) of the densities and fields.
+__global__ void k_update_1s(const FieldInst *__restrict__ fi) {
+  FOR_POINTS(F) {
+    const double rho0 = F.rho0, N = (double)F.N, Ng = (double)F.Ng;
+    const double li = F.lam_pl, lr = F.lam_mi;
+    const double hh = F.hhat[i];
+    const double hh2 = hh * hh;
+    const double gaa = F.gaa[i], gab = F.gab[i], gbb = F.gbb[i], gc = F.gc[i];
+    const double2 ra = F.rho[0][i], rb = F.rho[1][i];
+    const double2 rg = F.graft ? F.rho[2][i] : make_double2(0.0, 0.0);
+    const double2 enh = F.exp_nrH[i];
+    // w+  (:58-84)
+    {
+      const double evar = (i == 0) ? 1.0 : 0.0;
+      const double2 s = cadd(cadd(ra, rg), rb);  // rhoha + rhoda + rhog + rhog_exp + rhodb
+      // I*rho0*(exp_nrH - evar) + I*hhat*s
+      const double2 u = make_double2(enh.x - evar, enh.y);
+      const double2 F1 = make_double2(-rho0 * u.y - hh * s.y, rho0 * u.x + hh * s.x);
+      const double A = rho0 / F.kappa + F.phiD * rho0 * N * hh2 * (gaa + 2.0 * gab + gbb) +
+                       (F.phiG * Ng * gc) * rho0 * hh2;
+      const double B = A - rho0 / F.kappa;
+      const double2 w = F.w[0][i];
+      const double2 num = make_double2(w.x - li * (F1.x - B * w.x), w.y - li * (F1.y - B * w.y));
+      const double den = 1.0 + li * A;
+      F.w[0][i] = make_double2(num.x / den, num.y / den);
+    }
+    // AB (:87-166)
+    if (F.cab != 0.0) {
+      const double c = F.cab;
+      double2 wp = F.w[1][i], wm = F.w[2][i];
+      if (!F.neg_ab) {
+        double2 F1 = make_double2(-hh * (ra.y + rb.y), hh * (ra.x + rb.x));  // I*hhat*(ra+rb)
+        if (F.np_chem == 1) F1 = make_double2(F1.x - rho0 * enh.x, F1.y - rho0 * enh.y);
+        const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * (gaa + 2.0 * gab + gbb);
+        const double B = A - 2.0 * rho0 / c;
+        const double den = 1.0 + li * A;
+        wp = make_double2((wp.x - li * (F1.x - B * wp.x)) / den, (wp.y - li * (F1.y - B * wp.y)) / den);
+        double2 F2 = make_double2(hh * (rb.x - ra.x), hh * (rb.y - ra.y));
+        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
+        const double den2 = 1.0 + lr * 2.0 * rho0 / c;
+        wm = make_double2((wm.x - lr * F2.x) / den2, (wm.y - lr * F2.y) / den2);
+      } else {
+        const double2 F1 = make_double2(-hh * (ra.x + rb.x), -hh * (ra.y + rb.y));
+        const double den1 = 1.0 + lr * 2.0 * rho0 / c;
+        wp = make_double2((wp.x - lr * F1.x) / den1, (wp.y - lr * F1.y) / den1);
+        double2 F2 = make_double2(-hh * (ra.y - rb.y), hh * (ra.x - rb.x));  // I*hhat*(ra-rb)
+        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
+        const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * (gaa - gbb);
+        const double B = A - 2.0 * rho0 / c;
+        const double den = 1.0 + li * A;
+        wm = make_double2((wm.x - li * (F2.x - B * wm.x)) / den, (wm.y - li * (F2.y - B * wm.y)) / den);
+      }
+      F.w[1][i] = wp;
+      F.w[2][i] = wm;
+    } else {
+      F.w[1][i] = make_double2(0.0, 0.0);
+      F.w[2][i] = make_double2(0.0, 0.0);
+    }
+    // BC (:168-247)
+    if (F.cbc != 0.0) {
+      const double c = F.cbc;
+      double2 wp = F.w[3][i], wm = F.w[4][i];
+      if (!F.neg_bc) {
+        const double2 F1 = make_double2(-hh * (rg.y + rb.y), hh * (rg.x + rb.x));
+        const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * (+gbb) + F.phiG * rho0 * Ng * hh2 * gc;
+        const double B = A - 2.0 * rho0 / c;
+        const double den = 1.0 + li * A;
+        wp = make_double2((wp.x - li * (F1.x - B * wp.x)) / den, (wp.y - li * (F1.y - B * wp.y)) / den);
+        double2 F2 = make_double2(hh * (rg.x - rb.x), hh * (rg.y - rb.y));
+        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
+        const double den2 = 1.0 + lr * 2.0 * rho0 / c;
+        wm = make_double2((wm.x - lr * F2.x) / den2, (wm.y - lr * F2.y) / den2);
+      } else {
+        const double2 F1 = make_double2(-hh * (rb.x + rg.x), -hh * (rb.y + rg.y));
+        const double den1 = 1.0 + lr * 2.0 * rho0 / c;
+        wp = make_double2((wp.x - lr * F1.x) / den1, (wp.y - lr * F1.y) / den1);
+        // -I*hhat*(rg - rb) = (hh*(rg-rb).y, -hh*(rg-rb).x)
+        double2 F2 = make_double2(hh * (rg.y - rb.y), -hh * (rg.x - rb.x));
+        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
+        const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * gbb - F.phiG * Ng * hh2 * rho0 * gc;
+        const double B = A - 2.0 * rho0 / c;
+        const double den = 1.0 + li * A;
+        wm = make_double2((wm.x - li * (F2.x - B * wm.x)) / den, (wm.y - li * (F2.y - B * wm.y)) / den);
+      }
+      F.w[3][i] = wp;
+      F.w[4][i] = wm;
+    } else {
+      F.w[3][i] = make_double2(0.0, 0.0);
+      F.w[4][i] = make_double2(0.0, 0.0);
+    }
+    // AC (:250-329)
+    if (F.cac != 0.0) {
+      const double c = F.cac;
+      double2 wp = F.w[5][i], wm = F.w[6][i];
+      if (!F.neg_ac) {
+        const double2 F1 = make_double2(-hh * (rg.y + ra.y), hh * (rg.x + ra.x));
+        const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * gaa + F.phiG * Ng * hh2 * rho0 * gc;
+        const double B = A - 2.0 * rho0 / c;
+        const double den = 1.0 + li * A;
+        wp = make_double2((wp.x - li * (F1.x - B * wp.x)) / den, (wp.y - li * (F1.y - B * wp.y)) / den);
+        double2 F2 = make_double2(hh * (rg.x - ra.x), hh * (rg.y - ra.y));
+        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
+        const double den2 = 1.0 + lr * 2.0 * rho0 / c;
+        wm = make_double2((wm.x - lr * F2.x) / den2, (wm.y - lr * F2.y) / den2);
+      } else {
+        const double2 F1 = make_double2(-hh * (ra.x + rg.x), -hh * (ra.y + rg.y));
+        const double den1 = 1.0 + lr * 2.0 * rho0 / c;
+        wp = make_double2((wp.x - lr * F1.x) / den1, (wp.y - lr * F1.y) / den1);
+        double2 F2 = make_double2(hh * (rg.y - ra.y), -hh * (rg.x - ra.x));
+        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
+        const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * gaa - F.phiG * Ng * hh2 * rho0 * gc;
+        const double B = A - 2.0 * rho0 / c;
+        const double den = 1.0 + li * A;
+        wm = make_double2((wm.x - li * (F2.x - B * wm.x)) / den, (wm.y - li * (F2.y - B * wm.y)) / den);
+      }
+      F.w[5][i] = wp;
+      F.w[6][i] = wm;
+    } else {
+      F.w[5][i] = make_double2(0.0, 0.0);
+      F.w[6][i] = make_double2(0.0, 0.0);
+    }
+  }
+}
+
+// Partial sums for calc_H (code/calc_h.cpp:66-132).  out[(inst*4 + part)*nblk + blk],
+// part 0: wpl^2 rho0/kappa/2 - I rho0 (1 - rho_exp_nr) wpl; parts 1-3: (w+^2 + w-^2)
+// rho0/chi (+-1) for the BC, AC and AB pairs.
+__global__ void k_h_partials(const FieldInst *__restrict__ fi, double2 *__restrict__ out) {
+  __shared__ double2 red[32];
+  const FieldInst &F = fi[blockIdx.y];
+  double2 s[4];
+  for (int k = 0; k < 4; k++) s[k] = make_double2(0.0, 0.0);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < F.M;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double2 w = F.w[0][i];
+    const double2 w2 = cmul(w, w);
+    const double2 t1 = make_double2(w2.x * F.rho0 / F.kappa / 2.0, w2.y * F.rho0 / F.kappa / 2.0);
+    const double c = F.rho0 * (1.0 - 0.0 - F.rho_exp_nr[i]);
+    // I*c*w = (-c*w.y, c*w.x)
+    s[0] = cadd(s[0], make_double2(t1.x + c * w.y, t1.y - c * w.x));
+    const double chis[3] = {F.cbc, F.cac, F.cab};
+    const int negs[3] = {F.neg_bc, F.neg_ac, F.neg_ab};
+    const int idx[3] = {3, 5, 1};
+    for (int k = 0; k < 3; k++) {
+      if (chis[k] == 0.0) continue;
+      const double2 p = F.w[idx[k]][i], m = F.w[idx[k] + 1][i];
+      const double2 q = cadd(cmul(p, p), cmul(m, m));
+      const double f = F.rho0 / chis[k] * (negs[k] ? -1.0 : 1.0);
+      s[k + 1] = cadd(s[k + 1], make_double2(q.x * f, q.y * f));
+    }
+  }
+  for (int k = 0; k < 4; k++) {
+    double2 v = s[k];
+    for (int o = 16; o > 0; o >>= 1) {
+      v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+      v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+      const int nw = (blockDim.x + 31) >> 5;
+      v = l < nw ? red[l] : make_double2(0.0, 0.0);
+      for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+      }
+      if (l == 0) out[((long long)blockIdx.y * 4 + k) * gridDim.x + blockIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+cudaError_t launch_assemble(const FieldInst *fi, int ninst, int blocks, cudaStream_t st) {
+  k_assemble<<<dim3(blocks, ninst), 256, 0, st>>>(fi);
+  return cudaGetLastError();
+}
+cudaError_t launch_boltzmann(const FieldInst *fi, int ninst, int blocks, cudaStream_t st) {
+  k_boltzmann<<<dim3(blocks, ninst), 256, 0, st>>>(fi);
+  return cudaGetLastError();
+}
+cudaError_t launch_q_finalize(const FieldInst *fi, int ninst, cudaStream_t st) {
+  k_q_finalize<<<(ninst + 63) / 64, 64, 0, st>>>(fi, ninst);
+  return cudaGetLastError();
+}
+cudaError_t launch_density(const FieldInst *fi, int ninst, int blocks, cudaStream_t st) {
+  k_density<<<dim3(blocks, ninst), 256, 0, st>>>(fi);
+  return cudaGetLastError();
+}
+cudaError_t launch_update_1s(const FieldInst *fi, int ninst, int blocks, cudaStream_t st) {
+  k_update_1s<<<dim3(blocks, ninst), 256, 0, st>>>(fi);
+  return cudaGetLastError();
+}
+cudaError_t launch_graft_finalize(const FieldInst *fi, int ninst, int blocks, double2 *part, cudaStream_t st) {
+  k_graft_finalize<<<dim3(blocks, ninst), 256, 0, st>>>(fi, part);
+  return cudaGetLastError();
+}
+cudaError_t launch_qga_finalize(const FieldInst *fi, int ninst, int blocks, const double2 *part, cudaStream_t st) {
+  k_qga_finalize<<<(ninst + 63) / 64, 64, 0, st>>>(fi, ninst, blocks, part);
+  return cudaGetLastError();
+}
+cudaError_t launch_h_partials(const FieldInst *fi, int ninst, int blocks, double2 *out, cudaStream_t st) {
+  k_h_partials<<<dim3(blocks, ninst), 256, 0, st>>>(fi, out);
+  return cudaGetLastError();
+}
+
+}  // namespace scft

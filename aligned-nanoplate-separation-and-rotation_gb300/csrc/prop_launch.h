@@ -1,0 +1,24 @@
+// prop_launch.h -- launchers of the propagator and field kernels.
+#pragma once
+
+#include "inst.h"
+#include "launch.h"
+
+namespace scft {
+
+cudaError_t launch_prop_plane_f64(const LaunchShape &ls, const PropJob *jobs, int njobs, const PropInst *insts,
+                                  const DevGeom *geoms, const void *tw, int n, cudaStream_t st);
+
+cudaError_t launch_graft_plane_f64(const LaunchShape &ls, const PropJob *jobs, int njobs, const PropInst *insts,
+                                   const DevGeom *geoms, const void *tw, int sweep, int n, cudaStream_t st);
+cudaError_t launch_graft_finalize(const FieldInst *fi, int ninst, int blocks, double2 *part, cudaStream_t st);
+cudaError_t launch_qga_finalize(const FieldInst *fi, int ninst, int blocks, const double2 *part, cudaStream_t st);
+
+cudaError_t launch_assemble(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
+cudaError_t launch_boltzmann(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
+cudaError_t launch_q_finalize(const FieldInst *fi, int ninst, cudaStream_t st);
+cudaError_t launch_density(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
+cudaError_t launch_update_1s(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
+cudaError_t launch_h_partials(const FieldInst *fi, int ninst, int blocks, double2 *out, cudaStream_t st);
+
+}  // namespace scft

@@ -1,0 +1,152 @@
+/*
+ * scft.h -- C ABI of libscft, the GB300 (sm_103a) implementation of the SCFT
+ * hot path of the aligned-nanoplate code (AB diblock melt + explicit plates
+ * with grafted chains, discrete Gaussian chains, semi-implicit "1S" update).
+ *
+ * The reference has no plugin or FFI layer: its hot path is a set of C++ free
+ * functions on global state.  Each entry point below names the reference
+ * function it replaces (file:line inside the reference project):
+ *
+ *   scft_create            read_input() + initialize_1() + allocate() +
+ *                          initialize_2()   code/read_input.cpp:7-242,
+ *                          code/initialize.cpp:45-412, code/array_utils.cpp:336-547
+ *   scft_set_fields        read_resume_files() code/io_utils.cpp:183-240
+ *   scft_calc_poly_density calc_poly_density() code/calc_poly_density.cpp:37-161
+ *   scft_update_1s         update_1s()         code/1s_update.cpp:7-352
+ *   scft_calc_H            calc_H()            code/calc_h.cpp:9-64
+ *   scft_get_density       the rhoda/rhodb/rhog_exp globals after
+ *                          calc_poly_density   code/calc_poly_density.cpp:167-191
+ *   scft_diblock_density   diblock_discrete() + integrate_diblock_discrete()
+ *                          code/diblock_discrete.cpp:4-95,
+ *                          code/calc_poly_density.cpp:167-191
+ *   scft_homopolymer_density homopolymer_discrete() +
+ *                          integrate_homopoly_discrete()
+ *                          code/homopolymer_discrete.cpp:3-55,
+ *                          code/calc_poly_density.cpp:193-212
+ *   scft_fft3d             fft_fwd_wrapper()/fft_bck_wrapper()
+ *                          code/fft_wrappers.cpp:4-67
+ *
+ * Conventions (same as the reference):
+ *  - grids are 3-D, stack order index = x + Nx*(y + Ny*z);
+ *  - complex arrays are interleaved (re, im) doubles, M = Nx*Ny*Nz entries;
+ *  - forward FFT is scaled by 1/M, backward is unscaled;
+ *  - b-units (bond length 1), Rg^2 = (N-1)/6;
+ *  - the seven fields are ordered wpl, wabp, wabm, wbcp, wbcm, wacp, wacm.
+ *
+ * Ownership: the context owns all device memory; host buffers passed in are
+ * copied and may be reused on return.  Calls on one context must come from
+ * one host thread.  Every call returns SCFT_OK (0) or a negative error code;
+ * scft_last_error() gives a message for the calling thread.
+ */
+#ifndef SCFT_H
+#define SCFT_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SCFT_OK 0
+#define SCFT_ERR_ARG (-1)         /* bad argument or configuration */
+#define SCFT_ERR_CUDA (-2)        /* CUDA runtime error */
+#define SCFT_ERR_NAN (-3)         /* H is NaN (code/calc_h.cpp:37-61 exits) */
+#define SCFT_ERR_QNONPOS (-4)     /* graft q <= 0 (code/grafted_nanoparticle.cpp:87-107 exits) */
+#define SCFT_ERR_UNSUPPORTED (-5) /* feature or grid size not built */
+#define SCFT_ERR_NOMEM (-6)       /* device allocation failed */
+#define SCFT_ERR_COMPLEX (-7)     /* mixed precision needs real-valued (mean-field) w_A, w_B */
+
+/* Precision modes. */
+#define SCFT_PREC_FP64 0  /* plain method: complex FP64 throughout, as the reference */
+#define SCFT_PREC_MIXED 1 /* FP32 propagators/FFTs, FP64 fields, reductions, log Q, H */
+
+/* Plate shapes. */
+#define SCFT_PLATE_REFERENCE 0 /* 0.25 erfc((|u.r|-L/2)/xi) erfc((|u x r|-R)/xi), code/initialize.cpp:578-612 */
+#define SCFT_PLATE_CUBOID 1    /* product of three erfc slabs (extension, no reference counterpart) */
+
+/* One SCFT instance.  Field names and meanings follow bcp.input
+ * (code/read_input.cpp:30-236); negative chi selects the attractive branch. */
+typedef struct scft_params {
+  int Nda, Ndb;        /* beads in the A and B blocks */
+  double a_smear;      /* Gaussian smearing length a */
+  double rho0;         /* bulk segment density */
+  double chi_ab, chi_bc, chi_ac; /* signed, per segment */
+  double kappa;        /* compressibility; must be > 0 */
+  int Nx[3];           /* grid points (each a product of 2s, 3s and 5s, >= 2) */
+  double L[3];         /* box lengths */
+  double lam_pl, lam_mi; /* 1S step sizes for the + and - fields */
+  int n_exp_nr;        /* explicit plates: 0, 1 or 2 */
+  int np_chem;         /* 0 neutral, 1 A-like (code/1s_update.cpp:103-104) */
+  double sigma;        /* graft density (chains per b^2); 0 = bare */
+  int Ng;              /* beads per grafted chain */
+  double L_nr, R_nr, xi_nr; /* plate thickness, radius, interface width */
+  double center[2][3]; /* plate centres, fractions of L */
+  double orient[2][3]; /* plate axes (normalised on input, as the reference) */
+  int precision;       /* SCFT_PREC_FP64 or SCFT_PREC_MIXED */
+  int plate_shape;     /* SCFT_PLATE_REFERENCE or SCFT_PLATE_CUBOID */
+  double shell_lambda; /* extension: A-attractive shell potential added to w_A */
+  double shell_width;  /* width of that shell; ignored when shell_lambda == 0 */
+} scft_params;
+
+/* Derived per-instance quantities (code/initialize.cpp:249-386). */
+typedef struct scft_info {
+  long M;
+  double V, Vf, nD, phiD, phiG, np_frac, nP, ng_per_np;
+  int N;
+  double dx[3];
+} scft_info;
+
+typedef struct scft_ctx scft_ctx;
+
+const char *scft_last_error(void);
+int scft_version(void);
+
+/* Creates n_inst instances (sizes may differ) on the current CUDA device.
+ * Fields start at zero. */
+int scft_create(const scft_params *params, int n_inst, scft_ctx **out);
+void scft_destroy(scft_ctx *ctx);
+
+int scft_get_info(scft_ctx *ctx, int inst, scft_info *info);
+
+/* Sets/gets the seven fields of one instance: w[f*2*M + 2*i + {0,1}]. */
+int scft_set_fields(scft_ctx *ctx, int inst, const double *w);
+int scft_get_fields(scft_ctx *ctx, int inst, double *w);
+
+/* calc_poly_density() for every instance. */
+int scft_calc_poly_density(scft_ctx *ctx);
+
+/* n_iter x update_1s() for every instance (each ends with calc_poly_density). */
+int scft_update_1s(scft_ctx *ctx, int n_iter);
+
+/* calc_H() per instance.  out[5*inst + {0..4}] = Re H, Im H, Re Qd, Im Qd,
+ * Re Qga (Qga = 0 without grafted plates). */
+int scft_calc_H(scft_ctx *ctx, double *out);
+
+/* Densities of one instance after calc_poly_density (real space):
+ * rhoda, rhodb, rhog_exp (any may be NULL). */
+int scft_get_density(scft_ctx *ctx, int inst, double *rhoda, double *rhodb, double *rhog_exp);
+
+/* Smeared fields of one instance (smwa, smwb, smwg; any may be NULL). */
+int scft_get_smeared(scft_ctx *ctx, int inst, double *smwa, double *smwb, double *smwg);
+
+/* diblock_discrete + integrate_diblock_discrete on given smeared fields of
+ * instance `inst` (its grid, N, Nda, nD); writes rhoda, rhodb and Q[2]. */
+int scft_diblock_density(scft_ctx *ctx, int inst, const double *smwa, const double *smwb,
+                         double *rhoda, double *rhodb, double *Q);
+
+/* homopolymer_discrete(W, N) + integrate_homopoly_discrete with nK. */
+int scft_homopolymer_density(scft_ctx *ctx, int inst, const double *W, int N, double nK,
+                             double *rho, double *Q);
+
+/* 3-D FFT of `count` arrays of instance inst's grid (host buffers, in place):
+ * sign -1 forward (scaled 1/M), +1 backward (unscaled). */
+int scft_fft3d(scft_ctx *ctx, int inst, double *data, int count, int sign);
+
+/* Synchronises the context's stream; returns the first asynchronous error. */
+int scft_sync(scft_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SCFT_H */
