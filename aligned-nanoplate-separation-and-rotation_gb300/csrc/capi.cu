@@ -21,6 +21,8 @@ void ctx_fft3d(scft_ctx *c, int k, double *data, int count, int sign);
 void ctx_diblock_density(scft_ctx *c, int k, const double *smwa, const double *smwb, double *ra, double *rb,
                          double *Q);
 void ctx_override_nD(scft_ctx *c, int k, double nD);
+void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
+                      double *bytes_col);
 int error_code(const std::exception &e);
 }  // namespace scft
 
@@ -181,6 +183,26 @@ int scft_sync(scft_ctx *c) {
   if (!c) return fail(SCFT_ERR_ARG, "null context");
   cudaError_t e = cudaStreamSynchronize(c->st);
   if (e != cudaSuccess) return fail(SCFT_ERR_CUDA, cudaGetErrorString(e));
+  return SCFT_OK;
+}
+
+int scft_get_stream(scft_ctx *c, void **stream) {
+  if (!c || !stream) return fail(SCFT_ERR_ARG, "null argument");
+  *stream = (void *)c->st;
+  return SCFT_OK;
+}
+
+int scft_launch_count(scft_ctx *c, long long *count) {
+  if (!c || !count) return fail(SCFT_ERR_ARG, "null argument");
+  *count = c->launches;
+  return SCFT_OK;
+}
+
+int scft_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
+                      double *bytes_col) {
+  if (int s = check_ctx(c, 0)) return s;
+  if (reps < 1 || !ms_plane || !bytes_plane || !ms_col || !bytes_col) return fail(SCFT_ERR_ARG, "bad arguments");
+  API_BODY(scft::ctx_profile_step(c, reps, ms_plane, bytes_plane, ms_col, bytes_col));
   return SCFT_OK;
 }
 

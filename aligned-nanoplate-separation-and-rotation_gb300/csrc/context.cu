@@ -705,44 +705,51 @@ void build_jobs(scft_ctx *c) {
   c->d_hpart = dalloc<double2>(c, (size_t)n * 4 * c->hblocks);
 }
 
+// CK plus one kernel launch on the context's counter
+#define LK(x)        \
+  do {               \
+    CK(x);           \
+    c->launches++;   \
+  } while (0)
+
 // calc_poly_density for every instance (code/calc_poly_density.cpp:37-161)
 void seq_poly_density(scft_ctx *c) {
   const int n = (int)c->inst.size();
   cudaStream_t st = c->st;
-  CK(launch_assemble(c->d_fi, n, c->eblocks, st));
+  LK(launch_assemble(c->d_fi, n, c->eblocks, st));
   // smearing: smw = IFFT[ hhat * FFT[w] / M ]  (code/calc_poly_density.cpp:93-104)
-  CK(launch_plane_fft<double>(c->shp_plane, c->d_pj_sm, c->n_pj_sm, c->d_geoms, c->d_tw64, -1, 0, st));
-  CK(launch_col_fft<double>(c->shp_col, c->d_cj_sm, c->n_cj_sm, c->d_geoms, c->d_tw64, 2, 1, st));
-  CK(launch_plane_fft<double>(c->shp_plane, c->d_pj_sm, c->n_pj_sm, c->d_geoms, c->d_tw64, +1, 0, st));
-  CK(launch_boltzmann(c->d_fi, n, c->eblocks, st));
+  LK(launch_plane_fft<double>(c->shp_plane, c->d_pj_sm, c->n_pj_sm, c->d_geoms, c->d_tw64, -1, 0, st));
+  LK(launch_col_fft<double>(c->shp_col, c->d_cj_sm, c->n_cj_sm, c->d_geoms, c->d_tw64, 2, 1, st));
+  LK(launch_plane_fft<double>(c->shp_plane, c->d_pj_sm, c->n_pj_sm, c->d_geoms, c->d_tw64, +1, 0, st));
+  LK(launch_boltzmann(c->d_fi, n, c->eblocks, st));
   for (auto &I : c->inst)
     for (int q = 0; q < 2; q++)
       for (int s = 0; s < 2; s++) CK(cudaMemsetAsync(I.acc[q][s], 0, sizeof(double2) * I.M, st));
   // propagator sweep (code/diblock_discrete.cpp:18-85, code/calc_poly_density.cpp:178-190)
-  CK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[0], c->d_pi, c->d_geoms, c->d_tw64, 0, st));
+  LK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[0], c->d_pi, c->d_geoms, c->d_tw64, 0, st));
   for (int s = 1; s < c->nmax; s++) {
-    CK(launch_col_fft<double>(c->shp_col, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw64, 2, 1, st));
-    CK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[s], c->d_pi, c->d_geoms, c->d_tw64, s,
+    LK(launch_col_fft<double>(c->shp_col, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw64, 2, 1, st));
+    LK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[s], c->d_pi, c->d_geoms, c->d_tw64, s,
                              st));
   }
-  CK(launch_q_finalize(c->d_fi, n, st));
-  CK(launch_density(c->d_fi, n, c->eblocks, st));
+  LK(launch_q_finalize(c->d_fi, n, st));
+  LK(launch_density(c->d_fi, n, c->eblocks, st));
   // grafted chains (code/calc_poly_density.cpp:131-133,155-159)
   if (c->ngmax > 0) {
     for (auto &I : c->inst)
       if (I.graft) CK(cudaMemsetAsync(I.gacc, 0, sizeof(double2) * I.M, st));
     for (int sweep = 0; sweep < 2; sweep++) {
-      CK(launch_graft_plane_f64(c->shp_prop, c->d_graft_pj, c->graft_pj_count[0], c->d_pi, c->d_geoms, c->d_tw64,
+      LK(launch_graft_plane_f64(c->shp_prop, c->d_graft_pj, c->graft_pj_count[0], c->d_pi, c->d_geoms, c->d_tw64,
                                 sweep, 0, st));
       for (int s = 1; s < c->ngmax; s++) {
-        CK(launch_col_fft<double>(c->shp_col, c->d_graft_cj, c->graft_cj_count[s], c->d_geoms, c->d_tw64, 2, 1,
+        LK(launch_col_fft<double>(c->shp_col, c->d_graft_cj, c->graft_cj_count[s], c->d_geoms, c->d_tw64, 2, 1,
                                   st));
-        CK(launch_graft_plane_f64(c->shp_prop, c->d_graft_pj, c->graft_pj_count[s], c->d_pi, c->d_geoms,
+        LK(launch_graft_plane_f64(c->shp_prop, c->d_graft_pj, c->graft_pj_count[s], c->d_pi, c->d_geoms,
                                   c->d_tw64, sweep, s, st));
       }
     }
-    CK(launch_graft_finalize(c->d_fi, n, c->gblocks, c->d_gpart, st));
-    CK(launch_qga_finalize(c->d_fi, n, c->gblocks, c->d_gpart, st));
+    LK(launch_graft_finalize(c->d_fi, n, c->gblocks, c->d_gpart, st));
+    LK(launch_qga_finalize(c->d_fi, n, c->gblocks, c->d_gpart, st));
   }
 }
 
@@ -750,11 +757,11 @@ void seq_poly_density(scft_ctx *c) {
 void seq_update_1s(scft_ctx *c) {
   const int n = (int)c->inst.size();
   cudaStream_t st = c->st;
-  CK(launch_plane_fft<double>(c->shp_plane, c->d_pj_upd, c->n_pj_upd, c->d_geoms, c->d_tw64, -1, 0, st));
-  CK(launch_col_fft<double>(c->shp_col, c->d_cj_upd, c->n_cj_upd, c->d_geoms, c->d_tw64, 0, 1, st));
-  CK(launch_update_1s(c->d_fi, n, c->eblocks, st));
-  CK(launch_col_fft<double>(c->shp_col, c->d_cj_fld, c->n_cj_fld, c->d_geoms, c->d_tw64, 1, 0, st));
-  CK(launch_plane_fft<double>(c->shp_plane, c->d_pj_fld, c->n_pj_fld, c->d_geoms, c->d_tw64, +1, 0, st));
+  LK(launch_plane_fft<double>(c->shp_plane, c->d_pj_upd, c->n_pj_upd, c->d_geoms, c->d_tw64, -1, 0, st));
+  LK(launch_col_fft<double>(c->shp_col, c->d_cj_upd, c->n_cj_upd, c->d_geoms, c->d_tw64, 0, 1, st));
+  LK(launch_update_1s(c->d_fi, n, c->eblocks, st));
+  LK(launch_col_fft<double>(c->shp_col, c->d_cj_fld, c->n_cj_fld, c->d_geoms, c->d_tw64, 1, 0, st));
+  LK(launch_plane_fft<double>(c->shp_plane, c->d_pj_fld, c->n_pj_fld, c->d_geoms, c->d_tw64, +1, 0, st));
   seq_poly_density(c);
 }
 
@@ -821,8 +828,11 @@ void ctx_update(scft_ctx *c, int n_iter) {
     k = 1;
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+    const long long before = c->launches;
     try {
       seq_update_1s(c);
+      c->launches_per_update = c->launches - before;
+      c->launches = before;
     } catch (...) {
       cudaGraph_t g2;
       cudaStreamEndCapture(c->st, &g2);
@@ -832,8 +842,49 @@ void ctx_update(scft_ctx *c, int n_iter) {
     CK(cudaGraphInstantiate(&c->g_update, graph, 0));
     cudaGraphDestroy(graph);
   }
-  for (; k < n_iter; k++) CK(cudaGraphLaunch(c->g_update, c->st));
+  for (; k < n_iter; k++) {
+    CK(cudaGraphLaunch(c->g_update, c->st));
+    c->launches += c->launches_per_update;
+  }
   CK(cudaStreamSynchronize(c->st));
+}
+
+// Isolated timing of the two kernels of one propagator step (plain FP64).
+void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
+                      double *bytes_col) {
+  if (c->dirty_density) ctx_poly_density(c);
+  const int s = std::max(1, 3 * (c->nmax - 1) / 4);
+  cudaEvent_t e0, e1, e2;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventCreate(&e2));
+  CK(cudaEventRecord(e0, c->st));
+  for (int r = 0; r < reps; r++)
+    LK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[s], c->d_pi, c->d_geoms, c->d_tw64, s,
+                             c->st));
+  CK(cudaEventRecord(e1, c->st));
+  for (int r = 0; r < reps; r++)
+    LK(launch_col_fft<double>(c->shp_col, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw64, 2, 1, c->st));
+  CK(cudaEventRecord(e2, c->st));
+  CK(cudaEventSynchronize(e2));
+  float a = 0.f, b = 0.f;
+  CK(cudaEventElapsedTime(&a, e0, e1));
+  CK(cudaEventElapsedTime(&b, e1, e2));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaEventDestroy(e2);
+  double bp = 0.0, bc = 0.0;
+  for (auto &I : c->inst) {
+    if (I.N <= s) continue;
+    const double props = I.single ? 1.0 : 2.0;
+    bp += props * I.M * 6.0 * sizeof(double2);
+    bc += props * I.M * (2.0 * sizeof(double2) + sizeof(double));
+  }
+  *ms_plane = a / reps;
+  *ms_col = b / reps;
+  *bytes_plane = bp;
+  *bytes_col = bc;
+  c->dirty_density = 1;
 }
 
 // calc_H (code/calc_h.cpp:9-64); out per instance: Re H, Im H, Re Qd, Im Qd, Re Qga

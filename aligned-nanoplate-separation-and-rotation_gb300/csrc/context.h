@@ -81,6 +81,8 @@ struct scft_ctx {
   double2 *d_hpart = nullptr;
   int hblocks = 0;
   cudaGraphExec_t g_update = nullptr;
+  long long launches = 0;            // kernel launches issued (graph replays included)
+  long long launches_per_update = 0;  // kernels in one captured update_1s iteration
   int update_runs = 0;
   int dirty_density = 1;
 };

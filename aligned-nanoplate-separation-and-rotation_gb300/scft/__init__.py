@@ -24,7 +24,8 @@ FIELD_NAMES = ("wpl", "wabp", "wabm", "wbcp", "wbcm", "wacp", "wacm")
 EXPORTS = ("scft_last_error", "scft_version", "scft_create", "scft_destroy", "scft_get_info",
            "scft_set_fields", "scft_get_fields", "scft_calc_poly_density", "scft_update_1s",
            "scft_calc_H", "scft_get_density", "scft_get_smeared", "scft_diblock_density",
-           "scft_homopolymer_density", "scft_fft3d", "scft_sync")
+           "scft_homopolymer_density", "scft_fft3d", "scft_sync", "scft_get_stream", "scft_launch_count",
+           "scft_profile_step")
 
 
 class ScftError(RuntimeError):
@@ -93,6 +94,9 @@ def load(path: str | None = None):
     lib.scft_homopolymer_density.argtypes = [vp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, dp, dp]
     lib.scft_fft3d.argtypes = [vp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_int]
     lib.scft_sync.argtypes = [vp]
+    lib.scft_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
+    lib.scft_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
+    lib.scft_profile_step.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
     _lib = lib
     return lib
 
@@ -242,9 +246,43 @@ class Context:
                                                _ptr(r.view(np.float64)), _ptr(Q)))
         return r, complex(Q[0], Q[1])
 
+    def stream(self) -> int:
+        h = ctypes.c_void_p()
+        _check(load().scft_get_stream(self._h, ctypes.byref(h)))
+        return h.value or 0
+
+    def launch_count(self) -> int:
+        n = ctypes.c_longlong()
+        _check(load().scft_launch_count(self._h, ctypes.byref(n)))
+        return n.value
+
+    def profile_step(self, reps=20) -> dict:
+        v = [ctypes.c_double() for _ in range(4)]
+        _check(load().scft_profile_step(self._h, int(reps), *[ctypes.byref(x) for x in v]))
+        return {"ms_plane": v[0].value, "bytes_plane": v[1].value, "ms_col": v[2].value, "bytes_col": v[3].value}
+
+    def set_fields_raw(self, inst, ptr: int):
+        """set_fields from a host buffer given by address (7*M complex, e.g. pinned memory)."""
+        _check(load().scft_set_fields(self._h, inst, ctypes.cast(ptr, ctypes.POINTER(ctypes.c_double))))
+
+    def calc_H_raw(self, ptr: int):
+        """calc_H into a host buffer given by address (5 doubles per instance)."""
+        code = load().scft_calc_H(self._h, ctypes.cast(ptr, ctypes.POINTER(ctypes.c_double)))
+        if code not in (OK, ERR_NAN):
+            _check(code)
+        return code
+
     def fft3d(self, inst, data, sign):
         sh = self._shape(inst)
         a = np.ascontiguousarray(data, np.complex128).copy()
         count = a.size // int(np.prod(sh))
         _check(load().scft_fft3d(self._h, inst, _ptr(a.view(np.float64)), count, int(sign)))
         return a
+
+
+def mixed_available() -> bool:
+    """True when the library was built with the FP32-propagator (mixed) path."""
+    try:
+        return bool(load().scft_version() >= 2)
+    except ScftError:
+        return False

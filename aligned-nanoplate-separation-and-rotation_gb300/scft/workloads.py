@@ -1,0 +1,74 @@
+"""Workload definitions: the BASELINE configurations in the reference's b-units.
+
+Conversions (code/initialize.cpp:53-55): N = Nda + Ndb beads, bond length
+b = 1, Rg^2 = (N-1)/6.  chiN is per chain, so chi = chiN/N per segment;
+C = rho0 Rg^3 / N, so rho0 = C N / Rg^3; lengths quoted in Rg are multiplied
+by Rg.  A plate is the reference's explicit particle (code/initialize.cpp:
+578-612) with axis u = plate normal, thickness L_nr along u and radius R_nr.
+
+Initial fields are seeded synthetic inputs (there is no dataset): w+ = 0 and
+w_AB^- = 0.5*chi*cos(2*pi*x/Lx) + N(0, 0.01^2) per segment, from
+numpy.random.default_rng(seed).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+from . import PREC_FP64, PREC_MIXED, make_params
+
+SWEEP_ANGLES = (0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 20, 30, 45, 90)
+
+
+def rg(N: int) -> float:
+    return math.sqrt((N - 1) / 6.0)
+
+
+def plate_params(theta_deg: float, N: int = 100, fA: float = 0.5, chiN: float = 20.0, C: float = 50.0,
+                 grid=(64, 64, 64), box_rg=(6.4, 6.4, 6.4), precision=PREC_FP64, lam_pl=0.002, lam_mi=0.0005,
+                 centers=((0.5, 0.5, 0.5),), thickness_rg=0.2, radius_rg=0.8, xi_rg=0.1, sigma=0.0, Ng=0):
+    """Config 1 geometry: plate(s) rotated by theta about z, normal along x at 0."""
+    R = rg(N)
+    Nda = int(round(fA * N))
+    th = math.radians(theta_deg)
+    u = (math.cos(th), math.sin(th), 0.0)
+    cs = list(centers) + [(0.5, 0.5, 0.5)] * (2 - len(centers))
+    return make_params(Nda=Nda, Ndb=N - Nda, a_smear=0.2, rho0=C * N / R ** 3, chi_ab=chiN / N, kappa=50.0,
+                       Nx=grid, L=tuple(b * R for b in box_rg), lam_pl=lam_pl, lam_mi=lam_mi,
+                       n_exp_nr=len(centers), L_nr=thickness_rg * R, R_nr=radius_rg * R, xi_nr=xi_rg * R,
+                       center=cs, orient=(u, u), precision=precision, sigma=sigma, Ng=Ng)
+
+
+def seeded_fields(p, seed: int) -> dict:
+    nx, ny, nz = p.Nx[0], p.Nx[1], p.Nx[2]
+    rng = np.random.default_rng(seed)
+    x = np.arange(nx) * p.L[0] / nx
+    wabm = 0.5 * p.chi_ab * np.cos(2 * np.pi * x / p.L[0])[None, None, :] + 0.01 * rng.standard_normal((nz, ny, nx))
+    return {"wabm": wabm.astype(np.complex128)}
+
+
+def sweep15(precision=PREC_MIXED, grid=(64, 64, 64), N=100):
+    """The 15-angle sweep at 64^3, N=100 (one instance per angle)."""
+    return [plate_params(t, N=N, grid=grid, precision=precision) for t in SWEEP_ANGLES]
+
+
+def sweep15_mixed_sizes(precision=PREC_MIXED):
+    """Config 2: the 15 angles on a mix of 48^3, 64^3 and 96x64x64 grids with
+    N in {64, 100}; the assignment is fixed by seed 2."""
+    rng = np.random.default_rng(2)
+    grids = [(48, 48, 48), (64, 64, 64), (96, 64, 64)]
+    out = []
+    for t in SWEEP_ANGLES:
+        g = grids[int(rng.integers(3))]
+        N = (64, 100)[int(rng.integers(2))]
+        box = tuple(6.4 * n / 64 for n in g)
+        out.append(plate_params(t, N=N, grid=g, box_rg=box, precision=precision))
+    return out
+
+
+WORKLOADS = {
+    "plate64_N100": lambda prec: [plate_params(10.0, precision=prec)],
+    "sweep15_64_N100": lambda prec: sweep15(precision=prec),
+    "sweep15_mixed_sizes": lambda prec: sweep15_mixed_sizes(precision=prec),
+}

@@ -1,0 +1,302 @@
+"""Benchmark of the SCFT hot path: SCFT iterations/s (update_1s steps summed
+over all instances and ranks) at 64^3, N=100.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--form mixed|plain] [--workload NAME]
+
+A step is one update_1s iteration (k-space field update, smearing, both
+propagator sweeps, densities) of every instance of the batch.  `value` is
+timed with CUDA events on the library's own stream with the fields resident in
+HBM; `e2e` is the same metric through the C ABI with host buffers: each step
+copies every instance's seven fields from pinned host memory, runs the
+iteration and reads H back.  The working set of one step (propagator history,
+fields, tables: >1 GB for the 15-instance batch) is larger than L2, so no
+explicit L2 flush is done.
+
+--impl reference times the reference's own code (compiled from its sources by
+oracle/Makefile into oracle/_ref/scft_ref, FFTW API from the project's shim)
+on the host cores, one process per instance.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "aligned-nanoplate-separation-and-rotation_gb300")
+sys.path.insert(0, PKG)
+
+METRIC = "SCFT iters/s @64^3,N=100"
+UNIT = "iters/s"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index=0):
+        self.proc = None
+        self.path = None
+        self.dev = device_index
+
+    def start(self):
+        if not shutil.which("nvidia-smi"):
+            return
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), f"--query-gpu={self.QUERY}",
+                                      "--format=csv,noheader,nounits", "-lms", "200"],
+                                     stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+
+    def stop(self):
+        if not self.proc:
+            return None
+        time.sleep(0.25)
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.remove(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# the compiled reference on the host cores
+# ---------------------------------------------------------------------------
+def case_from_params(p, fields):
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from ref_case import Case
+
+    c = Case(Nda=p.Nda, Ndb=p.Ndb, a_smear=p.a_smear, rho0=p.rho0, chi_ab=p.chi_ab, chi_bc=p.chi_bc,
+             chi_ac=p.chi_ac, kappa=p.kappa, Nx=tuple(p.Nx), L=tuple(p.L), lam_pl=p.lam_pl, lam_mi=p.lam_mi,
+             n_exp_nr=p.n_exp_nr, np_chem=p.np_chem, sigma=p.sigma, Ng=p.Ng, L_nr=p.L_nr, R_nr=p.R_nr,
+             xi_nr=p.xi_nr, centers=tuple(tuple(p.center[j]) for j in range(2)),
+             orients=tuple(tuple(p.orient[j]) for j in range(2)))
+    c.fields = fields
+    return c
+
+
+def time_reference(params, fields, iters, max_procs):
+    """Runs `iters` update_1s of each instance in its own process (up to
+    max_procs at once); returns (aggregate iters/s, processes, per-instance s/iter)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    from ref_case import REF_BIN, time_reference as tref
+
+    if not os.path.exists(REF_BIN):
+        raise FileNotFoundError(REF_BIN)
+    tmp = tempfile.mkdtemp(prefix="scft_ref_")
+    cases = [case_from_params(p, f) for p, f in zip(params, fields)]
+    procs = max(1, min(max_procs, len(cases)))
+    with ThreadPoolExecutor(max_workers=procs) as ex:
+        secs = list(ex.map(lambda kc: tref(os.path.join(tmp, f"inst{kc[0]}"), kc[1], iters),
+                           list(enumerate(cases))))
+    shutil.rmtree(tmp, ignore_errors=True)
+    waves = -(-len(cases) // procs)
+    # instances run `procs` at a time; the batch takes `waves` rounds
+    wall_per_iter = max(secs) * waves
+    return len(cases) / wall_per_iter, procs, secs
+
+
+# ---------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--form", choices=["mixed", "plain"], default=None)
+    ap.add_argument("--workload", default="sweep15_64_N100")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    import scft
+    from scft.workloads import WORKLOADS, seeded_fields
+
+    form = args.form or ("mixed" if scft.mixed_available() else "plain")
+    prec = scft.PREC_MIXED if form == "mixed" else scft.PREC_FP64
+    params = WORKLOADS[args.workload](prec)
+    fields = [seeded_fields(p, 1000 + k) for k, p in enumerate(params)]
+    n_inst = len(params)
+    config = {"workload": f"{args.workload}: {n_inst} plate instance(s), 64^3 grid, N=100, chiN=20, C=50, "
+                          "1S update", "form": form, "instances_per_rank": n_inst,
+              "grid": list(params[0].Nx), "N": params[0].Nda + params[0].Ndb,
+              "l2": "working set per step larger than L2 (no flush)"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cores = os.cpu_count() or 1
+        iters = max(1, min(args.steps, 2))
+        try:
+            v, procs, secs = time_reference(params, fields, iters, cores)
+        except Exception as e:  # noqa: BLE001
+            print(json.dumps({"impl": "reference", "unavailable": f"reference binary failed: {e}"}))
+            return
+        sample = (f"{n_inst} instances x {iters} update_1s each, one process per instance "
+                  f"({procs} at a time); reference code/ with Dim=3, FFTs by the oracle shim")
+        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": iters,
+                "warmup": 0, "ms_per_step": 1e3 * n_inst / v, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "c128", "data": "synthetic seeded fields", "config": config,
+                "impl": "reference",
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "reference", "sample": sample},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    import torch
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def allmax(x):
+        if dist is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    ctx = scft.Context(params)
+    for k in range(n_inst):
+        ctx.set_fields(k, fields[k])
+    ctx.calc_poly_density()
+    stream = torch.cuda.ExternalStream(ctx.stream())
+    ctx.update_1s(max(3, args.warmup))
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region
+    clocks = ClockSampler(local)
+    barrier()
+    torch.cuda.synchronize()
+    clocks.start()
+    l0 = ctx.launch_count()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    ctx.update_1s(args.steps)
+    e1.record(stream)
+    e1.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    ck = clocks.stop()
+    launches = ctx.launch_count() - l0
+    ms = allmax(e0.elapsed_time(e1))
+    H = ctx.calc_H()
+    value = n_inst * args.steps * world / (ms / 1e3)
+
+    # ---- end to end through the C ABI with pinned host buffers
+    import numpy as np
+
+    M = [p.Nx[0] * p.Nx[1] * p.Nx[2] for p in params]
+    host_in = []
+    for k in range(n_inst):
+        t = torch.zeros(7 * 2 * M[k], dtype=torch.float64, pin_memory=True)
+        f = ctx.get_fields(k)
+        arr = np.stack([f[n] for n in scft.FIELD_NAMES]).view(np.float64).ravel()
+        t.numpy()[:] = arr
+        host_in.append(t)
+    host_out = torch.zeros(5 * n_inst, dtype=torch.float64, pin_memory=True)
+    e2e_steps = max(1, min(args.steps, 10))
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        for k in range(n_inst):
+            ctx.set_fields_raw(k, host_in[k].data_ptr())
+        ctx.update_1s(1)
+        ctx.calc_H_raw(host_out.data_ptr())
+    torch.cuda.synchronize()
+    t_e2e = allmax(time.perf_counter() - t0)
+    e2e = {"value": n_inst * e2e_steps * world / t_e2e, "unit": UNIT,
+           "h2d_bytes_per_step": int(sum(7 * 16 * m for m in M)), "d2h_bytes_per_step": int(5 * 8 * n_inst)}
+
+    # ---- dominant kernel, isolated (after the timed regions)
+    prof = ctx.profile_step(20)
+    hbm, peak_kind = peaks()
+    dom = "plane" if prof["ms_plane"] >= prof["ms_col"] else "col"
+    ms_k = prof["ms_" + dom]
+    by = prof["bytes_" + dom]
+    achieved = by / (ms_k / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                "traffic": None, "kernel": ("k_prop_plane" if dom == "plane" else "k_col_fft (bond kernel)"),
+                "peak_kind": peak_kind, "ms_per_launch": ms_k, "algorithmic_bytes_per_launch": by,
+                "other_kernel_ms_per_launch": prof["ms_col" if dom == "plane" else "ms_plane"]}
+    ctx.close()
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        try:
+            cores = os.cpu_count() or 1
+            nb = min(n_inst, cores)
+            v, procs, secs = time_reference(params[:nb], fields[:nb], 1, cores)
+            cpu = {"value": v, "unit": UNIT, "cores": procs, "kind": "reference",
+                   "sample": f"{nb} instances x 1 update_1s, one process each; reference code/ (Dim=3, "
+                             f"oracle FFT shim); {statistics.mean(secs):.2f} s/iter per process"}
+        except Exception as e:  # noqa: BLE001
+            cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "reference", "sample": f"failed: {e}"}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 propagators / f64 fields" if form == "mixed" else "c128 (complex f64)",
+                "data": "synthetic seeded fields", "config": config, "e2e": e2e, "roofline": roofline,
+                "cpu_baseline": cpu, "clocks": ck, "gpu_launches": launches,
+                "H_first_instance": float(H[0, 0])}
+        print(json.dumps(line))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -145,6 +145,26 @@ int scft_fft3d(scft_ctx *ctx, int inst, double *data, int count, int sign);
 /* Synchronises the context's stream; returns the first asynchronous error. */
 int scft_sync(scft_ctx *ctx);
 
+/* The cudaStream_t on which every kernel of this context runs (for callers
+ * that time or order work around it). */
+int scft_get_stream(scft_ctx *ctx, void **stream);
+
+/* Number of kernel launches this context has issued so far (kernels inside a
+ * replayed CUDA graph count once per replay). */
+int scft_launch_count(scft_ctx *ctx, long long *count);
+
+/* Times the two kernels of one propagator step in isolation on the context
+ * stream (CUDA events, `reps` launches each, all instances): the xy-plane pass
+ * at a step of the second half of the sweep and the z-column pass.  Writes
+ * the mean milliseconds per launch and the algorithmic bytes one launch has
+ * to move: per grid point of every propagator, the plane pass reads its input,
+ * the Boltzmann factor and the stored partner propagator, writes its output
+ * and read-modify-writes one density accumulator; the column pass reads and
+ * writes the array and reads the bond-kernel table.  Leaves the propagator
+ * buffers in an undefined state; call scft_calc_poly_density afterwards. */
+int scft_profile_step(scft_ctx *ctx, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
+                      double *bytes_col);
+
 #ifdef __cplusplus
 }
 #endif
