@@ -52,7 +52,7 @@ extern "C" {
 
 const char *scft_last_error(void) { return g_err.c_str(); }
 
-int scft_version(void) { return 1; }
+int scft_version(void) { return 2; }
 
 int scft_create(const scft_params *params, int n_inst, scft_ctx **out) {
   if (!out) return fail(SCFT_ERR_ARG, "null output pointer");

@@ -339,6 +339,8 @@ void validate(const scft_params &p) {
   }
   if (p.precision != SCFT_PREC_FP64 && p.precision != SCFT_PREC_MIXED) bad("unknown precision");
   if (p.sigma > 0 && p.Ng < 1) bad("grafted chains need Ng >= 1");
+  if (p.precision == SCFT_PREC_MIXED && p.sigma > 0 && p.Ng > 0 && p.n_exp_nr > 0)
+    throw ScftError(SCFT_ERR_UNSUPPORTED, "grafted chains are built for the FP64 method only");
 }
 
 void setup_instance(scft_ctx *c, Instance &I, int idx) {
@@ -410,22 +412,38 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
   I.gc = dupload(c, gc);
 
   // device arrays
+  I.mixed = (p.precision == SCFT_PREC_MIXED);
   for (int f = 0; f < 7; f++) I.w[f] = dalloc<double2>(c, M);
-  for (int f = 0; f < 3; f++) {
-    I.sm[f] = dalloc<double2>(c, M);
-    I.rho[f] = dalloc<double2>(c, M);
-    I.expw[f] = dalloc<double2>(c, M);
-  }
-  for (int q = 0; q < 2; q++)
-    for (int s = 0; s < 2; s++) I.acc[q][s] = dalloc<double2>(c, M);
-  for (int q = 0; q < 2; q++) {
-    if (q == 1 && I.single) {
-      I.work[1] = I.work[0];
-      I.hist[1] = I.hist[0];
-      continue;
+  for (int f = 0; f < 3; f++) I.rho[f] = dalloc<double2>(c, M);
+  if (!I.mixed) {
+    for (int f = 0; f < 3; f++) {
+      I.sm[f] = dalloc<double2>(c, M);
+      I.expw[f] = dalloc<double2>(c, M);
     }
-    I.work[q] = dalloc<double2>(c, M);
-    I.hist[q] = dalloc<double2>(c, (size_t)M * (I.hmax + 1));
+    for (int q = 0; q < 2; q++)
+      for (int s2 = 0; s2 < 2; s2++) I.acc[q][s2] = dalloc<double2>(c, M);
+    for (int q = 0; q < 2; q++) {
+      if (q == 1 && I.single) {
+        I.work[1] = I.work[0];
+        I.hist[1] = I.hist[0];
+        continue;
+      }
+      I.work[q] = dalloc<double2>(c, M);
+      I.hist[q] = dalloc<double2>(c, (size_t)M * (I.hmax + 1));
+    }
+  } else {
+    I.zr = dalloc<double2>(c, M);
+    I.zs = dalloc<double2>(c, M);
+    I.E32 = dalloc<float2>(c, M);
+    I.work32 = dalloc<float2>(c, M);
+    I.hist32 = dalloc<float2>(c, (size_t)M * (I.hmax + 1));
+    I.acc64[0] = dalloc<double>(c, M);
+    I.acc64[1] = dalloc<double>(c, M);
+    I.part = dalloc<double>(c, (size_t)2 * I.N * g.nz);
+    I.K = dalloc<int>(c, (size_t)2 * I.N);
+    std::vector<float> h32(M);
+    for (long long i = 0; i < M; i++) h32[i] = (float)(1.0 - pb[i]);
+    I.h32 = dupload(c, h32);
   }
   I.qpart = dalloc<double2>(c, g.nz);
   I.scal = dalloc<double2>(c, kNumScalars);
@@ -559,6 +577,15 @@ void build_jobs(scft_ctx *c) {
     F.gacc = I.gacc;
     F.ghist_last = I.graft ? I.ghist + (size_t)I.M * (I.Ng - 1) : nullptr;
     F.grafts = I.grafts;
+    F.nx = I.p.Nx[0];
+    F.ny = I.p.Nx[1];
+    F.zr = I.zr;
+    F.zs = I.zs;
+    F.E32 = I.E32;
+    F.acc64[0] = I.acc64[0];
+    F.acc64[1] = I.acc64[1];
+    F.K = I.K;
+    F.part64 = I.part;
 
     PropInst &P = pi[k];
     memset(&P, 0, sizeof P);
@@ -584,6 +611,29 @@ void build_jobs(scft_ctx *c) {
   }
   c->d_fi = dupload(c, fi);
   c->d_pi = dupload(c, pi);
+  c->mixed = c->inst[0].mixed;
+  for (auto &I : c->inst)
+    if (I.mixed != c->mixed) throw ScftError(SCFT_ERR_ARG, "all instances of a context must use one precision");
+  if (c->mixed) {
+    std::vector<MixInst> mi(n);
+    for (int k = 0; k < n; k++) {
+      Instance &I = c->inst[k];
+      MixInst &X = mi[k];
+      memset(&X, 0, sizeof X);
+      X.geom = I.geom;
+      X.N = I.N;
+      X.Na = I.Na;
+      X.hmax = I.hmax;
+      X.work = I.work32;
+      X.hist = I.hist32;
+      X.E = I.E32;
+      X.acc[0] = I.acc64[0];
+      X.acc[1] = I.acc64[1];
+      X.part = I.part;
+      X.K = I.K;
+    }
+    c->d_mi = dupload(c, mi);
+  }
 
   // field transform job lists
   std::vector<PlaneJob> pj_upd, pj_fld, pj_sm;
@@ -613,9 +663,15 @@ void build_jobs(scft_ctx *c) {
           for (int x0 = 0; x0 < g.nx; x0 += g.tx) cj.push_back(ColJob{a, kern, I.geom, x0, y});
       }
     };
-    add(upd, pj_upd, cj_upd, nullptr);
-    add(fld, pj_fld, cj_fld, nullptr);
-    add(smr, pj_sm, cj_sm, I.hhat);
+    if (!I.mixed) {
+      add(upd, pj_upd, cj_upd, nullptr);
+      add(fld, pj_fld, cj_fld, nullptr);
+      add(smr, pj_sm, cj_sm, I.hhat);
+    } else {
+      std::vector<double2 *> zr = {I.zr}, zs = {I.zs};
+      add(zr, pj_upd, cj_upd, nullptr);  // forward transform of rho_A + i rho_B
+      add(zs, pj_fld, cj_fld, nullptr);  // inverse transform of the smeared pair
+    }
   }
   c->shp_plane = choose_shape(emax_plane, sizeof(double2), (nxy_max + 32) * sizeof(double2));
   c->shp_col = choose_shape(emax_col, sizeof(double2), (nz_max + 32) * sizeof(double2));
@@ -662,6 +718,29 @@ void build_jobs(scft_ctx *c) {
       }
     }
   }
+  if (c->mixed) {
+    // one plane job per z (q and qdag packed), FP32 column jobs
+    ppj.clear();
+    pcj.clear();
+    for (int oi = 0; oi < n; oi++) {
+      const int k = order[oi];
+      Instance &I = c->inst[k];
+      const DevGeom &g = c->geoms[I.geom];
+      for (int z = 0; z < g.nz; z++) ppj.push_back(PropJob{k, 0, z});
+      for (int y = 0; y < g.ny; y++)
+        for (int x0 = 0; x0 < g.nx; x0 += g.tx) pcj.push_back(ColJob{I.work32, I.h32, I.geom, x0, y});
+      inst_pj_end[oi] = (int)ppj.size();
+      inst_cj_end[oi] = (int)pcj.size();
+    }
+    for (int s2 = 0; s2 < c->nmax; s2++)
+      for (int oi = 0; oi < n; oi++)
+        if (c->inst[order[oi]].N > s2) {
+          c->prop_pj_count[s2] = inst_pj_end[oi];
+          c->prop_cj_count[s2] = inst_cj_end[oi];
+        }
+    c->shp_mix = choose_shape(emax_plane, sizeof(float2), (nxy_max + 32) * sizeof(float2));
+    c->shp_col32 = choose_shape(emax_col, sizeof(float2), (nz_max + 32) * sizeof(float2));
+  }
   c->d_prop_pj = dupload(c, ppj);
   c->d_prop_cj = dupload(c, pcj);
 
@@ -703,6 +782,68 @@ void build_jobs(scft_ctx *c) {
   c->eblocks = (int)std::min<long long>(2048, (mmax + 255) / 256);
   c->hblocks = 64;
   c->d_hpart = dalloc<double2>(c, (size_t)n * 4 * c->hblocks);
+}
+
+// Largest |Im| and |Re| of w_A and w_B over the grid (mixed form input check).
+__global__ void k_real_check(const double2 *const *w, long long M, int neg_ab, int neg_bc, int neg_ac,
+                             double *out) {
+  __shared__ double ri[32], rr[32];
+  double mi = 0.0, mr = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
+    const double2 pl = w[0][i], abp = w[1][i], abm = w[2][i], bcp = w[3][i], bcm = w[4][i], acp = w[5][i],
+                  acm = w[6][i];
+    // imaginary parts of w_A, w_B (code/calc_poly_density.cpp:45-50)
+    const double ia = pl.x + (neg_ab ? abm.x - abp.y : abp.x - abm.y) + (neg_ac ? acm.x - acp.y : acp.x - acm.y);
+    const double ib = pl.x + (neg_ab ? -abm.x - abp.y : abp.x + abm.y) + (neg_bc ? bcm.x - bcp.y : bcp.x - bcm.y);
+    const double ra = -pl.y + (neg_ab ? -abm.y - abp.x : -abp.y - abm.x) + (neg_ac ? -acm.y - acp.x : -acp.y - acm.x);
+    const double rb = -pl.y + (neg_ab ? abm.y - abp.x : -abp.y + abm.x) + (neg_bc ? -bcm.y - bcp.x : -bcp.y - bcm.x);
+    mi = fmax(mi, fmax(fabs(ia), fabs(ib)));
+    mr = fmax(mr, fmax(fabs(ra), fabs(rb)));
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    mi = fmax(mi, __shfl_down_sync(0xffffffffu, mi, o));
+    mr = fmax(mr, __shfl_down_sync(0xffffffffu, mr, o));
+  }
+  const int wp = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { ri[wp] = mi; rr[wp] = mr; }
+  __syncthreads();
+  if (wp == 0) {
+    mi = l < (int)(blockDim.x >> 5) ? ri[l] : 0.0;
+    mr = l < (int)(blockDim.x >> 5) ? rr[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      mi = fmax(mi, __shfl_down_sync(0xffffffffu, mi, o));
+      mr = fmax(mr, __shfl_down_sync(0xffffffffu, mr, o));
+    }
+    if (l == 0) {
+      out[2 * blockIdx.x] = mi;
+      out[2 * blockIdx.x + 1] = mr;
+    }
+  }
+}
+
+void check_real_fields(scft_ctx *c, int k) {
+  Instance &I = c->inst[k];
+  const double2 **dw = nullptr;
+  double *dout = nullptr;
+  const int nb = 64;
+  CK(cudaMalloc(&dw, sizeof(double2 *) * 7));
+  CK(cudaMalloc(&dout, sizeof(double) * 2 * nb));
+  CK(cudaMemcpyAsync(dw, I.w, sizeof(double2 *) * 7, cudaMemcpyHostToDevice, c->st));
+  k_real_check<<<nb, 256, 0, c->st>>>(dw, I.M, I.neg_ab, I.neg_bc, I.neg_ac, dout);
+  std::vector<double> h(2 * nb);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), dout, sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost, c->st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
+  cudaFree(dw);
+  cudaFree(dout);
+  CK(e);
+  double mi = 0.0, mr = 0.0;
+  for (int b = 0; b < nb; b++) {
+    mi = std::max(mi, h[2 * b]);
+    mr = std::max(mr, h[2 * b + 1]);
+  }
+  if (mi > 1e-12 * std::max(1.0, mr))
+    throw ScftError(SCFT_ERR_COMPLEX, "mixed precision needs real w_A and w_B (mean-field phase convention)");
 }
 
 // CK plus one kernel launch on the context's counter
@@ -765,6 +906,51 @@ void seq_update_1s(scft_ctx *c) {
   seq_poly_density(c);
 }
 
+// Mixed form: FP32 packed propagator sweep over all instances (after E32).
+void seq_mix_sweep(scft_ctx *c) {
+  const int n = (int)c->inst.size();
+  cudaStream_t st = c->st;
+  for (auto &I : c->inst) {
+    CK(cudaMemsetAsync(I.acc64[0], 0, sizeof(double) * I.M, st));
+    CK(cudaMemsetAsync(I.acc64[1], 0, sizeof(double) * I.M, st));
+  }
+  LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[0], c->d_mi, c->d_geoms, c->d_tw32, 0, st));
+  for (int s = 1; s < c->nmax; s++) {
+    LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw32, 3, 1, st));
+    LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_geoms, c->d_tw32, s,
+                             st));
+  }
+  LK(launch_mix_q_finalize(c->d_fi, n, st));
+}
+
+// Mixed form: inverse transform of the packed smeared pair, Boltzmann factors, sweep.
+void seq_mix_from_zs(scft_ctx *c) {
+  const int n = (int)c->inst.size();
+  cudaStream_t st = c->st;
+  LK(launch_col_fft<double>(c->shp_col, c->d_cj_fld, c->n_cj_fld, c->d_geoms, c->d_tw64, 1, 0, st));
+  LK(launch_plane_fft<double>(c->shp_plane, c->d_pj_fld, c->n_pj_fld, c->d_geoms, c->d_tw64, +1, 0, st));
+  LK(launch_mix_boltzmann(c->d_fi, n, c->eblocks, st));
+  seq_mix_sweep(c);
+}
+
+// Mixed calc_poly_density from the k-space fields.
+void seq_mix_density(scft_ctx *c) {
+  LK(launch_mix_smear(c->d_fi, (int)c->inst.size(), c->eblocks, c->st));
+  seq_mix_from_zs(c);
+}
+
+// Mixed update_1s: densities -> packed forward transform -> k-space update
+// (which also forms the packed smeared pair) -> inverse -> sweep.
+void seq_mix_update(scft_ctx *c) {
+  const int n = (int)c->inst.size();
+  cudaStream_t st = c->st;
+  LK(launch_mix_rho_pack(c->d_fi, n, c->eblocks, 0, st));
+  LK(launch_plane_fft<double>(c->shp_plane, c->d_pj_upd, c->n_pj_upd, c->d_geoms, c->d_tw64, -1, 0, st));
+  LK(launch_col_fft<double>(c->shp_col, c->d_cj_upd, c->n_cj_upd, c->d_geoms, c->d_tw64, 0, 1, st));
+  LK(launch_mix_update(c->d_fi, n, c->eblocks, st));
+  seq_mix_from_zs(c);
+}
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -799,6 +985,9 @@ void ctx_create(scft_ctx *c, const scft_params *params, int n_inst) {
     }
   }
   c->d_tw64 = dupload(c, tw);
+  std::vector<float2> tw32(tw.size());
+  for (size_t t = 0; t < tw.size(); t++) tw32[t] = make_float2((float)tw[t].x, (float)tw[t].y);
+  c->d_tw32 = dupload(c, tw32);
   c->d_geoms = dupload(c, c->geoms);
   for (auto &I : c->inst) setup_plates(c, I);
   build_jobs(c);
@@ -812,7 +1001,10 @@ void ctx_destroy(scft_ctx *c) {
 }
 
 void ctx_poly_density(scft_ctx *c) {
-  seq_poly_density(c);
+  if (c->mixed)
+    seq_mix_density(c);
+  else
+    seq_poly_density(c);
   CK(cudaStreamSynchronize(c->st));
   c->dirty_density = 0;
 }
@@ -823,14 +1015,14 @@ void ctx_update(scft_ctx *c, int n_iter) {
   int k = 0;
   if (!c->g_update) {
     // first iteration runs eagerly (kernel attributes get set), then capture
-    seq_update_1s(c);
+    (c->mixed ? seq_mix_update(c) : seq_update_1s(c));
     CK(cudaStreamSynchronize(c->st));
     k = 1;
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
     const long long before = c->launches;
     try {
-      seq_update_1s(c);
+      (c->mixed ? seq_mix_update(c) : seq_update_1s(c));
       c->launches_per_update = c->launches - before;
       c->launches = before;
     } catch (...) {
@@ -859,12 +1051,22 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   CK(cudaEventCreate(&e1));
   CK(cudaEventCreate(&e2));
   CK(cudaEventRecord(e0, c->st));
-  for (int r = 0; r < reps; r++)
-    LK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[s], c->d_pi, c->d_geoms, c->d_tw64, s,
-                             c->st));
+  for (int r = 0; r < reps; r++) {
+    if (c->mixed)
+      LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_geoms, c->d_tw32, s,
+                               c->st));
+    else
+      LK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[s], c->d_pi, c->d_geoms, c->d_tw64, s,
+                               c->st));
+  }
   CK(cudaEventRecord(e1, c->st));
-  for (int r = 0; r < reps; r++)
-    LK(launch_col_fft<double>(c->shp_col, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw64, 2, 1, c->st));
+  for (int r = 0; r < reps; r++) {
+    if (c->mixed)
+      LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw32, 3, 1, c->st));
+    else
+      LK(launch_col_fft<double>(c->shp_col, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw64, 2, 1,
+                                c->st));
+  }
   CK(cudaEventRecord(e2, c->st));
   CK(cudaEventSynchronize(e2));
   float a = 0.f, b = 0.f;
@@ -876,9 +1078,16 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   double bp = 0.0, bc = 0.0;
   for (auto &I : c->inst) {
     if (I.N <= s) continue;
-    const double props = I.single ? 1.0 : 2.0;
-    bp += props * I.M * 6.0 * sizeof(double2);
-    bc += props * I.M * (2.0 * sizeof(double2) + sizeof(double));
+    if (I.mixed) {
+      // plane: read z, E (8 B each), stored pair (8 B), write z (8 B), RMW of
+      // the FP64 accumulators A and B (2 x 16 B); column: read + write z, g table
+      bp += I.M * (4.0 * sizeof(float2) + 4.0 * sizeof(double));
+      bc += I.M * (2.0 * sizeof(float2) + sizeof(float));
+    } else {
+      const double props = I.single ? 1.0 : 2.0;
+      bp += props * I.M * 6.0 * sizeof(double2);
+      bc += props * I.M * (2.0 * sizeof(double2) + sizeof(double));
+    }
   }
   *ms_plane = a / reps;
   *ms_col = b / reps;
@@ -891,7 +1100,10 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
 int ctx_calc_H(scft_ctx *c, double *out) {
   if (c->dirty_density) ctx_poly_density(c);
   const int n = (int)c->inst.size();
-  CK(launch_h_partials(c->d_fi, n, c->hblocks, c->d_hpart, c->st));
+  if (c->mixed)
+    CK(launch_mix_h_partials(c->d_fi, n, c->hblocks, c->d_hpart, c->st));
+  else
+    CK(launch_h_partials(c->d_fi, n, c->hblocks, c->d_hpart, c->st));
   std::vector<double2> hp((size_t)n * 4 * c->hblocks);
   CK(cudaMemcpyAsync(hp.data(), c->d_hpart, sizeof(double2) * hp.size(), cudaMemcpyDeviceToHost, c->st));
   std::vector<double2> sc((size_t)n * kNumScalars);
@@ -909,7 +1121,10 @@ int ctx_calc_H(scft_ctx *c, double *out) {
         const double2 v = hp[((size_t)k * 4 + j) * c->hblocks + b];
         s += cd(v.x, v.y);
       }
-      for (int d = 0; d < 3; d++) s *= I.info.dx[d];
+      if (I.mixed)
+        s *= I.info.V;  // Parseval: int f g = V sum_k f(k) g(-k)
+      else
+        for (int d = 0; d < 3; d++) s *= I.info.dx[d];
       part[j] = s;
     }
     if (I.cbc == 0.0) part[1] = 0.0;
@@ -936,12 +1151,28 @@ void ctx_set_fields(scft_ctx *c, int k, const double *w) {
   Instance &I = c->inst[k];
   for (int f = 0; f < 7; f++)
     CK(cudaMemcpyAsync(I.w[f], w + (size_t)f * 2 * I.M, sizeof(double2) * I.M, cudaMemcpyHostToDevice, c->st));
+  if (I.mixed) {
+    // the packed transforms need real w_A, w_B (the mean-field phase convention)
+    check_real_fields(c, k);
+    fft3d_arrays(c, I, std::vector<double2 *>(I.w, I.w + 7), -1);
+  }
   CK(cudaStreamSynchronize(c->st));
   c->dirty_density = 1;
 }
 
 void ctx_get_fields(scft_ctx *c, int k, double *w) {
   Instance &I = c->inst[k];
+  if (I.mixed) {
+    // fields are held as transforms; return them in real space
+    double2 *tmp = I.rho[2];
+    for (int f = 0; f < 7; f++) {
+      CK(cudaMemcpyAsync(tmp, I.w[f], sizeof(double2) * I.M, cudaMemcpyDeviceToDevice, c->st));
+      fft3d_arrays(c, I, {tmp}, +1);
+      CK(cudaMemcpyAsync(w + (size_t)f * 2 * I.M, tmp, sizeof(double2) * I.M, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+    }
+    return;
+  }
   for (int f = 0; f < 7; f++)
     CK(cudaMemcpyAsync(w + (size_t)f * 2 * I.M, I.w[f], sizeof(double2) * I.M, cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
@@ -950,6 +1181,11 @@ void ctx_get_fields(scft_ctx *c, int k, double *w) {
 void ctx_get_density(scft_ctx *c, int k, double *ra, double *rb, double *rg) {
   if (c->dirty_density) ctx_poly_density(c);
   Instance &I = c->inst[k];
+  if (I.mixed) {
+    // zr is rebuilt from the accumulators by the next update, so this is safe
+    CK(launch_mix_rho_pack(c->d_fi, (int)c->inst.size(), c->eblocks, 1, c->st));
+    CK(cudaMemsetAsync(I.rho[2], 0, sizeof(double2) * I.M, c->st));
+  }
   double *outs[3] = {ra, rb, rg};
   for (int f = 0; f < 3; f++)
     if (outs[f]) CK(cudaMemcpyAsync(outs[f], I.rho[f], sizeof(double2) * I.M, cudaMemcpyDeviceToHost, c->st));
@@ -959,6 +1195,18 @@ void ctx_get_density(scft_ctx *c, int k, double *ra, double *rb, double *rg) {
 void ctx_get_smeared(scft_ctx *c, int k, double *a, double *b, double *g) {
   if (c->dirty_density) ctx_poly_density(c);
   Instance &I = c->inst[k];
+  if (I.mixed) {
+    // zs holds smwa + i smwb (both real) in real space
+    std::vector<double2> h(I.M);
+    CK(cudaMemcpyAsync(h.data(), I.zs, sizeof(double2) * I.M, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (long long i = 0; i < I.M; i++) {
+      if (a) { a[2 * i] = h[i].x; a[2 * i + 1] = 0.0; }
+      if (b) { b[2 * i] = h[i].y; b[2 * i + 1] = 0.0; }
+      if (g) { g[2 * i] = 0.0; g[2 * i + 1] = 0.0; }
+    }
+    return;
+  }
   double *outs[3] = {a, b, g};
   for (int f = 0; f < 3; f++)
     if (outs[f]) CK(cudaMemcpyAsync(outs[f], I.sm[f], sizeof(double2) * I.M, cudaMemcpyDeviceToHost, c->st));
@@ -987,6 +1235,7 @@ void ctx_fft3d(scft_ctx *c, int k, double *data, int count, int sign) {
 void ctx_diblock_density(scft_ctx *c, int k, const double *smwa, const double *smwb, double *ra, double *rb,
                          double *Q) {
   Instance &I = c->inst[k];
+  if (I.mixed) throw ScftError(SCFT_ERR_UNSUPPORTED, "scft_diblock_density runs the FP64 method only");
   CK(cudaMemcpyAsync(I.sm[0], smwa, sizeof(double2) * I.M, cudaMemcpyHostToDevice, c->st));
   CK(cudaMemcpyAsync(I.sm[1], smwb, sizeof(double2) * I.M, cudaMemcpyHostToDevice, c->st));
   const int n = (int)c->inst.size();

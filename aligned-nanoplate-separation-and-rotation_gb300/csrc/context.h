@@ -40,6 +40,14 @@ struct Instance {
   double *hhat = nullptr, *gaa = nullptr, *gab = nullptr, *gbb = nullptr, *gc = nullptr;
   double *pbond = nullptr, *rho_exp_nr = nullptr;
   double2 *gwork = nullptr, *ghist = nullptr, *gacc = nullptr;  // graft sweeps
+  // mixed precision
+  int mixed = 0;
+  double2 *zr = nullptr, *zs = nullptr;
+  float2 *E32 = nullptr, *work32 = nullptr, *hist32 = nullptr;
+  double *acc64[2] = {};
+  double *part = nullptr;
+  int *K = nullptr;
+  float *h32 = nullptr;  // 1 - g(k), FP32
 };
 
 struct DevBuf {
@@ -76,6 +84,16 @@ struct scft_ctx {
   int ngmax = 0;
   double2 *d_gpart = nullptr;
   int gblocks = 0;
+  // mixed precision
+  int mixed = 0;
+  void *d_tw32 = nullptr;
+  scft::MixInst *d_mi = nullptr;
+  scft::PropJob *d_mix_pj = nullptr;
+  scft::ColJob *d_mix_cj = nullptr;
+  scft::PlaneJob *d_pj_zr = nullptr, *d_pj_zs = nullptr;
+  scft::ColJob *d_cj_zr = nullptr, *d_cj_zs = nullptr;
+  int n_pj_zr = 0, n_cj_zr = 0;
+  scft::LaunchShape shp_mix{}, shp_col32{};
   scft::LaunchShape shp_plane{}, shp_col{}, shp_prop{};
   int eblocks = 0;  // blocks per instance for pointwise kernels
   double2 *d_hpart = nullptr;

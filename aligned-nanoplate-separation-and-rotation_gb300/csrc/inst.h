@@ -35,6 +35,18 @@ struct PropInst {
   const double2 *grafts;   // normalised graft map (real space)
 };
 
+// View of one instance for the mixed-precision propagator sweep: q and qdag
+// packed as the real and imaginary parts of one FP32 complex array.
+struct MixInst {
+  int geom, N, Na, hmax;
+  float2 *work;    // z = q + i qdag of the current step
+  float2 *hist;    // steps 0..hmax
+  const float2 *E; // (e^{-smwa}, e^{-smwb})
+  double *acc[2];  // density sums for A and B, FP64
+  double *part;    // [2][N][nz] plane sums of the stored q, qdag (FP64)
+  int *K;          // [2][N] power-of-two exponents
+};
+
 struct PropJob {
   int inst;
   int p;
@@ -64,6 +76,14 @@ struct FieldInst {
   double2 *gacc;       // graft density accumulator
   const double2 *ghist_last;  // q_g[Ng-1]
   const double2 *grafts;
+  // mixed precision: w[] hold the k-space (1/M scaled) fields
+  int nx, ny;
+  double2 *zr;         // rho_A + i rho_B (real space), then its transform
+  double2 *zs;         // hhat*(w_A + i w_B) (k-space), then smwa + i smwb (real space)
+  float2 *E32;         // (e^{-smwa}, e^{-smwb})
+  double *acc64[2];
+  int *K;              // [2][N]
+  double *part64;      // [2][N][nz] plane sums of the stored propagators
 };
 
 }  // namespace scft

@@ -41,7 +41,11 @@ __global__ void __launch_bounds__(512) k_plane_fft(const PlaneJob *__restrict__ 
 }
 
 // MODE 0: forward z (sign -1); 1: inverse z (sign +1); 2: forward, multiply by
-// kern[x,y,z] * scale, inverse.
+// kern[x,y,z] * scale, inverse; 3 (FP32 propagator of the mixed form):
+// forward, drop the k = 0 coefficient (the mean is carried exactly in FP64 by
+// the plane pass), multiply by (1 - h) / M with h = 1 - g(k) tabulated and 1/M
+// applied as a two-float product, inverse.  Writing g = 1 - h keeps the
+// low-k bond factors, which decide Q, exact to eps*h instead of eps.
 template <typename T, int MODE, int MAXV>
 __global__ void __launch_bounds__(512) k_col_fft(const ColJob *__restrict__ jobs, const DevGeom *__restrict__ geoms,
                           const cx<T> *__restrict__ twbuf, int scale_by_M) {
@@ -74,6 +78,22 @@ __global__ void __launch_bounds__(512) k_col_fft(const ColJob *__restrict__ jobs
       const int z = e / tx, x = e - z * tx;
       const T kv = kern[z * plane + base + x];
       tile[e] = cscale(cscale(tile[e], s), kv);
+    }
+    __syncthreads();
+    fft_lines<T, +1, MAXV>(tile, g.ax[2], tx, 1, tx, twz);
+  }
+  if (MODE == 3) {
+    const T *kern = reinterpret_cast<const T *>(jb.kern);
+    const double sd = 1.0 / (double)g.M;
+    const T s_hi = (T)sd, s_lo = (T)(sd - (double)s_hi);
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      const int z = e / tx, x = e - z * tx;
+      const T h = kern[z * plane + base + x];
+      const C v = tile[e];
+      C t = mkc(fma(v.x, s_hi, v.x * s_lo), fma(v.y, s_hi, v.y * s_lo));
+      t = mkc(fma(-h, t.x, t.x), fma(-h, t.y, t.y));
+      if (e == 0 && jb.x0 == 0 && jb.y == 0) t = mkc((T)0, (T)0);
+      tile[e] = t;
     }
     __syncthreads();
     fft_lines<T, +1, MAXV>(tile, g.ax[2], tx, 1, tx, twz);
@@ -134,6 +154,7 @@ cudaError_t launch_col_fft(const LaunchShape &ls, const ColJob *jobs, int njobs,
   } while (0)
   if (mode == 0) SCFT_COL(0);
   if (mode == 1) SCFT_COL(1);
+  if (mode == 3) SCFT_COL(3);
   SCFT_COL(2);
 #undef SCFT_COL
 }

@@ -35,11 +35,13 @@ __device__ __host__ __forceinline__ double2 cdiv_d(double2 a, double2 b) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < FI.M; \
        i += (long long)gridDim.x * blockDim.x)
 
-// code/calc_poly_density.cpp:42-54
-__global__ void k_assemble(const FieldInst *__restrict__ fi) {
-  FOR_POINTS(F) {
-    const double2 pl = F.w[0][i], abp = F.w[1][i], abm = F.w[2][i];
-    const double2 bcp = F.w[3][i], bcm = F.w[4][i], acp = F.w[5][i], acm = F.w[6][i];
+// code/calc_poly_density.cpp:42-54: w_A, w_B, w_G from the seven fields
+// (linear, so it applies equally to real-space values and to transforms).
+__device__ __forceinline__ void assemble_point(const FieldInst &F, const double2 *w, double2 &wa, double2 &wb,
+                                               double2 &wg) {
+  {
+    const double2 pl = w[0], abp = w[1], abm = w[2];
+    const double2 bcp = w[3], bcm = w[4], acp = w[5], acm = w[6];
     // I*x = (-x.y, x.x)
     const double2 Ipl = make_double2(-pl.y, pl.x);
     double2 ab_a, ab_b, ac_a, bc_b, ac_g, bc_g;
@@ -64,9 +66,21 @@ __global__ void k_assemble(const FieldInst *__restrict__ fi) {
       bc_b = make_double2(-bcp.y - bcm.x, bcp.x - bcm.y);
       bc_g = make_double2(-bcp.y + bcm.x, bcp.x + bcm.y);
     }
-    F.sm[0][i] = cadd(cadd(Ipl, ab_a), ac_a);
-    F.sm[1][i] = cadd(cadd(Ipl, ab_b), bc_b);
-    if (F.graft) F.sm[2][i] = cadd(cadd(Ipl, ac_g), bc_g);
+    wa = cadd(cadd(Ipl, ab_a), ac_a);
+    wb = cadd(cadd(Ipl, ab_b), bc_b);
+    wg = cadd(cadd(Ipl, ac_g), bc_g);
+  }
+}
+
+__global__ void k_assemble(const FieldInst *__restrict__ fi) {
+  FOR_POINTS(F) {
+    double2 w[7];
+    for (int f = 0; f < 7; f++) w[f] = F.w[f][i];
+    double2 wa, wb, wg;
+    assemble_point(F, w, wa, wb, wg);
+    F.sm[0][i] = wa;
+    F.sm[1][i] = wb;
+    if (F.graft) F.sm[2][i] = wg;
   }
 }
 
@@ -178,129 +192,138 @@ __global__ void k_qga_finalize(const FieldInst *__restrict__ fi, int ninst, int 
   F.scal[kQg] = make_double2(cnt, 0.0);
 }
 
-// code/1s_update.cpp:58-329, k-space (mean-field: no noise, no film/channel,
-// no field nanoparticles, no homopolymer).  Arrays are the forward transforms
-// (1/M scaled) of the densities and fields.
+// code/1s_update.cpp:58-329 at one k-space point (mean-field: no noise, no
+// film/channel, no field nanoparticles, no homopolymer).  ra, rb, rg are the
+// forward transforms (1/M scaled) of rhoda, rhodb, rhog_exp at this point and
+// w[0..6] the transformed fields (wpl, wabp, wabm, wbcp, wbcm, wacp, wacm),
+// updated in place.
+__device__ __forceinline__ void update_1s_point(const FieldInst &F, long long i, double2 ra, double2 rb,
+                                                double2 rg, double2 *w) {
+  const double rho0 = F.rho0, N = (double)F.N, Ng = (double)F.Ng;
+  const double li = F.lam_pl, lr = F.lam_mi;
+  const double hh = F.hhat[i];
+  const double hh2 = hh * hh;
+  const double gaa = F.gaa[i], gab = F.gab[i], gbb = F.gbb[i], gc = F.gc[i];
+  const double2 enh = F.exp_nrH[i];
+  // w+  (:58-84)
+  {
+    const double evar = (i == 0) ? 1.0 : 0.0;
+    const double2 s = cadd(cadd(ra, rg), rb);  // rhoha + rhoda + rhog + rhog_exp + rhodb
+    // I*rho0*(exp_nrH - evar) + I*hhat*s
+    const double2 u = make_double2(enh.x - evar, enh.y);
+    const double2 F1 = make_double2(-rho0 * u.y - hh * s.y, rho0 * u.x + hh * s.x);
+    const double A = rho0 / F.kappa + F.phiD * rho0 * N * hh2 * (gaa + 2.0 * gab + gbb) +
+                     (F.phiG * Ng * gc) * rho0 * hh2;
+    const double B = A - rho0 / F.kappa;
+    const double2 wv = w[0];
+    const double2 num = make_double2(wv.x - li * (F1.x - B * wv.x), wv.y - li * (F1.y - B * wv.y));
+    const double den = 1.0 + li * A;
+    w[0] = make_double2(num.x / den, num.y / den);
+  }
+  // AB (:87-166)
+  if (F.cab != 0.0) {
+    const double c = F.cab;
+    double2 wp = w[1], wm = w[2];
+    if (!F.neg_ab) {
+      double2 F1 = make_double2(-hh * (ra.y + rb.y), hh * (ra.x + rb.x));  // I*hhat*(ra+rb)
+      if (F.np_chem == 1) F1 = make_double2(F1.x - rho0 * enh.x, F1.y - rho0 * enh.y);
+      const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * (gaa + 2.0 * gab + gbb);
+      const double B = A - 2.0 * rho0 / c;
+      const double den = 1.0 + li * A;
+      wp = make_double2((wp.x - li * (F1.x - B * wp.x)) / den, (wp.y - li * (F1.y - B * wp.y)) / den);
+      double2 F2 = make_double2(hh * (rb.x - ra.x), hh * (rb.y - ra.y));
+      if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
+      const double den2 = 1.0 + lr * 2.0 * rho0 / c;
+      wm = make_double2((wm.x - lr * F2.x) / den2, (wm.y - lr * F2.y) / den2);
+    } else {
+      const double2 F1 = make_double2(-hh * (ra.x + rb.x), -hh * (ra.y + rb.y));
+      const double den1 = 1.0 + lr * 2.0 * rho0 / c;
+      wp = make_double2((wp.x - lr * F1.x) / den1, (wp.y - lr * F1.y) / den1);
+      double2 F2 = make_double2(-hh * (ra.y - rb.y), hh * (ra.x - rb.x));  // I*hhat*(ra-rb)
+      if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
+      const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * (gaa - gbb);
+      const double B = A - 2.0 * rho0 / c;
+      const double den = 1.0 + li * A;
+      wm = make_double2((wm.x - li * (F2.x - B * wm.x)) / den, (wm.y - li * (F2.y - B * wm.y)) / den);
+    }
+    w[1] = wp;
+    w[2] = wm;
+  } else {
+    w[1] = make_double2(0.0, 0.0);
+    w[2] = make_double2(0.0, 0.0);
+  }
+  // BC (:168-247)
+  if (F.cbc != 0.0) {
+    const double c = F.cbc;
+    double2 wp = w[3], wm = w[4];
+    if (!F.neg_bc) {
+      const double2 F1 = make_double2(-hh * (rg.y + rb.y), hh * (rg.x + rb.x));
+      const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * (+gbb) + F.phiG * rho0 * Ng * hh2 * gc;
+      const double B = A - 2.0 * rho0 / c;
+      const double den = 1.0 + li * A;
+      wp = make_double2((wp.x - li * (F1.x - B * wp.x)) / den, (wp.y - li * (F1.y - B * wp.y)) / den);
+      double2 F2 = make_double2(hh * (rg.x - rb.x), hh * (rg.y - rb.y));
+      if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
+      const double den2 = 1.0 + lr * 2.0 * rho0 / c;
+      wm = make_double2((wm.x - lr * F2.x) / den2, (wm.y - lr * F2.y) / den2);
+    } else {
+      const double2 F1 = make_double2(-hh * (rb.x + rg.x), -hh * (rb.y + rg.y));
+      const double den1 = 1.0 + lr * 2.0 * rho0 / c;
+      wp = make_double2((wp.x - lr * F1.x) / den1, (wp.y - lr * F1.y) / den1);
+      // -I*hhat*(rg - rb) = (hh*(rg-rb).y, -hh*(rg-rb).x)
+      double2 F2 = make_double2(hh * (rg.y - rb.y), -hh * (rg.x - rb.x));
+      if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
+      const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * gbb - F.phiG * Ng * hh2 * rho0 * gc;
+      const double B = A - 2.0 * rho0 / c;
+      const double den = 1.0 + li * A;
+      wm = make_double2((wm.x - li * (F2.x - B * wm.x)) / den, (wm.y - li * (F2.y - B * wm.y)) / den);
+    }
+    w[3] = wp;
+    w[4] = wm;
+  } else {
+    w[3] = make_double2(0.0, 0.0);
+    w[4] = make_double2(0.0, 0.0);
+  }
+  // AC (:250-329)
+  if (F.cac != 0.0) {
+    const double c = F.cac;
+    double2 wp = w[5], wm = w[6];
+    if (!F.neg_ac) {
+      const double2 F1 = make_double2(-hh * (rg.y + ra.y), hh * (rg.x + ra.x));
+      const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * gaa + F.phiG * Ng * hh2 * rho0 * gc;
+      const double B = A - 2.0 * rho0 / c;
+      const double den = 1.0 + li * A;
+      wp = make_double2((wp.x - li * (F1.x - B * wp.x)) / den, (wp.y - li * (F1.y - B * wp.y)) / den);
+      double2 F2 = make_double2(hh * (rg.x - ra.x), hh * (rg.y - ra.y));
+      if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
+      const double den2 = 1.0 + lr * 2.0 * rho0 / c;
+      wm = make_double2((wm.x - lr * F2.x) / den2, (wm.y - lr * F2.y) / den2);
+    } else {
+      const double2 F1 = make_double2(-hh * (ra.x + rg.x), -hh * (ra.y + rg.y));
+      const double den1 = 1.0 + lr * 2.0 * rho0 / c;
+      wp = make_double2((wp.x - lr * F1.x) / den1, (wp.y - lr * F1.y) / den1);
+      double2 F2 = make_double2(hh * (rg.y - ra.y), -hh * (rg.x - ra.x));
+      if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
+      const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * gaa - F.phiG * Ng * hh2 * rho0 * gc;
+      const double B = A - 2.0 * rho0 / c;
+      const double den = 1.0 + li * A;
+      wm = make_double2((wm.x - li * (F2.x - B * wm.x)) / den, (wm.y - li * (F2.y - B * wm.y)) / den);
+    }
+    w[5] = wp;
+    w[6] = wm;
+  } else {
+    w[5] = make_double2(0.0, 0.0);
+    w[6] = make_double2(0.0, 0.0);
+  }
+}
+
 __global__ void k_update_1s(const FieldInst *__restrict__ fi) {
   FOR_POINTS(F) {
-    const double rho0 = F.rho0, N = (double)F.N, Ng = (double)F.Ng;
-    const double li = F.lam_pl, lr = F.lam_mi;
-    const double hh = F.hhat[i];
-    const double hh2 = hh * hh;
-    const double gaa = F.gaa[i], gab = F.gab[i], gbb = F.gbb[i], gc = F.gc[i];
-    const double2 ra = F.rho[0][i], rb = F.rho[1][i];
+    double2 w[7];
+    for (int f = 0; f < 7; f++) w[f] = F.w[f][i];
     const double2 rg = F.graft ? F.rho[2][i] : make_double2(0.0, 0.0);
-    const double2 enh = F.exp_nrH[i];
-    // w+  (:58-84)
-    {
-      const double evar = (i == 0) ? 1.0 : 0.0;
-      const double2 s = cadd(cadd(ra, rg), rb);  // rhoha + rhoda + rhog + rhog_exp + rhodb
-      // I*rho0*(exp_nrH - evar) + I*hhat*s
-      const double2 u = make_double2(enh.x - evar, enh.y);
-      const double2 F1 = make_double2(-rho0 * u.y - hh * s.y, rho0 * u.x + hh * s.x);
-      const double A = rho0 / F.kappa + F.phiD * rho0 * N * hh2 * (gaa + 2.0 * gab + gbb) +
-                       (F.phiG * Ng * gc) * rho0 * hh2;
-      const double B = A - rho0 / F.kappa;
-      const double2 w = F.w[0][i];
-      const double2 num = make_double2(w.x - li * (F1.x - B * w.x), w.y - li * (F1.y - B * w.y));
-      const double den = 1.0 + li * A;
-      F.w[0][i] = make_double2(num.x / den, num.y / den);
-    }
-    // AB (:87-166)
-    if (F.cab != 0.0) {
-      const double c = F.cab;
-      double2 wp = F.w[1][i], wm = F.w[2][i];
-      if (!F.neg_ab) {
-        double2 F1 = make_double2(-hh * (ra.y + rb.y), hh * (ra.x + rb.x));  // I*hhat*(ra+rb)
-        if (F.np_chem == 1) F1 = make_double2(F1.x - rho0 * enh.x, F1.y - rho0 * enh.y);
-        const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * (gaa + 2.0 * gab + gbb);
-        const double B = A - 2.0 * rho0 / c;
-        const double den = 1.0 + li * A;
-        wp = make_double2((wp.x - li * (F1.x - B * wp.x)) / den, (wp.y - li * (F1.y - B * wp.y)) / den);
-        double2 F2 = make_double2(hh * (rb.x - ra.x), hh * (rb.y - ra.y));
-        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
-        const double den2 = 1.0 + lr * 2.0 * rho0 / c;
-        wm = make_double2((wm.x - lr * F2.x) / den2, (wm.y - lr * F2.y) / den2);
-      } else {
-        const double2 F1 = make_double2(-hh * (ra.x + rb.x), -hh * (ra.y + rb.y));
-        const double den1 = 1.0 + lr * 2.0 * rho0 / c;
-        wp = make_double2((wp.x - lr * F1.x) / den1, (wp.y - lr * F1.y) / den1);
-        double2 F2 = make_double2(-hh * (ra.y - rb.y), hh * (ra.x - rb.x));  // I*hhat*(ra-rb)
-        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
-        const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * (gaa - gbb);
-        const double B = A - 2.0 * rho0 / c;
-        const double den = 1.0 + li * A;
-        wm = make_double2((wm.x - li * (F2.x - B * wm.x)) / den, (wm.y - li * (F2.y - B * wm.y)) / den);
-      }
-      F.w[1][i] = wp;
-      F.w[2][i] = wm;
-    } else {
-      F.w[1][i] = make_double2(0.0, 0.0);
-      F.w[2][i] = make_double2(0.0, 0.0);
-    }
-    // BC (:168-247)
-    if (F.cbc != 0.0) {
-      const double c = F.cbc;
-      double2 wp = F.w[3][i], wm = F.w[4][i];
-      if (!F.neg_bc) {
-        const double2 F1 = make_double2(-hh * (rg.y + rb.y), hh * (rg.x + rb.x));
-        const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * (+gbb) + F.phiG * rho0 * Ng * hh2 * gc;
-        const double B = A - 2.0 * rho0 / c;
-        const double den = 1.0 + li * A;
-        wp = make_double2((wp.x - li * (F1.x - B * wp.x)) / den, (wp.y - li * (F1.y - B * wp.y)) / den);
-        double2 F2 = make_double2(hh * (rg.x - rb.x), hh * (rg.y - rb.y));
-        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
-        const double den2 = 1.0 + lr * 2.0 * rho0 / c;
-        wm = make_double2((wm.x - lr * F2.x) / den2, (wm.y - lr * F2.y) / den2);
-      } else {
-        const double2 F1 = make_double2(-hh * (rb.x + rg.x), -hh * (rb.y + rg.y));
-        const double den1 = 1.0 + lr * 2.0 * rho0 / c;
-        wp = make_double2((wp.x - lr * F1.x) / den1, (wp.y - lr * F1.y) / den1);
-        // -I*hhat*(rg - rb) = (hh*(rg-rb).y, -hh*(rg-rb).x)
-        double2 F2 = make_double2(hh * (rg.y - rb.y), -hh * (rg.x - rb.x));
-        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
-        const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * gbb - F.phiG * Ng * hh2 * rho0 * gc;
-        const double B = A - 2.0 * rho0 / c;
-        const double den = 1.0 + li * A;
-        wm = make_double2((wm.x - li * (F2.x - B * wm.x)) / den, (wm.y - li * (F2.y - B * wm.y)) / den);
-      }
-      F.w[3][i] = wp;
-      F.w[4][i] = wm;
-    } else {
-      F.w[3][i] = make_double2(0.0, 0.0);
-      F.w[4][i] = make_double2(0.0, 0.0);
-    }
-    // AC (:250-329)
-    if (F.cac != 0.0) {
-      const double c = F.cac;
-      double2 wp = F.w[5][i], wm = F.w[6][i];
-      if (!F.neg_ac) {
-        const double2 F1 = make_double2(-hh * (rg.y + ra.y), hh * (rg.x + ra.x));
-        const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * gaa + F.phiG * Ng * hh2 * rho0 * gc;
-        const double B = A - 2.0 * rho0 / c;
-        const double den = 1.0 + li * A;
-        wp = make_double2((wp.x - li * (F1.x - B * wp.x)) / den, (wp.y - li * (F1.y - B * wp.y)) / den);
-        double2 F2 = make_double2(hh * (rg.x - ra.x), hh * (rg.y - ra.y));
-        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
-        const double den2 = 1.0 + lr * 2.0 * rho0 / c;
-        wm = make_double2((wm.x - lr * F2.x) / den2, (wm.y - lr * F2.y) / den2);
-      } else {
-        const double2 F1 = make_double2(-hh * (ra.x + rg.x), -hh * (ra.y + rg.y));
-        const double den1 = 1.0 + lr * 2.0 * rho0 / c;
-        wp = make_double2((wp.x - lr * F1.x) / den1, (wp.y - lr * F1.y) / den1);
-        double2 F2 = make_double2(hh * (rg.y - ra.y), -hh * (rg.x - ra.x));
-        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
-        const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * gaa - F.phiG * Ng * hh2 * rho0 * gc;
-        const double B = A - 2.0 * rho0 / c;
-        const double den = 1.0 + li * A;
-        wm = make_double2((wm.x - li * (F2.x - B * wm.x)) / den, (wm.y - li * (F2.y - B * wm.y)) / den);
-      }
-      F.w[5][i] = wp;
-      F.w[6][i] = wm;
-    } else {
-      F.w[5][i] = make_double2(0.0, 0.0);
-      F.w[6][i] = make_double2(0.0, 0.0);
-    }
+    update_1s_point(F, i, F.rho[0][i], F.rho[1][i], rg, w);
+    for (int f = 0; f < 7; f++) F.w[f][i] = w[f];
   }
 }
 
@@ -351,6 +374,165 @@ __global__ void k_h_partials(const FieldInst *__restrict__ fi, double2 *__restri
     }
     __syncthreads();
   }
+}
+
+// ---------------------------------------------------------------------------
+// mixed precision: fields in k-space, packed transforms of real pairs
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long neg_k(const FieldInst &F, long long i) {
+  const int nx = F.nx, ny = F.ny;
+  const long long ix = i % nx, iy = (i / nx) % ny, iz = i / ((long long)nx * ny);
+  const long long jx = ix ? nx - ix : 0, jy = iy ? ny - iy : 0, jz = iz ? F.nz - iz : 0;
+  return jx + (long long)nx * (jy + (long long)ny * jz);
+}
+
+// zs = hhat * (w_A + i w_B), the packed transform of the two smeared fields.
+__device__ __forceinline__ double2 smear_pack(const FieldInst &F, long long i, const double2 *w) {
+  double2 wa, wb, wg;
+  assemble_point(F, w, wa, wb, wg);
+  const double hh = F.hhat[i];
+  return make_double2(hh * (wa.x - wb.y), hh * (wa.y + wb.x));
+}
+
+__global__ void k_mix_smear(const FieldInst *__restrict__ fi) {
+  FOR_POINTS(F) {
+    double2 w[7];
+    for (int f = 0; f < 7; f++) w[f] = F.w[f][i];
+    F.zs[i] = smear_pack(F, i, w);
+  }
+}
+
+// 1S update on the k-space fields; the two density transforms come from one
+// packed transform Z of rho_A + i rho_B:
+//   rho_A(k) = (Z(k) + conj Z(-k)) / 2,  rho_B(k) = (Z(k) - conj Z(-k)) / (2i).
+__global__ void k_mix_update(const FieldInst *__restrict__ fi) {
+  FOR_POINTS(F) {
+    const double2 Z = F.zr[i], Zm = F.zr[neg_k(F, i)];
+    const double2 ra = make_double2(0.5 * (Z.x + Zm.x), 0.5 * (Z.y - Zm.y));
+    const double2 rb = make_double2(0.5 * (Z.y + Zm.y), 0.5 * (Zm.x - Z.x));
+    double2 w[7];
+    for (int f = 0; f < 7; f++) w[f] = F.w[f][i];
+    update_1s_point(F, i, ra, rb, make_double2(0.0, 0.0), w);
+    for (int f = 0; f < 7; f++) F.w[f][i] = w[f];
+    F.zs[i] = smear_pack(F, i, w);
+  }
+}
+
+// After the inverse transform zs = smwa + i smwb (real space): Boltzmann
+// factors for the FP32 sweep.
+__global__ void k_mix_boltzmann(const FieldInst *__restrict__ fi) {
+  FOR_POINTS(F) {
+    const double2 s = F.zs[i];
+    F.E32[i] = make_float2((float)exp(-s.x), (float)exp(-s.y));
+  }
+}
+
+// Q from the plane sums of q_{N-1} and its exponent; factor = nD / Q / V.
+__global__ void k_mix_q_finalize(const FieldInst *__restrict__ fi, int ninst) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ninst) return;
+  const FieldInst &F = fi[t];
+  double s = 0.0;
+  const double *pq = F.part64 + (long long)(F.N - 1) * F.nz;  // plane sums of q_{N-1}
+  for (int z = 0; z < F.nz; z++) s += pq[z];
+  s = ldexp(s, F.K[F.N - 1]);
+  for (int d = 0; d < 3; d++) s *= F.dx[d];
+  const double Q = s / F.V;
+  F.scal[kQd] = make_double2(Q, 0.0);
+  F.scal[kFactor] = make_double2(F.nD / Q / F.V, 0.0);
+}
+
+// rho_A, rho_B = acc * e^{+smw} * factor packed into zr (and optionally kept
+// as complex arrays for scft_get_density).
+__global__ void k_mix_rho_pack(const FieldInst *__restrict__ fi, int keep) {
+  FOR_POINTS(F) {
+    const double f = F.scal[kFactor].x;
+    const double2 s = F.zs[i];
+    const double ra = F.acc64[0][i] * (exp(s.x) * f);
+    const double rb = F.acc64[1][i] * (exp(s.y) * f);
+    F.zr[i] = make_double2(ra, rb);
+    if (keep) {
+      F.rho[0][i] = make_double2(ra, 0.0);
+      F.rho[1][i] = make_double2(rb, 0.0);
+    }
+  }
+}
+
+// calc_H field terms by Parseval on the k-space fields:
+//   int f g dr = V sum_k f(k) g(-k)  (transforms scaled by 1/M).
+// out[(inst*4 + part)*gridDim.x + blk]; the host multiplies by V.
+__global__ void k_mix_h_partials(const FieldInst *__restrict__ fi, double2 *__restrict__ out) {
+  __shared__ double2 red[32];
+  const FieldInst &F = fi[blockIdx.y];
+  double2 s[4];
+  for (int k = 0; k < 4; k++) s[k] = make_double2(0.0, 0.0);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < F.M;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long mi = neg_k(F, i);
+    const double2 w = F.w[0][i], wm = F.w[0][mi];
+    const double2 ww = cmul(w, wm);
+    // rho0/(2 kappa) w w  + I rho0 rho_exp(-k) w  (- I rho0 w(0) at k = 0)
+    const double2 re = F.exp_nrH[mi];
+    const double2 rw = cmul(re, w);
+    double2 t = make_double2(ww.x * F.rho0 / F.kappa / 2.0 - F.rho0 * rw.y,
+                             ww.y * F.rho0 / F.kappa / 2.0 + F.rho0 * rw.x);
+    if (i == 0) t = make_double2(t.x + F.rho0 * w.y, t.y - F.rho0 * w.x);
+    s[0] = cadd(s[0], t);
+    const double chis[3] = {F.cbc, F.cac, F.cab};
+    const int negs[3] = {F.neg_bc, F.neg_ac, F.neg_ab};
+    const int idx[3] = {3, 5, 1};
+    for (int k = 0; k < 3; k++) {
+      if (chis[k] == 0.0) continue;
+      const double2 q = cadd(cmul(F.w[idx[k]][i], F.w[idx[k]][mi]), cmul(F.w[idx[k] + 1][i], F.w[idx[k] + 1][mi]));
+      const double f = F.rho0 / chis[k] * (negs[k] ? -1.0 : 1.0);
+      s[k + 1] = cadd(s[k + 1], make_double2(q.x * f, q.y * f));
+    }
+  }
+  for (int k = 0; k < 4; k++) {
+    double2 v = s[k];
+    for (int o = 16; o > 0; o >>= 1) {
+      v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+      v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+    }
+    const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) red[w] = v;
+    __syncthreads();
+    if (w == 0) {
+      const int nw = (blockDim.x + 31) >> 5;
+      v = l < nw ? red[l] : make_double2(0.0, 0.0);
+      for (int o = 16; o > 0; o >>= 1) {
+        v.x += __shfl_down_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_down_sync(0xffffffffu, v.y, o);
+      }
+      if (l == 0) out[((long long)blockIdx.y * 4 + k) * gridDim.x + blockIdx.x] = v;
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_mix_smear(const FieldInst *fi, int ninst, int blocks, cudaStream_t st) {
+  k_mix_smear<<<dim3(blocks, ninst), 256, 0, st>>>(fi);
+  return cudaGetLastError();
+}
+cudaError_t launch_mix_update(const FieldInst *fi, int ninst, int blocks, cudaStream_t st) {
+  k_mix_update<<<dim3(blocks, ninst), 256, 0, st>>>(fi);
+  return cudaGetLastError();
+}
+cudaError_t launch_mix_boltzmann(const FieldInst *fi, int ninst, int blocks, cudaStream_t st) {
+  k_mix_boltzmann<<<dim3(blocks, ninst), 256, 0, st>>>(fi);
+  return cudaGetLastError();
+}
+cudaError_t launch_mix_q_finalize(const FieldInst *fi, int ninst, cudaStream_t st) {
+  k_mix_q_finalize<<<(ninst + 63) / 64, 64, 0, st>>>(fi, ninst);
+  return cudaGetLastError();
+}
+cudaError_t launch_mix_rho_pack(const FieldInst *fi, int ninst, int blocks, int keep, cudaStream_t st) {
+  k_mix_rho_pack<<<dim3(blocks, ninst), 256, 0, st>>>(fi, keep);
+  return cudaGetLastError();
+}
+cudaError_t launch_mix_h_partials(const FieldInst *fi, int ninst, int blocks, double2 *out, cudaStream_t st) {
+  k_mix_h_partials<<<dim3(blocks, ninst), 256, 0, st>>>(fi, out);
+  return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------

@@ -1,0 +1,206 @@
+// kernels_mixed.cu -- propagator sweep of the mixed-precision form.
+//
+// Mean-field fields are real, so q_n and qdag_n are real and the bond kernel
+// g(k) = exp(-k^2/6) is real and even: the convolution maps real arrays to
+// real arrays.  One FP32 complex array z = q + i*qdag therefore carries both
+// propagators through a single transform per step (the recurrence of
+// code/diblock_discrete.cpp:31-85, for q and qdag at once).  The xy-plane pass
+// applies e^{-w} separately to the real part (q, field of step n for q) and
+// the imaginary part (qdag), which is exact for real fields.
+//
+// Mean in FP64: the plane pass writes exact (FP64) plane sums of what it
+// stores; the next step's column pass drops the FP32 k = 0 coefficient and the
+// plane pass adds the FP64 mean back, as a two-float constant, before the
+// Boltzmann factor.  Rounding of the mean mode would otherwise be one
+// coherent error per step that does not average over the grid.
+//
+// Range: each step is rescaled by a power of two chosen from that mean (lag 1,
+// so no extra synchronisation), which is exact in floating point.  Integer
+// exponents K[p][n] (q_true = q_stored * 2^K) are kept per instance; the
+// density terms q_j qdag_{N-1-j} and Q are accumulated in FP64 with the
+// exponents folded back in.
+//
+// Density terms are accumulated as in the FP64 kernel: for n > (N-1)/2 the
+// terms j = n and j = N-1-n pair the current step with the stored half of
+// the history; the middle term of odd N is formed in place at n = (N-1)/2.
+#include "fft_core.cuh"
+#include "inst.h"
+#include "launch.h"
+#include "prop_launch.h"
+
+namespace scft {
+
+template <int MAXV>
+__global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restrict__ jobs,
+                                                       const MixInst *__restrict__ insts,
+                                                       const DevGeom *__restrict__ geoms,
+                                                       const float2 *__restrict__ twbuf, int n) {
+  typedef float2 C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double s_red[2][32];
+  __shared__ int s_exp[2];
+  const PropJob jb = jobs[blockIdx.x];
+  const MixInst &P = insts[jb.inst];
+  const int N = P.N, Na = P.Na;
+  if (n >= N) return;
+  const DevGeom g = geoms[P.geom];
+  const int E = g.nx * g.ny;
+  const int nz = g.nz;
+  C *plane = reinterpret_cast<C *>(smem_raw);
+  C *twx = plane + E;
+  C *twy = twx + g.nx;
+  const long long zoff = (long long)jb.z * E;
+  const long long M = g.M;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // previous step's means (FP64, same summation order in every CTA) and the
+  // power-of-two exponents chosen from them
+  __shared__ double s_mu[2];
+  if (warp == 0) {
+    double a = 0.0, b = 0.0;
+    if (n > 0) {
+      const double *pq = P.part + (long long)(n - 1) * nz;
+      const double *pd = P.part + (long long)(N + n - 1) * nz;
+      for (int z = lane; z < nz; z += 32) {
+        a += pq[z];
+        b += pd[z];
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+      const double ma = a / (double)M, mb = b / (double)M;
+      int ea = 0, eb = 0;
+      if (n > 0 && isfinite(ma) && ma > 0.0) frexp(ma, &ea);
+      if (n > 0 && isfinite(mb) && mb > 0.0) frexp(mb, &eb);
+      s_exp[0] = ea;
+      s_exp[1] = eb;
+      s_mu[0] = ma;
+      s_mu[1] = mb;
+    }
+  }
+  load_tw<float>(twx, twbuf, g.ax[0]);
+  load_tw<float>(twy, twbuf, g.ax[1]);
+  const C *Ew = P.E + zoff;
+  C *work = P.work + zoff;
+  const bool useA_q = (Na > 0 && n < Na);
+  const bool useA_d = !(n <= N - Na - 1);
+  if (n == 0) {
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      const C v = Ew[e];
+      plane[e] = make_float2(useA_q ? v.x : v.y, useA_d ? v.x : v.y);
+    }
+    __syncthreads();
+  } else {
+    for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = work[e];
+    __syncthreads();
+    fft_plane<float, +1, MAXV>(plane, g, twx, twy);
+  }
+  const int eq = s_exp[0], ed = s_exp[1];
+  const int Kq = (n == 0) ? 0 : P.K[n - 1] + eq;
+  const int Kd = (n == 0) ? 0 : P.K[N + n - 1] + ed;
+  if (n > 0) {
+    // q = (conv + mean) * e^{-w} * 2^{-e}, the mean as a two-float constant
+    const float sq = ldexpf(1.0f, -eq), sd = ldexpf(1.0f, -ed);
+    const double mq = s_mu[0], md = s_mu[1];
+    const float mq_hi = (float)mq, mq_lo = (float)(mq - (double)mq_hi);
+    const float md_hi = (float)md, md_lo = (float)(md - (double)md_hi);
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      const C v = Ew[e];
+      const C z = plane[e];
+      const float eq_ = useA_q ? v.x : v.y, ed_ = useA_d ? v.x : v.y;
+      const float uq = fmaf(z.x, eq_, fmaf(mq_hi, eq_, mq_lo * eq_));
+      const float ud = fmaf(z.y, ed_, fmaf(md_hi, ed_, md_lo * ed_));
+      plane[e] = make_float2(uq * sq, ud * sd);
+    }
+  }
+  if (jb.z == 0 && threadIdx.x == 0) {
+    P.K[n] = Kq;
+    P.K[N + n] = Kd;
+  }
+  // history (first half) and exact plane sums (mean of the next step, Q)
+  double aq = 0.0, ad = 0.0;
+  C *hst = P.hist + (long long)n * M + zoff;
+  const bool keep = (n <= P.hmax);
+  for (int e = threadIdx.x; e < E; e += blockDim.x) {
+    const C z = plane[e];
+    aq += (double)z.x;
+    ad += (double)z.y;
+    if (keep) hst[e] = z;
+  }
+  // density terms
+  const int m2 = N - 1 - n;
+  if (m2 < n) {
+    const C *o = P.hist + (long long)m2 * M + zoff;
+    const double f1 = ldexp(1.0, Kq + P.K[N + m2]);  // q_n * qdag_{m2}
+    const double f2 = ldexp(1.0, P.K[m2] + Kd);      // q_{m2} * qdag_n
+    double *a1 = P.acc[n < Na ? 0 : 1] + zoff;
+    double *a2 = P.acc[m2 < Na ? 0 : 1] + zoff;
+    if (a1 == a2) {
+      for (int e = threadIdx.x; e < E; e += blockDim.x) {
+        const C z = plane[e], h = o[e];
+        a1[e] += (double)z.x * (double)h.y * f1 + (double)h.x * (double)z.y * f2;
+      }
+    } else {
+      for (int e = threadIdx.x; e < E; e += blockDim.x) {
+        const C z = plane[e], h = o[e];
+        a1[e] += (double)z.x * (double)h.y * f1;
+        a2[e] += (double)h.x * (double)z.y * f2;
+      }
+    }
+  } else if (m2 == n) {
+    const double f = ldexp(1.0, Kq + Kd);
+    double *a1 = P.acc[n < Na ? 0 : 1] + zoff;
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      const C z = plane[e];
+      a1[e] += (double)z.x * (double)z.y * f;
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    aq += __shfl_down_sync(0xffffffffu, aq, o);
+    ad += __shfl_down_sync(0xffffffffu, ad, o);
+  }
+  if (lane == 0) {
+    s_red[0][warp] = aq;
+    s_red[1][warp] = ad;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    aq = lane < nw ? s_red[0][lane] : 0.0;
+    ad = lane < nw ? s_red[1][lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      aq += __shfl_down_sync(0xffffffffu, aq, o);
+      ad += __shfl_down_sync(0xffffffffu, ad, o);
+    }
+    if (lane == 0) {
+      P.part[(long long)n * nz + jb.z] = aq;
+      P.part[(long long)(N + n) * nz + jb.z] = ad;
+    }
+  }
+  if (n == N - 1) return;
+  __syncthreads();
+  fft_plane<float, -1, MAXV>(plane, g, twx, twy);
+  for (int e = threadIdx.x; e < E; e += blockDim.x) work[e] = plane[e];
+}
+
+template <int MAXV>
+static cudaError_t launch_mix_t(const LaunchShape &ls, const PropJob *jobs, int njobs, const MixInst *insts,
+                                const DevGeom *geoms, const void *tw, int n, cudaStream_t st) {
+  auto kfn = k_mix_prop_plane<MAXV>;
+  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, ls.smem);
+  if (e != cudaSuccess) return e;
+  kfn<<<njobs, ls.threads, ls.smem, st>>>(jobs, insts, geoms, reinterpret_cast<const float2 *>(tw), n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mix_prop_plane(const LaunchShape &ls, const PropJob *jobs, int njobs, const MixInst *insts,
+                                  const DevGeom *geoms, const void *tw, int n, cudaStream_t st) {
+  if (njobs <= 0) return cudaSuccess;
+  if (ls.maxv <= 8) return launch_mix_t<8>(ls, jobs, njobs, insts, geoms, tw, n, st);
+  if (ls.maxv <= 16) return launch_mix_t<16>(ls, jobs, njobs, insts, geoms, tw, n, st);
+  return launch_mix_t<32>(ls, jobs, njobs, insts, geoms, tw, n, st);
+}
+
+}  // namespace scft

@@ -21,4 +21,13 @@ cudaError_t launch_density(const FieldInst *fi, int ninst, int blocks, cudaStrea
 cudaError_t launch_update_1s(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
 cudaError_t launch_h_partials(const FieldInst *fi, int ninst, int blocks, double2 *out, cudaStream_t st);
 
+cudaError_t launch_mix_prop_plane(const LaunchShape &ls, const PropJob *jobs, int njobs, const MixInst *insts,
+                                  const DevGeom *geoms, const void *tw, int n, cudaStream_t st);
+cudaError_t launch_mix_smear(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
+cudaError_t launch_mix_update(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
+cudaError_t launch_mix_boltzmann(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
+cudaError_t launch_mix_q_finalize(const FieldInst *fi, int ninst, cudaStream_t st);
+cudaError_t launch_mix_rho_pack(const FieldInst *fi, int ninst, int blocks, int keep, cudaStream_t st);
+cudaError_t launch_mix_h_partials(const FieldInst *fi, int ninst, int blocks, double2 *out, cudaStream_t st);
+
 }  // namespace scft

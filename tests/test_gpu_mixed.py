@@ -1,0 +1,128 @@
+"""The mixed-precision form (FP32 packed propagators, FP64 k-space fields,
+reductions, log Q and H) against the plain FP64 method on the same inputs.
+
+Tolerances written here are the measured FP32 floor of this form on small
+grids (N <= 64): H relative 2e-5, Q relative 2e-5, densities 2e-5 (max over
+the grid).  The error is coherent: the per-step FP32 rounding of the dominant
+low-k modes repeats every step, so log Q drifts by ~N * 1e-7 (an FP32
+transform in numpy shows the same ~1e-6 at N = 32).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+H_TOL = 2e-5
+RHO_TOL = 2e-5
+Q_TOL = 2e-5
+
+
+@pytest.fixture(scope="module")
+def scft():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.fail("gpu tests need a CUDA device")
+    import scft as S
+
+    assert S.mixed_available()
+    return S
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+def run_pair(S, params, fields, iters):
+    out = {}
+    for prec in (S.PREC_FP64, S.PREC_MIXED):
+        ps = []
+        for p in params:
+            q = S.Params.from_buffer_copy(p)
+            q.precision = prec
+            ps.append(q)
+        with S.Context(ps) as ctx:
+            for k, f in enumerate(fields):
+                ctx.set_fields(k, f)
+            ctx.calc_poly_density()
+            H = [ctx.calc_H()]
+            for _ in range(iters):
+                ctx.update_1s(1)
+                H.append(ctx.calc_H())
+            dens = [ctx.density(k) for k in range(len(params))]
+            flds = [ctx.get_fields(k) for k in range(len(params))]
+        out[prec] = (np.array(H), dens, flds)
+    return out[S.PREC_FP64], out[S.PREC_MIXED]
+
+
+def test_mixed_matches_fp64_single_plate(scft):
+    from scft.workloads import plate_params, seeded_fields
+
+    p = plate_params(10.0, N=32, grid=(32, 32, 32))
+    (H64, d64, _), (H32, d32, _) = run_pair(scft, [p], [seeded_fields(p, 3)], 10)
+    assert np.abs(H32[:, 0, 0] - H64[:, 0, 0]).max() <= H_TOL * np.abs(H64[:, 0, 0]).max()
+    assert np.abs(H32[:, 0, 2] - H64[:, 0, 2]).max() <= Q_TOL * np.abs(H64[:, 0, 2]).max()
+    assert rel(d32[0][0].real, d64[0][0].real) < RHO_TOL
+    assert rel(d32[0][1].real, d64[0][1].real) < RHO_TOL
+
+
+def test_mixed_uneven_batch_matches_fp64(scft):
+    """Different grids (incl. 5 and 3 factors), N odd and even, one plate or none."""
+    from scft.workloads import plate_params, seeded_fields
+
+    params = [plate_params(0.0, N=21, grid=(24, 20, 16)),
+              plate_params(30.0, N=32, grid=(32, 32, 32)),
+              plate_params(90.0, N=16, grid=(16, 24, 30), centers=())]
+    fields = [seeded_fields(p, 10 + k) for k, p in enumerate(params)]
+    (H64, d64, _), (H32, d32, _) = run_pair(scft, params, fields, 6)
+    for k in range(len(params)):
+        assert np.abs(H32[:, k, 0] - H64[:, k, 0]).max() <= H_TOL * np.abs(H64[:, k, 0]).max()
+        assert rel(d32[k][0].real, d64[k][0].real) < RHO_TOL
+        assert rel(d32[k][1].real, d64[k][1].real) < RHO_TOL
+
+
+def test_mixed_field_round_trip_and_fields_match(scft):
+    from scft.workloads import plate_params, seeded_fields
+
+    p = plate_params(10.0, N=16, grid=(16, 16, 16))
+    f = seeded_fields(p, 4)
+    q = scft.Params.from_buffer_copy(p)
+    q.precision = scft.PREC_MIXED
+    with scft.Context(q) as ctx:
+        ctx.set_fields(0, f)
+        g = ctx.get_fields(0)
+    assert rel(g["wabm"], f["wabm"]) < 1e-13
+    assert np.abs(g["wpl"]).max() < 1e-14
+    (_, _, f64), (_, _, f32) = run_pair(scft, [p], [f], 5)
+    for name in ("wpl", "wabp", "wabm"):
+        assert rel(f32[0][name], f64[0][name]) < 5e-5, name
+
+
+def test_mixed_rejects_complex_fields(scft):
+    from scft.workloads import plate_params
+
+    p = plate_params(0.0, N=8, grid=(8, 8, 8), precision=scft.PREC_MIXED)
+    rng = np.random.default_rng(0)
+    with scft.Context(p) as ctx:
+        bad = {"wabm": rng.standard_normal((8, 8, 8)) + 0.1j * rng.standard_normal((8, 8, 8))}
+        with pytest.raises(scft.ScftError) as e:
+            ctx.set_fields(0, bad)
+        assert e.value.code == scft.ERR_COMPLEX
+
+
+def test_mixed_range_normalisation_long_chain(scft):
+    """N=200 on a resolved grid (dx ~ 0.5 b) with fields strong enough that Q
+    is ~1e53, far outside FP32's range: the power-of-two rescaling keeps the
+    FP32 sweep in range.  Bars for this extreme case: Q 1e-4 (on the same
+    fields), H 1e-5 relative."""
+    from scft.workloads import plate_params, seeded_fields
+
+    p = plate_params(20.0, N=200, fA=0.4, chiN=30.0, grid=(32, 32, 32), box_rg=(2.8, 2.8, 2.8),
+                     lam_pl=0.001, lam_mi=0.0002)
+    f = seeded_fields(p, 5)
+    f["wabm"] = f["wabm"] * 10.0
+    (H64, d64, _), (H32, d32, _) = run_pair(scft, [p], [f], 1)
+    assert np.isfinite(H64).all() and H64[0, 0, 2] > 1e45
+    assert abs(H32[0, 0, 2] - H64[0, 0, 2]) <= 1e-4 * abs(H64[0, 0, 2])  # same fields
+    assert np.abs(H32[:, 0, 0] - H64[:, 0, 0]).max() <= 1e-5 * np.abs(H64[:, 0, 0]).max()
+    assert rel(d32[0][0].real, d64[0][0].real) < 1e-3
