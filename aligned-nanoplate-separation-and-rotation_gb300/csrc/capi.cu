@@ -24,6 +24,8 @@ void ctx_override_nD(scft_ctx *c, int k, double nD);
 void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
                       double *bytes_col);
 int error_code(const std::exception &e);
+int noalloc_diblock(const int *Nx, const double *L, int Nda, int Ndb, double nD, const double *smwa,
+                    const double *smwb, double *rhoda, double *rhodb, double *Q, void *stream, std::string &msg);
 }  // namespace scft
 
 static thread_local std::string g_err;
@@ -203,6 +205,17 @@ int scft_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   if (int s = check_ctx(c, 0)) return s;
   if (reps < 1 || !ms_plane || !bytes_plane || !ms_col || !bytes_col) return fail(SCFT_ERR_ARG, "bad arguments");
   API_BODY(scft::ctx_profile_step(c, reps, ms_plane, bytes_plane, ms_col, bytes_col));
+  return SCFT_OK;
+}
+
+// No allocation: see csrc/noalloc.cu for the scratch array, its limit and the
+// first-call set-up.
+int scft_diblock_density_noalloc(const int Nx[3], const double L[3], int Nda, int Ndb, double nD,
+                                 const double *smwa, const double *smwb, double *rhoda, double *rhodb, double *Q,
+                                 void *stream) {
+  std::string msg;
+  const int st = scft::noalloc_diblock(Nx, L, Nda, Ndb, nD, smwa, smwb, rhoda, rhodb, Q, stream, msg);
+  if (st != SCFT_OK) return fail(st, msg);
   return SCFT_OK;
 }
 

@@ -25,7 +25,7 @@ EXPORTS = ("scft_last_error", "scft_version", "scft_create", "scft_destroy", "sc
            "scft_set_fields", "scft_get_fields", "scft_calc_poly_density", "scft_update_1s",
            "scft_calc_H", "scft_get_density", "scft_get_smeared", "scft_diblock_density",
            "scft_homopolymer_density", "scft_fft3d", "scft_sync", "scft_get_stream", "scft_launch_count",
-           "scft_profile_step")
+           "scft_profile_step", "scft_diblock_density_noalloc")
 
 
 class ScftError(RuntimeError):
@@ -97,6 +97,8 @@ def load(path: str | None = None):
     lib.scft_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
     lib.scft_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
     lib.scft_profile_step.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
+    lib.scft_diblock_density_noalloc.argtypes = [ctypes.POINTER(ctypes.c_int), dp, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_double, vp, vp, vp, vp, vp, vp]
     _lib = lib
     return lib
 

@@ -138,6 +138,27 @@ int scft_diblock_density(scft_ctx *ctx, int inst, const double *smwa, const doub
 int scft_homopolymer_density(scft_ctx *ctx, int inst, const double *W, int N, double nK,
                              double *rho, double *Q);
 
+/* The same computation as scft_diblock_density (FP64 method) for callers that
+ * cannot allocate GPU memory: code running while a stream is captured into a
+ * CUDA graph in global capture mode (cudaMalloc is refused there), code whose
+ * device memory belongs to another framework's pool allocator, and services
+ * with a fixed memory budget.  No counterpart in the reference.
+ *
+ * All pointers except Nx and L are DEVICE pointers owned by the caller:
+ * smwa, smwb (inputs) and rhoda, rhodb (outputs) hold M complex values each,
+ * Q receives 2 doubles; nD is the number of chains (the reference's nD).
+ * Work is queued on `stream` (a cudaStream_t, NULL for the default stream)
+ * and the call returns without synchronising.  Nothing is allocated: the
+ * scratch is one file-scope device array of 64 MiB that every GPU loading
+ * libscft holds until exit, enough for about
+ * M * (200 + 32 * ((Nda + Ndb - 1)/2 + 1)) bytes (32^3 grid up to N ~ 64);
+ * larger problems are rejected with SCFT_ERR_ARG.  The first call on a device
+ * looks up the array's device address (make that call before any stream
+ * capture).  Calls share the array: calls that overlap on the GPU race. */
+int scft_diblock_density_noalloc(const int Nx[3], const double L[3], int Nda, int Ndb, double nD,
+                                 const double *smwa, const double *smwb, double *rhoda, double *rhodb,
+                                 double *Q, void *stream);
+
 /* 3-D FFT of `count` arrays of instance inst's grid (host buffers, in place):
  * sign -1 forward (scaled 1/M), +1 backward (unscaled). */
 int scft_fft3d(scft_ctx *ctx, int inst, double *data, int count, int sign);
