@@ -437,10 +437,10 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
     I.E32 = dalloc<float2>(c, M);
     I.work32 = dalloc<float2>(c, M);
     I.hist32 = dalloc<float2>(c, (size_t)M * (I.hmax + 1));
-    I.acc64[0] = dalloc<double>(c, M);
-    I.acc64[1] = dalloc<double>(c, M);
+    I.acc32[0] = dalloc<float>(c, M);
+    I.acc32[1] = dalloc<float>(c, M);
     I.part = dalloc<double>(c, (size_t)2 * I.N * g.nz);
-    I.K = dalloc<int>(c, (size_t)2 * I.N);
+    I.K = dalloc<int>(c, (size_t)2 * I.N + 1);
     std::vector<float> h32(M);
     for (long long i = 0; i < M; i++) h32[i] = (float)(1.0 - pb[i]);
     I.h32 = dupload(c, h32);
@@ -582,8 +582,8 @@ void build_jobs(scft_ctx *c) {
     F.zr = I.zr;
     F.zs = I.zs;
     F.E32 = I.E32;
-    F.acc64[0] = I.acc64[0];
-    F.acc64[1] = I.acc64[1];
+    F.acc32[0] = I.acc32[0];
+    F.acc32[1] = I.acc32[1];
     F.K = I.K;
     F.part64 = I.part;
 
@@ -627,8 +627,8 @@ void build_jobs(scft_ctx *c) {
       X.work = I.work32;
       X.hist = I.hist32;
       X.E = I.E32;
-      X.acc[0] = I.acc64[0];
-      X.acc[1] = I.acc64[1];
+      X.acc[0] = I.acc32[0];
+      X.acc[1] = I.acc32[1];
       X.part = I.part;
       X.K = I.K;
     }
@@ -739,6 +739,9 @@ void build_jobs(scft_ctx *c) {
           c->prop_cj_count[s2] = inst_cj_end[oi];
         }
     c->shp_mix = choose_shape(emax_plane, sizeof(float2), (nxy_max + 32) * sizeof(float2));
+    c->all64 = 1;
+    for (auto &I : c->inst)
+      if (I.p.Nx[0] != 64 || I.p.Nx[1] != 64 || I.p.Nx[2] != 64) c->all64 = 0;
     c->shp_col32 = choose_shape(emax_col, sizeof(float2), (nz_max + 32) * sizeof(float2));
   }
   c->d_prop_pj = dupload(c, ppj);
@@ -911,14 +914,23 @@ void seq_mix_sweep(scft_ctx *c) {
   const int n = (int)c->inst.size();
   cudaStream_t st = c->st;
   for (auto &I : c->inst) {
-    CK(cudaMemsetAsync(I.acc64[0], 0, sizeof(double) * I.M, st));
-    CK(cudaMemsetAsync(I.acc64[1], 0, sizeof(double) * I.M, st));
+    CK(cudaMemsetAsync(I.acc32[0], 0, sizeof(float) * I.M, st));
+    CK(cudaMemsetAsync(I.acc32[1], 0, sizeof(float) * I.M, st));
   }
-  LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[0], c->d_mi, c->d_geoms, c->d_tw32, 0, st));
-  for (int s = 1; s < c->nmax; s++) {
-    LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw32, 3, 1, st));
-    LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_geoms, c->d_tw32, s,
+  if (c->all64) {
+    LK(launch_mix_plane64(c->d_prop_pj, c->prop_pj_count[0], c->d_mi, c->d_tw32_64, 0, st));
+    for (int s = 1; s < c->nmax; s++) {
+      LK(launch_mix_col64(c->d_prop_cj, c->prop_cj_count[s], c->d_tw32_64, 64, 64, st));
+      LK(launch_mix_plane64(c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_tw32_64, s, st));
+    }
+  } else {
+    LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[0], c->d_mi, c->d_geoms, c->d_tw32, 0,
                              st));
+    for (int s = 1; s < c->nmax; s++) {
+      LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw32, 3, 1, st));
+      LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_geoms, c->d_tw32, s,
+                               st));
+    }
   }
   LK(launch_mix_q_finalize(c->d_fi, n, st));
 }
@@ -988,6 +1000,7 @@ void ctx_create(scft_ctx *c, const scft_params *params, int n_inst) {
   std::vector<float2> tw32(tw.size());
   for (size_t t = 0; t < tw.size(); t++) tw32[t] = make_float2((float)tw[t].x, (float)tw[t].y);
   c->d_tw32 = dupload(c, tw32);
+  if (off.count(64)) c->d_tw32_64 = static_cast<float2 *>(c->d_tw32) + off[64];
   c->d_geoms = dupload(c, c->geoms);
   for (auto &I : c->inst) setup_plates(c, I);
   build_jobs(c);
@@ -1052,7 +1065,9 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   CK(cudaEventCreate(&e2));
   CK(cudaEventRecord(e0, c->st));
   for (int r = 0; r < reps; r++) {
-    if (c->mixed)
+    if (c->mixed && c->all64)
+      LK(launch_mix_plane64(c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_tw32_64, s, c->st));
+    else if (c->mixed)
       LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_geoms, c->d_tw32, s,
                                c->st));
     else
@@ -1061,7 +1076,9 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   }
   CK(cudaEventRecord(e1, c->st));
   for (int r = 0; r < reps; r++) {
-    if (c->mixed)
+    if (c->mixed && c->all64)
+      LK(launch_mix_col64(c->d_prop_cj, c->prop_cj_count[s], c->d_tw32_64, 64, 64, c->st));
+    else if (c->mixed)
       LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw32, 3, 1, c->st));
     else
       LK(launch_col_fft<double>(c->shp_col, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw64, 2, 1,
@@ -1080,8 +1097,8 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
     if (I.N <= s) continue;
     if (I.mixed) {
       // plane: read z, E (8 B each), stored pair (8 B), write z (8 B), RMW of
-      // the FP64 accumulators A and B (2 x 16 B); column: read + write z, g table
-      bp += I.M * (4.0 * sizeof(float2) + 4.0 * sizeof(double));
+      // the FP32 accumulators A and B (2 x 8 B); column: read + write z, h table
+      bp += I.M * (4.0 * sizeof(float2) + 4.0 * sizeof(float));
       bc += I.M * (2.0 * sizeof(float2) + sizeof(float));
     } else {
       const double props = I.single ? 1.0 : 2.0;

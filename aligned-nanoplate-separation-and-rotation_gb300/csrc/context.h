@@ -44,7 +44,7 @@ struct Instance {
   int mixed = 0;
   double2 *zr = nullptr, *zs = nullptr;
   float2 *E32 = nullptr, *work32 = nullptr, *hist32 = nullptr;
-  double *acc64[2] = {};
+  float *acc32[2] = {};
   double *part = nullptr;
   int *K = nullptr;
   float *h32 = nullptr;  // 1 - g(k), FP32
@@ -86,6 +86,8 @@ struct scft_ctx {
   int gblocks = 0;
   // mixed precision
   int mixed = 0;
+  int all64 = 0;         // every instance is 64^3: specialised propagator kernels
+  void *d_tw32_64 = nullptr;  // the 64-point twiddle table inside d_tw32
   void *d_tw32 = nullptr;
   scft::MixInst *d_mi = nullptr;
   scft::PropJob *d_mix_pj = nullptr;

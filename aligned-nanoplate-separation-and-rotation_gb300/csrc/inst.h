@@ -42,9 +42,9 @@ struct MixInst {
   float2 *work;    // z = q + i qdag of the current step
   float2 *hist;    // steps 0..hmax
   const float2 *E; // (e^{-smwa}, e^{-smwb})
-  double *acc[2];  // density sums for A and B, FP64
+  float *acc[2];   // density sums for A and B, scaled by 2^-K[2N]
   double *part;    // [2][N][nz] plane sums of the stored q, qdag (FP64)
-  int *K;          // [2][N] power-of-two exponents
+  int *K;          // [2][N] power-of-two exponents, then K[2N] = reference exponent of acc
 };
 
 struct PropJob {
@@ -81,8 +81,8 @@ struct FieldInst {
   double2 *zr;         // rho_A + i rho_B (real space), then its transform
   double2 *zs;         // hhat*(w_A + i w_B) (k-space), then smwa + i smwb (real space)
   float2 *E32;         // (e^{-smwa}, e^{-smwb})
-  double *acc64[2];
-  int *K;              // [2][N]
+  float *acc32[2];     // density sums, scaled by 2^-K[2N]
+  int *K;              // [2][N] + 1
   double *part64;      // [2][N][nz] plane sums of the stored propagators
 };
 

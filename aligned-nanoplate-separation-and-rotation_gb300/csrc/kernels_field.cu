@@ -446,10 +446,10 @@ __global__ void k_mix_q_finalize(const FieldInst *__restrict__ fi, int ninst) {
 // as complex arrays for scft_get_density).
 __global__ void k_mix_rho_pack(const FieldInst *__restrict__ fi, int keep) {
   FOR_POINTS(F) {
-    const double f = F.scal[kFactor].x;
+    const double f = ldexp(F.scal[kFactor].x, F.K[2 * F.N]);  // accumulators are scaled by 2^-Kref
     const double2 s = F.zs[i];
-    const double ra = F.acc64[0][i] * (exp(s.x) * f);
-    const double rb = F.acc64[1][i] * (exp(s.y) * f);
+    const double ra = (double)F.acc32[0][i] * (exp(s.x) * f);
+    const double rb = (double)F.acc32[1][i] * (exp(s.y) * f);
     F.zr[i] = make_double2(ra, rb);
     if (keep) {
       F.rho[0][i] = make_double2(ra, 0.0);

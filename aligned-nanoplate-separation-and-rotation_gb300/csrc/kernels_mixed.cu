@@ -16,9 +16,12 @@
 //
 // Range: each step is rescaled by a power of two chosen from that mean (lag 1,
 // so no extra synchronisation), which is exact in floating point.  Integer
-// exponents K[p][n] (q_true = q_stored * 2^K) are kept per instance; the
-// density terms q_j qdag_{N-1-j} and Q are accumulated in FP64 with the
-// exponents folded back in.
+// exponents K[p][n] (q_true = q_stored * 2^K) are kept per instance.  The
+// density terms q_j qdag_{N-1-j} all have about the same magnitude, so they
+// are accumulated in FP32 relative to one reference exponent K[2N] fixed at
+// the first accumulating step; Q and the finalised densities are FP64.  No
+// FP64 arithmetic runs per grid point here: GB300 issues FP64 at a small
+// fraction of its FP32 rate.
 //
 // Density terms are accumulated as in the FP64 kernel: for n > (N-1)/2 the
 // terms j = n and j = N-1-n pair the current step with the stored half of
@@ -119,42 +122,49 @@ __global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restric
     P.K[n] = Kq;
     P.K[N + n] = Kd;
   }
-  // history (first half) and exact plane sums (mean of the next step, Q)
-  double aq = 0.0, ad = 0.0;
+  // history (first half) and plane sums (mean of the next step, Q): each
+  // thread sums its few values in FP32, the block in FP64
+  float aqf = 0.f, adf = 0.f;
   C *hst = P.hist + (long long)n * M + zoff;
   const bool keep = (n <= P.hmax);
   for (int e = threadIdx.x; e < E; e += blockDim.x) {
     const C z = plane[e];
-    aq += (double)z.x;
-    ad += (double)z.y;
+    aqf += z.x;
+    adf += z.y;
     if (keep) hst[e] = z;
   }
-  // density terms
+  double aq = (double)aqf, ad = (double)adf;
+  // density terms, relative to the reference exponent Kref
   const int m2 = N - 1 - n;
-  if (m2 < n) {
-    const C *o = P.hist + (long long)m2 * M + zoff;
-    const double f1 = ldexp(1.0, Kq + P.K[N + m2]);  // q_n * qdag_{m2}
-    const double f2 = ldexp(1.0, P.K[m2] + Kd);      // q_{m2} * qdag_n
-    double *a1 = P.acc[n < Na ? 0 : 1] + zoff;
-    double *a2 = P.acc[m2 < Na ? 0 : 1] + zoff;
-    if (a1 == a2) {
-      for (int e = threadIdx.x; e < E; e += blockDim.x) {
-        const C z = plane[e], h = o[e];
-        a1[e] += (double)z.x * (double)h.y * f1 + (double)h.x * (double)z.y * f2;
+  const int n0 = N / 2;  // first step that adds a term
+  if (m2 <= n) {
+    const int Kref = (n == n0) ? Kq + (m2 == n ? Kd : P.K[N + m2]) : P.K[2 * N];
+    if (n == n0 && jb.z == 0 && threadIdx.x == 0) P.K[2 * N] = Kref;
+    if (m2 < n) {
+      const C *o = P.hist + (long long)m2 * M + zoff;
+      const float f1 = ldexpf(1.0f, Kq + P.K[N + m2] - Kref);  // q_n * qdag_{m2}
+      const float f2 = ldexpf(1.0f, P.K[m2] + Kd - Kref);      // q_{m2} * qdag_n
+      float *a1 = P.acc[n < Na ? 0 : 1] + zoff;
+      float *a2 = P.acc[m2 < Na ? 0 : 1] + zoff;
+      if (a1 == a2) {
+        for (int e = threadIdx.x; e < E; e += blockDim.x) {
+          const C z = plane[e], h = o[e];
+          a1[e] += fmaf(z.x * h.y, f1, (h.x * z.y) * f2);
+        }
+      } else {
+        for (int e = threadIdx.x; e < E; e += blockDim.x) {
+          const C z = plane[e], h = o[e];
+          a1[e] += (z.x * h.y) * f1;
+          a2[e] += (h.x * z.y) * f2;
+        }
       }
     } else {
+      const float f = ldexpf(1.0f, Kq + Kd - Kref);
+      float *a1 = P.acc[n < Na ? 0 : 1] + zoff;
       for (int e = threadIdx.x; e < E; e += blockDim.x) {
-        const C z = plane[e], h = o[e];
-        a1[e] += (double)z.x * (double)h.y * f1;
-        a2[e] += (double)h.x * (double)z.y * f2;
+        const C z = plane[e];
+        a1[e] += (z.x * z.y) * f;
       }
-    }
-  } else if (m2 == n) {
-    const double f = ldexp(1.0, Kq + Kd);
-    double *a1 = P.acc[n < Na ? 0 : 1] + zoff;
-    for (int e = threadIdx.x; e < E; e += blockDim.x) {
-      const C z = plane[e];
-      a1[e] += (double)z.x * (double)z.y * f;
     }
   }
   for (int o = 16; o > 0; o >>= 1) {

@@ -23,6 +23,9 @@ cudaError_t launch_h_partials(const FieldInst *fi, int ninst, int blocks, double
 
 cudaError_t launch_mix_prop_plane(const LaunchShape &ls, const PropJob *jobs, int njobs, const MixInst *insts,
                                   const DevGeom *geoms, const void *tw, int n, cudaStream_t st);
+cudaError_t launch_mix_plane64(const PropJob *jobs, int njobs, const MixInst *insts, const void *tw64, int n,
+                               cudaStream_t st);
+cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw64, int nx, int ny, cudaStream_t st);
 cudaError_t launch_mix_smear(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
 cudaError_t launch_mix_update(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
 cudaError_t launch_mix_boltzmann(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);

@@ -126,3 +126,17 @@ def test_mixed_range_normalisation_long_chain(scft):
     assert abs(H32[0, 0, 2] - H64[0, 0, 2]) <= 1e-4 * abs(H64[0, 0, 2])  # same fields
     assert np.abs(H32[:, 0, 0] - H64[:, 0, 0]).max() <= 1e-5 * np.abs(H64[:, 0, 0]).max()
     assert rel(d32[0][0].real, d64[0][0].real) < 1e-3
+
+
+def test_mixed_64cubed_specialised_kernels_match_fp64(scft):
+    """All-64^3 batches take the specialised 64-point kernels; uneven N."""
+    from scft.workloads import plate_params, seeded_fields
+
+    params = [plate_params(10.0, N=20), plate_params(45.0, N=13)]
+    fields = [seeded_fields(p, 20 + k) for k, p in enumerate(params)]
+    (H64, d64, _), (H32, d32, _) = run_pair(scft, params, fields, 3)
+    for k in range(len(params)):
+        assert np.abs(H32[:, k, 0] - H64[:, k, 0]).max() <= H_TOL * np.abs(H64[:, k, 0]).max()
+        assert np.abs(H32[:, k, 2] - H64[:, k, 2]).max() <= Q_TOL * np.abs(H64[:, k, 2]).max()
+        assert rel(d32[k][0].real, d64[k][0].real) < RHO_TOL
+        assert rel(d32[k][1].real, d64[k][1].real) < RHO_TOL
