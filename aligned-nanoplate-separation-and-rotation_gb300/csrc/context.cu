@@ -444,6 +444,15 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
     std::vector<float> h32(M);
     for (long long i = 0; i < M; i++) h32[i] = (float)(1.0 - pb[i]);
     I.h32 = dupload(c, h32);
+    // per-axis k^2/6 with get_k's branch (code/array_utils.cpp:248-265)
+    std::vector<float> k2t;
+    for (int d = 0; d < 3; d++)
+      for (int nn = 0; nn < p.Nx[d]; nn++) {
+        const double k = (double(nn) < double(p.Nx[d]) / 2.) ? 2 * kPI * double(nn) / p.L[d]
+                                                            : 2 * kPI * double(nn - p.Nx[d]) / p.L[d];
+        k2t.push_back((float)(k * k / 6.0));
+      }
+    I.k2tab32 = dupload(c, k2t);
   }
   I.qpart = dalloc<double2>(c, g.nz);
   I.scal = dalloc<double2>(c, kNumScalars);
@@ -742,6 +751,14 @@ void build_jobs(scft_ctx *c) {
     c->all64 = 1;
     for (auto &I : c->inst)
       if (I.p.Nx[0] != 64 || I.p.Nx[1] != 64 || I.p.Nx[2] != 64) c->all64 = 0;
+    if (c->all64) {
+      std::vector<ColJob> cj64(pcj);
+      for (auto &j : cj64) {
+        for (auto &I : c->inst)
+          if (j.ptr == I.work32) j.kern = I.k2tab32;
+      }
+      c->d_mix64_cj = dupload(c, cj64);
+    }
     c->shp_col32 = choose_shape(emax_col, sizeof(float2), (nz_max + 32) * sizeof(float2));
   }
   c->d_prop_pj = dupload(c, ppj);
@@ -920,7 +937,7 @@ void seq_mix_sweep(scft_ctx *c) {
   if (c->all64) {
     LK(launch_mix_plane64(c->d_prop_pj, c->prop_pj_count[0], c->d_mi, c->d_tw32_64, 0, st));
     for (int s = 1; s < c->nmax; s++) {
-      LK(launch_mix_col64(c->d_prop_cj, c->prop_cj_count[s], c->d_tw32_64, 64, 64, st));
+      LK(launch_mix_col64(c->d_mix64_cj, c->prop_cj_count[s], c->d_tw32_64, 64, 64, st));
       LK(launch_mix_plane64(c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_tw32_64, s, st));
     }
   } else {
@@ -1077,7 +1094,7 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   CK(cudaEventRecord(e1, c->st));
   for (int r = 0; r < reps; r++) {
     if (c->mixed && c->all64)
-      LK(launch_mix_col64(c->d_prop_cj, c->prop_cj_count[s], c->d_tw32_64, 64, 64, c->st));
+      LK(launch_mix_col64(c->d_mix64_cj, c->prop_cj_count[s], c->d_tw32_64, 64, 64, c->st));
     else if (c->mixed)
       LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw32, 3, 1, c->st));
     else

@@ -47,7 +47,8 @@ struct Instance {
   float *acc32[2] = {};
   double *part = nullptr;
   int *K = nullptr;
-  float *h32 = nullptr;  // 1 - g(k), FP32
+  float *h32 = nullptr;    // 1 - g(k), FP32
+  float *k2tab32 = nullptr;  // [kx^2/6 | ky^2/6 | kz^2/6], FP32
 };
 
 struct DevBuf {
@@ -89,6 +90,7 @@ struct scft_ctx {
   int all64 = 0;         // every instance is 64^3: specialised propagator kernels
   void *d_tw32_64 = nullptr;  // the 64-point twiddle table inside d_tw32
   void *d_tw32 = nullptr;
+  scft::ColJob *d_mix64_cj = nullptr;  // z-pass jobs of the 64^3 kernels
   scft::MixInst *d_mi = nullptr;
   scft::PropJob *d_mix_pj = nullptr;
   scft::ColJob *d_mix_cj = nullptr;

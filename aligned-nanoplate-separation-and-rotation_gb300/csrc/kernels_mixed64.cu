@@ -10,7 +10,16 @@
 //   X[t + 8d] = sum_b Y[b][t] w8^(b d)            (DFT8 in registers)
 // so the output comes back in the same "t + 8j" order as the input.  Shared
 // layouts are padded so that every exchange is free of bank conflicts, and no
-// index needs a runtime division.
+// index needs a runtime division.  Exchanges between the 8 threads of one row
+// stay inside a warp (warp barrier); exchanges along y cross warps (block
+// barrier).
+//
+// The plane pass prefetches, with cp.async at kernel start, the Boltzmann
+// factors and the stored history plane it will need after the inverse
+// transforms, so that their memory latency overlaps the transform work.
+// Plane sums are formed with error-free FP32 two-sums per thread and across
+// the warp (FP64 only for the 16 warp results): GB300 issues FP64 at a small
+// fraction of its FP32 rate.
 #include "fft_core.cuh"
 #include "inst.h"
 #include "launch.h"
@@ -20,42 +29,85 @@ namespace scft {
 
 namespace {
 
-constexpr int kRowPad = 72;  // padded row stride (float2) of the 64 x 64 plane buffer
+constexpr int kRowPad = 72;              // padded row stride (float2) of a 64 x 64 plane
+constexpr int kPlanePad = 64 * kRowPad;  // float2 per padded plane
 
 template <int SIGN> __device__ __forceinline__ void dft8f(float2 *v) { Dft<8, SIGN, float2>::run(v); }
 
-// twiddle multiply by w64^(t c) (SIGN < 0) or its conjugate
 template <int SIGN> __device__ __forceinline__ void tw64(float2 *v, int t, const float2 *tw) {
 #pragma unroll
   for (int c = 1; c < 8; c++) v[c] = ctw<SIGN>(v[c], tw[t * c]);
 }
 
-// 64-point transform of a group of 8 threads.  Thread t of the group holds
-// v[a] = x[t + 8a]; the exchange goes through xch with element (b, c) of the
-// group at xch[b * sb + c * sc] (strides chosen by the caller so that a warp's
-// accesses spread over the banks).  On return v[d] = X[t + 8d].
-template <int SIGN>
+// 64-point transform of a group of 8 threads (see above).  Element (b, c) of
+// the exchange lives at xch[b * sb + c * sc].  WARP: the 8 threads and their
+// exchange area belong to one warp, so a warp barrier suffices.
+template <int SIGN, bool WARP>
 __device__ __forceinline__ void fft64_group(float2 *v, int t, float2 *xch, int sb, int sc, const float2 *tw) {
   dft8f<SIGN>(v);
   tw64<SIGN>(v, t, tw);
 #pragma unroll
   for (int c = 0; c < 8; c++) xch[t * sb + c * sc] = v[c];
-  __syncthreads();
+  if (WARP) __syncwarp(); else __syncthreads();
 #pragma unroll
   for (int b = 0; b < 8; b++) v[b] = xch[b * sb + t * sc];
-  __syncthreads();
+  if (WARP) __syncwarp(); else __syncthreads();
   dft8f<SIGN>(v);
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// L2 policies: the history is written once and read once about N/2 steps
+// later, so it is streamed with evict-first; the Boltzmann factors are read by
+// every step and kept with evict-last.  The per-step arrays (propagator,
+// factors, accumulators) then stay in L2 while the history streams past.
+__device__ __forceinline__ uint64_t l2_policy_first() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ uint64_t l2_policy_last() {
+  uint64_t p;
+  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
+  return p;
+}
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, uint64_t pol) {
+  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "l"(pol));
+}
+__device__ __forceinline__ void st_stream(float2 *g, float2 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;\n" ::"l"(g), "f"(v.x), "f"(v.y), "l"(pol)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
+
+// Copies one 64 x 64 float2 plane into a padded shared plane (16 B per copy).
+__device__ __forceinline__ void prefetch_plane(float2 *dst, const float2 *src, uint64_t pol) {
+#pragma unroll
+  for (int k = 0; k < 4; k++) {
+    const int c = threadIdx.x + 512 * k;  // 16-byte chunk: two float2
+    const int row = c >> 5, x = (2 * c) & 63;
+    cp_async16(dst + row * kRowPad + x, src + 2 * c, pol);
+  }
 }
 
 }  // namespace
 
-// Plane pass of step n for 64 x 64 xy planes, 512 threads: column phase
-// (thread = column x, part t) for the y transforms, row phase (thread = row y,
-// part t) for the x transforms and all pointwise work.
+// Plane pass of step n for 64 x 64 xy planes, 512 threads.  Dynamic shared
+// memory: exchange/transpose plane, prefetched Boltzmann plane, prefetched
+// history plane (3 padded planes, 110.6 KB; two CTAs per SM).
 __global__ void __launch_bounds__(512, 2) k_mix_plane64(const PropJob *__restrict__ jobs,
                                                         const MixInst *__restrict__ insts,
                                                         const float2 *__restrict__ tw_g, int n) {
-  __shared__ __align__(16) float2 buf[64 * kRowPad];
+  extern __shared__ __align__(16) float2 dsm[];
+  float2 *buf = dsm;
+  float2 *Es = dsm + kPlanePad;
+  float2 *Hs = dsm + 2 * kPlanePad;
   __shared__ float2 tw[64];
   __shared__ double s_red[2][16];
   __shared__ double s_mu[2];
@@ -69,6 +121,12 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const PropJob *__restric
   const long long zoff = (long long)jb.z * 4096;
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
+  const int m2 = N - 1 - n;
+  const bool pair = (m2 < n);  // a stored partner plane is needed
+  const uint64_t pol_first = l2_policy_first();
+  prefetch_plane(Es, P.E + zoff, l2_policy_last());
+  if (pair) prefetch_plane(Hs, P.hist + (long long)m2 * M + zoff, pol_first);
+  cp_async_commit();
   if (tid < 64) tw[tid] = tw_g[tid];
   if (warp == 0) {
     double a = 0.0, b = 0.0;
@@ -95,36 +153,38 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const PropJob *__restric
       s_mu[1] = mb;
     }
   }
-  // row-phase coordinates: this thread owns (y = row, x = t + 8d)
+  // row-phase ownership: (y = row, x = tr + 8d); column phase: (y = tc + 8d, x = col)
   const int row = tid >> 3, tr = tid & 7;
-  // column-phase coordinates: this thread owns (y = tc + 8d, x = col)
   const int col = tid & 63, tc = tid >> 6;
   float2 v[8];
-  const float2 *Ew = P.E + zoff;
   float2 *work = P.work + zoff;
   const bool useA_q = (Na > 0 && n < Na);
   const bool useA_d = !(n <= N - Na - 1);
   __syncthreads();  // tw, s_mu, s_exp
-  if (n == 0) {
-#pragma unroll
-    for (int d = 0; d < 8; d++) {
-      const float2 e = Ew[row * 64 + tr + 8 * d];
-      v[d] = make_float2(useA_q ? e.x : e.y, useA_d ? e.x : e.y);
-    }
-  } else {
+  if (n > 0) {
     // inverse y transform (column phase)
 #pragma unroll
     for (int a = 0; a < 8; a++) v[a] = work[(tc + 8 * a) * 64 + col];
-    fft64_group<+1>(v, tc, buf + col, 8 * 64, 64, tw);
-    // to the row phase through the padded plane
+    fft64_group<+1, false>(v, tc, buf + col, 8 * 64, 64, tw);
 #pragma unroll
     for (int d = 0; d < 8; d++) buf[(tc + 8 * d) * kRowPad + col] = v[d];
     __syncthreads();
 #pragma unroll
     for (int a = 0; a < 8; a++) v[a] = buf[row * kRowPad + tr + 8 * a];
     __syncthreads();
-    // inverse x transform (row phase)
-    fft64_group<+1>(v, tr, buf + row * kRowPad, 9, 1, tw);
+    // inverse x transform (row phase, inside one warp)
+    fft64_group<+1, true>(v, tr, buf + row * kRowPad, 9, 1, tw);
+  }
+  cp_async_wait_all();
+  __syncthreads();  // prefetched planes visible
+  const float2 *Er = Es + row * kRowPad + tr;
+  if (n == 0) {
+#pragma unroll
+    for (int d = 0; d < 8; d++) {
+      const float2 e = Er[8 * d];
+      v[d] = make_float2(useA_q ? e.x : e.y, useA_d ? e.x : e.y);
+    }
+  } else {
     // q = (conv + mean) * e^{-w} * 2^{-e}, the mean as a two-float constant
     const int eq = s_exp[0], ed = s_exp[1];
     const float sq = ldexpf(1.0f, -eq), sd = ldexpf(1.0f, -ed);
@@ -133,7 +193,7 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const PropJob *__restric
     const float md_hi = (float)md, md_lo = (float)(md - (double)md_hi);
 #pragma unroll
     for (int d = 0; d < 8; d++) {
-      const float2 e = Ew[row * 64 + tr + 8 * d];
+      const float2 e = Er[8 * d];
       const float eq_ = useA_q ? e.x : e.y, ed_ = useA_d ? e.x : e.y;
       const float uq = fmaf(v[d].x, eq_, fmaf(mq_hi, eq_, mq_lo * eq_));
       const float ud = fmaf(v[d].y, ed_, fmaf(md_hi, ed_, md_lo * ed_));
@@ -146,62 +206,72 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const PropJob *__restric
     P.K[n] = Kq;
     P.K[N + n] = Kd;
   }
-  // history, plane sums, density terms (row phase ownership)
-  float aqf = 0.f, adf = 0.f;
-  const bool keep = (n <= P.hmax);
-  float2 *hst = P.hist + (long long)n * M + zoff;
+  // history, density terms, plane sums (row-phase ownership)
+  const int gi = row * 64 + tr;  // global index of element d = 0 in this plane
+  if (n <= P.hmax) {
+    float2 *hst = P.hist + (long long)n * M + zoff + gi;
 #pragma unroll
-  for (int d = 0; d < 8; d++) {
-    aqf += v[d].x;
-    adf += v[d].y;
-    if (keep) hst[row * 64 + tr + 8 * d] = v[d];
+    for (int d = 0; d < 8; d++) st_stream(hst + 8 * d, v[d], pol_first);
   }
-  const int m2 = N - 1 - n;
   const int n0 = N / 2;
   if (m2 <= n) {
     const int Kref = (n == n0) ? Kq + (m2 == n ? Kd : P.K[N + m2]) : P.K[2 * N];
     if (n == n0 && jb.z == 0 && tid == 0) P.K[2 * N] = Kref;
-    if (m2 < n) {
-      const float2 *o = P.hist + (long long)m2 * M + zoff;
+    if (pair) {
+      const float2 *Hr = Hs + row * kRowPad + tr;
       const float f1 = ldexpf(1.0f, Kq + P.K[N + m2] - Kref);
       const float f2 = ldexpf(1.0f, P.K[m2] + Kd - Kref);
-      float *a1 = P.acc[n < Na ? 0 : 1] + zoff;
-      float *a2 = P.acc[m2 < Na ? 0 : 1] + zoff;
+      float *a1 = P.acc[n < Na ? 0 : 1] + zoff + gi;
+      float *a2 = P.acc[m2 < Na ? 0 : 1] + zoff + gi;
+      if (a1 == a2) {
 #pragma unroll
-      for (int d = 0; d < 8; d++) {
-        const int i = row * 64 + tr + 8 * d;
-        const float2 h = o[i];
-        if (a1 == a2) {
-          a1[i] += fmaf(v[d].x * h.y, f1, (h.x * v[d].y) * f2);
-        } else {
-          a1[i] += (v[d].x * h.y) * f1;
-          a2[i] += (h.x * v[d].y) * f2;
+        for (int d = 0; d < 8; d++) {
+          const float2 h = Hr[8 * d];
+          a1[8 * d] += fmaf(v[d].x * h.y, f1, (h.x * v[d].y) * f2);
+        }
+      } else {
+#pragma unroll
+        for (int d = 0; d < 8; d++) {
+          const float2 h = Hr[8 * d];
+          a1[8 * d] += (v[d].x * h.y) * f1;
+          a2[8 * d] += (h.x * v[d].y) * f2;
         }
       }
     } else {
       const float f = ldexpf(1.0f, Kq + Kd - Kref);
-      float *a1 = P.acc[n < Na ? 0 : 1] + zoff;
+      float *a1 = P.acc[n < Na ? 0 : 1] + zoff + gi;
 #pragma unroll
-      for (int d = 0; d < 8; d++) {
-        const int i = row * 64 + tr + 8 * d;
-        a1[i] += (v[d].x * v[d].y) * f;
-      }
+      for (int d = 0; d < 8; d++) a1[8 * d] += (v[d].x * v[d].y) * f;
     }
   }
-  double aq = (double)aqf, ad = (double)adf;
+  // plane sums: error-free FP32 two-sums within the thread and the warp
+  float sq_ = 0.f, cq = 0.f, sd_ = 0.f, cd = 0.f;
+#pragma unroll
+  for (int d = 0; d < 8; d++) {
+    float e;
+    two_sum(sq_, v[d].x, sq_, e);
+    cq += e;
+    two_sum(sd_, v[d].y, sd_, e);
+    cd += e;
+  }
   for (int o = 16; o > 0; o >>= 1) {
-    aq += __shfl_down_sync(0xffffffffu, aq, o);
-    ad += __shfl_down_sync(0xffffffffu, ad, o);
+    const float s2 = __shfl_down_sync(0xffffffffu, sq_, o), c2 = __shfl_down_sync(0xffffffffu, cq, o);
+    const float t2 = __shfl_down_sync(0xffffffffu, sd_, o), d2 = __shfl_down_sync(0xffffffffu, cd, o);
+    float e;
+    two_sum(sq_, s2, sq_, e);
+    cq += c2 + e;
+    two_sum(sd_, t2, sd_, e);
+    cd += d2 + e;
   }
   if (lane == 0) {
-    s_red[0][warp] = aq;
-    s_red[1][warp] = ad;
+    s_red[0][warp] = (double)sq_ + (double)cq;
+    s_red[1][warp] = (double)sd_ + (double)cd;
   }
   __syncthreads();
   if (warp == 0) {
-    aq = lane < 16 ? s_red[0][lane] : 0.0;
-    ad = lane < 16 ? s_red[1][lane] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) {
+    double aq = lane < 16 ? s_red[0][lane] : 0.0;
+    double ad = lane < 16 ? s_red[1][lane] : 0.0;
+    for (int o = 8; o > 0; o >>= 1) {
       aq += __shfl_down_sync(0xffffffffu, aq, o);
       ad += __shfl_down_sync(0xffffffffu, ad, o);
     }
@@ -212,23 +282,26 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const PropJob *__restric
   }
   if (n == N - 1) return;
   // forward x transform (row phase), then to the column phase, forward y
-  fft64_group<-1>(v, tr, buf + row * kRowPad, 9, 1, tw);
+  fft64_group<-1, true>(v, tr, buf + row * kRowPad, 9, 1, tw);
 #pragma unroll
   for (int d = 0; d < 8; d++) buf[row * kRowPad + tr + 8 * d] = v[d];
   __syncthreads();
 #pragma unroll
   for (int a = 0; a < 8; a++) v[a] = buf[(tc + 8 * a) * kRowPad + col];
   __syncthreads();
-  fft64_group<-1>(v, tc, buf + col, 8 * 64, 64, tw);
+  fft64_group<-1, false>(v, tc, buf + col, 8 * 64, 64, tw);
 #pragma unroll
   for (int d = 0; d < 8; d++) work[(tc + 8 * d) * 64 + col] = v[d];
 }
 
-// z pass for nz = 64, mode 3 of the generic column pass: tile of TX x columns
-// at one y, 8 threads per column.
+// z pass for nz = 64 (mode 3 of the generic column pass): tile of TX x columns
+// at one y, 8 threads per column.  h = 1 - g(k) is formed on the fly as
+// -expm1(-(kx^2 + ky^2 + kz^2)/6) from per-axis tables k2 = [kx^2/6 | ky^2/6 |
+// kz^2/6] (jb.kern), so the pass moves only the propagator itself.
 template <int TX>
 __global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__ jobs,
-                                                      const float2 *__restrict__ tw_g, int nx, int ny) {
+                                                      const float2 *__restrict__ tw_g, int nx, int ny, float s_hi,
+                                                      float s_lo) {
   __shared__ __align__(16) float2 buf[64 * TX];
   __shared__ float2 tw[64];
   const ColJob jb = jobs[blockIdx.x];
@@ -238,24 +311,23 @@ __global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__
   const long long plane = (long long)nx * ny;
   const long long base = (long long)jb.y * nx + jb.x0 + col;
   float2 *a = reinterpret_cast<float2 *>(jb.ptr);
-  const float *h = reinterpret_cast<const float *>(jb.kern);
+  const float *k2 = reinterpret_cast<const float *>(jb.kern);
+  const float kxy = k2[jb.x0 + col] + k2[nx + jb.y];
   float2 v[8];
 #pragma unroll
   for (int j = 0; j < 8; j++) v[j] = a[(t + 8 * j) * plane + base];
   __syncthreads();  // tw
-  fft64_group<-1>(v, t, buf + col, 8 * TX, TX, tw);
-  const double sdbl = 1.0 / (double)(plane * 64);
-  const float s_hi = (float)sdbl, s_lo = (float)(sdbl - (double)s_hi);
+  fft64_group<-1, false>(v, t, buf + col, 8 * TX, TX, tw);
 #pragma unroll
   for (int d = 0; d < 8; d++) {
     const int kz = t + 8 * d;
-    const float hv = h[kz * plane + base];
+    const float hv = -expm1f(-(kxy + k2[nx + ny + kz]));
     float2 u = make_float2(fmaf(v[d].x, s_hi, v[d].x * s_lo), fmaf(v[d].y, s_hi, v[d].y * s_lo));
     u = make_float2(fmaf(-hv, u.x, u.x), fmaf(-hv, u.y, u.y));
     if (kz == 0 && jb.y == 0 && jb.x0 + col == 0) u = make_float2(0.f, 0.f);
     v[d] = u;
   }
-  fft64_group<+1>(v, t, buf + col, 8 * TX, TX, tw);
+  fft64_group<+1, false>(v, t, buf + col, 8 * TX, TX, tw);
 #pragma unroll
   for (int j = 0; j < 8; j++) a[(t + 8 * j) * plane + base] = v[j];
 }
@@ -263,13 +335,20 @@ __global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__
 cudaError_t launch_mix_plane64(const PropJob *jobs, int njobs, const MixInst *insts, const void *tw64,
                                int n, cudaStream_t st) {
   if (njobs <= 0) return cudaSuccess;
-  k_mix_plane64<<<njobs, 512, 0, st>>>(jobs, insts, reinterpret_cast<const float2 *>(tw64), n);
+  const int smem = 3 * kPlanePad * (int)sizeof(float2);
+  cudaError_t e = cudaFuncSetAttribute(k_mix_plane64, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_mix_plane64, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return e;
+  k_mix_plane64<<<njobs, 512, smem, st>>>(jobs, insts, reinterpret_cast<const float2 *>(tw64), n);
   return cudaGetLastError();
 }
 
 cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw64, int nx, int ny, cudaStream_t st) {
   if (njobs <= 0) return cudaSuccess;
-  k_mix_col64<16><<<njobs, 128, 0, st>>>(jobs, reinterpret_cast<const float2 *>(tw64), nx, ny);
+  const double s = 1.0 / ((double)nx * ny * 64);
+  const float s_hi = (float)s, s_lo = (float)(s - (double)s_hi);
+  k_mix_col64<16><<<njobs, 128, 0, st>>>(jobs, reinterpret_cast<const float2 *>(tw64), nx, ny, s_hi, s_lo);
   return cudaGetLastError();
 }
 
