@@ -131,6 +131,14 @@ int scft_get_density(scft_ctx *c, int inst, double *ra, double *rb, double *rg) 
   return SCFT_OK;
 }
 
+int scft_get_plate_density(scft_ctx *c, int inst, double *rho) {
+  if (int s = check_ctx(c, inst)) return s;
+  if (!rho) return fail(SCFT_ERR_ARG, "null output");
+  cudaError_t e = cudaMemcpy(rho, c->inst[inst].rho_exp_nr, sizeof(double) * c->inst[inst].M, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fail(SCFT_ERR_CUDA, cudaGetErrorString(e));
+  return SCFT_OK;
+}
+
 int scft_get_smeared(scft_ctx *c, int inst, double *a, double *b, double *g) {
   if (int s = check_ctx(c, inst)) return s;
   API_BODY(scft::ctx_get_smeared(c, inst, a, b, g));

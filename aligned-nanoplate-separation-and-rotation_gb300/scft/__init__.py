@@ -23,7 +23,7 @@ FIELD_NAMES = ("wpl", "wabp", "wabm", "wbcp", "wbcm", "wacp", "wacm")
 # Every extern "C" symbol declared in include/scft.h.
 EXPORTS = ("scft_last_error", "scft_version", "scft_create", "scft_destroy", "scft_get_info",
            "scft_set_fields", "scft_get_fields", "scft_calc_poly_density", "scft_update_1s",
-           "scft_calc_H", "scft_get_density", "scft_get_smeared", "scft_diblock_density",
+           "scft_calc_H", "scft_get_density", "scft_get_plate_density", "scft_get_smeared", "scft_diblock_density",
            "scft_homopolymer_density", "scft_fft3d", "scft_sync", "scft_get_stream", "scft_launch_count",
            "scft_profile_step", "scft_diblock_density_noalloc")
 
@@ -90,6 +90,7 @@ def load(path: str | None = None):
     lib.scft_calc_H.argtypes = [vp, dp]
     lib.scft_get_density.argtypes = [vp, ctypes.c_int, dp, dp, dp]
     lib.scft_get_smeared.argtypes = [vp, ctypes.c_int, dp, dp, dp]
+    lib.scft_get_plate_density.argtypes = [vp, ctypes.c_int, dp]
     lib.scft_diblock_density.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp, dp]
     lib.scft_homopolymer_density.argtypes = [vp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, dp, dp]
     lib.scft_fft3d.argtypes = [vp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_int]

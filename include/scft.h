@@ -126,6 +126,10 @@ int scft_calc_H(scft_ctx *ctx, double *out);
  * rhoda, rhodb, rhog_exp (any may be NULL). */
 int scft_get_density(scft_ctx *ctx, int inst, double *rhoda, double *rhodb, double *rhog_exp);
 
+/* The explicit plates' density rho_exp_nr of one instance (M real values),
+ * as built at set-up (code/initialize.cpp:210-239). */
+int scft_get_plate_density(scft_ctx *ctx, int inst, double *rho_exp_nr);
+
 /* Smeared fields of one instance (smwa, smwb, smwg; any may be NULL). */
 int scft_get_smeared(scft_ctx *ctx, int inst, double *smwa, double *smwb, double *smwg);
 

@@ -16,14 +16,26 @@
  * Usage (run inside a directory holding bcp.input and optional w*.res):
  *   scft_ref dump  <iters> [hist]   writes scalars.txt, trace.txt, *.f64
  *   scft_ref time  <iters>          prints "seconds_per_iter <t>"
+ *   scft_ref simulate 0             the reference's own main(): read_input,
+ *                                   initialize_1, allocate, simulate
+ *                                   (writes data.dat and *.p0.bin)
  * Arrays are written as raw little-endian complex<double> (2*ML doubles).
  */
 #include <chrono>
+#include <csignal>
+#include <unistd.h>
 
 #define MAIN
 #include "main.hpp"
 
 void update_1s(void);
+double simulate(void);
+
+// simulate() has no return statement (code/simulate.cpp:16-167).  Built at
+// -O0 (oracle/Makefile), GCC ends it with a trap instruction, which runs only
+// after the loop has finished and data.dat is closed: that trap is the end of
+// a completed run.
+static void simulate_fell_off_end(int) { _exit(0); }
 
 static void dump(const char *name, const complex<double> *a) {
   char fn[256];
@@ -61,6 +73,17 @@ int main(int argc, char **argv) {
     return 2;
   }
   const int iters = atoi(argv[2]);
+  if (!strcmp(argv[1], "simulate")) {
+    signal(SIGILL, simulate_fell_off_end);
+    myrank = 0;
+    nprocs = 1;
+    idum = -12345;
+    read_input();
+    initialize_1();
+    allocate();
+    simulate();
+    return 0;
+  }
   if (!strcmp(argv[1], "time")) {
     setup();
     calc_H();

@@ -105,8 +105,49 @@ def case_json(c: Case) -> str:
     return json.dumps(d)
 
 
+def driver_cases() -> dict:
+    """Runs of the reference's own driver (simulate(), data.dat and *.p0.bin)."""
+    base = dict(Nx=(8, 10, 6), L=(4.0, 5.0, 3.5), a_smear=0.2, rho0=5.0, kappa=50.0, lam_pl=0.005,
+                lam_mi=0.005, L_nr=0.6, R_nr=1.2, xi_nr=0.3, Nda=3, Ndb=5, chi_ab=0.5, n_exp_nr=1,
+                centers=((0.4, 0.55, 0.5), (0.5, 0.5, 0.5)), orients=((0.9, 0.3, 0.1), (1.0, 0.0, 0.0)),
+                itermax=12, print_freq=3)
+    cases = {}
+    c = Case(**base)
+    c.fields = seeded_fields(c, 1, 0.3, 0.01, False)
+    cases["driver_res"] = c
+    c = Case(ic=((-2, 1.0, 0, 1.0), (-4, 1.0, 1, 1.0)), **base)
+    c.fields = {}
+    cases["driver_cos"] = c
+    return cases
+
+
+DRIVER_OUTPUTS = ["data.dat", "wpl.p0.bin", "wabp.p0.bin", "wabm.p0.bin", "rhoda.p0.bin", "rhodb.p0.bin",
+                  "rhoda_c.p0.bin"]
+
+
+def make_driver_fixtures(tmp):
+    import shutil
+    import subprocess
+
+    from ref_case import REF_BIN, write_case
+
+    for name, c in driver_cases().items():
+        run = os.path.join(tmp, name)
+        write_case(run, c)
+        r = subprocess.run([REF_BIN, "simulate", "0"], cwd=run, capture_output=True, text=True, timeout=600)
+        if r.returncode != 0:
+            raise RuntimeError(r.stderr)
+        out = os.path.join(HERE, name)
+        os.makedirs(out, exist_ok=True)
+        for f in ["bcp.input"] + [n + ".res" for n in c.fields] + DRIVER_OUTPUTS:
+            shutil.copy(os.path.join(run, f), os.path.join(out, f if f == "bcp.input" or f.endswith(".res")
+                                                           else f + ".ref"))
+        print(name, open(os.path.join(run, "data.dat")).read().splitlines()[-1])
+
+
 def main():
     tmp = tempfile.mkdtemp(prefix="golden_")
+    make_driver_fixtures(tmp)
     for name, (c, iters, hist) in tiny_cases().items():
         out = run_reference(os.path.join(tmp, name), c, iters, hist=hist)
         z = {"case_json": case_json(c), "trace": out["trace"], "scalars_json": json.dumps(out["scalars"])}
