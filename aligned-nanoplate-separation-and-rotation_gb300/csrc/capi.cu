@@ -21,6 +21,7 @@ void ctx_fft3d(scft_ctx *c, int k, double *data, int count, int sign);
 void ctx_diblock_density(scft_ctx *c, int k, const double *smwa, const double *smwb, double *ra, double *rb,
                          double *Q);
 void ctx_override_nD(scft_ctx *c, int k, double nD);
+int ctx_grad_geom(scft_ctx *c, double *out);
 void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
                       double *bytes_col);
 int error_code(const std::exception &e);
@@ -194,6 +195,15 @@ int scft_sync(scft_ctx *c) {
   cudaError_t e = cudaStreamSynchronize(c->st);
   if (e != cudaSuccess) return fail(SCFT_ERR_CUDA, cudaGetErrorString(e));
   return SCFT_OK;
+}
+
+int scft_grad_geom(scft_ctx *c, double *out) {
+  if (int s = check_ctx(c, 0)) return s;
+  if (!out) return fail(SCFT_ERR_ARG, "null output");
+  int st = SCFT_OK;
+  API_BODY(st = scft::ctx_grad_geom(c, out));
+  if (st == SCFT_ERR_UNSUPPORTED) return fail(st, "geometric derivatives are built for bare plates of the reference shape");
+  return st;
 }
 
 int scft_get_stream(scft_ctx *c, void **stream) {

@@ -16,6 +16,7 @@
 #include "context.h"
 #include "fft_core.cuh"
 #include "prop_launch.h"
+#include "grad.h"
 
 namespace scft {
 
@@ -1301,6 +1302,82 @@ int error_code(const std::exception &e) {
 }  // namespace scft
 
 namespace scft {
+// dH/d(plate rotation about z) and dH/d(plate centre) at the current fields
+// (kernels_grad.cu): out[8*inst + 4*j + {0, 1, 2, 3}] for plate j.
+int ctx_grad_geom(scft_ctx *c, double *out) {
+  if (c->dirty_density) ctx_poly_density(c);
+  const int n = (int)c->inst.size();
+  const int blocks = 128;
+  double *part = nullptr;
+  CK(cudaMalloc(&part, sizeof(double) * blocks * 2 * kGradPerPlate));
+  std::vector<double> hp(blocks * 2 * kGradPerPlate);
+  std::vector<double2> sc(kNumScalars);
+  int status = SCFT_OK;
+  try {
+    for (int k = 0; k < n; k++) {
+      Instance &I = c->inst[k];
+      for (int j = 0; j < 8; j++) out[8 * k + j] = 0.0;
+      const scft_params &p = I.p;
+      if (p.n_exp_nr == 0) continue;
+      if (I.graft || p.plate_shape != SCFT_PLATE_REFERENCE) {
+        status = SCFT_ERR_UNSUPPORTED;
+        continue;
+      }
+      const double2 *wpl = I.w[0];
+      if (I.mixed) {  // fields are held as transforms
+        CK(cudaMemcpyAsync(I.rho[2], I.w[0], sizeof(double2) * I.M, cudaMemcpyDeviceToDevice, c->st));
+        fft3d_arrays(c, I, {I.rho[2]}, +1);
+        wpl = I.rho[2];
+      }
+      GradArgs g;
+      g.nx = p.Nx[0];
+      g.ny = p.Nx[1];
+      g.nz = p.Nx[2];
+      g.nplates = p.n_exp_nr;
+      for (int d = 0; d < 3; d++) {
+        g.dx[d] = I.info.dx[d];
+        g.L[d] = p.L[d];
+      }
+      for (int j = 0; j < p.n_exp_nr; j++) {
+        double un = 0.0;
+        for (int d = 0; d < 3; d++) un += p.orient[j][d] * p.orient[j][d];
+        un = sqrt(un);
+        for (int d = 0; d < 3; d++) {
+          g.c[j][d] = p.center[j][d] * p.L[d];
+          g.u[j][d] = p.orient[j][d] / un;
+        }
+      }
+      g.len = p.L_nr;
+      g.rad = p.R_nr;
+      g.xi = p.xi_nr;
+      CK(launch_geom_grad(g, wpl, part, blocks, c->st));
+      const int nv = g.nplates * kGradPerPlate;
+      CK(cudaMemcpyAsync(hp.data(), part, sizeof(double) * blocks * nv, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaMemcpyAsync(sc.data(), I.scal, sizeof(double2) * kNumScalars, cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      const cd logQ = std::log(cd(sc[kQd].x, sc[kQd].y));
+      const double dV = I.info.dx[0] * I.info.dx[1] * I.info.dx[2];
+      for (int j = 0; j < g.nplates; j++)
+        for (int q = 0; q < 4; q++) {
+          double sr = 0.0, si = 0.0, s0 = 0.0;
+          for (int b = 0; b < blocks; b++) {
+            sr += hp[(size_t)b * nv + j * kGradPerPlate + 3 * q + 0];
+            si += hp[(size_t)b * nv + j * kGradPerPlate + 3 * q + 1];
+            s0 += hp[(size_t)b * nv + j * kGradPerPlate + 3 * q + 2];
+          }
+          // Re[ i rho0 dV sum(drho w+) ] + (rho0/N) dV sum(drho) Re log Qd
+          const cd t = cd(0.0, p.rho0) * cd(sr, si) * dV + (p.rho0 / I.N) * dV * s0 * logQ;
+          out[8 * k + 4 * j + q] = t.real();
+        }
+    }
+  } catch (...) {
+    cudaFree(part);
+    throw;
+  }
+  cudaFree(part);
+  return status;
+}
+
 // Replaces nD of instance k (used by the homopolymer entry point, where the
 // chain count nK is an argument).
 void ctx_override_nD(scft_ctx *c, int k, double nD) {

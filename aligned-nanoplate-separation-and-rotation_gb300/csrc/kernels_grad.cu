@@ -1,0 +1,87 @@
+// kernels_grad.cu -- geometric derivatives of H with respect to the plates.
+//
+// The plate core density (code/initialize.cpp:578-612)
+//   rho_p(r) = 1/4 erfc(a) erfc(b),  a = (|u.dr| - L/2)/xi,  b = (|u x dr| - R)/xi,
+// dr = r - c (minimum image), enters H at fixed fields through
+//   -i rho0 int (1 - rho_p) w+           (code/calc_h.cpp:66-87)
+//   -nD log Qd with nD = rho0 (Vf - V_exp - phiG Vf)/N, V_exp = int rho_p
+//                                          (code/initialize.cpp:251-351),
+// so dH/dg = i rho0 int (d rho_p/dg) w+ + (rho0/N) log Qd int (d rho_p/dg)
+// for g = a rotation angle of the plate axis u about z (du/dtheta = z x u) or
+// a centre coordinate.  This kernel forms, per plate, the grid sums of
+// d rho_p/dg * w+ and of d rho_p/dg (FP64); the host assembles dH/dg.
+#include "fft_core.cuh"
+#include "grad.h"
+
+namespace scft {
+
+__device__ __forceinline__ double derfc(double x) {
+  // d/dx erfc(x) = -2/sqrt(pi) exp(-x^2)
+  return -1.1283791670955125738961589031215452 * exp(-x * x);
+}
+
+__global__ void k_geom_grad(GradArgs g, const double2 *__restrict__ wpl, double *__restrict__ part) {
+  __shared__ double red[32];
+  double acc[kGradPerPlate * 2];
+  for (int k = 0; k < kGradPerPlate * 2; k++) acc[k] = 0.0;
+  const long long M = (long long)g.nx * g.ny * g.nz;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
+    const int n[3] = {(int)(i % g.nx), (int)((i / g.nx) % g.ny), (int)(i / ((long long)g.nx * g.ny))};
+    const double2 w = wpl[i];
+    for (int j = 0; j < g.nplates; j++) {
+      double dr[3];
+      for (int d = 0; d < 3; d++) {
+        double r = double(n[d]) * g.dx[d] - g.c[j][d];
+        if (r >= 0.5 * g.L[d]) r -= g.L[d];
+        else if (r < -0.5 * g.L[d]) r += g.L[d];
+        dr[d] = r;
+      }
+      const double *u = g.u[j];
+      const double ud = u[0] * dr[0] + u[1] * dr[1] + u[2] * dr[2];
+      const double cx = u[1] * dr[2] - u[2] * dr[1], cy = u[2] * dr[0] - u[0] * dr[2], cz = u[0] * dr[1] - u[1] * dr[0];
+      const double uc = sqrt(cx * cx + cy * cy + cz * cz);
+      const double a = (fabs(ud) - 0.5 * g.len) / g.xi, b = (uc - g.rad) / g.xi;
+      const double Ea = erfc(a), Eb = erfc(b);
+      const double dEa = derfc(a) / g.xi, dEb = derfc(b) / g.xi;  // d/d|u.dr|, d/d|u x dr|
+      const double sg = ud > 0.0 ? 1.0 : (ud < 0.0 ? -1.0 : 0.0);
+      // rotation about z: du = (-u_y, u_x, 0) dtheta
+      const double du[3] = {-u[1], u[0], 0.0};
+      const double dud_dth = sg * (du[0] * dr[0] + du[1] * dr[1] + du[2] * dr[2]);
+      const double duc_dth = uc > 1e-300 ? -ud * (du[0] * dr[0] + du[1] * dr[1] + du[2] * dr[2]) / uc : 0.0;
+      double dg[4];
+      dg[0] = 0.25 * (dEa * dud_dth * Eb + Ea * dEb * duc_dth);
+      // centre: d dr / d c_k = -e_k
+      for (int k = 0; k < 3; k++) {
+        const double dud_dc = -sg * u[k];
+        const double duc_dc = uc > 1e-300 ? -(dr[k] - ud * u[k]) / uc : 0.0;
+        dg[1 + k] = 0.25 * (dEa * dud_dc * Eb + Ea * dEb * duc_dc);
+      }
+      for (int k = 0; k < 4; k++) {
+        acc[j * kGradPerPlate + 3 * k + 0] += dg[k] * w.x;
+        acc[j * kGradPerPlate + 3 * k + 1] += dg[k] * w.y;
+        acc[j * kGradPerPlate + 3 * k + 2] += dg[k];
+      }
+    }
+  }
+  const int nv = g.nplates * kGradPerPlate;
+  for (int k = 0; k < nv; k++) {
+    double v = acc[k];
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    const int wp = threadIdx.x >> 5, l = threadIdx.x & 31;
+    if (l == 0) red[wp] = v;
+    __syncthreads();
+    if (wp == 0) {
+      v = l < (int)(blockDim.x >> 5) ? red[l] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+      if (l == 0) part[(long long)blockIdx.x * nv + k] = v;
+    }
+    __syncthreads();
+  }
+}
+
+cudaError_t launch_geom_grad(const GradArgs &g, const double2 *wpl, double *part, int blocks, cudaStream_t st) {
+  k_geom_grad<<<blocks, 256, 0, st>>>(g, wpl, part);
+  return cudaGetLastError();
+}
+
+}  // namespace scft

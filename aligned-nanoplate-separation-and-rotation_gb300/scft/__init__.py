@@ -23,7 +23,7 @@ FIELD_NAMES = ("wpl", "wabp", "wabm", "wbcp", "wbcm", "wacp", "wacm")
 # Every extern "C" symbol declared in include/scft.h.
 EXPORTS = ("scft_last_error", "scft_version", "scft_create", "scft_destroy", "scft_get_info",
            "scft_set_fields", "scft_get_fields", "scft_calc_poly_density", "scft_update_1s",
-           "scft_calc_H", "scft_get_density", "scft_get_plate_density", "scft_get_smeared", "scft_diblock_density",
+           "scft_calc_H", "scft_grad_geom", "scft_get_density", "scft_get_plate_density", "scft_get_smeared", "scft_diblock_density",
            "scft_homopolymer_density", "scft_fft3d", "scft_sync", "scft_get_stream", "scft_launch_count",
            "scft_profile_step", "scft_diblock_density_noalloc")
 
@@ -91,6 +91,7 @@ def load(path: str | None = None):
     lib.scft_get_density.argtypes = [vp, ctypes.c_int, dp, dp, dp]
     lib.scft_get_smeared.argtypes = [vp, ctypes.c_int, dp, dp, dp]
     lib.scft_get_plate_density.argtypes = [vp, ctypes.c_int, dp]
+    lib.scft_grad_geom.argtypes = [vp, dp]
     lib.scft_diblock_density.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp, dp]
     lib.scft_homopolymer_density.argtypes = [vp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_double, dp, dp]
     lib.scft_fft3d.argtypes = [vp, ctypes.c_int, dp, ctypes.c_int, ctypes.c_int]
@@ -212,6 +213,12 @@ class Context:
         if code not in (OK, ERR_NAN):
             _check(code)
         self.last_status = code
+        return out
+
+    def grad_geom(self) -> np.ndarray:
+        """dH/d(theta_z, c_x, c_y, c_z) per instance and plate: shape (n, 2, 4)."""
+        out = np.zeros((self.n, 2, 4), np.float64)
+        _check(load().scft_grad_geom(self._h, _ptr(out)))
         return out
 
     def density(self, inst):

@@ -126,6 +126,17 @@ int scft_calc_H(scft_ctx *ctx, double *out);
  * rhoda, rhodb, rhog_exp (any may be NULL). */
 int scft_get_density(scft_ctx *ctx, int inst, double *rhoda, double *rhodb, double *rhog_exp);
 
+/* Derivatives of H (real part) with respect to the plate geometry at the
+ * current fields: out[8*inst + 4*j + {0,1,2,3}] = dH/dtheta, dH/dc_x,
+ * dH/dc_y, dH/dc_z for plate j (0 or 1), theta a rotation of the plate axis
+ * about z in radians, c the centre in b-units.  At a converged saddle point
+ * (delta H / delta w = 0) these are the total derivatives of the converged
+ * H; a separation d of two plates along an axis e gives
+ * dH/dd = (dH/dc_2 - dH/dc_1).e / 2.  The reference has no derivative code;
+ * this replaces finite differences over its sweeps (angle-rotation/,
+ * particle-separation/).  SCFT_ERR_UNSUPPORTED for grafted plates. */
+int scft_grad_geom(scft_ctx *ctx, double *out);
+
 /* The explicit plates' density rho_exp_nr of one instance (M real values),
  * as built at set-up (code/initialize.cpp:210-239). */
 int scft_get_plate_density(scft_ctx *ctx, int inst, double *rho_exp_nr);
