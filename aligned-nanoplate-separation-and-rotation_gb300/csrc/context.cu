@@ -344,6 +344,15 @@ void validate(const scft_params &p) {
     throw ScftError(SCFT_ERR_UNSUPPORTED, "grafted chains are built for the FP64 method only");
 }
 
+// alpha, beta of w <- alpha w - beta F for each field and sign branch of
+// code/1s_update.cpp:58-329: semi-implicit fields (lam_pl with A and B)
+// alpha = (1 + lam B)/(1 + lam A), beta = lam/(1 + lam A); explicit fields
+// (lam_mi) alpha = 1/(1 + lam 2 rho0/chi), beta = lam/(1 + lam 2 rho0/chi).
+// phiD and phiG are those of the set-up; they are final once the plates are
+// built, so this runs again from setup_plates (mix_coefficients_final).
+void mix_coefficients(scft_ctx *c, Instance &I, const std::vector<double> &hh, const std::vector<double> &gaa,
+                      const std::vector<double> &gab, const std::vector<double> &gbb, const std::vector<double> &gc);
+
 void setup_instance(scft_ctx *c, Instance &I, int idx) {
   const scft_params &p = I.p;
   I.N = p.Nda + p.Ndb;
@@ -454,6 +463,7 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
         k2t.push_back((float)(k * k / 6.0));
       }
     I.k2tab32 = dupload(c, k2t);
+    mix_coefficients(c, I, hh, gaa, gab, gbb, gc);
   }
   I.qpart = dalloc<double2>(c, g.nz);
   I.scal = dalloc<double2>(c, kNumScalars);
@@ -461,6 +471,84 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
   I.grafts = dalloc<double2>(c, M);
   I.rho_exp_nr = dalloc<double>(c, M);
   (void)idx;
+}
+
+void mix_coefficients(scft_ctx *c, Instance &I, const std::vector<double> &hh, const std::vector<double> &gaa,
+                      const std::vector<double> &gab, const std::vector<double> &gbb, const std::vector<double> &gc) {
+  (void)c;
+  I.tab_hh = hh;
+  I.tab_gaa = gaa;
+  I.tab_gab = gab;
+  I.tab_gbb = gbb;
+  I.tab_gc = gc;
+}
+
+void mix_coefficients_final(scft_ctx *c, Instance &I) {
+  const long long M = I.M;
+  const scft_params &p = I.p;
+  const double rho0 = p.rho0, N = I.N, Ng = I.Ng, phiD = I.info.phiD, phiG = I.info.phiG;
+  const double li = p.lam_pl, lr = p.lam_mi;
+  std::vector<double> a(M), b(M);
+  auto semi = [&](int f, auto Afun, double Boff) {
+    for (long long i = 0; i < M; i++) {
+      const double A = Afun(i), B = A - Boff;
+      a[i] = (1.0 + li * B) / (1.0 + li * A);
+      b[i] = li / (1.0 + li * A);
+    }
+    I.alpha[f] = dupload(c, a);
+    I.beta[f] = dupload(c, b);
+  };
+  auto expl = [&](int f, double chi) {
+    const double d = 1.0 + lr * 2.0 * rho0 / chi;
+    for (long long i = 0; i < M; i++) {
+      a[i] = 1.0 / d;
+      b[i] = lr / d;
+    }
+    I.alpha[f] = dupload(c, a);
+    I.beta[f] = dupload(c, b);
+  };
+  const auto &hh = I.tab_hh, &gaa = I.tab_gaa, &gab = I.tab_gab, &gbb = I.tab_gbb, &gc = I.tab_gc;
+  // w+ (:67-83)
+  semi(0, [&](long long i) {
+    return rho0 / p.kappa + phiD * rho0 * N * hh[i] * hh[i] * (gaa[i] + 2.0 * gab[i] + gbb[i]) +
+           (phiG * Ng * gc[i]) * rho0 * hh[i] * hh[i];
+  }, rho0 / p.kappa);
+  if (I.cab != 0.0) {
+    const double cc = I.cab;
+    if (!I.neg_ab) {
+      semi(1, [&](long long i) { return 2.0 * rho0 / cc + phiD * rho0 * N * hh[i] * hh[i] * (gaa[i] + 2.0 * gab[i] + gbb[i]); },
+           2.0 * rho0 / cc);
+      expl(2, cc);
+    } else {
+      expl(1, cc);
+      semi(2, [&](long long i) { return 2.0 * rho0 / cc + phiD * rho0 * N * hh[i] * hh[i] * (gaa[i] - gbb[i]); },
+           2.0 * rho0 / cc);
+    }
+  }
+  if (I.cbc != 0.0) {
+    const double cc = I.cbc;
+    if (!I.neg_bc) {
+      semi(3, [&](long long i) { return 2.0 * rho0 / cc + phiD * rho0 * N * hh[i] * hh[i] * gbb[i] + phiG * rho0 * Ng * hh[i] * hh[i] * gc[i]; },
+           2.0 * rho0 / cc);
+      expl(4, cc);
+    } else {
+      expl(3, cc);
+      semi(4, [&](long long i) { return 2.0 * rho0 / cc + phiD * rho0 * N * hh[i] * hh[i] * gbb[i] - phiG * Ng * hh[i] * hh[i] * rho0 * gc[i]; },
+           2.0 * rho0 / cc);
+    }
+  }
+  if (I.cac != 0.0) {
+    const double cc = I.cac;
+    if (!I.neg_ac) {
+      semi(5, [&](long long i) { return 2.0 * rho0 / cc + phiD * rho0 * N * hh[i] * hh[i] * gaa[i] + phiG * Ng * hh[i] * hh[i] * rho0 * gc[i]; },
+           2.0 * rho0 / cc);
+      expl(6, cc);
+    } else {
+      expl(5, cc);
+      semi(6, [&](long long i) { return 2.0 * rho0 / cc + phiD * rho0 * N * hh[i] * hh[i] * gaa[i] - phiG * Ng * hh[i] * hh[i] * rho0 * gc[i]; },
+           2.0 * rho0 / cc);
+    }
+  }
 }
 
 // Plate profile, graft map and chain counts (code/initialize.cpp:139-386).
@@ -549,6 +637,14 @@ void setup_plates(scft_ctx *c, Instance &I) {
     I.ghist = dalloc<double2>(c, (size_t)M * p.Ng);
     I.gacc = dalloc<double2>(c, M);
   }
+  if (I.mixed) {
+    mix_coefficients_final(c, I);
+    I.tab_hh.clear();
+    I.tab_gaa.clear();
+    I.tab_gab.clear();
+    I.tab_gbb.clear();
+    I.tab_gc.clear();
+  }
   CK(cudaStreamSynchronize(c->st));
 }
 
@@ -596,6 +692,10 @@ void build_jobs(scft_ctx *c) {
     F.acc32[1] = I.acc32[1];
     F.K = I.K;
     F.part64 = I.part;
+    for (int f = 0; f < 7; f++) {
+      F.alpha[f] = I.alpha[f];
+      F.beta[f] = I.beta[f];
+    }
 
     PropInst &P = pi[k];
     memset(&P, 0, sizeof P);

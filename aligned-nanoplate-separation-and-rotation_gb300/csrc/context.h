@@ -49,6 +49,8 @@ struct Instance {
   int *K = nullptr;
   float *h32 = nullptr;    // 1 - g(k), FP32
   float *k2tab32 = nullptr;  // [kx^2/6 | ky^2/6 | kz^2/6], FP32
+  double *alpha[7] = {}, *beta[7] = {};  // tabulated 1S coefficients (mixed form)
+  std::vector<double> tab_hh, tab_gaa, tab_gab, tab_gbb, tab_gc;  // host copies, set-up only
 };
 
 struct DevBuf {

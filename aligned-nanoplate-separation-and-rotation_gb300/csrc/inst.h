@@ -84,6 +84,9 @@ struct FieldInst {
   float *acc32[2];     // density sums, scaled by 2^-K[2N]
   int *K;              // [2][N] + 1
   double *part64;      // [2][N][nz] plane sums of the stored propagators
+  // mixed precision: the 1S update of field f is w <- alpha_f(k) w - beta_f(k) F_f(k)
+  // (NULL for fields whose chi is zero)
+  const double *alpha[7], *beta[7];
 };
 
 }  // namespace scft

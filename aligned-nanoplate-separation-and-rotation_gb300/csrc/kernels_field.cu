@@ -418,12 +418,100 @@ __global__ void k_mix_update(const FieldInst *__restrict__ fi) {
   }
 }
 
+// The same update with the k-only coefficients tabulated at set-up: for
+// every field and sign branch of code/1s_update.cpp:58-329 the step is
+// w <- (w - lam (F - B w)) / (1 + lam A) = alpha w - beta F, alpha, beta
+// functions of k alone.  No division per iteration; only fields with
+// nonzero chi are read and written.
+__global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
+  FOR_POINTS(F) {
+    const double2 Z = F.zr[i], Zm = F.zr[neg_k(F, i)];
+    const double2 ra = make_double2(0.5 * (Z.x + Zm.x), 0.5 * (Z.y - Zm.y));
+    const double2 rb = make_double2(0.5 * (Z.y + Zm.y), 0.5 * (Zm.x - Z.x));
+    const double rho0 = F.rho0, hh = F.hhat[i];
+    const double2 enh = F.exp_nrH[i];
+    double2 w[7];
+    for (int f = 0; f < 7; f++) w[f] = F.alpha[f] ? F.w[f][i] : make_double2(0.0, 0.0);
+    auto step = [&](int f, double2 Fv) {
+      const double a = F.alpha[f][i], b = F.beta[f][i];
+      w[f] = make_double2(a * w[f].x - b * Fv.x, a * w[f].y - b * Fv.y);
+    };
+    // w+ : I rho0 (exp_nrH - evar) + I hhat (rhoda + rhodb)
+    {
+      const double evar = (i == 0) ? 1.0 : 0.0;
+      const double2 sr = cadd(ra, rb);
+      const double2 u = make_double2(enh.x - evar, enh.y);
+      step(0, make_double2(-rho0 * u.y - hh * sr.y, rho0 * u.x + hh * sr.x));
+    }
+    if (F.alpha[1]) {  // AB pair
+      if (!F.neg_ab) {
+        double2 F1 = make_double2(-hh * (ra.y + rb.y), hh * (ra.x + rb.x));
+        if (F.np_chem == 1) F1 = make_double2(F1.x - rho0 * enh.x, F1.y - rho0 * enh.y);
+        double2 F2 = make_double2(hh * (rb.x - ra.x), hh * (rb.y - ra.y));
+        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
+        step(1, F1);
+        step(2, F2);
+      } else {
+        const double2 F1 = make_double2(-hh * (ra.x + rb.x), -hh * (ra.y + rb.y));
+        double2 F2 = make_double2(-hh * (ra.y - rb.y), hh * (ra.x - rb.x));
+        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
+        step(1, F1);
+        step(2, F2);
+      }
+    }
+    // BC and AC pairs see no graft density here (grafts run in the FP64 method)
+    const double2 zero = make_double2(0.0, 0.0);
+    if (F.alpha[3]) {
+      const double2 rg = zero;
+      if (!F.neg_bc) {
+        const double2 F1 = make_double2(-hh * (rg.y + rb.y), hh * (rg.x + rb.x));
+        double2 F2 = make_double2(hh * (rg.x - rb.x), hh * (rg.y - rb.y));
+        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
+        step(3, F1);
+        step(4, F2);
+      } else {
+        const double2 F1 = make_double2(-hh * (rb.x + rg.x), -hh * (rb.y + rg.y));
+        double2 F2 = make_double2(hh * (rg.y - rb.y), -hh * (rg.x - rb.x));
+        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
+        step(3, F1);
+        step(4, F2);
+      }
+    }
+    if (F.alpha[5]) {
+      const double2 rg = zero;
+      if (!F.neg_ac) {
+        const double2 F1 = make_double2(-hh * (rg.y + ra.y), hh * (rg.x + ra.x));
+        double2 F2 = make_double2(hh * (rg.x - ra.x), hh * (rg.y - ra.y));
+        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
+        step(5, F1);
+        step(6, F2);
+      } else {
+        const double2 F1 = make_double2(-hh * (ra.x + rg.x), -hh * (ra.y + rg.y));
+        double2 F2 = make_double2(hh * (rg.y - ra.y), -hh * (rg.x - ra.x));
+        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
+        step(5, F1);
+        step(6, F2);
+      }
+    }
+    for (int f = 0; f < 7; f++)
+      if (F.alpha[f]) F.w[f][i] = w[f];
+    double2 wa, wb, wg;
+    assemble_point(F, w, wa, wb, wg);
+    F.zs[i] = make_double2(hh * (wa.x - wb.y), hh * (wa.y + wb.x));
+  }
+}
+
 // After the inverse transform zs = smwa + i smwb (real space): Boltzmann
-// factors for the FP32 sweep.
+// factors for the FP32 sweep.  exp(-s) is evaluated in FP32 from a two-float
+// split s = s_hi + s_lo: exp(-s) = expf(-s_hi) (1 - s_lo), the neglected term
+// being O(s_lo^2) ~ 1e-14 relative, so the result carries expf's accuracy
+// without an FP64 exponential.
 __global__ void k_mix_boltzmann(const FieldInst *__restrict__ fi) {
   FOR_POINTS(F) {
     const double2 s = F.zs[i];
-    F.E32[i] = make_float2((float)exp(-s.x), (float)exp(-s.y));
+    const float ah = (float)s.x, al = (float)(s.x - (double)ah);
+    const float bh = (float)s.y, bl = (float)(s.y - (double)bh);
+    F.E32[i] = make_float2(expf(-ah) * (1.0f - al), expf(-bh) * (1.0f - bl));
   }
 }
 
@@ -447,9 +535,10 @@ __global__ void k_mix_q_finalize(const FieldInst *__restrict__ fi, int ninst) {
 __global__ void k_mix_rho_pack(const FieldInst *__restrict__ fi, int keep) {
   FOR_POINTS(F) {
     const double f = ldexp(F.scal[kFactor].x, F.K[2 * F.N]);  // accumulators are scaled by 2^-Kref
-    const double2 s = F.zs[i];
-    const double ra = (double)F.acc32[0][i] * (exp(s.x) * f);
-    const double rb = (double)F.acc32[1][i] * (exp(s.y) * f);
+    // e^{+smw} = 1 / e^{-smw}: the FP32 reciprocal of the Boltzmann factor
+    const float2 E = F.E32[i];
+    const double ra = (double)(F.acc32[0][i] * __frcp_rn(E.x)) * f;
+    const double rb = (double)(F.acc32[1][i] * __frcp_rn(E.y)) * f;
     F.zr[i] = make_double2(ra, rb);
     if (keep) {
       F.rho[0][i] = make_double2(ra, 0.0);
@@ -515,7 +604,7 @@ cudaError_t launch_mix_smear(const FieldInst *fi, int ninst, int blocks, cudaStr
   return cudaGetLastError();
 }
 cudaError_t launch_mix_update(const FieldInst *fi, int ninst, int blocks, cudaStream_t st) {
-  k_mix_update<<<dim3(blocks, ninst), 256, 0, st>>>(fi);
+  k_mix_update_tab<<<dim3(blocks, ninst), 256, 0, st>>>(fi);
   return cudaGetLastError();
 }
 cudaError_t launch_mix_boltzmann(const FieldInst *fi, int ninst, int blocks, cudaStream_t st) {

@@ -146,6 +146,9 @@ def main():
     ap.add_argument("--form", choices=["mixed", "plain"], default=None)
     ap.add_argument("--workload", default="sweep15_64_N100")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--iterations-only", action="store_true",
+                    help="warm-up + timed iterations only (for ncu launch lists)")
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -233,6 +236,11 @@ def main():
     ms = allmax(e0.elapsed_time(e1))
     H = ctx.calc_H()
     value = n_inst * args.steps * world / (ms / 1e3)
+    if args.iterations_only:
+        ctx.close()
+        if rank == 0:
+            print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "iterations_only": True}))
+        return
 
     # ---- end to end through the C ABI with pinned host buffers
     import numpy as np
@@ -259,6 +267,33 @@ def main():
     t_e2e = allmax(time.perf_counter() - t0)
     e2e = {"value": n_inst * e2e_steps * world / t_e2e, "unit": UNIT,
            "h2d_bytes_per_step": int(sum(7 * 16 * m for m in M)), "d2h_bytes_per_step": int(5 * 8 * n_inst)}
+
+    # ---- the plain FP64 method on the same batch, same iteration count:
+    # its rate (the metric's comparison) and the mixed form's H error
+    plain = None
+    if form == "mixed" and not args.no_plain:
+        pp = WORKLOADS[args.workload](scft.PREC_FP64)
+        with scft.Context(pp) as c64:
+            for k in range(n_inst):
+                c64.set_fields(k, fields[k])
+            c64.calc_poly_density()
+            c64.update_1s(max(3, args.warmup))
+            s64 = torch.cuda.ExternalStream(c64.stream())
+            f0 = torch.cuda.Event(enable_timing=True)
+            f1 = torch.cuda.Event(enable_timing=True)
+            barrier()
+            f0.record(s64)
+            c64.update_1s(args.steps)
+            f1.record(s64)
+            f1.synchronize()
+            ms64 = allmax(f0.elapsed_time(f1))
+            H64 = c64.calc_H()
+        dH = np.abs(H[:, 0] - H64[:, 0]) / np.abs(H64[:, 0])
+        plain = {"value": n_inst * args.steps * world / (ms64 / 1e3), "unit": UNIT, "ms_per_step": ms64 / args.steps,
+                 "mixed_over_plain": (n_inst * args.steps * world / (ms / 1e3)) / (n_inst * args.steps * world /
+                                                                                    (ms64 / 1e3)),
+                 "dH_rel_max": float(dH.max()), "dH_rel_median": float(np.median(dH)),
+                 "note": "same batch and fields, max(3, warmup) + steps iterations each"}
 
     # ---- dominant kernel, isolated (after the timed regions)
     prof = ctx.profile_step(20)
@@ -292,7 +327,7 @@ def main():
                 "dtype": "f32 propagators / f64 fields" if form == "mixed" else "c128 (complex f64)",
                 "data": "synthetic seeded fields", "config": config, "e2e": e2e, "roofline": roofline,
                 "cpu_baseline": cpu, "clocks": ck, "gpu_launches": launches,
-                "H_first_instance": float(H[0, 0])}
+                "plain_fp64": plain, "H_first_instance": float(H[0, 0])}
         print(json.dumps(line))
     if dist is not None:
         dist.destroy_process_group()
