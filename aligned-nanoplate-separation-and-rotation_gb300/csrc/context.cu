@@ -1172,7 +1172,8 @@ void ctx_update(scft_ctx *c, int n_iter) {
   CK(cudaStreamSynchronize(c->st));
 }
 
-// Isolated timing of the two kernels of one propagator step (plain FP64).
+// Isolated timing of the two kernels of one propagator step (step 3(N-1)/4,
+// a paired step) with their algorithmic bytes.
 void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
                       double *bytes_col) {
   if (c->dirty_density) ctx_poly_density(c);
@@ -1215,9 +1216,10 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
     if (I.N <= s) continue;
     if (I.mixed) {
       // plane: read z, E (8 B each), stored pair (8 B), write z (8 B), RMW of
-      // the FP32 accumulators A and B (2 x 8 B); column: read + write z, h table
+      // the FP32 accumulators A and B (2 x 8 B); column: read + write z, plus
+      // the h table in the generic pass (the 64-point pass forms h on the fly)
       bp += I.M * (4.0 * sizeof(float2) + 4.0 * sizeof(float));
-      bc += I.M * (2.0 * sizeof(float2) + sizeof(float));
+      bc += I.M * (2.0 * sizeof(float2) + (c->all64 ? 0.0 : sizeof(float)));
     } else {
       const double props = I.single ? 1.0 : 2.0;
       bp += props * I.M * 6.0 * sizeof(double2);

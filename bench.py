@@ -35,6 +35,10 @@ PKG = os.path.join(ROOT, "aligned-nanoplate-separation-and-rotation_gb300")
 sys.path.insert(0, PKG)
 
 METRIC = "SCFT iters/s @64^3,N=100"
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant
+# kernel, from an ncu capture of the same workload (the paired plane-pass step;
+# profiles/mixed_kernels_sweep15_64_N100_ncu.txt).  Only valid for that workload.
+NCU_TRAFFIC = {("sweep15_64_N100", "mixed"): 125.928704e6 + 15.102208e6}
 UNIT = "iters/s"
 
 
@@ -149,6 +153,9 @@ def main():
     ap.add_argument("--iterations-only", action="store_true",
                     help="warm-up + timed iterations only (for ncu launch lists)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
+    ap.add_argument("--relax", type=int, default=500,
+                    help="untimed mixed-form iterations from the seeded fields before anything is measured, so "
+                         "that timing and the FP64 comparison start near the saddle point (0: seeded fields)")
     args = ap.parse_args()
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -163,9 +170,12 @@ def main():
     params = WORKLOADS[args.workload](prec)
     fields = [seeded_fields(p, 1000 + k) for k, p in enumerate(params)]
     n_inst = len(params)
-    config = {"workload": f"{args.workload}: {n_inst} plate instance(s), 64^3 grid, N=100, chiN=20, C=50, "
-                          "1S update", "form": form, "instances_per_rank": n_inst,
+    grids = sorted({"x".join(str(v) for v in p.Nx) for p in params})
+    chains = sorted({p.Nda + p.Ndb for p in params})
+    config = {"workload": f"{args.workload}: {n_inst} plate instance(s), grid(s) {', '.join(grids)}, "
+                          f"N in {chains}, chiN=20, C=50, 1S update", "form": form, "instances_per_rank": n_inst,
               "grid": list(params[0].Nx), "N": params[0].Nda + params[0].Ndb,
+              "relax_iterations": args.relax,
               "l2": "working set per step larger than L2 (no flush)"}
 
     if args.impl == "reference":
@@ -209,6 +219,14 @@ def main():
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         return float(t.item())
 
+    if args.relax > 0 and scft.mixed_available():
+        # near-saddle start: relax the seeded fields with the mixed form
+        with scft.Context(WORKLOADS[args.workload](scft.PREC_MIXED)) as cr:
+            for k in range(n_inst):
+                cr.set_fields(k, fields[k])
+            cr.calc_poly_density()
+            cr.update_1s(args.relax)
+            fields = [cr.get_fields(k) for k in range(n_inst)]
     ctx = scft.Context(params)
     for k in range(n_inst):
         ctx.set_fields(k, fields[k])
@@ -236,6 +254,8 @@ def main():
     ms = allmax(e0.elapsed_time(e1))
     H = ctx.calc_H()
     value = n_inst * args.steps * world / (ms / 1e3)
+    rho_mixed = [ctx.density(k) for k in range(n_inst)] if (form == "mixed" and not args.no_plain
+                                                             and not args.iterations_only) else None
     if args.iterations_only:
         ctx.close()
         if rank == 0:
@@ -288,22 +308,38 @@ def main():
             f1.synchronize()
             ms64 = allmax(f0.elapsed_time(f1))
             H64 = c64.calc_H()
+            drho = []
+            for k in range(n_inst):
+                a64, b64, _ = c64.density(k)
+                a32, b32, _ = rho_mixed[k]
+                drho.append(max(np.abs(a32 - a64).max() / np.abs(a64).max(),
+                                np.abs(b32 - b64).max() / np.abs(b64).max()))
         dH = np.abs(H[:, 0] - H64[:, 0]) / np.abs(H64[:, 0])
         plain = {"value": n_inst * args.steps * world / (ms64 / 1e3), "unit": UNIT, "ms_per_step": ms64 / args.steps,
                  "mixed_over_plain": (n_inst * args.steps * world / (ms / 1e3)) / (n_inst * args.steps * world /
                                                                                     (ms64 / 1e3)),
                  "dH_rel_max": float(dH.max()), "dH_rel_median": float(np.median(dH)),
-                 "note": "same batch and fields, max(3, warmup) + steps iterations each"}
+                 "dH_abs_max": float(np.abs(H[:, 0] - H64[:, 0]).max()),
+                 "drho_rel_max": float(max(drho)),
+                 "per_instance": [{"grid": list(p.Nx), "N": p.Nda + p.Ndb, "dH_rel": float(d), "drho_rel": float(r)}
+                                  for p, d, r in zip(params, dH, drho)],
+                 "note": f"same batch, both from the fields after {args.relax} mixed-form iterations from the "
+                         f"seeded start, then max(3, warmup) + steps iterations each; drho = max |rho32 - rho64| / "
+                         f"max |rho64| over rho_A, rho_B"}
 
     # ---- dominant kernel, isolated (after the timed regions)
     prof = ctx.profile_step(20)
+    all64 = all(tuple(p.Nx) == (64, 64, 64) for p in params)
+    kernel_names = {"mixed": ("k_mix_plane64", "k_mix_col64") if all64 else ("k_mix_prop_plane", "k_col_fft<float>"),
+                    "plain": ("k_prop_plane_f64", "k_col_fft<double> (bond kernel)")}
     hbm, peak_kind = peaks()
     dom = "plane" if prof["ms_plane"] >= prof["ms_col"] else "col"
     ms_k = prof["ms_" + dom]
     by = prof["bytes_" + dom]
     achieved = by / (ms_k / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": None, "kernel": ("k_prop_plane" if dom == "plane" else "k_col_fft (bond kernel)"),
+                "traffic": NCU_TRAFFIC.get((args.workload, form)) if dom == "plane" else None,
+                "kernel": kernel_names[form][0 if dom == "plane" else 1],
                 "peak_kind": peak_kind, "ms_per_launch": ms_k, "algorithmic_bytes_per_launch": by,
                 "other_kernel_ms_per_launch": prof["ms_col" if dom == "plane" else "ms_plane"]}
     ctx.close()
