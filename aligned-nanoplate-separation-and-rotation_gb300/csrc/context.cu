@@ -454,15 +454,16 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
     std::vector<float> h32(M);
     for (long long i = 0; i < M; i++) h32[i] = (float)(1.0 - pb[i]);
     I.h32 = dupload(c, h32);
-    // per-axis k^2/6 with get_k's branch (code/array_utils.cpp:248-265)
-    std::vector<float> k2t;
+    // per-axis h_d = 1 - exp(-k_d^2/6) with get_k's branch
+    // (code/array_utils.cpp:248-265); g(k) = prod_d (1 - h_d)
+    std::vector<float> ht;
     for (int d = 0; d < 3; d++)
       for (int nn = 0; nn < p.Nx[d]; nn++) {
         const double k = (double(nn) < double(p.Nx[d]) / 2.) ? 2 * kPI * double(nn) / p.L[d]
                                                             : 2 * kPI * double(nn - p.Nx[d]) / p.L[d];
-        k2t.push_back((float)(k * k / 6.0));
+        ht.push_back((float)(-std::expm1(-k * k / 6.0)));
       }
-    I.k2tab32 = dupload(c, k2t);
+    I.htab32 = dupload(c, ht);
     mix_coefficients(c, I, hh, gaa, gab, gbb, gc);
   }
   I.qpart = dalloc<double2>(c, g.nz);
@@ -743,6 +744,7 @@ void build_jobs(scft_ctx *c) {
       X.K = I.K;
     }
     c->d_mi = dupload(c, mi);
+    c->h_mi = mi;
   }
 
   // field transform job lists
@@ -856,9 +858,11 @@ void build_jobs(scft_ctx *c) {
       std::vector<ColJob> cj64(pcj);
       for (auto &j : cj64) {
         for (auto &I : c->inst)
-          if (j.ptr == I.work32) j.kern = I.k2tab32;
+          if (j.ptr == I.work32) j.kern = I.htab32;
       }
       c->d_mix64_cj = dupload(c, cj64);
+      c->mix64_tab.clear();
+      for (int oi = 0; oi < n; oi++) c->mix64_tab.push_back(c->h_mi[order[oi]]);
     }
     c->shp_col32 = choose_shape(emax_col, sizeof(float2), (nz_max + 32) * sizeof(float2));
   }
@@ -1036,10 +1040,10 @@ void seq_mix_sweep(scft_ctx *c) {
     CK(cudaMemsetAsync(I.acc32[1], 0, sizeof(float) * I.M, st));
   }
   if (c->all64) {
-    LK(launch_mix_plane64(c->d_prop_pj, c->prop_pj_count[0], c->d_mi, c->d_tw32_64, 0, st));
+    LK(launch_mix_plane64(c->mix64_tab.data(), c->prop_pj_count[0] / 64, c->d_tw32_64, 0, st));
     for (int s = 1; s < c->nmax; s++) {
       LK(launch_mix_col64(c->d_mix64_cj, c->prop_cj_count[s], c->d_tw32_64, 64, 64, st));
-      LK(launch_mix_plane64(c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_tw32_64, s, st));
+      LK(launch_mix_plane64(c->mix64_tab.data(), c->prop_pj_count[s] / 64, c->d_tw32_64, s, st));
     }
   } else {
     LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[0], c->d_mi, c->d_geoms, c->d_tw32, 0,
@@ -1185,7 +1189,7 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   CK(cudaEventRecord(e0, c->st));
   for (int r = 0; r < reps; r++) {
     if (c->mixed && c->all64)
-      LK(launch_mix_plane64(c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_tw32_64, s, c->st));
+      LK(launch_mix_plane64(c->mix64_tab.data(), c->prop_pj_count[s] / 64, c->d_tw32_64, s, c->st));
     else if (c->mixed)
       LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_geoms, c->d_tw32, s,
                                c->st));

@@ -48,7 +48,7 @@ struct Instance {
   double *part = nullptr;
   int *K = nullptr;
   float *h32 = nullptr;    // 1 - g(k), FP32
-  float *k2tab32 = nullptr;  // [kx^2/6 | ky^2/6 | kz^2/6], FP32
+  float *htab32 = nullptr;  // [hx | hy | hz], h_d = 1 - exp(-k_d^2/6), FP32
   double *alpha[7] = {}, *beta[7] = {};  // tabulated 1S coefficients (mixed form)
   std::vector<double> tab_hh, tab_gaa, tab_gab, tab_gbb, tab_gc;  // host copies, set-up only
 };
@@ -94,6 +94,8 @@ struct scft_ctx {
   void *d_tw32 = nullptr;
   scft::ColJob *d_mix64_cj = nullptr;  // z-pass jobs of the 64^3 kernels
   scft::MixInst *d_mi = nullptr;
+  std::vector<scft::MixInst> h_mi;       // host copy of d_mi
+  std::vector<scft::MixInst> mix64_tab;  // instances in job order (64^3 plane pass)
   scft::PropJob *d_mix_pj = nullptr;
   scft::ColJob *d_mix_cj = nullptr;
   scft::PlaneJob *d_pj_zr = nullptr, *d_pj_zs = nullptr;

@@ -25,6 +25,8 @@
 #include "launch.h"
 #include "prop_launch.h"
 
+#include <string.h>
+
 namespace scft {
 
 namespace {
@@ -98,11 +100,13 @@ __device__ __forceinline__ void prefetch_plane(float2 *dst, const float2 *src, u
 
 }  // namespace
 
-// Plane pass of step n for 64 x 64 xy planes, 512 threads.  Dynamic shared
-// memory: exchange/transpose plane, prefetched Boltzmann plane, prefetched
-// history plane (3 padded planes, 110.6 KB; two CTAs per SM).
-__global__ void __launch_bounds__(512, 2) k_mix_plane64(const PropJob *__restrict__ jobs,
-                                                        const MixInst *__restrict__ insts,
+// Plane pass of step n for 64 x 64 xy planes, 512 threads, one CTA per
+// (instance, z plane): CTA b works on plane b % 64 of T.inst[b / 64].  The
+// instance table is a kernel parameter, so the first global loads (the
+// working plane, the prefetches) depend on nothing loaded before them.
+// Dynamic shared memory: exchange/transpose plane, prefetched Boltzmann
+// plane, prefetched history plane (3 padded planes, 110.6 KB; two CTAs per SM).
+__global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ Mix64Table T,
                                                         const float2 *__restrict__ tw_g, int n) {
   extern __shared__ __align__(16) float2 dsm[];
   float2 *buf = dsm;
@@ -112,59 +116,67 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const PropJob *__restric
   __shared__ double s_red[2][16];
   __shared__ double s_mu[2];
   __shared__ int s_exp[2];
-  const PropJob jb = jobs[blockIdx.x];
-  const MixInst &P = insts[jb.inst];
+  const MixInst &P = T.inst[blockIdx.x >> 6];
+  const int zz = blockIdx.x & 63;
   const int N = P.N, Na = P.Na;
   if (n >= N) return;
   const int nz = 64;
   const long long M = 64LL * 64 * 64;
-  const long long zoff = (long long)jb.z * 4096;
+  const long long zoff = (long long)zz * 4096;
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
+  // row-phase ownership: (y = row, x = tr + 8d); column phase: (y = tc + 8d, x = col)
+  const int row = tid >> 3, tr = tid & 7;
+  const int col = tid & 63, tc = tid >> 6;
+  float2 v[8];
+  float2 *work = P.work + zoff;
+  if (n > 0) {
+#pragma unroll
+    for (int a = 0; a < 8; a++) v[a] = work[(tc + 8 * a) * 64 + col];
+  }
   const int m2 = N - 1 - n;
   const bool pair = (m2 < n);  // a stored partner plane is needed
   const uint64_t pol_first = l2_policy_first();
   prefetch_plane(Es, P.E + zoff, l2_policy_last());
   if (pair) prefetch_plane(Hs, P.hist + (long long)m2 * M + zoff, pol_first);
   cp_async_commit();
-  if (tid < 64) tw[tid] = tw_g[tid];
-  if (warp == 0) {
-    double a = 0.0, b = 0.0;
-    if (n > 0) {
-      const double *pq = P.part + (long long)(n - 1) * nz;
-      const double *pd = P.part + (long long)(N + n - 1) * nz;
-      for (int z = lane; z < nz; z += 32) {
-        a += pq[z];
-        b += pd[z];
-      }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      a += __shfl_down_sync(0xffffffffu, a, o);
-      b += __shfl_down_sync(0xffffffffu, b, o);
-    }
-    if (lane == 0) {
-      const double ma = a / (double)M, mb = b / (double)M;
-      int ea = 0, eb = 0;
-      if (n > 0 && isfinite(ma) && ma > 0.0) frexp(ma, &ea);
-      if (n > 0 && isfinite(mb) && mb > 0.0) frexp(mb, &eb);
-      s_exp[0] = ea;
-      s_exp[1] = eb;
-      s_mu[0] = ma;
-      s_mu[1] = mb;
+  // accumulators of a paired step, loaded now so that their latency overlaps
+  // the inverse transforms (row-phase ownership, as they are used)
+  const int gi = row * 64 + tr;  // global index of element d = 0 in this plane
+  float acc1[8], acc2[8];
+  float *a1 = P.acc[n < Na ? 0 : 1] + zoff + gi;
+  float *a2 = P.acc[m2 < Na ? 0 : 1] + zoff + gi;
+  const bool same_acc = (a1 == a2);
+  if (pair) {
+#pragma unroll
+    for (int d = 0; d < 8; d++) acc1[d] = a1[8 * d];
+    if (!same_acc) {
+#pragma unroll
+      for (int d = 0; d < 8; d++) acc2[d] = a2[8 * d];
     }
   }
-  // row-phase ownership: (y = row, x = tr + 8d); column phase: (y = tc + 8d, x = col)
-  const int row = tid >> 3, tr = tid & 7;
-  const int col = tid & 63, tc = tid >> 6;
-  float2 v[8];
-  float2 *work = P.work + zoff;
+  if (tid < 64) tw[tid] = tw_g[tid];
+  if (warp < 2) {
+    // warp 0: mean of q_{n-1}; warp 1: mean of qdag_{n-1} (64 FP64 plane sums each)
+    double a = 0.0;
+    if (n > 0) {
+      const double *pp = P.part + (long long)(warp * N + n - 1) * nz;
+      a = pp[lane] + pp[lane + 32];
+    }
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) {
+      const double ma = a * (1.0 / (double)M);  // M = 2^18: exact
+      int ea = 0;
+      if (n > 0 && isfinite(ma) && ma > 0.0) frexp(ma, &ea);
+      s_exp[warp] = ea;
+      s_mu[warp] = ma;
+    }
+  }
   const bool useA_q = (Na > 0 && n < Na);
   const bool useA_d = !(n <= N - Na - 1);
   __syncthreads();  // tw, s_mu, s_exp
   if (n > 0) {
     // inverse y transform (column phase)
-#pragma unroll
-    for (int a = 0; a < 8; a++) v[a] = work[(tc + 8 * a) * 64 + col];
     fft64_group<+1, false>(v, tc, buf + col, 8 * 64, 64, tw);
 #pragma unroll
     for (int d = 0; d < 8; d++) buf[(tc + 8 * d) * kRowPad + col] = v[d];
@@ -202,12 +214,11 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const PropJob *__restric
   }
   const int Kq = (n == 0) ? 0 : P.K[n - 1] + s_exp[0];
   const int Kd = (n == 0) ? 0 : P.K[N + n - 1] + s_exp[1];
-  if (jb.z == 0 && tid == 0) {
+  if (zz == 0 && tid == 0) {
     P.K[n] = Kq;
     P.K[N + n] = Kd;
   }
   // history, density terms, plane sums (row-phase ownership)
-  const int gi = row * 64 + tr;  // global index of element d = 0 in this plane
   if (n <= P.hmax) {
     float2 *hst = P.hist + (long long)n * M + zoff + gi;
 #pragma unroll
@@ -216,30 +227,27 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const PropJob *__restric
   const int n0 = N / 2;
   if (m2 <= n) {
     const int Kref = (n == n0) ? Kq + (m2 == n ? Kd : P.K[N + m2]) : P.K[2 * N];
-    if (n == n0 && jb.z == 0 && tid == 0) P.K[2 * N] = Kref;
+    if (n == n0 && zz == 0 && tid == 0) P.K[2 * N] = Kref;
     if (pair) {
       const float2 *Hr = Hs + row * kRowPad + tr;
       const float f1 = ldexpf(1.0f, Kq + P.K[N + m2] - Kref);
       const float f2 = ldexpf(1.0f, P.K[m2] + Kd - Kref);
-      float *a1 = P.acc[n < Na ? 0 : 1] + zoff + gi;
-      float *a2 = P.acc[m2 < Na ? 0 : 1] + zoff + gi;
-      if (a1 == a2) {
+      if (same_acc) {
 #pragma unroll
         for (int d = 0; d < 8; d++) {
           const float2 h = Hr[8 * d];
-          a1[8 * d] += fmaf(v[d].x * h.y, f1, (h.x * v[d].y) * f2);
+          a1[8 * d] = acc1[d] + fmaf(v[d].x * h.y, f1, (h.x * v[d].y) * f2);
         }
       } else {
 #pragma unroll
         for (int d = 0; d < 8; d++) {
           const float2 h = Hr[8 * d];
-          a1[8 * d] += (v[d].x * h.y) * f1;
-          a2[8 * d] += (h.x * v[d].y) * f2;
+          a1[8 * d] = acc1[d] + (v[d].x * h.y) * f1;
+          a2[8 * d] = acc2[d] + (h.x * v[d].y) * f2;
         }
       }
     } else {
       const float f = ldexpf(1.0f, Kq + Kd - Kref);
-      float *a1 = P.acc[n < Na ? 0 : 1] + zoff + gi;
 #pragma unroll
       for (int d = 0; d < 8; d++) a1[8 * d] += (v[d].x * v[d].y) * f;
     }
@@ -276,8 +284,8 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const PropJob *__restric
       ad += __shfl_down_sync(0xffffffffu, ad, o);
     }
     if (lane == 0) {
-      P.part[(long long)n * nz + jb.z] = aq;
-      P.part[(long long)(N + n) * nz + jb.z] = ad;
+      P.part[(long long)n * nz + zz] = aq;
+      P.part[(long long)(N + n) * nz + zz] = ad;
     }
   }
   if (n == N - 1) return;
@@ -295,9 +303,12 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const PropJob *__restric
 }
 
 // z pass for nz = 64 (mode 3 of the generic column pass): tile of TX x columns
-// at one y, 8 threads per column.  h = 1 - g(k) is formed on the fly as
-// -expm1(-(kx^2 + ky^2 + kz^2)/6) from per-axis tables k2 = [kx^2/6 | ky^2/6 |
-// kz^2/6] (jb.kern), so the pass moves only the propagator itself.
+// at one y, 8 threads per column.  g(k) = gx gy gz factorises over the axes,
+// so h = 1 - g(k) is formed on the fly from per-axis tables h_d = 1 - g_d
+// (jb.kern = [hx | hy | hz], each -expm1(-k_d^2/6) rounded once) as
+// 1 - (1 - a)(1 - b) = a + b - a b, applied twice: every term is positive, so
+// h keeps its relative accuracy where it is small.  The pass moves only the
+// propagator itself.
 template <int TX>
 __global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__ jobs,
                                                       const float2 *__restrict__ tw_g, int nx, int ny, float s_hi,
@@ -311,8 +322,9 @@ __global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__
   const long long plane = (long long)nx * ny;
   const long long base = (long long)jb.y * nx + jb.x0 + col;
   float2 *a = reinterpret_cast<float2 *>(jb.ptr);
-  const float *k2 = reinterpret_cast<const float *>(jb.kern);
-  const float kxy = k2[jb.x0 + col] + k2[nx + jb.y];
+  const float *ht = reinterpret_cast<const float *>(jb.kern);
+  const float hx = ht[jb.x0 + col], hy = ht[nx + jb.y];
+  const float hxy = fmaf(-hx, hy, hx + hy);
   float2 v[8];
 #pragma unroll
   for (int j = 0; j < 8; j++) v[j] = a[(t + 8 * j) * plane + base];
@@ -321,7 +333,8 @@ __global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__
 #pragma unroll
   for (int d = 0; d < 8; d++) {
     const int kz = t + 8 * d;
-    const float hv = -expm1f(-(kxy + k2[nx + ny + kz]));
+    const float hz = ht[nx + ny + kz];
+    const float hv = fmaf(-hxy, hz, hxy + hz);
     float2 u = make_float2(fmaf(v[d].x, s_hi, v[d].x * s_lo), fmaf(v[d].y, s_hi, v[d].y * s_lo));
     u = make_float2(fmaf(-hv, u.x, u.x), fmaf(-hv, u.y, u.y));
     if (kz == 0 && jb.y == 0 && jb.x0 + col == 0) u = make_float2(0.f, 0.f);
@@ -332,16 +345,23 @@ __global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__
   for (int j = 0; j < 8; j++) a[(t + 8 * j) * plane + base] = v[j];
 }
 
-cudaError_t launch_mix_plane64(const PropJob *jobs, int njobs, const MixInst *insts, const void *tw64,
-                               int n, cudaStream_t st) {
-  if (njobs <= 0) return cudaSuccess;
+cudaError_t launch_mix_plane64(const MixInst *insts, int ninst, const void *tw64, int n, cudaStream_t st) {
+  if (ninst <= 0) return cudaSuccess;
   const int smem = 3 * kPlanePad * (int)sizeof(float2);
   cudaError_t e = cudaFuncSetAttribute(k_mix_plane64, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_mix_plane64, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e != cudaSuccess) return e;
-  k_mix_plane64<<<njobs, 512, smem, st>>>(jobs, insts, reinterpret_cast<const float2 *>(tw64), n);
-  return cudaGetLastError();
+  for (int i0 = 0; i0 < ninst; i0 += kMix64MaxInst) {
+    const int cnt = ninst - i0 < kMix64MaxInst ? ninst - i0 : kMix64MaxInst;
+    Mix64Table T;
+    memset(&T, 0, sizeof T);
+    for (int k = 0; k < cnt; k++) T.inst[k] = insts[i0 + k];
+    k_mix_plane64<<<64 * cnt, 512, smem, st>>>(T, reinterpret_cast<const float2 *>(tw64), n);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw64, int nx, int ny, cudaStream_t st) {

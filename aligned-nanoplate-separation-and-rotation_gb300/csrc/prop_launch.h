@@ -23,8 +23,14 @@ cudaError_t launch_h_partials(const FieldInst *fi, int ninst, int blocks, double
 
 cudaError_t launch_mix_prop_plane(const LaunchShape &ls, const PropJob *jobs, int njobs, const MixInst *insts,
                                   const DevGeom *geoms, const void *tw, int n, cudaStream_t st);
-cudaError_t launch_mix_plane64(const PropJob *jobs, int njobs, const MixInst *insts, const void *tw64, int n,
-                               cudaStream_t st);
+// Instances of one 64^3 plane-pass launch, passed by value as the kernel
+// parameter (3.5 KB); larger batches are launched in chunks.
+constexpr int kMix64MaxInst = 48;
+struct Mix64Table {
+  MixInst inst[kMix64MaxInst];
+};
+// insts: host array of the active instances in job order (64 CTAs each)
+cudaError_t launch_mix_plane64(const MixInst *insts, int ninst, const void *tw64, int n, cudaStream_t st);
 cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw64, int nx, int ny, cudaStream_t st);
 cudaError_t launch_mix_smear(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
 cudaError_t launch_mix_update(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
