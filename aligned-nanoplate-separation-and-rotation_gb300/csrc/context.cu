@@ -239,6 +239,12 @@ __global__ void k_scale_c(double2 *a, double2 s, long long M, int divide) {
   }
 }
 
+// U = lam * (Re big - Re core): the shell between the enlarged and the core plate.
+__global__ void k_shell_potential(double *out, const double2 *big, const double2 *core, double lam, long long M) {
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x)
+    out[i] = lam * (big[i].x - core[i].x);
+}
+
 __global__ void k_real_part(double *out, const double2 *in, long long M) {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x)
     out[i] = in[i].x;
@@ -339,6 +345,10 @@ void validate(const scft_params &p) {
     if (!(p.xi_nr > 0)) bad("xi_nr must be positive");
   }
   if (p.precision != SCFT_PREC_FP64 && p.precision != SCFT_PREC_MIXED) bad("unknown precision");
+  if (p.shell_lambda != 0.0) {
+    if (p.n_exp_nr == 0) bad("the shell potential needs at least one plate");
+    if (!(p.shell_width > 0)) bad("shell_width must be positive when shell_lambda != 0");
+  }
   if (p.sigma > 0 && p.Ng < 1) bad("grafted chains need Ng >= 1");
   if (p.precision == SCFT_PREC_MIXED && p.sigma > 0 && p.Ng > 0 && p.n_exp_nr > 0)
     throw ScftError(SCFT_ERR_UNSUPPORTED, "grafted chains are built for the FP64 method only");
@@ -604,6 +614,20 @@ void setup_plates(scft_ctx *c, Instance &I) {
   }
   k_real_part<<<blocks, 256, 0, c->st>>>(I.rho_exp_nr, rho_np, M);
   CK(cudaGetLastError());
+  // A-attractive shell (extension, no reference counterpart): U_A = Lambda *
+  // sum_j [rho_p(L + 2w, R + w) - rho_p(L, R)], acting on A segments like an
+  // external field added to the smeared w_A
+  if (p.shell_lambda != 0.0 && p.n_exp_nr > 0) {
+    double2 *big = dalloc<double2>(c, M);
+    for (int j = 0; j < p.n_exp_nr; j++) {
+      k_plate<<<blocks, 256, 0, c->st>>>(big, plate_args(j, p.L_nr + 2.0 * p.shell_width, p.R_nr + p.shell_width),
+                                         1);
+      CK(cudaGetLastError());
+    }
+    I.shellU = dalloc<double>(c, M);
+    k_shell_potential<<<blocks, 256, 0, c->st>>>(I.shellU, big, rho_np, p.shell_lambda, M);
+    CK(cudaGetLastError());
+  }
   CK(cudaMemcpyAsync(I.exp_nrH, rho_np, sizeof(double2) * M, cudaMemcpyDeviceToDevice, c->st));
   fft3d_arrays(c, I, {I.exp_nrH}, -1);
   // volumes and counts (code/initialize.cpp:249-386), no film, no field NPs
@@ -676,6 +700,7 @@ void build_jobs(scft_ctx *c) {
     F.hhat = I.hhat; F.gaa = I.gaa; F.gab = I.gab; F.gbb = I.gbb; F.gc = I.gc;
     F.rho_exp_nr = I.rho_exp_nr;
     F.exp_nrH = I.exp_nrH;
+    F.shellU = I.shellU;
     for (int q = 0; q < 2; q++)
       for (int s = 0; s < 2; s++) F.acc[q][s] = I.acc[q][s];
     F.qpart = I.qpart;
@@ -1420,6 +1445,10 @@ int ctx_grad_geom(scft_ctx *c, double *out) {
   std::vector<double2> sc(kNumScalars);
   int status = SCFT_OK;
   try {
+    bool any_shell = false;
+    for (auto &I : c->inst) any_shell = any_shell || (I.shellU != nullptr);
+    if (c->mixed && any_shell)  // real-space rho_A of every instance (zr is rebuilt by the next update)
+      CK(launch_mix_rho_pack(c->d_fi, n, c->eblocks, 1, c->st));
     for (int k = 0; k < n; k++) {
       Instance &I = c->inst[k];
       for (int j = 0; j < 8; j++) out[8 * k + j] = 0.0;
@@ -1456,7 +1485,10 @@ int ctx_grad_geom(scft_ctx *c, double *out) {
       g.len = p.L_nr;
       g.rad = p.R_nr;
       g.xi = p.xi_nr;
-      CK(launch_geom_grad(g, wpl, part, blocks, c->st));
+      g.shell = I.shellU != nullptr;
+      g.len_big = p.L_nr + 2.0 * p.shell_width;
+      g.rad_big = p.R_nr + p.shell_width;
+      CK(launch_geom_grad(g, wpl, I.rho[0], part, blocks, c->st));
       const int nv = g.nplates * kGradPerPlate;
       CK(cudaMemcpyAsync(hp.data(), part, sizeof(double) * blocks * nv, cudaMemcpyDeviceToHost, c->st));
       CK(cudaMemcpyAsync(sc.data(), I.scal, sizeof(double2) * kNumScalars, cudaMemcpyDeviceToHost, c->st));
@@ -1465,15 +1497,14 @@ int ctx_grad_geom(scft_ctx *c, double *out) {
       const double dV = I.info.dx[0] * I.info.dx[1] * I.info.dx[2];
       for (int j = 0; j < g.nplates; j++)
         for (int q = 0; q < 4; q++) {
-          double sr = 0.0, si = 0.0, s0 = 0.0;
-          for (int b = 0; b < blocks; b++) {
-            sr += hp[(size_t)b * nv + j * kGradPerPlate + 3 * q + 0];
-            si += hp[(size_t)b * nv + j * kGradPerPlate + 3 * q + 1];
-            s0 += hp[(size_t)b * nv + j * kGradPerPlate + 3 * q + 2];
-          }
+          double sv[kGradTerms] = {};
+          for (int b = 0; b < blocks; b++)
+            for (int t = 0; t < kGradTerms; t++) sv[t] += hp[(size_t)b * nv + j * kGradPerPlate + kGradTerms * q + t];
           // Re[ i rho0 dV sum(drho w+) ] + (rho0/N) dV sum(drho) Re log Qd
-          const cd t = cd(0.0, p.rho0) * cd(sr, si) * dV + (p.rho0 / I.N) * dV * s0 * logQ;
-          out[8 * k + 4 * j + q] = t.real();
+          const cd t = cd(0.0, p.rho0) * cd(sv[0], sv[1]) * dV + (p.rho0 / I.N) * dV * sv[2] * logQ;
+          // shell: Lambda dV sum(rho_A d(rho_big - rho_p))
+          const double ts = g.shell ? p.shell_lambda * dV * (sv[3] - sv[4]) : 0.0;
+          out[8 * k + 4 * j + q] = t.real() + ts;
         }
     }
   } catch (...) {

@@ -69,6 +69,7 @@ struct FieldInst {
   double2 *expw[3];    // e^{-smwa}, e^{-smwb}, e^{-smwg}
   const double *hhat, *gaa, *gab, *gbb, *gc, *rho_exp_nr;
   const double2 *exp_nrH;
+  const double *shellU;  // A-segment shell potential (extension), or NULL
   double2 *acc[2][2];
   double2 *qpart;
   int nz;

@@ -89,7 +89,8 @@ __global__ void k_boltzmann(const FieldInst *__restrict__ fi) {
   FOR_POINTS(F) {
     const int nf = F.graft ? 3 : 2;
     for (int f = 0; f < nf; f++) {
-      const double2 s = F.sm[f][i];
+      double2 s = F.sm[f][i];
+      if (f == 0 && F.shellU) s.x += F.shellU[i];
       F.expw[f][i] = cexp_d(make_double2(-s.x, -s.y));
     }
   }
@@ -119,7 +120,9 @@ __global__ void k_density(const FieldInst *__restrict__ fi) {
       a = cadd(a, F.acc[1][0][i]);
       b = cadd(b, F.acc[1][1][i]);
     }
-    F.rho[0][i] = cmul(a, cmul(cexp_d(F.sm[0][i]), fac));
+    double2 sa = F.sm[0][i];
+    if (F.shellU) sa.x += F.shellU[i];
+    F.rho[0][i] = cmul(a, cmul(cexp_d(sa), fac));
     F.rho[1][i] = cmul(b, cmul(cexp_d(F.sm[1][i]), fac));
   }
 }
@@ -508,7 +511,8 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
 // without an FP64 exponential.
 __global__ void k_mix_boltzmann(const FieldInst *__restrict__ fi) {
   FOR_POINTS(F) {
-    const double2 s = F.zs[i];
+    double2 s = F.zs[i];
+    if (F.shellU) s.x += F.shellU[i];
     const float ah = (float)s.x, al = (float)(s.x - (double)ah);
     const float bh = (float)s.y, bl = (float)(s.y - (double)bh);
     F.E32[i] = make_float2(expf(-ah) * (1.0f - al), expf(-bh) * (1.0f - bl));

@@ -8,8 +8,12 @@
 //                                          (code/initialize.cpp:251-351),
 // so dH/dg = i rho0 int (d rho_p/dg) w+ + (rho0/N) log Qd int (d rho_p/dg)
 // for g = a rotation angle of the plate axis u about z (du/dtheta = z x u) or
-// a centre coordinate.  This kernel forms, per plate, the grid sums of
-// d rho_p/dg * w+ and of d rho_p/dg (FP64); the host assembles dH/dg.
+// a centre coordinate.  With the shell potential U_A = Lambda (rho_big -
+// rho_p) on A segments (an extension), -nD log Qd depends on the plate
+// through U_A as well: its derivative with respect to U_A(r) is rho_A(r), so
+// dH/dg gains Lambda int rho_A d(rho_big - rho_p)/dg.  This kernel forms, per
+// plate, the grid sums of d rho_p/dg * w+, of d rho_p/dg and of the shell
+// terms (FP64); the host assembles dH/dg.
 #include "fft_core.cuh"
 #include "grad.h"
 
@@ -20,7 +24,32 @@ __device__ __forceinline__ double derfc(double x) {
   return -1.1283791670955125738961589031215452 * exp(-x * x);
 }
 
-__global__ void k_geom_grad(GradArgs g, const double2 *__restrict__ wpl, double *__restrict__ part) {
+// d rho_p/dg for g = (theta_z, c_x, c_y, c_z) of a plate of thickness len and
+// radius rad at minimum-image offset dr from its centre, axis u.
+__device__ __forceinline__ void plate_derivs(const double dr[3], const double *u, double len, double rad, double xi,
+                                             double dg[4]) {
+  const double ud = u[0] * dr[0] + u[1] * dr[1] + u[2] * dr[2];
+  const double cx = u[1] * dr[2] - u[2] * dr[1], cy = u[2] * dr[0] - u[0] * dr[2], cz = u[0] * dr[1] - u[1] * dr[0];
+  const double uc = sqrt(cx * cx + cy * cy + cz * cz);
+  const double a = (fabs(ud) - 0.5 * len) / xi, b = (uc - rad) / xi;
+  const double Ea = erfc(a), Eb = erfc(b);
+  const double dEa = derfc(a) / xi, dEb = derfc(b) / xi;  // d/d|u.dr|, d/d|u x dr|
+  const double sg = ud > 0.0 ? 1.0 : (ud < 0.0 ? -1.0 : 0.0);
+  // rotation about z: du = (-u_y, u_x, 0) dtheta
+  const double dudr = -u[1] * dr[0] + u[0] * dr[1];
+  const double dud_dth = sg * dudr;
+  const double duc_dth = uc > 1e-300 ? -ud * dudr / uc : 0.0;
+  dg[0] = 0.25 * (dEa * dud_dth * Eb + Ea * dEb * duc_dth);
+  // centre: d dr / d c_k = -e_k
+  for (int k = 0; k < 3; k++) {
+    const double dud_dc = -sg * u[k];
+    const double duc_dc = uc > 1e-300 ? -(dr[k] - ud * u[k]) / uc : 0.0;
+    dg[1 + k] = 0.25 * (dEa * dud_dc * Eb + Ea * dEb * duc_dc);
+  }
+}
+
+__global__ void k_geom_grad(GradArgs g, const double2 *__restrict__ wpl, const double2 *__restrict__ rhoA,
+                            double *__restrict__ part) {
   __shared__ double red[32];
   double acc[kGradPerPlate * 2];
   for (int k = 0; k < kGradPerPlate * 2; k++) acc[k] = 0.0;
@@ -28,6 +57,7 @@ __global__ void k_geom_grad(GradArgs g, const double2 *__restrict__ wpl, double 
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
     const int n[3] = {(int)(i % g.nx), (int)((i / g.nx) % g.ny), (int)(i / ((long long)g.nx * g.ny))};
     const double2 w = wpl[i];
+    const double ra = g.shell ? rhoA[i].x : 0.0;
     for (int j = 0; j < g.nplates; j++) {
       double dr[3];
       for (int d = 0; d < 3; d++) {
@@ -36,30 +66,18 @@ __global__ void k_geom_grad(GradArgs g, const double2 *__restrict__ wpl, double 
         else if (r < -0.5 * g.L[d]) r += g.L[d];
         dr[d] = r;
       }
-      const double *u = g.u[j];
-      const double ud = u[0] * dr[0] + u[1] * dr[1] + u[2] * dr[2];
-      const double cx = u[1] * dr[2] - u[2] * dr[1], cy = u[2] * dr[0] - u[0] * dr[2], cz = u[0] * dr[1] - u[1] * dr[0];
-      const double uc = sqrt(cx * cx + cy * cy + cz * cz);
-      const double a = (fabs(ud) - 0.5 * g.len) / g.xi, b = (uc - g.rad) / g.xi;
-      const double Ea = erfc(a), Eb = erfc(b);
-      const double dEa = derfc(a) / g.xi, dEb = derfc(b) / g.xi;  // d/d|u.dr|, d/d|u x dr|
-      const double sg = ud > 0.0 ? 1.0 : (ud < 0.0 ? -1.0 : 0.0);
-      // rotation about z: du = (-u_y, u_x, 0) dtheta
-      const double du[3] = {-u[1], u[0], 0.0};
-      const double dud_dth = sg * (du[0] * dr[0] + du[1] * dr[1] + du[2] * dr[2]);
-      const double duc_dth = uc > 1e-300 ? -ud * (du[0] * dr[0] + du[1] * dr[1] + du[2] * dr[2]) / uc : 0.0;
-      double dg[4];
-      dg[0] = 0.25 * (dEa * dud_dth * Eb + Ea * dEb * duc_dth);
-      // centre: d dr / d c_k = -e_k
-      for (int k = 0; k < 3; k++) {
-        const double dud_dc = -sg * u[k];
-        const double duc_dc = uc > 1e-300 ? -(dr[k] - ud * u[k]) / uc : 0.0;
-        dg[1 + k] = 0.25 * (dEa * dud_dc * Eb + Ea * dEb * duc_dc);
-      }
+      double dg[4], db[4];
+      plate_derivs(dr, g.u[j], g.len, g.rad, g.xi, dg);
+      if (g.shell) plate_derivs(dr, g.u[j], g.len_big, g.rad_big, g.xi, db);
       for (int k = 0; k < 4; k++) {
-        acc[j * kGradPerPlate + 3 * k + 0] += dg[k] * w.x;
-        acc[j * kGradPerPlate + 3 * k + 1] += dg[k] * w.y;
-        acc[j * kGradPerPlate + 3 * k + 2] += dg[k];
+        double *a = acc + j * kGradPerPlate + kGradTerms * k;
+        a[0] += dg[k] * w.x;
+        a[1] += dg[k] * w.y;
+        a[2] += dg[k];
+        if (g.shell) {
+          a[3] += db[k] * ra;
+          a[4] += dg[k] * ra;
+        }
       }
     }
   }
@@ -79,8 +97,9 @@ __global__ void k_geom_grad(GradArgs g, const double2 *__restrict__ wpl, double 
   }
 }
 
-cudaError_t launch_geom_grad(const GradArgs &g, const double2 *wpl, double *part, int blocks, cudaStream_t st) {
-  k_geom_grad<<<blocks, 256, 0, st>>>(g, wpl, part);
+cudaError_t launch_geom_grad(const GradArgs &g, const double2 *wpl, const double2 *rhoA, double *part, int blocks,
+                             cudaStream_t st) {
+  k_geom_grad<<<blocks, 256, 0, st>>>(g, wpl, rhoA, part);
   return cudaGetLastError();
 }
 

@@ -27,8 +27,10 @@ def rg(N: int) -> float:
 
 def plate_params(theta_deg: float, N: int = 100, fA: float = 0.5, chiN: float = 20.0, C: float = 50.0,
                  grid=(64, 64, 64), box_rg=(6.4, 6.4, 6.4), precision=PREC_FP64, lam_pl=0.002, lam_mi=0.0005,
-                 centers=((0.5, 0.5, 0.5),), thickness_rg=0.2, radius_rg=0.8, xi_rg=0.1, sigma=0.0, Ng=0):
-    """Config 1 geometry: plate(s) rotated by theta about z, normal along x at 0."""
+                 centers=((0.5, 0.5, 0.5),), thickness_rg=0.2, radius_rg=0.8, xi_rg=0.1, sigma=0.0, Ng=0,
+                 shell=False):
+    """Config 1 geometry: plate(s) rotated by theta about z, normal along x at 0.
+    shell=True adds the A-attractive shell Lambda = -1/N in a 0.1 Rg shell."""
     R = rg(N)
     Nda = int(round(fA * N))
     th = math.radians(theta_deg)
@@ -37,7 +39,8 @@ def plate_params(theta_deg: float, N: int = 100, fA: float = 0.5, chiN: float = 
     return make_params(Nda=Nda, Ndb=N - Nda, a_smear=0.2, rho0=C * N / R ** 3, chi_ab=chiN / N, kappa=50.0,
                        Nx=grid, L=tuple(b * R for b in box_rg), lam_pl=lam_pl, lam_mi=lam_mi,
                        n_exp_nr=len(centers), L_nr=thickness_rg * R, R_nr=radius_rg * R, xi_nr=xi_rg * R,
-                       center=cs, orient=(u, u), precision=precision, sigma=sigma, Ng=Ng)
+                       center=cs, orient=(u, u), precision=precision, sigma=sigma, Ng=Ng,
+                       shell_lambda=(-1.0 / N if shell else 0.0), shell_width=(0.1 * R if shell else 0.0))
 
 
 def seeded_fields(p, seed: int) -> dict:
@@ -69,6 +72,8 @@ def sweep15_mixed_sizes(precision=PREC_MIXED):
 
 WORKLOADS = {
     "plate64_N100": lambda prec: [plate_params(10.0, precision=prec)],
+    "plate64_N100_shell": lambda prec: [plate_params(10.0, precision=prec, shell=True)],
+    "sweep15_64_N100_shell": lambda prec: [plate_params(t, precision=prec, shell=True) for t in SWEEP_ANGLES],
     "sweep15_64_N100": lambda prec: sweep15(precision=prec),
     "sweep15_mixed_sizes": lambda prec: sweep15_mixed_sizes(precision=prec),
 }

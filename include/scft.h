@@ -84,8 +84,13 @@ typedef struct scft_params {
   double orient[2][3]; /* plate axes (normalised on input, as the reference) */
   int precision;       /* SCFT_PREC_FP64 or SCFT_PREC_MIXED */
   int plate_shape;     /* SCFT_PLATE_REFERENCE or SCFT_PLATE_CUBOID */
-  double shell_lambda; /* extension: A-attractive shell potential added to w_A */
-  double shell_width;  /* width of that shell; ignored when shell_lambda == 0 */
+  /* Extension (no counterpart in the reference): a potential on A segments
+   * in a shell around the plates, U_A = shell_lambda * sum_j [rho_p(L_nr +
+   * 2 w, R_nr + w) - rho_p(L_nr, R_nr)] with w = shell_width, added to the
+   * smeared w_A wherever the propagators and densities use it (negative:
+   * A-attractive).  Needs a plate and w > 0; 0 turns it off. */
+  double shell_lambda;
+  double shell_width;
 } scft_params;
 
 /* Derived per-instance quantities (code/initialize.cpp:249-386). */
@@ -134,7 +139,9 @@ int scft_get_density(scft_ctx *ctx, int inst, double *rhoda, double *rhodb, doub
  * H; a separation d of two plates along an axis e gives
  * dH/dd = (dH/dc_2 - dH/dc_1).e / 2.  The reference has no derivative code;
  * this replaces finite differences over its sweeps (angle-rotation/,
- * particle-separation/).  SCFT_ERR_UNSUPPORTED for grafted plates. */
+ * particle-separation/).  With the shell potential the derivative includes
+ * shell_lambda * int rho_A d(shell)/dg.  SCFT_ERR_UNSUPPORTED for grafted
+ * plates and for SCFT_PLATE_CUBOID. */
 int scft_grad_geom(scft_ctx *ctx, double *out);
 
 /* The explicit plates' density rho_exp_nr of one instance (M real values),

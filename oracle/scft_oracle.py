@@ -210,6 +210,10 @@ class System:
     xi_nr: float = 0.2
     centers: tuple = ((0.5, 0.5, 0.5), (0.5, 0.5, 0.5))
     orients: tuple = ((1.0, 0.0, 0.0), (1.0, 0.0, 0.0))
+    # project extension without a reference counterpart: potential lam on A
+    # segments in the shell between the plate and the plate enlarged by w
+    shell_lambda: float = 0.0
+    shell_width: float = 0.0
     tables: dict = field(default_factory=dict)
 
     def __post_init__(self):
@@ -259,6 +263,13 @@ class System:
                                                        self.centers[i], self.orients[i])
         t["rho_exp_nr"] = rho_exp_nr
         t["exp_nrH"] = fft_fwd(g, rho_exp_nr)
+        # extension: U_A = lam * sum_j [rho_p(L + 2w, R + w) - rho_p(L, R)]
+        shellU = np.zeros(g.shape)
+        if self.shell_lambda != 0.0:
+            big = sum(explicit_nanorod(g, self.L_nr + 2 * self.shell_width, self.R_nr + self.shell_width,
+                                       self.xi_nr, self.centers[i], self.orients[i]) for i in range(self.n_exp_nr))
+            shellU = self.shell_lambda * (big.real - rho_exp_nr.real)
+        t["shellU"] = shellU
         # code/initialize.cpp:249-386: volumes and chain counts (no film, no field NPs)
         V_exp = integ_trapPBC(g, rho_exp_nr).real
         self.Vf = g.V
@@ -423,8 +434,9 @@ def calc_poly_density(s: System, st: State, keep_hist=False):
     o = st.out
     o.update(smwa=smwa, smwb=smwb, smwg=smwg)
     if s.nD > 0.0:
-        Qd, q, qd = diblock_discrete(s, smwa, smwb)
-        o["rhoda"], o["rhodb"] = integrate_diblock_discrete(s, q, qd, Qd, s.nD, smwa, smwb)
+        ua = smwa + s.tables["shellU"]  # the extension's shell potential acts on A segments
+        Qd, q, qd = diblock_discrete(s, ua, smwb)
+        o["rhoda"], o["rhodb"] = integrate_diblock_discrete(s, q, qd, Qd, s.nD, ua, smwb)
         if keep_hist:
             o["qd"], o["qddag"] = q, qd
     else:

@@ -158,3 +158,19 @@ def test_restatement_config0_trace():
     for k in ("rhoda", "rhodb", "wpl", "wabm"):
         src = st.out[k] if k.startswith("rho") else getattr(st, k)
         assert rel(digest(src), z["digest_" + k]) < 1e-10, k
+
+
+def test_shell_extension_profile():
+    """The shell potential (an extension of the restatement, no reference
+    counterpart): zero with Lambda = 0, of Lambda's sign, largest just outside
+    the plate, and without effect on the reference path when off."""
+    import dataclasses
+
+    c, _ = load_golden("tiny_plate")
+    s0 = O.System.from_case(c)
+    assert np.abs(s0.tables["shellU"]).max() == 0.0
+    s = dataclasses.replace(s0, shell_lambda=-0.3, shell_width=0.4)
+    U = s.tables["shellU"]
+    assert U.max() <= 1e-15 and U.min() < -0.05
+    core = s.tables["rho_exp_nr"].real
+    assert U[core > 0.9].mean() > U.min() / 4  # weak inside the core
