@@ -335,7 +335,9 @@ void validate(const scft_params &p) {
     AxisPlan ap;
     if (!make_axis_plan(p.Nx[d], ap)) throw ScftError(SCFT_ERR_UNSUPPORTED, "grid sizes must be 2^a 3^b 5^c");
   }
-  if (!(p.kappa > 0)) bad("kappa must be > 0 (code/1s_update.cpp:72-78 leaves B unset otherwise)");
+  if (p.update_scheme != SCFT_UPDATE_1S && p.update_scheme != SCFT_UPDATE_EULER) bad("unknown update_scheme");
+  if (p.update_scheme == SCFT_UPDATE_1S && !(p.kappa > 0))
+    bad("kappa must be > 0 with the 1S update (code/1s_update.cpp:72-78 leaves B unset otherwise)");
   if (!(p.rho0 > 0)) bad("rho0 must be positive");
   if (p.n_exp_nr < 0 || p.n_exp_nr > 2) bad("n_exp_nr must be 0, 1 or 2 (code/globals.h:57-58)");
   if (p.n_exp_nr > 0) {
@@ -518,6 +520,25 @@ void mix_coefficients_final(scft_ctx *c, Instance &I) {
     I.alpha[f] = dupload(c, a);
     I.beta[f] = dupload(c, b);
   };
+  if (p.update_scheme == SCFT_UPDATE_EULER) {
+    // explicit step w <- (1 - lam c) w - lam F (code/Euler_update.cpp:54-179)
+    auto eul = [&](int f, double lam, double cc) {
+      for (long long i = 0; i < M; i++) {
+        a[i] = 1.0 - lam * cc;
+        b[i] = lam;
+      }
+      I.alpha[f] = dupload(c, a);
+      I.beta[f] = dupload(c, b);
+    };
+    eul(0, li, p.kappa > 0.0 ? rho0 / p.kappa : 0.0);
+    const double chis[3] = {I.cab, I.cbc, I.cac};
+    for (int k = 0; k < 3; k++)
+      if (chis[k] != 0.0) {
+        eul(1 + 2 * k, li, 2.0 * rho0 / chis[k]);
+        eul(2 + 2 * k, lr, 2.0 * rho0 / chis[k]);
+      }
+    return;
+  }
   const auto &hh = I.tab_hh, &gaa = I.tab_gaa, &gab = I.tab_gab, &gbb = I.tab_gbb, &gc = I.tab_gc;
   // w+ (:67-83)
   semi(0, [&](long long i) {
@@ -686,6 +707,8 @@ void build_jobs(scft_ctx *c) {
     F.geom = I.geom;
     F.rho0 = I.p.rho0;
     F.kappa = I.p.kappa;
+    F.ikappa = I.p.kappa > 0.0 ? 1.0 / I.p.kappa : 0.0;
+    F.euler = I.p.update_scheme == SCFT_UPDATE_EULER;
     F.cab = I.cab; F.cbc = I.cbc; F.cac = I.cac;
     F.neg_ab = I.neg_ab; F.neg_bc = I.neg_bc; F.neg_ac = I.neg_ac;
     F.phiD = I.info.phiD; F.phiG = I.info.phiG;

@@ -58,6 +58,8 @@ struct FieldInst {
   long long M;
   int geom;
   double rho0, kappa, cab, cbc, cac;
+  double ikappa;  // 1/kappa, 0 for kappa <= 0 (no w+^2 term)
+  int euler;      // explicit Euler update (code/Euler_update.cpp) instead of 1S
   int neg_ab, neg_bc, neg_ac;
   double phiD, phiG, lam_pl, lam_mi, nD, V, dx[3];
   int N, Ng, np_chem, graft, single;

@@ -320,12 +320,56 @@ __device__ __forceinline__ void update_1s_point(const FieldInst &F, long long i,
   }
 }
 
+// Explicit Euler step of the fields at one k point (code/Euler_update.cpp:54-179,
+// mean field): w <- w - lam dH/dw with lam_pl for w+ and the + fields, lam_mi
+// for the - fields, no Debye terms and no np_chem terms.  Arguments as
+// update_1s_point.
+__device__ __forceinline__ void euler_pair(const FieldInst &F, double c, int neg, double2 X, double2 Y, double hh,
+                                           double2 &wp, double2 &wm) {
+  const double rho0 = F.rho0, li = F.lam_pl, lr = F.lam_mi;
+  const double2 s = cadd(X, Y), d = csub(X, Y);
+  // + : 2 rho0 wp / c + hhat (X + Y) (neg ? -1 : I)
+  const double2 Fp = neg ? make_double2(2.0 * rho0 * wp.x / c - hh * s.x, 2.0 * rho0 * wp.y / c - hh * s.y)
+                         : make_double2(2.0 * rho0 * wp.x / c - hh * s.y, 2.0 * rho0 * wp.y / c + hh * s.x);
+  // - : 2 rho0 wm / c + (neg ? I hhat (X - Y) : hhat (Y - X))
+  const double2 Fm = neg ? make_double2(2.0 * rho0 * wm.x / c - hh * d.y, 2.0 * rho0 * wm.y / c + hh * d.x)
+                         : make_double2(2.0 * rho0 * wm.x / c - hh * d.x, 2.0 * rho0 * wm.y / c - hh * d.y);
+  wp = make_double2(wp.x - li * Fp.x, wp.y - li * Fp.y);
+  wm = make_double2(wm.x - lr * Fm.x, wm.y - lr * Fm.y);
+}
+
+__device__ __forceinline__ void euler_point(const FieldInst &F, long long i, double2 ra, double2 rb, double2 rg,
+                                            double2 *w) {
+  const double rho0 = F.rho0;
+  const double hh = F.hhat[i];
+  const double2 enh = F.exp_nrH[i];
+  {
+    const double evar = (i == 0) ? 1.0 : 0.0;
+    const double2 s = cadd(cadd(ra, rg), rb);
+    const double2 wv = w[0];
+    // rho0 w+ / kappa + I rho0 (exp_nrH - evar) + I hhat s
+    const double2 Fv = make_double2(rho0 * F.ikappa * wv.x - rho0 * enh.y - hh * s.y,
+                                    rho0 * F.ikappa * wv.y + rho0 * (enh.x - evar) + hh * s.x);
+    w[0] = make_double2(wv.x - F.lam_pl * Fv.x, wv.y - F.lam_pl * Fv.y);
+  }
+  const double2 z = make_double2(0.0, 0.0);
+  if (F.cab != 0.0) euler_pair(F, F.cab, F.neg_ab, ra, rb, hh, w[1], w[2]);
+  else w[1] = w[2] = z;
+  if (F.cbc != 0.0) euler_pair(F, F.cbc, F.neg_bc, rb, rg, hh, w[3], w[4]);
+  else w[3] = w[4] = z;
+  if (F.cac != 0.0) euler_pair(F, F.cac, F.neg_ac, ra, rg, hh, w[5], w[6]);
+  else w[5] = w[6] = z;
+}
+
 __global__ void k_update_1s(const FieldInst *__restrict__ fi) {
   FOR_POINTS(F) {
     double2 w[7];
     for (int f = 0; f < 7; f++) w[f] = F.w[f][i];
     const double2 rg = F.graft ? F.rho[2][i] : make_double2(0.0, 0.0);
-    update_1s_point(F, i, F.rho[0][i], F.rho[1][i], rg, w);
+    if (F.euler)
+      euler_point(F, i, F.rho[0][i], F.rho[1][i], rg, w);
+    else
+      update_1s_point(F, i, F.rho[0][i], F.rho[1][i], rg, w);
     for (int f = 0; f < 7; f++) F.w[f][i] = w[f];
   }
 }
@@ -342,7 +386,7 @@ __global__ void k_h_partials(const FieldInst *__restrict__ fi, double2 *__restri
        i += (long long)gridDim.x * blockDim.x) {
     const double2 w = F.w[0][i];
     const double2 w2 = cmul(w, w);
-    const double2 t1 = make_double2(w2.x * F.rho0 / F.kappa / 2.0, w2.y * F.rho0 / F.kappa / 2.0);
+    const double2 t1 = make_double2(w2.x * F.rho0 * F.ikappa / 2.0, w2.y * F.rho0 * F.ikappa / 2.0);
     const double c = F.rho0 * (1.0 - 0.0 - F.rho_exp_nr[i]);
     // I*c*w = (-c*w.y, c*w.x)
     s[0] = cadd(s[0], make_double2(t1.x + c * w.y, t1.y - c * w.x));
@@ -449,15 +493,15 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
     if (F.alpha[1]) {  // AB pair
       if (!F.neg_ab) {
         double2 F1 = make_double2(-hh * (ra.y + rb.y), hh * (ra.x + rb.x));
-        if (F.np_chem == 1) F1 = make_double2(F1.x - rho0 * enh.x, F1.y - rho0 * enh.y);
+        if (F.np_chem == 1 && !F.euler) F1 = make_double2(F1.x - rho0 * enh.x, F1.y - rho0 * enh.y);
         double2 F2 = make_double2(hh * (rb.x - ra.x), hh * (rb.y - ra.y));
-        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
+        if (F.np_chem == 1 && !F.euler) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
         step(1, F1);
         step(2, F2);
       } else {
         const double2 F1 = make_double2(-hh * (ra.x + rb.x), -hh * (ra.y + rb.y));
         double2 F2 = make_double2(-hh * (ra.y - rb.y), hh * (ra.x - rb.x));
-        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
+        if (F.np_chem == 1 && !F.euler) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
         step(1, F1);
         step(2, F2);
       }
@@ -469,13 +513,13 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
       if (!F.neg_bc) {
         const double2 F1 = make_double2(-hh * (rg.y + rb.y), hh * (rg.x + rb.x));
         double2 F2 = make_double2(hh * (rg.x - rb.x), hh * (rg.y - rb.y));
-        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
+        if (F.np_chem == 1 && !F.euler) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
         step(3, F1);
         step(4, F2);
       } else {
         const double2 F1 = make_double2(-hh * (rb.x + rg.x), -hh * (rb.y + rg.y));
         double2 F2 = make_double2(hh * (rg.y - rb.y), -hh * (rg.x - rb.x));
-        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
+        if (F.np_chem == 1 && !F.euler) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
         step(3, F1);
         step(4, F2);
       }
@@ -485,13 +529,13 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
       if (!F.neg_ac) {
         const double2 F1 = make_double2(-hh * (rg.y + ra.y), hh * (rg.x + ra.x));
         double2 F2 = make_double2(hh * (rg.x - ra.x), hh * (rg.y - ra.y));
-        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
+        if (F.np_chem == 1 && !F.euler) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
         step(5, F1);
         step(6, F2);
       } else {
         const double2 F1 = make_double2(-hh * (ra.x + rg.x), -hh * (ra.y + rg.y));
         double2 F2 = make_double2(hh * (rg.y - ra.y), -hh * (rg.x - ra.x));
-        if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
+        if (F.np_chem == 1 && !F.euler) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
         step(5, F1);
         step(6, F2);
       }
@@ -567,8 +611,8 @@ __global__ void k_mix_h_partials(const FieldInst *__restrict__ fi, double2 *__re
     // rho0/(2 kappa) w w  + I rho0 rho_exp(-k) w  (- I rho0 w(0) at k = 0)
     const double2 re = F.exp_nrH[mi];
     const double2 rw = cmul(re, w);
-    double2 t = make_double2(ww.x * F.rho0 / F.kappa / 2.0 - F.rho0 * rw.y,
-                             ww.y * F.rho0 / F.kappa / 2.0 + F.rho0 * rw.x);
+    double2 t = make_double2(ww.x * F.rho0 * F.ikappa / 2.0 - F.rho0 * rw.y,
+                             ww.y * F.rho0 * F.ikappa / 2.0 + F.rho0 * rw.x);
     if (i == 0) t = make_double2(t.x + F.rho0 * w.y, t.y - F.rho0 * w.x);
     s[0] = cadd(s[0], t);
     const double chis[3] = {F.cbc, F.cac, F.cab};

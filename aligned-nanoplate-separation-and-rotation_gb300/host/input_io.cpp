@@ -91,7 +91,6 @@ std::string read_input(const std::string &path, Input &in) {
   if (in.do_fld_np) return "No field-based nanoparticles (code/read_input.cpp:184-189)";
   if (in.do_film && in.do_channel) return "Can't do film and channel in same simulation";
   if (in.do_film || in.do_channel) return "films and channels are not built here";
-  if (in.update_scheme != 1) return "only the 1S update scheme (update_scheme = 1) is built here";
   if (in.do_CL) return "complex Langevin sampling (do_CL = 1) is not built here";
   if (in.n_exp_nr > 0 && in.np_type != 2) return "explicit particles must be nanorods/plates (np_type = 2)";
   for (int j = 0; j < in.n_exp_nr; j++)
@@ -133,6 +132,8 @@ scft_params to_params(const Input &in, int precision) {
       p.orient[j][d] = in.orient[j][d];
     }
   p.precision = precision;
+  // code/simulate.cpp:86-89: update_scheme 0 runs update_Euler, anything else update_1s
+  p.update_scheme = in.update_scheme == 0 ? SCFT_UPDATE_EULER : SCFT_UPDATE_1S;
   p.plate_shape = SCFT_PLATE_REFERENCE;
   return p;
 }

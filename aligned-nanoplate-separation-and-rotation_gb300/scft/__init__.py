@@ -18,6 +18,7 @@ OK = 0
 ERR_ARG, ERR_CUDA, ERR_NAN, ERR_QNONPOS, ERR_UNSUPPORTED, ERR_NOMEM, ERR_COMPLEX = -1, -2, -3, -4, -5, -6, -7
 PREC_FP64, PREC_MIXED = 0, 1
 PLATE_REFERENCE, PLATE_CUBOID = 0, 1
+UPDATE_1S, UPDATE_EULER = 0, 1
 FIELD_NAMES = ("wpl", "wabp", "wabm", "wbcp", "wbcm", "wacp", "wacm")
 
 # Every extern "C" symbol declared in include/scft.h.
@@ -47,7 +48,7 @@ class Params(ctypes.Structure):
         ("L_nr", ctypes.c_double), ("R_nr", ctypes.c_double), ("xi_nr", ctypes.c_double),
         ("center", (ctypes.c_double * 3) * 2), ("orient", (ctypes.c_double * 3) * 2),
         ("precision", ctypes.c_int), ("plate_shape", ctypes.c_int),
-        ("shell_lambda", ctypes.c_double), ("shell_width", ctypes.c_double),
+        ("shell_lambda", ctypes.c_double), ("shell_width", ctypes.c_double), ("update_scheme", ctypes.c_int),
     ]
 
 
@@ -123,7 +124,8 @@ def make_params(**kw) -> Params:
                     Nx=(8, 8, 8), L=(4.0, 4.0, 4.0), lam_pl=0.005, lam_mi=0.005, n_exp_nr=0, np_chem=0,
                     sigma=0.0, Ng=0, L_nr=1.0, R_nr=1.0, xi_nr=0.2,
                     center=((0.5, 0.5, 0.5), (0.5, 0.5, 0.5)), orient=((1.0, 0.0, 0.0), (1.0, 0.0, 0.0)),
-                    precision=PREC_FP64, plate_shape=PLATE_REFERENCE, shell_lambda=0.0, shell_width=0.0)
+                    precision=PREC_FP64, plate_shape=PLATE_REFERENCE, shell_lambda=0.0, shell_width=0.0,
+                    update_scheme=UPDATE_1S)
     defaults.update(kw)
     for k, v in defaults.items():
         if k in ("Nx", "L"):

@@ -64,6 +64,10 @@ extern "C" {
 #define SCFT_PLATE_REFERENCE 0 /* 0.25 erfc((|u.r|-L/2)/xi) erfc((|u x r|-R)/xi), code/initialize.cpp:578-612 */
 #define SCFT_PLATE_CUBOID 1    /* product of three erfc slabs (extension, no reference counterpart) */
 
+/* Field update schemes (scft_params.update_scheme). */
+#define SCFT_UPDATE_1S 0    /* semi-implicit, code/1s_update.cpp:7-352 */
+#define SCFT_UPDATE_EULER 1 /* explicit, code/Euler_update.cpp:5-213 */
+
 /* One SCFT instance.  Field names and meanings follow bcp.input
  * (code/read_input.cpp:30-236); negative chi selects the attractive branch. */
 typedef struct scft_params {
@@ -91,6 +95,10 @@ typedef struct scft_params {
    * A-attractive).  Needs a plate and w > 0; 0 turns it off. */
   double shell_lambda;
   double shell_width;
+  /* SCFT_UPDATE_1S (0) or SCFT_UPDATE_EULER (1): the reference's
+   * update_scheme 1 (update_1s, code/1s_update.cpp) and 0 (update_Euler,
+   * code/Euler_update.cpp).  kappa <= 0 (no w+^2 term) is allowed with Euler. */
+  int update_scheme;
 } scft_params;
 
 /* Derived per-instance quantities (code/initialize.cpp:249-386). */
@@ -120,7 +128,9 @@ int scft_get_fields(scft_ctx *ctx, int inst, double *w);
 /* calc_poly_density() for every instance. */
 int scft_calc_poly_density(scft_ctx *ctx);
 
-/* n_iter x update_1s() for every instance (each ends with calc_poly_density). */
+/* n_iter field updates of every instance, each followed by
+ * calc_poly_density: update_1s(), or update_Euler() for instances with
+ * update_scheme = SCFT_UPDATE_EULER (code/simulate.cpp:86-89). */
 int scft_update_1s(scft_ctx *ctx, int n_iter);
 
 /* calc_H() per instance.  out[5*inst + {0..4}] = Re H, Im H, Re Qd, Im Qd,

@@ -214,6 +214,7 @@ class System:
     # segments in the shell between the plate and the plate enlarged by w
     shell_lambda: float = 0.0
     shell_width: float = 0.0
+    update_scheme: int = 1  # bcp.input numbering: 0 = Euler, otherwise 1S (code/simulate.cpp:86-89)
     tables: dict = field(default_factory=dict)
 
     def __post_init__(self):
@@ -235,7 +236,8 @@ class System:
                    chi_bc=c.chi_bc, chi_ac=c.chi_ac, kappa=c.kappa, Nx=c.Nx, L=c.L,
                    lam_pl=c.lam_pl, lam_mi=c.lam_mi, n_exp_nr=c.n_exp_nr, np_type=c.np_type,
                    np_chem=c.np_chem, sigma=c.sigma, Ng=c.Ng, L_nr=c.L_nr, R_nr=c.R_nr,
-                   xi_nr=c.xi_nr, centers=c.centers, orients=c.orients)
+                   xi_nr=c.xi_nr, centers=c.centers, orients=c.orients,
+                   update_scheme=getattr(c, "update_scheme", 1))
 
     def initialize(self):
         g = self.g
@@ -576,6 +578,41 @@ def update_1s(s: System, st: State):
     return calc_poly_density(s, st)
 
 
+def update_euler(s: System, st: State):
+    """code/Euler_update.cpp:5-213 (mean field: no noise, homopolymer, field
+    NPs, channel or film): w <- w - lam dH/dw in k-space, lam_pl for w+ and
+    the + fields, lam_mi for the - fields."""
+    g = s.g
+    I = 1j
+    t = s.tables
+    hh = t["hhat"]
+    o = st.out
+    rho0, li, lr = s.rho0, s.lam_pl, s.lam_mi
+    z = np.zeros(g.shape, np.complex128)
+    rhoda = fft_fwd(g, o["rhoda"]) if s.nD > 0.0 else o["rhoda"]
+    rhodb = fft_fwd(g, o["rhodb"]) if s.nD > 0.0 else o["rhodb"]
+    rhog_exp = fft_fwd(g, o["rhog_exp"]) if (s.sigma > 0.0 and s.n_exp_nr > 0) else o["rhog_exp"]
+    evar = np.zeros(g.shape)
+    evar.flat[0] = 1.0
+    wpl = fft_fwd(g, st.wpl)
+    F = (0.0 if s.kappa <= 0.0 else rho0 * wpl / s.kappa) + I * rho0 * (t["exp_nrH"] - evar) \
+        + I * hh * (rhoda + rhodb + rhog_exp)
+    st.wpl = fft_bck(g, wpl - li * F)
+
+    def pair(c, neg, wp, wm, X, Y):
+        if c == 0.0:
+            return z.copy(), z.copy()
+        wp, wm = fft_fwd(g, wp), fft_fwd(g, wm)
+        Fp = 2.0 * rho0 * wp / c + hh * (X * (-1 if neg else I) + Y * (-1 if neg else I))
+        Fm = 2.0 * rho0 * wm / c + hh * (X * (I if neg else -1) + Y * (-I if neg else 1))
+        return fft_bck(g, wp - li * Fp), fft_bck(g, wm - lr * Fm)
+
+    st.wabp, st.wabm = pair(s.cab, s.neg_ab, st.wabp, st.wabm, rhoda, rhodb)
+    st.wbcp, st.wbcm = pair(s.cbc, s.neg_bc, st.wbcp, st.wbcm, rhodb, rhog_exp)
+    st.wacp, st.wacm = pair(s.cac, s.neg_ac, st.wacp, st.wacm, rhoda, rhog_exp)
+    return calc_poly_density(s, st)
+
+
 def calc_H(s: System, st: State) -> complex:
     """code/calc_h.cpp:9-132."""
     g = s.g
@@ -610,8 +647,9 @@ def run(s: System, st: State, iters: int):
         rows.append([it, H.real, H.imag, Qd.real, Qd.imag, Qga.real, Qga.imag])
 
     row(0)
+    step = update_euler if s.update_scheme == 0 else update_1s
     for it in range(1, iters + 1):
-        update_1s(s, st)
+        step(s, st)
         row(it)
     return np.array(rows)
 

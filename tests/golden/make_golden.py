@@ -118,11 +118,18 @@ def driver_cases() -> dict:
     c = Case(ic=((-2, 1.0, 0, 1.0), (-4, 1.0, 1, 1.0)), **base)
     c.fields = {}
     cases["driver_cos"] = c
+    # explicit Euler update (update_scheme 0, code/Euler_update.cpp), both chi signs
+    c = Case(update_scheme=0, **base)
+    c.fields = seeded_fields(c, 2, 0.3, 0.01, False)
+    cases["driver_euler"] = c
+    c = Case(update_scheme=0, **dict(base, chi_ab=-0.5))
+    c.fields = seeded_fields(c, 3, 0.3, 0.01, False)
+    cases["driver_euler_negab"] = c
     return cases
 
 
 DRIVER_OUTPUTS = ["data.dat", "wpl.p0.bin", "wabp.p0.bin", "wabm.p0.bin", "rhoda.p0.bin", "rhodb.p0.bin",
-                  "rhoda_c.p0.bin"]
+                  "rhoda_c.p0.bin", "rhodb_c.p0.bin"]
 
 
 def make_driver_fixtures(tmp):
@@ -148,6 +155,8 @@ def make_driver_fixtures(tmp):
 def main():
     tmp = tempfile.mkdtemp(prefix="golden_")
     make_driver_fixtures(tmp)
+    if "--driver-only" in sys.argv:
+        return
     for name, (c, iters, hist) in tiny_cases().items():
         out = run_reference(os.path.join(tmp, name), c, iters, hist=hist)
         z = {"case_json": case_json(c), "trace": out["trace"], "scalars_json": json.dumps(out["scalars"])}

@@ -17,7 +17,7 @@ import pytest
 from conftest import GOLDEN, PKG
 
 DRIVER = os.path.join(PKG, "build", "scft_run")
-CASES = ["driver_res", "driver_cos"]
+CASES = ["driver_res", "driver_cos", "driver_euler", "driver_euler_negab"]
 
 
 def read_bin(path):
@@ -71,6 +71,7 @@ def test_driver_matches_reference_run(tmp_path, name):
 
 @pytest.mark.gpu
 def test_driver_batch_of_directories(tmp_path):
+    """Runs with both update schemes in one batch."""
     runs = [stage(str(tmp_path), n) for n in CASES]
     r = subprocess.run([DRIVER, "--quiet"] + runs, capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
@@ -79,11 +80,12 @@ def test_driver_batch_of_directories(tmp_path):
 
 
 @pytest.mark.gpu
-def test_driver_mixed_precision(tmp_path):
-    run = stage(str(tmp_path), "driver_res")
+@pytest.mark.parametrize("name", ["driver_res", "driver_euler"])
+def test_driver_mixed_precision(tmp_path, name):
+    run = stage(str(tmp_path), name)
     r = subprocess.run([DRIVER, "--quiet", "--mixed", run], capture_output=True, text=True, timeout=600)
     assert r.returncode == 0, r.stderr
-    ref = read_dat(os.path.join(GOLDEN, "driver_res", "data.dat.ref"))
+    ref = read_dat(os.path.join(GOLDEN, name, "data.dat.ref"))
     got = read_dat(os.path.join(run, "data.dat"))
     assert np.abs(got[:, 1] - ref[:, 1]).max() <= 2e-5 * np.abs(ref[:, 1]).max()
 
@@ -99,7 +101,7 @@ def _driver_or_skip():
 @pytest.mark.parametrize("edit,message", [
     (lambda s: s.replace("0.0 0  phiAH, Nah", "0.1 10  phiAH, Nah"), "homopolymer"),
     (lambda s: s.replace("0  do_fld_np", "1  do_fld_np"), "field-based"),
-    (lambda s: s.replace("1  Update scheme", "0  Update scheme"), "1S update"),
+    (lambda s: s.replace("0  do_CL", "1  do_CL"), "complex Langevin"),
 ])
 def test_driver_rejects_inputs_like_the_reference(tmp_path, edit, message):
     """Input errors are reported before any GPU work (code/read_input.cpp:40-45,

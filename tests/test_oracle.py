@@ -174,3 +174,32 @@ def test_shell_extension_profile():
     assert U.max() <= 1e-15 and U.min() < -0.05
     core = s.tables["rho_exp_nr"].real
     assert U[core > 0.9].mean() > U.min() / 4  # weak inside the core
+
+
+@pytest.mark.parametrize("name", ["driver_euler", "driver_euler_negab"])
+def test_restatement_euler_matches_reference_driver(name):
+    """update_Euler (code/Euler_update.cpp) in the restatement against the
+    reference's own simulate() run: itermax + 1 = 13 explicit steps (the loop
+    runs iter = 0..itermax, code/simulate.cpp:85) from the same .res fields;
+    final fields and unsmeared densities (*_c.p0.bin) from its output."""
+    import struct
+
+    _sys.path.insert(0, GOLDEN)
+    from make_golden import driver_cases
+
+    c = driver_cases()[name]
+    s = O.System.from_case(c)
+    assert s.update_scheme == 0
+    st = O.State.from_fields(s.g, c.fields)
+    O.run(s, st, 13)
+
+    def read_bin(f):
+        with open(os.path.join(GOLDEN, name, f + ".p0.bin.ref"), "rb") as fh:
+            fh.read(4 + 12 + 24)
+            _, ml = struct.unpack("2i", fh.read(8))
+            return np.frombuffer(fh.read(16 * ml), dtype=np.complex128)
+
+    got = {"wpl": st.wpl, "wabp": st.wabp, "wabm": st.wabm, "rhoda_c": st.out["rhoda"], "rhodb_c": st.out["rhodb"]}
+    for k, v in got.items():
+        ref = read_bin(k)
+        assert np.abs(v.ravel() - ref).max() <= 1e-10 * np.abs(ref).max(), k
