@@ -22,6 +22,8 @@ void ctx_diblock_density(scft_ctx *c, int k, const double *smwa, const double *s
                          double *Q);
 void ctx_override_nD(scft_ctx *c, int k, double nD);
 int ctx_grad_geom(scft_ctx *c, double *out);
+void ctx_set_sweep_groups(scft_ctx *c, int groups);
+void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *tx_out, double *ms_out);
 void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
                       double *bytes_col);
 int error_code(const std::exception &e);
@@ -223,6 +225,20 @@ int scft_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   if (int s = check_ctx(c, 0)) return s;
   if (reps < 1 || !ms_plane || !bytes_plane || !ms_col || !bytes_col) return fail(SCFT_ERR_ARG, "bad arguments");
   API_BODY(scft::ctx_profile_step(c, reps, ms_plane, bytes_plane, ms_col, bytes_col));
+  return SCFT_OK;
+}
+
+int scft_set_sweep_groups(scft_ctx *c, int groups) {
+  if (int s = check_ctx(c, 0)) return s;
+  if (groups < 1) return fail(SCFT_ERR_ARG, "groups must be >= 1");
+  API_BODY(scft::ctx_set_sweep_groups(c, groups));
+  return SCFT_OK;
+}
+
+int scft_autotune(scft_ctx *c, int reps, int *groups, int *col_tile, double *ms_per_sweep) {
+  if (int s = check_ctx(c, 0)) return s;
+  if (reps < 1 || !groups || !col_tile || !ms_per_sweep) return fail(SCFT_ERR_ARG, "bad arguments");
+  API_BODY(scft::ctx_autotune(c, reps, groups, col_tile, ms_per_sweep));
   return SCFT_OK;
 }
 

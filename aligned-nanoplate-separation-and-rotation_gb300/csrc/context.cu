@@ -694,6 +694,52 @@ void setup_plates(scft_ctx *c, Instance &I) {
   CK(cudaStreamSynchronize(c->st));
 }
 
+ColJob *col64_jobs(scft_ctx *c) { return c->d_mix64_cj_tx[c->col64_tx == 8 ? 0 : (c->col64_tx == 16 ? 1 : 2)]; }
+
+// Sweep groups: contiguous ranges of the job order with about equal N * M.
+void build_groups(scft_ctx *c) {
+  const int n = (int)c->inst.size();
+  const std::vector<int> &order = c->job_order;
+  const int G = std::max(1, std::min(c->sweep_streams, n));
+  double total = 0.0;
+  for (auto &I : c->inst) total += (double)I.N * (double)I.M;
+  c->groups.clear();
+  int i0 = 0;
+  double acc = 0.0;
+  for (int g = 0; g < G; g++) {
+    int i1 = i0;
+    const double target = total * (g + 1) / G;
+    while (i1 < n && (g == G - 1 || acc + 0.5 * (double)c->inst[order[i1]].N * c->inst[order[i1]].M < target)) {
+      acc += (double)c->inst[order[i1]].N * (double)c->inst[order[i1]].M;
+      i1++;
+    }
+    if (i1 == i0 && i1 < n) {  // every group gets at least one instance
+      acc += (double)c->inst[order[i1]].N * (double)c->inst[order[i1]].M;
+      i1++;
+    }
+    if (i1 == i0) break;
+    scft_ctx::SweepGroup gr;
+    gr.inst_begin = i0;
+    gr.inst_end = i1;
+    gr.pj_begin = i0 ? c->inst_pj_end[i0 - 1] : 0;
+    gr.pj_end = c->inst_pj_end[i1 - 1];
+    gr.cj_begin = i0 ? c->inst_cj_end[i0 - 1] : 0;
+    gr.cj_end = c->inst_cj_end[i1 - 1];
+    c->groups.push_back(gr);
+    i0 = i1;
+  }
+  const int ng = (int)c->groups.size();
+  while ((int)c->side.size() < ng) {
+    cudaStream_t sst;
+    CK(cudaStreamCreateWithFlags(&sst, cudaStreamNonBlocking));
+    c->side.push_back(sst);
+    cudaEvent_t ev;
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    c->ev_join.push_back(ev);
+  }
+  if (!c->ev_fork) CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+}
+
 // Builds the device views and job lists once all instances exist.
 void build_jobs(scft_ctx *c) {
   const int n = (int)c->inst.size();
@@ -898,17 +944,25 @@ void build_jobs(scft_ctx *c) {
           c->prop_pj_count[s2] = inst_pj_end[oi];
           c->prop_cj_count[s2] = inst_cj_end[oi];
         }
+    c->job_order = order;
+    c->inst_pj_end = inst_pj_end;
+    c->inst_cj_end = inst_cj_end;
+    build_groups(c);
     c->shp_mix = choose_shape(emax_plane, sizeof(float2), (nxy_max + 32) * sizeof(float2));
     c->all64 = 1;
     for (auto &I : c->inst)
       if (I.p.Nx[0] != 64 || I.p.Nx[1] != 64 || I.p.Nx[2] != 64) c->all64 = 0;
     if (c->all64) {
-      std::vector<ColJob> cj64(pcj);
-      for (auto &j : cj64) {
-        for (auto &I : c->inst)
-          if (j.ptr == I.work32) j.kern = I.htab32;
+      for (int t = 0; t < 3; t++) {
+        const int tx = 8 << t;
+        std::vector<ColJob> cj64;
+        for (int oi = 0; oi < n; oi++) {
+          Instance &I = c->inst[order[oi]];
+          for (int y = 0; y < 64; y++)
+            for (int x0 = 0; x0 < 64; x0 += tx) cj64.push_back(ColJob{I.work32, I.htab32, I.geom, x0, y});
+        }
+        c->d_mix64_cj_tx[t] = dupload(c, cj64);
       }
-      c->d_mix64_cj = dupload(c, cj64);
       c->mix64_tab.clear();
       for (int oi = 0; oi < n; oi++) c->mix64_tab.push_back(c->h_mi[order[oi]]);
     }
@@ -1079,7 +1133,8 @@ void seq_update_1s(scft_ctx *c) {
   seq_poly_density(c);
 }
 
-// Mixed form: FP32 packed propagator sweep over all instances (after E32).
+// Mixed form: FP32 packed propagator sweep over all instances (after E32),
+// as one chain of launches per sweep group, each on its own side stream.
 void seq_mix_sweep(scft_ctx *c) {
   const int n = (int)c->inst.size();
   cudaStream_t st = c->st;
@@ -1087,21 +1142,49 @@ void seq_mix_sweep(scft_ctx *c) {
     CK(cudaMemsetAsync(I.acc32[0], 0, sizeof(float) * I.M, st));
     CK(cudaMemsetAsync(I.acc32[1], 0, sizeof(float) * I.M, st));
   }
-  if (c->all64) {
-    LK(launch_mix_plane64(c->mix64_tab.data(), c->prop_pj_count[0] / 64, c->d_tw32_64, 0, st));
-    for (int s = 1; s < c->nmax; s++) {
-      LK(launch_mix_col64(c->d_mix64_cj, c->prop_cj_count[s], c->d_tw32_64, 64, 64, st));
-      LK(launch_mix_plane64(c->mix64_tab.data(), c->prop_pj_count[s] / 64, c->d_tw32_64, s, st));
-    }
-  } else {
-    LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[0], c->d_mi, c->d_geoms, c->d_tw32, 0,
-                             st));
-    for (int s = 1; s < c->nmax; s++) {
-      LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw32, 3, 1, st));
-      LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_geoms, c->d_tw32, s,
-                               st));
-    }
+  const int G = (int)c->groups.size();
+  const bool fork = G > 1;
+  if (fork) {
+    CK(cudaEventRecord(c->ev_fork, st));
+    for (int g = 0; g < G; g++) CK(cudaStreamWaitEvent(c->side[g], c->ev_fork, 0));
   }
+  auto clampc = [](int v, int lo, int hi) { return std::min(std::max(v, lo), hi) - lo; };
+  auto plane = [&](int g, int s) {
+    const scft_ctx::SweepGroup &gr = c->groups[g];
+    cudaStream_t sg = fork ? c->side[g] : st;
+    const int cnt = clampc(c->prop_pj_count[s], gr.pj_begin, gr.pj_end);
+    if (cnt <= 0) return;
+    if (c->all64)
+      LK(launch_mix_plane64(c->mix64_tab.data() + gr.inst_begin, cnt / 64, c->d_tw32_64, s, sg));
+    else
+      LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj + gr.pj_begin, cnt, c->d_mi, c->d_geoms, c->d_tw32, s, sg));
+  };
+  auto column = [&](int g, int s) {
+    const scft_ctx::SweepGroup &gr = c->groups[g];
+    cudaStream_t sg = fork ? c->side[g] : st;
+    const int cnt = clampc(c->prop_cj_count[s], gr.cj_begin, gr.cj_end);
+    if (cnt <= 0) return;
+    if (c->all64) {
+      // 64 * 64 / tx jobs per instance, in job order
+      const int per = 64 * (64 / c->col64_tx);
+      const int act = clampc(c->prop_pj_count[s], gr.pj_begin, gr.pj_end) / 64;
+      if (act > 0)
+        LK(launch_mix_col64(col64_jobs(c) + (size_t)gr.inst_begin * per, act * per, c->d_tw32_64, 64, 64,
+                            c->col64_tx, sg));
+    } else
+      LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cnt, c->d_geoms, c->d_tw32, 3, 1, sg));
+  };
+  for (int g = 0; g < G; g++) plane(g, 0);
+  for (int s = 1; s < c->nmax; s++)
+    for (int g = 0; g < G; g++) {
+      column(g, s);
+      plane(g, s);
+    }
+  if (fork)
+    for (int g = 0; g < G; g++) {
+      CK(cudaEventRecord(c->ev_join[g], c->side[g]));
+      CK(cudaStreamWaitEvent(st, c->ev_join[g], 0));
+    }
   LK(launch_mix_q_finalize(c->d_fi, n, st));
 }
 
@@ -1180,6 +1263,9 @@ void ctx_create(scft_ctx *c, const scft_params *params, int n_inst) {
 void ctx_destroy(scft_ctx *c) {
   if (c->g_update) cudaGraphExecDestroy(c->g_update);
   for (void *p : c->allocs) cudaFree(p);
+  for (cudaStream_t sst : c->side) cudaStreamDestroy(sst);
+  for (cudaEvent_t ev : c->ev_join) cudaEventDestroy(ev);
+  if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->st) cudaStreamDestroy(c->st);
 }
 
@@ -1224,6 +1310,73 @@ void ctx_update(scft_ctx *c, int n_iter) {
   CK(cudaStreamSynchronize(c->st));
 }
 
+// Number of independent launch chains of the mixed sweep (1 = one chain).
+void ctx_set_sweep_groups(scft_ctx *c, int groups) {
+  if (groups < 1) throw ScftError(SCFT_ERR_ARG, "groups must be >= 1");
+  c->sweep_streams = groups;
+  if (!c->mixed) return;
+  build_groups(c);
+  if (c->g_update) {  // the captured iteration holds the old launch chains
+    CK(cudaGraphExecDestroy(c->g_update));
+    c->g_update = nullptr;
+  }
+}
+
+// Autotuner of the mixed sweep's launch schedule: for every candidate
+// (number of sweep groups, z-pass columns per CTA of the 64-point kernels)
+// it times `reps` complete propagator sweeps of the batch with CUDA events on
+// the context stream, after one untimed sweep, and keeps the fastest.  The
+// sweeps recompute the current densities, so the state is unchanged.
+void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *tx_out, double *ms_out) {
+  *groups_out = 1;
+  *tx_out = 0;
+  *ms_out = 0.0;
+  if (!c->mixed) return;  // the FP64 method has a single schedule
+  if (c->dirty_density) ctx_poly_density(c);
+  const int n = (int)c->inst.size();
+  std::vector<int> gs, txs;
+  for (int g : {1, 2, 3, 4, 5, 6, 8})
+    if (g <= n) gs.push_back(g);
+  if (c->all64)
+    txs = {8, 16, 32};
+  else
+    txs = {c->col64_tx};
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  double best = 1e300;
+  int bg = c->sweep_streams, bt = c->col64_tx;
+  for (int g : gs)
+    for (int tx : txs) {
+      c->sweep_streams = g;
+      c->col64_tx = tx;
+      build_groups(c);
+      seq_mix_sweep(c);
+      CK(cudaEventRecord(e0, c->st));
+      for (int r = 0; r < reps; r++) seq_mix_sweep(c);
+      CK(cudaEventRecord(e1, c->st));
+      CK(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      CK(cudaEventElapsedTime(&ms, e0, e1));
+      if (ms / reps < best) {
+        best = ms / reps;
+        bg = g;
+        bt = tx;
+      }
+    }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  c->col64_tx = bt;
+  ctx_set_sweep_groups(c, bg);
+  if (c->g_update) {
+    CK(cudaGraphExecDestroy(c->g_update));
+    c->g_update = nullptr;
+  }
+  *groups_out = (int)c->groups.size();
+  *tx_out = c->all64 ? bt : 0;
+  *ms_out = best;
+}
+
 // Isolated timing of the two kernels of one propagator step (step 3(N-1)/4,
 // a paired step) with their algorithmic bytes.
 void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
@@ -1248,7 +1401,8 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   CK(cudaEventRecord(e1, c->st));
   for (int r = 0; r < reps; r++) {
     if (c->mixed && c->all64)
-      LK(launch_mix_col64(c->d_mix64_cj, c->prop_cj_count[s], c->d_tw32_64, 64, 64, c->st));
+      LK(launch_mix_col64(col64_jobs(c), c->prop_pj_count[s] * (64 / c->col64_tx), c->d_tw32_64, 64, 64,
+                          c->col64_tx, c->st));
     else if (c->mixed)
       LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw32, 3, 1, c->st));
     else

@@ -93,10 +93,24 @@ struct scft_ctx {
   int all64 = 0;         // every instance is 64^3: specialised propagator kernels
   void *d_tw32_64 = nullptr;  // the 64-point twiddle table inside d_tw32
   void *d_tw32 = nullptr;
-  scft::ColJob *d_mix64_cj = nullptr;  // z-pass jobs of the 64^3 kernels
+  scft::ColJob *d_mix64_cj_tx[3] = {};  // z-pass jobs of the 64^3 kernels for 8, 16, 32 columns per CTA
+  int col64_tx = 16;                      // columns per CTA of the 64^3 z pass
   scft::MixInst *d_mi = nullptr;
   std::vector<scft::MixInst> h_mi;       // host copy of d_mi
   std::vector<scft::MixInst> mix64_tab;  // instances in job order (64^3 plane pass)
+  // The mixed sweep of a batch runs as `groups` independent chains of
+  // launches on side streams (contiguous instance ranges in job order), so
+  // that one group's column passes fill the last wave of another group's
+  // plane pass; all of it sits in one captured graph.
+  struct SweepGroup {
+    int inst_begin, inst_end, pj_begin, pj_end, cj_begin, cj_end;
+  };
+  std::vector<SweepGroup> groups;
+  std::vector<int> job_order, inst_pj_end, inst_cj_end;  // mixed job lists, by instance
+  int sweep_streams = 2;  // requested number of groups (1 = a single chain)
+  std::vector<cudaStream_t> side;
+  std::vector<cudaEvent_t> ev_join;
+  cudaEvent_t ev_fork = nullptr;
   scft::PropJob *d_mix_pj = nullptr;
   scft::ColJob *d_mix_cj = nullptr;
   scft::PlaneJob *d_pj_zr = nullptr, *d_pj_zs = nullptr;

@@ -364,11 +364,18 @@ cudaError_t launch_mix_plane64(const MixInst *insts, int ninst, const void *tw64
   return cudaSuccess;
 }
 
-cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw64, int nx, int ny, cudaStream_t st) {
+cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw64, int nx, int ny, int tx,
+                             cudaStream_t st) {
   if (njobs <= 0) return cudaSuccess;
   const double s = 1.0 / ((double)nx * ny * 64);
   const float s_hi = (float)s, s_lo = (float)(s - (double)s_hi);
-  k_mix_col64<16><<<njobs, 128, 0, st>>>(jobs, reinterpret_cast<const float2 *>(tw64), nx, ny, s_hi, s_lo);
+  const float2 *tw = reinterpret_cast<const float2 *>(tw64);
+  switch (tx) {
+    case 8: k_mix_col64<8><<<njobs, 64, 0, st>>>(jobs, tw, nx, ny, s_hi, s_lo); break;
+    case 16: k_mix_col64<16><<<njobs, 128, 0, st>>>(jobs, tw, nx, ny, s_hi, s_lo); break;
+    case 32: k_mix_col64<32><<<njobs, 256, 0, st>>>(jobs, tw, nx, ny, s_hi, s_lo); break;
+    default: return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 

@@ -31,7 +31,9 @@ struct Mix64Table {
 };
 // insts: host array of the active instances in job order (64 CTAs each)
 cudaError_t launch_mix_plane64(const MixInst *insts, int ninst, const void *tw64, int n, cudaStream_t st);
-cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw64, int nx, int ny, cudaStream_t st);
+// tx: x columns per CTA (8, 16 or 32); jobs must be built for that width
+cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw64, int nx, int ny, int tx,
+                             cudaStream_t st);
 cudaError_t launch_mix_smear(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
 cudaError_t launch_mix_update(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
 cudaError_t launch_mix_boltzmann(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);

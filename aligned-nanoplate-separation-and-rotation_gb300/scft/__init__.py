@@ -26,7 +26,7 @@ EXPORTS = ("scft_last_error", "scft_version", "scft_create", "scft_destroy", "sc
            "scft_set_fields", "scft_get_fields", "scft_calc_poly_density", "scft_update_1s",
            "scft_calc_H", "scft_grad_geom", "scft_get_density", "scft_get_plate_density", "scft_get_smeared", "scft_diblock_density",
            "scft_homopolymer_density", "scft_fft3d", "scft_sync", "scft_get_stream", "scft_launch_count",
-           "scft_profile_step", "scft_diblock_density_noalloc")
+           "scft_profile_step", "scft_diblock_density_noalloc", "scft_set_sweep_groups", "scft_autotune")
 
 
 class ScftError(RuntimeError):
@@ -100,6 +100,9 @@ def load(path: str | None = None):
     lib.scft_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
     lib.scft_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
     lib.scft_profile_step.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
+    lib.scft_set_sweep_groups.argtypes = [vp, ctypes.c_int]
+    ip = ctypes.POINTER(ctypes.c_int)
+    lib.scft_autotune.argtypes = [vp, ctypes.c_int, ip, ip, dp]
     lib.scft_diblock_density_noalloc.argtypes = [ctypes.POINTER(ctypes.c_int), dp, ctypes.c_int, ctypes.c_int,
                                                  ctypes.c_double, vp, vp, vp, vp, vp, vp]
     _lib = lib
@@ -257,6 +260,14 @@ class Context:
         _check(load().scft_homopolymer_density(self._h, inst, _ptr(w.view(np.float64)), int(N), float(nK),
                                                _ptr(r.view(np.float64)), _ptr(Q)))
         return r, complex(Q[0], Q[1])
+
+    def set_sweep_groups(self, groups: int):
+        _check(load().scft_set_sweep_groups(self._h, groups))
+
+    def autotune(self, reps=3) -> dict:
+        g, t, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _check(load().scft_autotune(self._h, reps, ctypes.byref(g), ctypes.byref(t), ctypes.byref(ms)))
+        return {"groups": g.value, "col_tile": t.value, "ms_per_sweep": ms.value}
 
     def stream(self) -> int:
         h = ctypes.c_void_p()

@@ -153,6 +153,8 @@ def main():
     ap.add_argument("--iterations-only", action="store_true",
                     help="warm-up + timed iterations only (for ncu launch lists)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
+    ap.add_argument("--no-autotune", action="store_true", help="keep the default launch schedule")
+    ap.add_argument("--sweep-groups", type=int, default=0, help="fixed number of sweep groups (0: default)")
     ap.add_argument("--relax", type=int, default=500,
                     help="untimed mixed-form iterations from the seeded fields before anything is measured, so "
                          "that timing and the FP64 comparison start near the saddle point (0: seeded fields)")
@@ -231,6 +233,14 @@ def main():
     for k in range(n_inst):
         ctx.set_fields(k, fields[k])
     ctx.calc_poly_density()
+    schedule = None
+    if form == "mixed":
+        if args.sweep_groups > 0:
+            ctx.set_sweep_groups(args.sweep_groups)
+            schedule = {"groups": args.sweep_groups, "tuned": False}
+        elif not args.no_autotune:
+            schedule = dict(ctx.autotune(3), tuned=True)
+    config["schedule"] = schedule
     stream = torch.cuda.ExternalStream(ctx.stream())
     ctx.update_1s(max(3, args.warmup))
     torch.cuda.synchronize()

@@ -140,3 +140,35 @@ def test_mixed_64cubed_specialised_kernels_match_fp64(scft):
         assert np.abs(H32[:, k, 2] - H64[:, k, 2]).max() <= Q_TOL * np.abs(H64[:, k, 2]).max()
         assert rel(d32[k][0].real, d64[k][0].real) < RHO_TOL
         assert rel(d32[k][1].real, d64[k][1].real) < RHO_TOL
+
+
+@pytest.mark.parametrize("grids", [((64, 64, 64),) * 5, ((48, 48, 48), (32, 32, 32), (48, 48, 48))])
+def test_sweep_schedule_does_not_change_results(scft, grids):
+    """Sweep groups and z-pass tile widths only regroup independent work:
+    every schedule gives bit-identical H, Q and densities; the autotuner
+    reports a valid choice."""
+    from scft.workloads import plate_params, seeded_fields
+
+    params = [plate_params(5.0 * k, N=24 + 4 * k, grid=g, box_rg=(4.0, 4.0, 4.0), precision=scft.PREC_MIXED)
+              for k, g in enumerate(grids)]
+    fields = [seeded_fields(p, 40 + k) for k, p in enumerate(params)]
+    res = []
+    for mode in ("g1", "g3", "tuned"):
+        with scft.Context(params) as ctx:
+            for k, f in enumerate(fields):
+                ctx.set_fields(k, f)
+            ctx.calc_poly_density()
+            if mode == "g1":
+                ctx.set_sweep_groups(1)
+            elif mode == "g3":
+                ctx.set_sweep_groups(3)
+            else:
+                t = ctx.autotune(2)
+                assert 1 <= t["groups"] <= len(params) and t["ms_per_sweep"] > 0
+                assert t["col_tile"] in ((8, 16, 32) if grids[0] == (64, 64, 64) else (0,))
+            ctx.update_1s(3)
+            res.append((ctx.calc_H(), [ctx.density(k)[0] for k in range(len(params))]))
+    for H, d in res[1:]:
+        assert np.array_equal(H, res[0][0])
+        for a, b in zip(d, res[0][1]):
+            assert np.array_equal(a, b)
