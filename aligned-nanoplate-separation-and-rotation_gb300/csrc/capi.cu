@@ -22,8 +22,8 @@ void ctx_diblock_density(scft_ctx *c, int k, const double *smwa, const double *s
                          double *Q);
 void ctx_override_nD(scft_ctx *c, int k, double nD);
 int ctx_grad_geom(scft_ctx *c, double *out);
-void ctx_set_sweep_groups(scft_ctx *c, int groups);
-void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *tx_out, double *ms_out);
+void ctx_set_sweep_groups(scft_ctx *c, int groups, int phases);
+void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *tx_out, double *ms_out);
 void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
                       double *bytes_col);
 int error_code(const std::exception &e);
@@ -228,17 +228,17 @@ int scft_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   return SCFT_OK;
 }
 
-int scft_set_sweep_groups(scft_ctx *c, int groups) {
+int scft_set_sweep_groups(scft_ctx *c, int groups, int phases) {
   if (int s = check_ctx(c, 0)) return s;
-  if (groups < 1) return fail(SCFT_ERR_ARG, "groups must be >= 1");
-  API_BODY(scft::ctx_set_sweep_groups(c, groups));
+  if (groups < 1 || phases < 1) return fail(SCFT_ERR_ARG, "groups and phases must be >= 1");
+  API_BODY(scft::ctx_set_sweep_groups(c, groups, phases));
   return SCFT_OK;
 }
 
-int scft_autotune(scft_ctx *c, int reps, int *groups, int *col_tile, double *ms_per_sweep) {
+int scft_autotune(scft_ctx *c, int reps, int *groups, int *phases, int *col_tile, double *ms_per_sweep) {
   if (int s = check_ctx(c, 0)) return s;
-  if (reps < 1 || !groups || !col_tile || !ms_per_sweep) return fail(SCFT_ERR_ARG, "bad arguments");
-  API_BODY(scft::ctx_autotune(c, reps, groups, col_tile, ms_per_sweep));
+  if (reps < 1 || !groups || !phases || !col_tile || !ms_per_sweep) return fail(SCFT_ERR_ARG, "bad arguments");
+  API_BODY(scft::ctx_autotune(c, reps, groups, phases, col_tile, ms_per_sweep));
   return SCFT_OK;
 }
 

@@ -696,37 +696,56 @@ void setup_plates(scft_ctx *c, Instance &I) {
 
 ColJob *col64_jobs(scft_ctx *c) { return c->d_mix64_cj_tx[c->col64_tx == 8 ? 0 : (c->col64_tx == 16 ? 1 : 2)]; }
 
-// Sweep groups: contiguous ranges of the job order with about equal N * M.
+// Sweep groups: the job order is cut into `sweep_phases` contiguous phases and
+// each phase into `sweep_streams` contiguous groups, all of about equal N * M.
 void build_groups(scft_ctx *c) {
   const int n = (int)c->inst.size();
   const std::vector<int> &order = c->job_order;
-  const int G = std::max(1, std::min(c->sweep_streams, n));
-  double total = 0.0;
-  for (auto &I : c->inst) total += (double)I.N * (double)I.M;
+  const int P = std::max(1, std::min(c->sweep_phases, n));
+  auto work = [&](int oi) { return (double)c->inst[order[oi]].N * (double)c->inst[order[oi]].M; };
+  // cuts [lo, hi) into k contiguous pieces of about equal work, none empty
+  auto cut = [&](int lo, int hi, int k) {
+    std::vector<int> ends;
+    double total = 0.0;
+    for (int oi = lo; oi < hi; oi++) total += work(oi);
+    double acc = 0.0;
+    int i = lo;
+    for (int g = 0; g < k && i < hi; g++) {
+      const double target = total * (g + 1) / k;
+      int j = i;
+      const int left = k - g - 1;  // pieces still to fill after this one
+      while (j < hi && (g == k - 1 || acc + 0.5 * work(j) < target) && hi - j > left) {
+        acc += work(j);
+        j++;
+      }
+      if (j == i) {
+        acc += work(j);
+        j++;
+      }
+      ends.push_back(j);
+      i = j;
+    }
+    return ends;
+  };
   c->groups.clear();
-  int i0 = 0;
-  double acc = 0.0;
-  for (int g = 0; g < G; g++) {
-    int i1 = i0;
-    const double target = total * (g + 1) / G;
-    while (i1 < n && (g == G - 1 || acc + 0.5 * (double)c->inst[order[i1]].N * c->inst[order[i1]].M < target)) {
-      acc += (double)c->inst[order[i1]].N * (double)c->inst[order[i1]].M;
-      i1++;
+  int p0 = 0, ph = 0;
+  for (int pe : cut(0, n, P)) {
+    const int G = std::max(1, std::min(c->sweep_streams, pe - p0));
+    int i0 = p0;
+    for (int i1 : cut(p0, pe, G)) {
+      scft_ctx::SweepGroup gr;
+      gr.inst_begin = i0;
+      gr.inst_end = i1;
+      gr.pj_begin = i0 ? c->inst_pj_end[i0 - 1] : 0;
+      gr.pj_end = c->inst_pj_end[i1 - 1];
+      gr.cj_begin = i0 ? c->inst_cj_end[i0 - 1] : 0;
+      gr.cj_end = c->inst_cj_end[i1 - 1];
+      gr.phase = ph;
+      c->groups.push_back(gr);
+      i0 = i1;
     }
-    if (i1 == i0 && i1 < n) {  // every group gets at least one instance
-      acc += (double)c->inst[order[i1]].N * (double)c->inst[order[i1]].M;
-      i1++;
-    }
-    if (i1 == i0) break;
-    scft_ctx::SweepGroup gr;
-    gr.inst_begin = i0;
-    gr.inst_end = i1;
-    gr.pj_begin = i0 ? c->inst_pj_end[i0 - 1] : 0;
-    gr.pj_end = c->inst_pj_end[i1 - 1];
-    gr.cj_begin = i0 ? c->inst_cj_end[i0 - 1] : 0;
-    gr.cj_end = c->inst_cj_end[i1 - 1];
-    c->groups.push_back(gr);
-    i0 = i1;
+    p0 = pe;
+    ph++;
   }
   const int ng = (int)c->groups.size();
   while ((int)c->side.size() < ng) {
@@ -1144,10 +1163,6 @@ void seq_mix_sweep(scft_ctx *c) {
   }
   const int G = (int)c->groups.size();
   const bool fork = G > 1;
-  if (fork) {
-    CK(cudaEventRecord(c->ev_fork, st));
-    for (int g = 0; g < G; g++) CK(cudaStreamWaitEvent(c->side[g], c->ev_fork, 0));
-  }
   auto clampc = [](int v, int lo, int hi) { return std::min(std::max(v, lo), hi) - lo; };
   auto plane = [&](int g, int s) {
     const scft_ctx::SweepGroup &gr = c->groups[g];
@@ -1162,8 +1177,6 @@ void seq_mix_sweep(scft_ctx *c) {
   auto column = [&](int g, int s) {
     const scft_ctx::SweepGroup &gr = c->groups[g];
     cudaStream_t sg = fork ? c->side[g] : st;
-    const int cnt = clampc(c->prop_cj_count[s], gr.cj_begin, gr.cj_end);
-    if (cnt <= 0) return;
     if (c->all64) {
       // 64 * 64 / tx jobs per instance, in job order
       const int per = 64 * (64 / c->col64_tx);
@@ -1171,20 +1184,32 @@ void seq_mix_sweep(scft_ctx *c) {
       if (act > 0)
         LK(launch_mix_col64(col64_jobs(c) + (size_t)gr.inst_begin * per, act * per, c->d_tw32_64, 64, 64,
                             c->col64_tx, sg));
-    } else
-      LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cnt, c->d_geoms, c->d_tw32, 3, 1, sg));
+    } else {
+      const int cnt = clampc(c->prop_cj_count[s], gr.cj_begin, gr.cj_end);
+      if (cnt > 0)
+        LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cnt, c->d_geoms, c->d_tw32, 3, 1, sg));
+    }
   };
-  for (int g = 0; g < G; g++) plane(g, 0);
-  for (int s = 1; s < c->nmax; s++)
-    for (int g = 0; g < G; g++) {
-      column(g, s);
-      plane(g, s);
+  for (int g0 = 0; g0 < G;) {
+    int g1 = g0;
+    while (g1 < G && c->groups[g1].phase == c->groups[g0].phase) g1++;
+    if (fork) {
+      CK(cudaEventRecord(c->ev_fork, st));
+      for (int g = g0; g < g1; g++) CK(cudaStreamWaitEvent(c->side[g], c->ev_fork, 0));
     }
-  if (fork)
-    for (int g = 0; g < G; g++) {
-      CK(cudaEventRecord(c->ev_join[g], c->side[g]));
-      CK(cudaStreamWaitEvent(st, c->ev_join[g], 0));
-    }
+    for (int g = g0; g < g1; g++) plane(g, 0);
+    for (int s = 1; s < c->nmax; s++)
+      for (int g = g0; g < g1; g++) {
+        column(g, s);
+        plane(g, s);
+      }
+    if (fork)
+      for (int g = g0; g < g1; g++) {
+        CK(cudaEventRecord(c->ev_join[g], c->side[g]));
+        CK(cudaStreamWaitEvent(st, c->ev_join[g], 0));
+      }
+    g0 = g1;
+  }
   LK(launch_mix_q_finalize(c->d_fi, n, st));
 }
 
@@ -1311,9 +1336,10 @@ void ctx_update(scft_ctx *c, int n_iter) {
 }
 
 // Number of independent launch chains of the mixed sweep (1 = one chain).
-void ctx_set_sweep_groups(scft_ctx *c, int groups) {
-  if (groups < 1) throw ScftError(SCFT_ERR_ARG, "groups must be >= 1");
+void ctx_set_sweep_groups(scft_ctx *c, int groups, int phases) {
+  if (groups < 1 || phases < 1) throw ScftError(SCFT_ERR_ARG, "groups and phases must be >= 1");
   c->sweep_streams = groups;
+  c->sweep_phases = phases;
   if (!c->mixed) return;
   build_groups(c);
   if (c->g_update) {  // the captured iteration holds the old launch chains
@@ -1327,8 +1353,9 @@ void ctx_set_sweep_groups(scft_ctx *c, int groups) {
 // it times `reps` complete propagator sweeps of the batch with CUDA events on
 // the context stream, after one untimed sweep, and keeps the fastest.  The
 // sweeps recompute the current densities, so the state is unchanged.
-void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *tx_out, double *ms_out) {
+void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *tx_out, double *ms_out) {
   *groups_out = 1;
+  *phases_out = 1;
   *tx_out = 0;
   *ms_out = 0.0;
   if (!c->mixed) return;  // the FP64 method has a single schedule
@@ -1344,10 +1371,16 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *tx_out, double *m
   cudaEvent_t e0, e1;
   CK(cudaEventCreate(&e0));
   CK(cudaEventCreate(&e1));
+  std::vector<int> ps;
+  for (int ph : {1, 2, 3, 4})
+    if (ph <= n) ps.push_back(ph);
   double best = 1e300;
-  int bg = c->sweep_streams, bt = c->col64_tx;
+  int bg = c->sweep_streams, bt = c->col64_tx, bp = c->sweep_phases;
+  for (int ph : ps)
   for (int g : gs)
     for (int tx : txs) {
+      if (g * ph > n) continue;
+      c->sweep_phases = ph;
       c->sweep_streams = g;
       c->col64_tx = tx;
       build_groups(c);
@@ -1362,17 +1395,19 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *tx_out, double *m
         best = ms / reps;
         bg = g;
         bt = tx;
+        bp = ph;
       }
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   c->col64_tx = bt;
-  ctx_set_sweep_groups(c, bg);
+  ctx_set_sweep_groups(c, bg, bp);
   if (c->g_update) {
     CK(cudaGraphExecDestroy(c->g_update));
     c->g_update = nullptr;
   }
-  *groups_out = (int)c->groups.size();
+  *groups_out = bg;
+  *phases_out = bp;
   *tx_out = c->all64 ? bt : 0;
   *ms_out = best;
 }

@@ -102,10 +102,13 @@ struct scft_ctx {
   // launches on side streams (contiguous instance ranges in job order), so
   // that one group's column passes fill the last wave of another group's
   // plane pass; all of it sits in one captured graph.
+  // Phases run one after another (each phase's working set can stay in L2);
+  // the groups of one phase run concurrently.
   struct SweepGroup {
-    int inst_begin, inst_end, pj_begin, pj_end, cj_begin, cj_end;
+    int inst_begin, inst_end, pj_begin, pj_end, cj_begin, cj_end, phase;
   };
   std::vector<SweepGroup> groups;
+  int sweep_phases = 1;  // requested number of sequential phases
   std::vector<int> job_order, inst_pj_end, inst_cj_end;  // mixed job lists, by instance
   int sweep_streams = 2;  // requested number of groups (1 = a single chain)
   std::vector<cudaStream_t> side;

@@ -100,9 +100,9 @@ def load(path: str | None = None):
     lib.scft_get_stream.argtypes = [vp, ctypes.POINTER(vp)]
     lib.scft_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
     lib.scft_profile_step.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
-    lib.scft_set_sweep_groups.argtypes = [vp, ctypes.c_int]
+    lib.scft_set_sweep_groups.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     ip = ctypes.POINTER(ctypes.c_int)
-    lib.scft_autotune.argtypes = [vp, ctypes.c_int, ip, ip, dp]
+    lib.scft_autotune.argtypes = [vp, ctypes.c_int, ip, ip, ip, dp]
     lib.scft_diblock_density_noalloc.argtypes = [ctypes.POINTER(ctypes.c_int), dp, ctypes.c_int, ctypes.c_int,
                                                  ctypes.c_double, vp, vp, vp, vp, vp, vp]
     _lib = lib
@@ -261,13 +261,14 @@ class Context:
                                                _ptr(r.view(np.float64)), _ptr(Q)))
         return r, complex(Q[0], Q[1])
 
-    def set_sweep_groups(self, groups: int):
-        _check(load().scft_set_sweep_groups(self._h, groups))
+    def set_sweep_groups(self, groups: int, phases: int = 1):
+        _check(load().scft_set_sweep_groups(self._h, groups, phases))
 
     def autotune(self, reps=3) -> dict:
-        g, t, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
-        _check(load().scft_autotune(self._h, reps, ctypes.byref(g), ctypes.byref(t), ctypes.byref(ms)))
-        return {"groups": g.value, "col_tile": t.value, "ms_per_sweep": ms.value}
+        g, ph, t, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        _check(load().scft_autotune(self._h, reps, ctypes.byref(g), ctypes.byref(ph), ctypes.byref(t),
+                                    ctypes.byref(ms)))
+        return {"groups": g.value, "phases": ph.value, "col_tile": t.value, "ms_per_sweep": ms.value}
 
     def stream(self) -> int:
         h = ctypes.c_void_p()

@@ -154,7 +154,8 @@ def main():
                     help="warm-up + timed iterations only (for ncu launch lists)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch schedule")
-    ap.add_argument("--sweep-groups", type=int, default=0, help="fixed number of sweep groups (0: default)")
+    ap.add_argument("--sweep-groups", type=int, default=0, help="fixed number of sweep groups (0: autotune)")
+    ap.add_argument("--sweep-phases", type=int, default=1, help="sequential phases with --sweep-groups")
     ap.add_argument("--relax", type=int, default=500,
                     help="untimed mixed-form iterations from the seeded fields before anything is measured, so "
                          "that timing and the FP64 comparison start near the saddle point (0: seeded fields)")
@@ -236,8 +237,8 @@ def main():
     schedule = None
     if form == "mixed":
         if args.sweep_groups > 0:
-            ctx.set_sweep_groups(args.sweep_groups)
-            schedule = {"groups": args.sweep_groups, "tuned": False}
+            ctx.set_sweep_groups(args.sweep_groups, args.sweep_phases)
+            schedule = {"groups": args.sweep_groups, "phases": args.sweep_phases, "tuned": False}
         elif not args.no_autotune:
             schedule = dict(ctx.autotune(3), tuned=True)
     config["schedule"] = schedule
@@ -264,8 +265,10 @@ def main():
     ms = allmax(e0.elapsed_time(e1))
     H = ctx.calc_H()
     value = n_inst * args.steps * world / (ms / 1e3)
-    rho_mixed = [ctx.density(k) for k in range(n_inst)] if (form == "mixed" and not args.no_plain
-                                                             and not args.iterations_only) else None
+    rho_mixed = g_mixed = None
+    if form == "mixed" and not args.no_plain and not args.iterations_only:
+        rho_mixed = [ctx.density(k) for k in range(n_inst)]
+        g_mixed = ctx.grad_geom()
     if args.iterations_only:
         ctx.close()
         if rank == 0:
@@ -318,6 +321,7 @@ def main():
             f1.synchronize()
             ms64 = allmax(f0.elapsed_time(f1))
             H64 = c64.calc_H()
+            g64 = c64.grad_geom()
             drho = []
             for k in range(n_inst):
                 a64, b64, _ = c64.density(k)
@@ -325,14 +329,18 @@ def main():
                 drho.append(max(np.abs(a32 - a64).max() / np.abs(a64).max(),
                                 np.abs(b32 - b64).max() / np.abs(b64).max()))
         dH = np.abs(H[:, 0] - H64[:, 0]) / np.abs(H64[:, 0])
+        # dH/dtheta and dH/dc of the plate: max error over the instance's components
+        # relative to its largest component
+        dg = [float(np.abs(a[0] - b[0]).max() / max(np.abs(b[0]).max(), 1e-300)) for a, b in zip(g_mixed, g64)]
         plain = {"value": n_inst * args.steps * world / (ms64 / 1e3), "unit": UNIT, "ms_per_step": ms64 / args.steps,
                  "mixed_over_plain": (n_inst * args.steps * world / (ms / 1e3)) / (n_inst * args.steps * world /
                                                                                     (ms64 / 1e3)),
                  "dH_rel_max": float(dH.max()), "dH_rel_median": float(np.median(dH)),
                  "dH_abs_max": float(np.abs(H[:, 0] - H64[:, 0]).max()),
                  "drho_rel_max": float(max(drho)),
-                 "per_instance": [{"grid": list(p.Nx), "N": p.Nda + p.Ndb, "dH_rel": float(d), "drho_rel": float(r)}
-                                  for p, d, r in zip(params, dH, drho)],
+                 "dgrad_rel_max": float(max(dg)),
+                 "per_instance": [{"grid": list(p.Nx), "N": p.Nda + p.Ndb, "dH_rel": float(d), "drho_rel": float(r),
+                                   "dgrad_rel": float(gg)} for p, d, r, gg in zip(params, dH, drho, dg)],
                  "note": f"same batch, both from the fields after {args.relax} mixed-form iterations from the "
                          f"seeded start, then max(3, warmup) + steps iterations each; drho = max |rho32 - rho64| / "
                          f"max |rho64| over rho_A, rho_B"}

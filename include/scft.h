@@ -207,18 +207,20 @@ int scft_get_stream(scft_ctx *ctx, void **stream);
 int scft_launch_count(scft_ctx *ctx, long long *count);
 
 /* Launch schedule of the mixed form's propagator sweep (no counterpart in
- * the reference).  The sweep of a batch runs as `groups` independent chains
- * of launches (contiguous instance ranges, about equal work) on side streams
- * inside the captured iteration, so that one chain's z passes fill the last
- * wave of another chain's plane pass.  Default 2. */
-int scft_set_sweep_groups(scft_ctx *ctx, int groups);
+ * the reference).  The batch is cut into `phases` sub-batches that sweep one
+ * after another (so that a sub-batch's working set can stay in L2), and each
+ * sub-batch into `groups` independent chains of launches (contiguous instance
+ * ranges, about equal work) on side streams inside the captured iteration, so
+ * that one chain's z passes fill the last wave of another chain's plane pass.
+ * Default 2 groups, 1 phase. */
+int scft_set_sweep_groups(scft_ctx *ctx, int groups, int phases);
 
 /* Autotuner: times reps full propagator sweeps of the batch for every
- * candidate schedule (1-6 or 8 groups; for 64-point grids also 8, 16 or 32
- * z-pass columns per CTA) with CUDA events and keeps the fastest.  Reports
- * the choice (col_tile 0 where it does not apply) and its time per sweep.
- * FP64 contexts have a single schedule (groups = 1). */
-int scft_autotune(scft_ctx *ctx, int reps, int *groups, int *col_tile, double *ms_per_sweep);
+ * candidate schedule (1-4 phases x 1-6 or 8 groups; for 64-point grids also
+ * 8, 16 or 32 z-pass columns per CTA) with CUDA events and keeps the
+ * fastest.  Reports the choice (col_tile 0 where it does not apply) and its
+ * time per sweep.  FP64 contexts have a single schedule (1 group, 1 phase). */
+int scft_autotune(scft_ctx *ctx, int reps, int *groups, int *phases, int *col_tile, double *ms_per_sweep);
 
 /* Times the two kernels of one propagator step in isolation on the context
  * stream (CUDA events, `reps` launches each, all instances): the xy-plane pass

@@ -153,7 +153,7 @@ def test_sweep_schedule_does_not_change_results(scft, grids):
               for k, g in enumerate(grids)]
     fields = [seeded_fields(p, 40 + k) for k, p in enumerate(params)]
     res = []
-    for mode in ("g1", "g3", "tuned"):
+    for mode in ("g1", "g3", "g2p2", "tuned"):
         with scft.Context(params) as ctx:
             for k, f in enumerate(fields):
                 ctx.set_fields(k, f)
@@ -162,6 +162,8 @@ def test_sweep_schedule_does_not_change_results(scft, grids):
                 ctx.set_sweep_groups(1)
             elif mode == "g3":
                 ctx.set_sweep_groups(3)
+            elif mode == "g2p2":
+                ctx.set_sweep_groups(2, 2)
             else:
                 t = ctx.autotune(2)
                 assert 1 <= t["groups"] <= len(params) and t["ms_per_sweep"] > 0
