@@ -352,8 +352,6 @@ void validate(const scft_params &p) {
     if (!(p.shell_width > 0)) bad("shell_width must be positive when shell_lambda != 0");
   }
   if (p.sigma > 0 && p.Ng < 1) bad("grafted chains need Ng >= 1");
-  if (p.precision == SCFT_PREC_MIXED && p.sigma > 0 && p.Ng > 0 && p.n_exp_nr > 0)
-    throw ScftError(SCFT_ERR_UNSUPPORTED, "grafted chains are built for the FP64 method only");
 }
 
 // alpha, beta of w <- alpha w - beta F for each field and sign branch of
@@ -678,10 +676,19 @@ void setup_plates(scft_ctx *c, Instance &I) {
   I.info.phiD = phiD;
   I.info.nD = phiD * p.rho0 * Vf / I.N;
   I.graft = (sigma > 0.0 && p.n_exp_nr > 0 && nP > 0.0) ? 1 : 0;
-  if (I.graft) {
+  if (I.graft && !I.mixed) {
     I.gwork = dalloc<double2>(c, M);
     I.ghist = dalloc<double2>(c, (size_t)M * p.Ng);
     I.gacc = dalloc<double2>(c, M);
+  } else if (I.graft) {
+    I.zg = dalloc<double2>(c, M);
+    I.Eg32 = dalloc<float>(c, M);
+    I.ghist32 = dalloc<float>(c, (size_t)M * p.Ng);
+    I.gacc32 = dalloc<float>(c, M);
+    I.gwork32 = dalloc<float2>(c, M);
+    I.gK = dalloc<int>(c, (size_t)2 * p.Ng);
+    I.gpart = dalloc<double>(c, (size_t)2 * p.Ng * p.Nx[2]);
+    I.sm[2] = dalloc<double2>(c, M);
   }
   if (I.mixed) {
     mix_coefficients_final(c, I);
@@ -795,12 +802,17 @@ void build_jobs(scft_ctx *c) {
     F.nz = I.p.Nx[2];
     F.scal = I.scal;
     F.gacc = I.gacc;
-    F.ghist_last = I.graft ? I.ghist + (size_t)I.M * (I.Ng - 1) : nullptr;
+    F.ghist_last = (I.graft && !I.mixed) ? I.ghist + (size_t)I.M * (I.Ng - 1) : nullptr;
     F.grafts = I.grafts;
     F.nx = I.p.Nx[0];
     F.ny = I.p.Nx[1];
     F.zr = I.zr;
     F.zs = I.zs;
+    F.zg = I.zg;
+    F.Eg32 = I.Eg32;
+    F.gacc32 = I.gacc32;
+    F.ghist32_last = (I.graft && I.mixed) ? I.ghist32 + (size_t)I.M * (I.Ng - 1) : nullptr;
+    F.gK = I.gK;
     F.E32 = I.E32;
     F.acc32[0] = I.acc32[0];
     F.acc32[1] = I.acc32[1];
@@ -858,6 +870,23 @@ void build_jobs(scft_ctx *c) {
     }
     c->d_mi = dupload(c, mi);
     c->h_mi = mi;
+    std::vector<GraftMixInst> gmi(n);
+    for (int k = 0; k < n; k++) {
+      Instance &I = c->inst[k];
+      GraftMixInst &X = gmi[k];
+      memset(&X, 0, sizeof X);
+      if (!I.graft) continue;
+      X.geom = I.geom;
+      X.Ng = I.Ng;
+      X.work = I.gwork32;
+      X.hist = I.ghist32;
+      X.Eg = I.Eg32;
+      X.acc = I.gacc32;
+      X.part = I.gpart;
+      X.K = I.gK;
+      X.grafts = I.grafts;
+    }
+    c->d_gmi = dupload(c, gmi);
   }
 
   // field transform job lists
@@ -894,6 +923,10 @@ void build_jobs(scft_ctx *c) {
       add(smr, pj_sm, cj_sm, I.hhat);
     } else {
       std::vector<double2 *> zr = {I.zr}, zs = {I.zs};
+      if (I.graft) {  // rho_g forward, hhat w_G inverse
+        zr.push_back(I.zg);
+        zs.push_back(I.zg);
+      }
       add(zr, pj_upd, cj_upd, nullptr);  // forward transform of rho_A + i rho_B
       add(zs, pj_fld, cj_fld, nullptr);  // inverse transform of the smeared pair
     }
@@ -1005,7 +1038,8 @@ void build_jobs(scft_ctx *c) {
     c->ngmax = std::max(c->ngmax, I.Ng);
     for (int z = 0; z < g.nz; z++) gpj.push_back(PropJob{k, 0, z});
     for (int y = 0; y < g.ny; y++)
-      for (int x0 = 0; x0 < g.nx; x0 += g.tx) gcj.push_back(ColJob{I.gwork, I.pbond, I.geom, x0, y});
+      for (int x0 = 0; x0 < g.nx; x0 += g.tx)
+        gcj.push_back(I.mixed ? ColJob{I.gwork32, I.h32, I.geom, x0, y} : ColJob{I.gwork, I.pbond, I.geom, x0, y});
     gp_end.push_back((int)gpj.size());
     gc_end.push_back((int)gcj.size());
   }
@@ -1031,7 +1065,7 @@ void build_jobs(scft_ctx *c) {
 }
 
 // Largest |Im| and |Re| of w_A and w_B over the grid (mixed form input check).
-__global__ void k_real_check(const double2 *const *w, long long M, int neg_ab, int neg_bc, int neg_ac,
+__global__ void k_real_check(const double2 *const *w, long long M, int neg_ab, int neg_bc, int neg_ac, int graft,
                              double *out) {
   __shared__ double ri[32], rr[32];
   double mi = 0.0, mr = 0.0;
@@ -1045,6 +1079,12 @@ __global__ void k_real_check(const double2 *const *w, long long M, int neg_ab, i
     const double rb = -pl.y + (neg_ab ? abm.y - abp.x : -abp.y + abm.x) + (neg_bc ? -bcm.y - bcp.x : -bcp.y - bcm.x);
     mi = fmax(mi, fmax(fabs(ia), fabs(ib)));
     mr = fmax(mr, fmax(fabs(ra), fabs(rb)));
+    if (graft) {  // w_G (code/calc_poly_density.cpp:51-54)
+      const double ig = pl.x + (neg_ac ? -acm.x - acp.y : acp.x + acm.y) + (neg_bc ? -bcm.x - bcp.y : bcp.x + bcm.y);
+      const double rg = -pl.y + (neg_ac ? acm.y - acp.x : -acp.y + acm.x) + (neg_bc ? bcm.y - bcp.x : -bcp.y + bcm.x);
+      mi = fmax(mi, fabs(ig));
+      mr = fmax(mr, fabs(rg));
+    }
   }
   for (int o = 16; o > 0; o >>= 1) {
     mi = fmax(mi, __shfl_down_sync(0xffffffffu, mi, o));
@@ -1075,7 +1115,7 @@ void check_real_fields(scft_ctx *c, int k) {
   CK(cudaMalloc(&dw, sizeof(double2 *) * 7));
   CK(cudaMalloc(&dout, sizeof(double) * 2 * nb));
   CK(cudaMemcpyAsync(dw, I.w, sizeof(double2 *) * 7, cudaMemcpyHostToDevice, c->st));
-  k_real_check<<<nb, 256, 0, c->st>>>(dw, I.M, I.neg_ab, I.neg_bc, I.neg_ac, dout);
+  k_real_check<<<nb, 256, 0, c->st>>>(dw, I.M, I.neg_ab, I.neg_bc, I.neg_ac, I.graft, dout);
   std::vector<double> h(2 * nb);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), dout, sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost, c->st);
@@ -1089,7 +1129,8 @@ void check_real_fields(scft_ctx *c, int k) {
     mr = std::max(mr, h[2 * b + 1]);
   }
   if (mi > 1e-12 * std::max(1.0, mr))
-    throw ScftError(SCFT_ERR_COMPLEX, "mixed precision needs real w_A and w_B (mean-field phase convention)");
+    throw ScftError(SCFT_ERR_COMPLEX, "mixed precision needs real w_A, w_B (and w_G with grafts): the mean-field "
+                                      "phase convention");
 }
 
 // CK plus one kernel launch on the context's counter
@@ -1211,6 +1252,23 @@ void seq_mix_sweep(scft_ctx *c) {
     g0 = g1;
   }
   LK(launch_mix_q_finalize(c->d_fi, n, st));
+  // grafted chains (code/calc_poly_density.cpp:131-133,155-159)
+  if (c->ngmax > 0) {
+    for (auto &I : c->inst)
+      if (I.graft) CK(cudaMemsetAsync(I.gacc32, 0, sizeof(float) * I.M, st));
+    for (int sweep = 0; sweep < 2; sweep++) {
+      LK(launch_mix_graft_plane(c->shp_mix, c->d_graft_pj, c->graft_pj_count[0], c->d_gmi, c->d_geoms, c->d_tw32,
+                                sweep, 0, st));
+      for (int s = 1; s < c->ngmax; s++) {
+        LK(launch_col_fft<float>(c->shp_col32, c->d_graft_cj, c->graft_cj_count[s], c->d_geoms, c->d_tw32, 3, 1,
+                                 st));
+        LK(launch_mix_graft_plane(c->shp_mix, c->d_graft_pj, c->graft_pj_count[s], c->d_gmi, c->d_geoms, c->d_tw32,
+                                  sweep, s, st));
+      }
+    }
+    LK(launch_mix_graft_finalize(c->d_fi, n, c->gblocks, c->d_gpart, st));
+    LK(launch_qga_finalize(c->d_fi, n, c->gblocks, c->d_gpart, st));
+  }
 }
 
 // Mixed form: inverse transform of the packed smeared pair, Boltzmann factors, sweep.
@@ -1562,7 +1620,7 @@ void ctx_get_density(scft_ctx *c, int k, double *ra, double *rb, double *rg) {
   if (I.mixed) {
     // zr is rebuilt from the accumulators by the next update, so this is safe
     CK(launch_mix_rho_pack(c->d_fi, (int)c->inst.size(), c->eblocks, 1, c->st));
-    CK(cudaMemsetAsync(I.rho[2], 0, sizeof(double2) * I.M, c->st));
+    if (!I.graft) CK(cudaMemsetAsync(I.rho[2], 0, sizeof(double2) * I.M, c->st));
   }
   double *outs[3] = {ra, rb, rg};
   for (int f = 0; f < 3; f++)
@@ -1583,6 +1641,7 @@ void ctx_get_smeared(scft_ctx *c, int k, double *a, double *b, double *g) {
       if (b) { b[2 * i] = h[i].y; b[2 * i + 1] = 0.0; }
       if (g) { g[2 * i] = 0.0; g[2 * i + 1] = 0.0; }
     }
+    if (g && I.graft) CK(cudaMemcpy(g, I.sm[2], sizeof(double2) * I.M, cudaMemcpyDeviceToHost));
     return;
   }
   double *outs[3] = {a, b, g};

@@ -43,6 +43,12 @@ struct Instance {
   // mixed precision
   int mixed = 0;
   double2 *zr = nullptr, *zs = nullptr;
+  // mixed form with grafts
+  double2 *zg = nullptr;
+  float *Eg32 = nullptr, *ghist32 = nullptr, *gacc32 = nullptr;
+  float2 *gwork32 = nullptr;
+  int *gK = nullptr;
+  double *gpart = nullptr;
   float2 *E32 = nullptr, *work32 = nullptr, *hist32 = nullptr;
   float *acc32[2] = {};
   double *part = nullptr;
@@ -96,6 +102,7 @@ struct scft_ctx {
   scft::ColJob *d_mix64_cj_tx[3] = {};  // z-pass jobs of the 64^3 kernels for 8, 16, 32 columns per CTA
   int col64_tx = 16;                      // columns per CTA of the 64^3 z pass
   scft::MixInst *d_mi = nullptr;
+  scft::GraftMixInst *d_gmi = nullptr;  // per instance (zero for instances without grafts)
   std::vector<scft::MixInst> h_mi;       // host copy of d_mi
   std::vector<scft::MixInst> mix64_tab;  // instances in job order (64^3 plane pass)
   // The mixed sweep of a batch runs as `groups` independent chains of

@@ -47,6 +47,22 @@ struct MixInst {
   int *K;          // [2][N] power-of-two exponents, then K[2N] = reference exponent of acc
 };
 
+// View of one grafted instance for the mixed-precision graft sweeps
+// (code/grafted_nanoparticle.cpp:15-117): q_g from the free end, all Ng steps
+// stored (real, FP32), then qdag_g from the grafting surface, paired with
+// the stored steps into the graft density.  The working array is complex FP32
+// with imaginary part zero (a real field through the complex transform).
+struct GraftMixInst {
+  int geom, Ng;
+  float2 *work;
+  float *hist;            // [Ng][M] q_g, scaled by 2^-K[0][n]
+  const float *Eg;        // e^{-smwg}
+  float *acc;             // sum_j q_g[Ng-1-j] qdag_g[j] (true scale)
+  double *part;           // [2][Ng][nz] FP64 plane sums of q_g, qdag_g
+  int *K;                 // [2][Ng] power-of-two exponents
+  const double2 *grafts;  // normalised graft map
+};
+
 struct PropJob {
   int inst;
   int p;
@@ -87,6 +103,13 @@ struct FieldInst {
   float *acc32[2];     // density sums, scaled by 2^-K[2N]
   int *K;              // [2][N] + 1
   double *part64;      // [2][N][nz] plane sums of the stored propagators
+  // mixed precision, grafted instances: zg = rho_g (real space), then its
+  // transform, then hhat w_G (k-space), then smwg (real space)
+  double2 *zg;
+  float *Eg32;           // e^{-smwg}
+  float *gacc32;         // graft density sum (true scale)
+  const float *ghist32_last;  // q_g[Ng-1], scaled by 2^-gK[Ng-1]
+  const int *gK;
   // mixed precision: the 1S update of field f is w <- alpha_f(k) w - beta_f(k) F_f(k)
   // (NULL for fields whose chi is zero)
   const double *alpha[7], *beta[7];

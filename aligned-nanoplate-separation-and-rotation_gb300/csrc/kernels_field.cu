@@ -433,6 +433,14 @@ __device__ __forceinline__ long long neg_k(const FieldInst &F, long long i) {
   return jx + (long long)nx * (jy + (long long)ny * jz);
 }
 
+// zg = hhat * w_G, the transform of the smeared graft field.
+__device__ __forceinline__ double2 smear_graft(const FieldInst &F, long long i, const double2 *w) {
+  double2 wa, wb, wg;
+  assemble_point(F, w, wa, wb, wg);
+  const double hh = F.hhat[i];
+  return make_double2(hh * wg.x, hh * wg.y);
+}
+
 // zs = hhat * (w_A + i w_B), the packed transform of the two smeared fields.
 __device__ __forceinline__ double2 smear_pack(const FieldInst &F, long long i, const double2 *w) {
   double2 wa, wb, wg;
@@ -446,6 +454,7 @@ __global__ void k_mix_smear(const FieldInst *__restrict__ fi) {
     double2 w[7];
     for (int f = 0; f < 7; f++) w[f] = F.w[f][i];
     F.zs[i] = smear_pack(F, i, w);
+    if (F.graft) F.zg[i] = smear_graft(F, i, w);
   }
 }
 
@@ -477,6 +486,7 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
     const double2 rb = make_double2(0.5 * (Z.y + Zm.y), 0.5 * (Zm.x - Z.x));
     const double rho0 = F.rho0, hh = F.hhat[i];
     const double2 enh = F.exp_nrH[i];
+    const double2 rg = F.graft ? F.zg[i] : make_double2(0.0, 0.0);
     double2 w[7];
     for (int f = 0; f < 7; f++) w[f] = F.alpha[f] ? F.w[f][i] : make_double2(0.0, 0.0);
     auto step = [&](int f, double2 Fv) {
@@ -486,7 +496,7 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
     // w+ : I rho0 (exp_nrH - evar) + I hhat (rhoda + rhodb)
     {
       const double evar = (i == 0) ? 1.0 : 0.0;
-      const double2 sr = cadd(ra, rb);
+      const double2 sr = cadd(cadd(ra, rb), rg);
       const double2 u = make_double2(enh.x - evar, enh.y);
       step(0, make_double2(-rho0 * u.y - hh * sr.y, rho0 * u.x + hh * sr.x));
     }
@@ -506,10 +516,8 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
         step(2, F2);
       }
     }
-    // BC and AC pairs see no graft density here (grafts run in the FP64 method)
-    const double2 zero = make_double2(0.0, 0.0);
+    // BC and AC pairs: graft density transform rg
     if (F.alpha[3]) {
-      const double2 rg = zero;
       if (!F.neg_bc) {
         const double2 F1 = make_double2(-hh * (rg.y + rb.y), hh * (rg.x + rb.x));
         double2 F2 = make_double2(hh * (rg.x - rb.x), hh * (rg.y - rb.y));
@@ -525,7 +533,6 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
       }
     }
     if (F.alpha[5]) {
-      const double2 rg = zero;
       if (!F.neg_ac) {
         const double2 F1 = make_double2(-hh * (rg.y + ra.y), hh * (rg.x + ra.x));
         double2 F2 = make_double2(hh * (rg.x - ra.x), hh * (rg.y - ra.y));
@@ -545,6 +552,7 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
     double2 wa, wb, wg;
     assemble_point(F, w, wa, wb, wg);
     F.zs[i] = make_double2(hh * (wa.x - wb.y), hh * (wa.y + wb.x));
+    if (F.graft) F.zg[i] = make_double2(hh * wg.x, hh * wg.y);
   }
 }
 
@@ -555,6 +563,12 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
 // without an FP64 exponential.
 __global__ void k_mix_boltzmann(const FieldInst *__restrict__ fi) {
   FOR_POINTS(F) {
+    if (F.graft) {
+      const double sg = F.zg[i].x;
+      const float gh = (float)sg, gl = (float)(sg - (double)gh);
+      F.Eg32[i] = expf(-gh) * (1.0f - gl);
+      F.sm[2][i] = make_double2(sg, F.zg[i].y);
+    }
     double2 s = F.zs[i];
     if (F.shellU) s.x += F.shellU[i];
     const float ah = (float)s.x, al = (float)(s.x - (double)ah);
@@ -591,6 +605,57 @@ __global__ void k_mix_rho_pack(const FieldInst *__restrict__ fi, int keep) {
     if (keep) {
       F.rho[0][i] = make_double2(ra, 0.0);
       F.rho[1][i] = make_double2(rb, 0.0);
+    }
+  }
+}
+
+// Mixed form, grafted instances (code/grafted_nanoparticle.cpp:100-117):
+//   rhog = ng_per_np n_exp e^{+smwg} sum_j q_g qdag_g   (FP64, into zg and rho[2])
+//   Qga integrand: Re(grafts) <= 0 ? 0 : grafts log(q_g[Ng-1]) with the stored
+//   q_g[Ng-1] times 2^K.  part as k_graft_finalize.
+__global__ void k_mix_graft_finalize(const FieldInst *__restrict__ fi, double2 *__restrict__ part) {
+  __shared__ double2 red[32];
+  __shared__ double redc[32];
+  const FieldInst &F = fi[blockIdx.y];
+  if (!F.graft) return;
+  const double s = F.ng_per_np * F.n_exp_nr;
+  const double lk = (double)F.gK[F.Ng - 1] * 0.693147180559945309417232121458176568;
+  double2 acc = make_double2(0.0, 0.0);
+  double cnt = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < F.M;
+       i += (long long)gridDim.x * blockDim.x) {
+    const double rg = (double)F.gacc32[i] * (s * exp(F.zg[i].x));
+    F.zg[i] = make_double2(rg, 0.0);
+    F.rho[2][i] = make_double2(rg, 0.0);
+    const double2 gr = F.grafts[i];
+    const double ql = (double)F.ghist32_last[i];
+    if (gr.x > 0.0) {
+      const double2 lg = make_double2(log(fabs(ql)) + lk, ql < 0.0 ? 3.14159265358979323846 : 0.0);
+      acc = cadd(acc, cmul(gr, lg));
+    }
+    if (ql <= 0.0) cnt += 1.0;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+    acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+    cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) { red[w] = acc; redc[w] = cnt; }
+  __syncthreads();
+  if (w == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    acc = l < nw ? red[l] : make_double2(0.0, 0.0);
+    cnt = l < nw ? redc[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) {
+      acc.x += __shfl_down_sync(0xffffffffu, acc.x, o);
+      acc.y += __shfl_down_sync(0xffffffffu, acc.y, o);
+      cnt += __shfl_down_sync(0xffffffffu, cnt, o);
+    }
+    if (l == 0) {
+      const long long b = (long long)blockIdx.y * gridDim.x + blockIdx.x;
+      part[2 * b] = acc;
+      part[2 * b + 1] = make_double2(cnt, 0.0);
     }
   }
 }
@@ -649,6 +714,10 @@ __global__ void k_mix_h_partials(const FieldInst *__restrict__ fi, double2 *__re
 
 cudaError_t launch_mix_smear(const FieldInst *fi, int ninst, int blocks, cudaStream_t st) {
   k_mix_smear<<<dim3(blocks, ninst), 256, 0, st>>>(fi);
+  return cudaGetLastError();
+}
+cudaError_t launch_mix_graft_finalize(const FieldInst *fi, int ninst, int blocks, double2 *part, cudaStream_t st) {
+  k_mix_graft_finalize<<<dim3(blocks, ninst), 256, 0, st>>>(fi, part);
   return cudaGetLastError();
 }
 cudaError_t launch_mix_update(const FieldInst *fi, int ninst, int blocks, cudaStream_t st) {

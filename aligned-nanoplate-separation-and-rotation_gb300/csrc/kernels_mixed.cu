@@ -195,6 +195,134 @@ __global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restric
   for (int e = threadIdx.x; e < E; e += blockDim.x) work[e] = plane[e];
 }
 
+// Graft sweeps of the mixed form (code/grafted_nanoparticle.cpp:15-117), one
+// real propagator through the complex FP32 transform (imaginary part zero):
+// sweep 0 advances q_g from the free end, q_g[0] = e^{-smwg}, and stores
+// every step; sweep 1 advances qdag_g from qdag_g[0] = grafts e^{-smwg} /
+// q_g[Ng-1] and accumulates qdag_g[n] q_g[Ng-1-n].  Mean in FP64 and
+// power-of-two rescaling exactly as in the diblock sweep; with qdag_g[0]
+// scaled by 2^-K[0][Ng-1] the products need no reference exponent.
+template <int MAXV>
+__global__ void __launch_bounds__(512) k_mix_graft_plane(const PropJob *__restrict__ jobs,
+                                                        const GraftMixInst *__restrict__ insts,
+                                                        const DevGeom *__restrict__ geoms,
+                                                        const float2 *__restrict__ twbuf, int sweep, int n) {
+  typedef float2 C;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ double s_red[32];
+  __shared__ double s_mu;
+  __shared__ int s_exp;
+  const PropJob jb = jobs[blockIdx.x];
+  const GraftMixInst &P = insts[jb.inst];
+  const int Ng = P.Ng;
+  if (n >= Ng) return;
+  const DevGeom g = geoms[P.geom];
+  const int E = g.nx * g.ny;
+  const int nz = g.nz;
+  C *plane = reinterpret_cast<C *>(smem_raw);
+  C *twx = plane + E;
+  C *twy = twx + g.nx;
+  const long long zoff = (long long)jb.z * E;
+  const long long M = g.M;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  double *part = P.part + (long long)sweep * Ng * nz;
+  int *K = P.K + sweep * Ng;
+  if (warp == 0) {
+    double a = 0.0;
+    if (n > 0)
+      for (int z = lane; z < nz; z += 32) a += part[(long long)(n - 1) * nz + z];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) {
+      const double ma = a / (double)M;
+      int ea = 0;
+      if (n > 0 && isfinite(ma) && ma > 0.0) frexp(ma, &ea);
+      s_exp = ea;
+      s_mu = ma;
+    }
+  }
+  load_tw<float>(twx, twbuf, g.ax[0]);
+  load_tw<float>(twy, twbuf, g.ax[1]);
+  const float *Eg = P.Eg + zoff;
+  C *work = P.work + zoff;
+  if (n == 0) {
+    if (sweep == 0) {
+      for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = make_float2(Eg[e], 0.f);
+    } else {
+      const float *last = P.hist + (long long)(Ng - 1) * M + zoff;
+      const double2 *gr = P.grafts + zoff;
+      for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = make_float2((float)gr[e].x * Eg[e] / last[e], 0.f);
+    }
+    __syncthreads();
+  } else {
+    for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = work[e];
+    __syncthreads();
+    fft_plane<float, +1, MAXV>(plane, g, twx, twy);
+  }
+  const int ex = s_exp;
+  const int Kn = (n > 0) ? K[n - 1] + ex : (sweep == 0 ? 0 : -P.K[Ng - 1]);
+  if (n > 0) {
+    const float sc = ldexpf(1.0f, -ex);
+    const double m = s_mu;
+    const float m_hi = (float)m, m_lo = (float)(m - (double)m_hi);
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      const float eg = Eg[e];
+      plane[e] = make_float2(fmaf(plane[e].x, eg, fmaf(m_hi, eg, m_lo * eg)) * sc, 0.f);
+    }
+  }
+  if (jb.z == 0 && threadIdx.x == 0) K[n] = Kn;
+  float af = 0.f;
+  if (sweep == 0) {
+    float *h = P.hist + (long long)n * M + zoff;
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      const float v = plane[e].x;
+      af += v;
+      h[e] = v;
+    }
+  } else {
+    const float *o = P.hist + (long long)(Ng - 1 - n) * M + zoff;
+    const float f = ldexpf(1.0f, Kn + P.K[Ng - 1 - n]);
+    float *acc = P.acc + zoff;
+    for (int e = threadIdx.x; e < E; e += blockDim.x) {
+      const float v = plane[e].x;
+      af += v;
+      acc[e] += (v * o[e]) * f;
+    }
+  }
+  double a = (double)af;
+  for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+  if (lane == 0) s_red[warp] = a;
+  __syncthreads();
+  if (warp == 0) {
+    const int nw = (blockDim.x + 31) >> 5;
+    a = lane < nw ? s_red[lane] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) part[(long long)n * nz + jb.z] = a;
+  }
+  if (n == Ng - 1) return;
+  __syncthreads();
+  fft_plane<float, -1, MAXV>(plane, g, twx, twy);
+  for (int e = threadIdx.x; e < E; e += blockDim.x) work[e] = plane[e];
+}
+
+template <int MAXV>
+static cudaError_t launch_mix_graft_t(const LaunchShape &ls, const PropJob *jobs, int njobs,
+                                      const GraftMixInst *insts, const DevGeom *geoms, const void *tw, int sweep,
+                                      int n, cudaStream_t st) {
+  auto kfn = k_mix_graft_plane<MAXV>;
+  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, ls.smem);
+  if (e != cudaSuccess) return e;
+  kfn<<<njobs, ls.threads, ls.smem, st>>>(jobs, insts, geoms, reinterpret_cast<const float2 *>(tw), sweep, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_mix_graft_plane(const LaunchShape &ls, const PropJob *jobs, int njobs, const GraftMixInst *insts,
+                                   const DevGeom *geoms, const void *tw, int sweep, int n, cudaStream_t st) {
+  if (njobs <= 0) return cudaSuccess;
+  if (ls.maxv <= 8) return launch_mix_graft_t<8>(ls, jobs, njobs, insts, geoms, tw, sweep, n, st);
+  if (ls.maxv <= 16) return launch_mix_graft_t<16>(ls, jobs, njobs, insts, geoms, tw, sweep, n, st);
+  return launch_mix_graft_t<32>(ls, jobs, njobs, insts, geoms, tw, sweep, n, st);
+}
+
 template <int MAXV>
 static cudaError_t launch_mix_t(const LaunchShape &ls, const PropJob *jobs, int njobs, const MixInst *insts,
                                 const DevGeom *geoms, const void *tw, int n, cudaStream_t st) {

@@ -34,6 +34,9 @@ cudaError_t launch_mix_plane64(const MixInst *insts, int ninst, const void *tw64
 // tx: x columns per CTA (8, 16 or 32); jobs must be built for that width
 cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw64, int nx, int ny, int tx,
                              cudaStream_t st);
+cudaError_t launch_mix_graft_plane(const LaunchShape &ls, const PropJob *jobs, int njobs, const GraftMixInst *insts,
+                                   const DevGeom *geoms, const void *tw, int sweep, int n, cudaStream_t st);
+cudaError_t launch_mix_graft_finalize(const FieldInst *fi, int ninst, int blocks, double2 *part, cudaStream_t st);
 cudaError_t launch_mix_smear(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
 cudaError_t launch_mix_update(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
 cudaError_t launch_mix_boltzmann(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);

@@ -174,3 +174,40 @@ def test_sweep_schedule_does_not_change_results(scft, grids):
         assert np.array_equal(H, res[0][0])
         for a, b in zip(d, res[0][1]):
             assert np.array_equal(a, b)
+
+
+def grafted_params(scft, prec, theta=20.0):
+    """Config 4's chemistry at a small size: two rotated plates grafted with
+    chains of the A-like species C (chi_AC = 0, chi_BC = chi_AB)."""
+    from scft.workloads import plate_params, rg
+
+    N = 32
+    p = plate_params(theta, N=N, fA=0.4, chiN=30.0, grid=(32, 32, 32), box_rg=(4.0, 4.0, 4.0), precision=prec,
+                     centers=((0.5, 0.5, 0.375), (0.5, 0.5, 0.625)), thickness_rg=0.3, radius_rg=0.8, xi_rg=0.2,
+                     sigma=0.5 / rg(N) ** 2, Ng=8, lam_pl=0.002, lam_mi=0.001)
+    p.chi_bc = p.chi_ab
+    return p
+
+
+def test_mixed_grafted_plates_match_fp64(scft):
+    from scft.workloads import seeded_fields
+
+    f = seeded_fields(grafted_params(scft, scft.PREC_FP64), 21)
+    out = {}
+    for prec in (scft.PREC_FP64, scft.PREC_MIXED):
+        with scft.Context(grafted_params(scft, prec)) as ctx:
+            assert ctx.info(0)["phiG"] > 0
+            ctx.set_fields(0, f)
+            ctx.calc_poly_density()
+            H = [ctx.calc_H()[0]]
+            for _ in range(4):
+                ctx.update_1s(1)
+                H.append(ctx.calc_H()[0])
+            out[prec] = (np.array(H), ctx.density(0), ctx.get_fields(0))
+    (H64, d64, f64), (H32, d32, f32) = out[scft.PREC_FP64], out[scft.PREC_MIXED]
+    assert np.abs(H32[:, 0] - H64[:, 0]).max() <= H_TOL * np.abs(H64[:, 0]).max()
+    assert np.abs(H32[:, 4] - H64[:, 4]).max() <= Q_TOL * np.abs(H64[:, 4]).max()  # Re Qga
+    for a, b in zip(d32, d64):
+        assert rel(a, b) < RHO_TOL
+    for k in ("wpl", "wbcp", "wbcm"):
+        assert rel(f32[k], f64[k]) < RHO_TOL, k
