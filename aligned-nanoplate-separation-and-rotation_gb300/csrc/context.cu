@@ -65,6 +65,11 @@ static LaunchShape choose_shape(int E, size_t elem, size_t extra) {
   s.threads = t;
   s.maxv = maxv;
   s.smem = (int)(E * elem + extra);
+  s.gm = 0;
+  if (s.smem > 227 * 1024) {  // plane worked on in place in global memory
+    s.gm = 1;
+    s.smem = (int)extra;
+  }
   return s;
 }
 
@@ -352,6 +357,8 @@ void validate(const scft_params &p) {
     if (!(p.shell_width > 0)) bad("shell_width must be positive when shell_lambda != 0");
   }
   if (p.sigma > 0 && p.Ng < 1) bad("grafted chains need Ng >= 1");
+  // the z pass holds 16 columns of nz complex FP64 values in shared memory
+  if (p.Nx[2] > 768) throw ScftError(SCFT_ERR_UNSUPPORTED, "Nx[2] above 768 is not supported by the z pass");
 }
 
 // alpha, beta of w <- alpha w - beta F for each field and sign branch of
@@ -934,8 +941,7 @@ void build_jobs(scft_ctx *c) {
   c->shp_plane = choose_shape(emax_plane, sizeof(double2), (nxy_max + 32) * sizeof(double2));
   c->shp_col = choose_shape(emax_col, sizeof(double2), (nz_max + 32) * sizeof(double2));
   c->shp_prop = c->shp_plane;
-  if (c->shp_plane.smem > 227 * 1024)
-    throw ScftError(SCFT_ERR_UNSUPPORTED, "xy plane too large for the FP64 plane pass (nx*ny*16 B > 227 KB)");
+  if (c->shp_col.gm) throw ScftError(SCFT_ERR_UNSUPPORTED, "z columns too long for the z pass (16 nz tx B > 227 KB)");
   c->d_pj_upd = dupload(c, pj_upd); c->n_pj_upd = (int)pj_upd.size();
   c->d_pj_fld = dupload(c, pj_fld); c->n_pj_fld = (int)pj_fld.size();
   c->d_pj_sm = dupload(c, pj_sm); c->n_pj_sm = (int)pj_sm.size();
@@ -1019,6 +1025,9 @@ void build_jobs(scft_ctx *c) {
       for (int oi = 0; oi < n; oi++) c->mix64_tab.push_back(c->h_mi[order[oi]]);
     }
     c->shp_col32 = choose_shape(emax_col, sizeof(float2), (nz_max + 32) * sizeof(float2));
+    if (c->shp_mix.gm)
+      throw ScftError(SCFT_ERR_UNSUPPORTED, "xy plane too large for the mixed plane pass (nx*ny*8 B > 227 KB)");
+    if (c->shp_col32.gm) throw ScftError(SCFT_ERR_UNSUPPORTED, "z columns too long for the mixed z pass");
   }
   c->d_prop_pj = dupload(c, ppj);
   c->d_prop_cj = dupload(c, pcj);

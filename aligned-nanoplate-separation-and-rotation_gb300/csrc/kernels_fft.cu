@@ -15,7 +15,8 @@
 
 namespace scft {
 
-template <typename T, int SIGN, int MAXV>
+// GM: the plane is transformed in place in global memory (see LaunchShape).
+template <typename T, int SIGN, int MAXV, bool GM>
 __global__ void __launch_bounds__(512) k_plane_fft(const PlaneJob *__restrict__ jobs, const DevGeom *__restrict__ geoms,
                             const cx<T> *__restrict__ twbuf, int scale_by_M) {
   typedef cx<T> C;
@@ -23,19 +24,20 @@ __global__ void __launch_bounds__(512) k_plane_fft(const PlaneJob *__restrict__ 
   const PlaneJob jb = jobs[blockIdx.x];
   const DevGeom g = geoms[jb.geom];
   const int E = g.nx * g.ny;
-  C *plane = reinterpret_cast<C *>(smem_raw);
-  C *twx = plane + E;
+  C *a = reinterpret_cast<C *>(jb.ptr) + (long long)jb.z * E;
+  C *plane = GM ? a : reinterpret_cast<C *>(smem_raw);
+  C *twx = GM ? reinterpret_cast<C *>(smem_raw) : plane + E;
   C *twy = twx + g.nx;
   load_tw<T>(twx, twbuf, g.ax[0]);
   load_tw<T>(twy, twbuf, g.ax[1]);
-  C *a = reinterpret_cast<C *>(jb.ptr) + (long long)jb.z * E;
-  for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = a[e];
+  if (!GM)
+    for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = a[e];
   __syncthreads();
   fft_plane<T, SIGN, MAXV>(plane, g, twx, twy);
   if (scale_by_M) {
     const T s = (T)(1.0 / (double)g.M);
     for (int e = threadIdx.x; e < E; e += blockDim.x) a[e] = cscale(plane[e], s);
-  } else {
+  } else if (!GM) {
     for (int e = threadIdx.x; e < E; e += blockDim.x) a[e] = plane[e];
   }
 }
@@ -111,7 +113,7 @@ __global__ void __launch_bounds__(512) k_col_fft(const ColJob *__restrict__ jobs
 template <typename T, int SIGN, int MAXV>
 static cudaError_t launch_plane_t(const LaunchShape &ls, const PlaneJob *jobs, int njobs, const DevGeom *geoms,
                                   const void *tw, int scale, cudaStream_t st) {
-  auto kfn = k_plane_fft<T, SIGN, MAXV>;
+  auto kfn = ls.gm ? k_plane_fft<T, SIGN, MAXV, true> : k_plane_fft<T, SIGN, MAXV, false>;
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, ls.smem);
   if (e != cudaSuccess) return e;
   kfn<<<njobs, ls.threads, ls.smem, st>>>(jobs, geoms, reinterpret_cast<const cx<T> *>(tw), scale);

@@ -44,7 +44,9 @@ __device__ __forceinline__ double2 block_sum_d2(double2 v, double2 *red) {
   return v;
 }
 
-template <int MAXV>
+// GM: the plane is worked on in place in the working array in global memory
+// (planes too large for shared memory, see LaunchShape).
+template <int MAXV, bool GM>
 __global__ void __launch_bounds__(512) k_prop_plane_f64(const PropJob *__restrict__ jobs, const PropInst *__restrict__ insts,
                                  const DevGeom *__restrict__ geoms, const double2 *__restrict__ twbuf, int n) {
   typedef double2 C;
@@ -53,24 +55,25 @@ __global__ void __launch_bounds__(512) k_prop_plane_f64(const PropJob *__restric
   const PropInst &P = insts[jb.inst];
   const DevGeom g = geoms[P.geom];
   const int E = g.nx * g.ny;
-  C *plane = reinterpret_cast<C *>(smem_raw);
-  C *twx = plane + E;
-  C *twy = twx + g.nx;
-  C *red = twy + g.ny;
   const int N = P.N, Na = P.Na, p = jb.p;
   if (n >= N) return;
   const long long zoff = (long long)jb.z * E;
   const long long M = g.M;
+  C *work = reinterpret_cast<C *>(P.work[p]) + zoff;
+  C *plane = GM ? work : reinterpret_cast<C *>(smem_raw);
+  C *twx = GM ? reinterpret_cast<C *>(smem_raw) : plane + E;
+  C *twy = twx + g.nx;
+  C *red = twy + g.ny;
   // field switch: code/diblock_discrete.cpp:20-28,38-41,62-65
   const bool useA = (p == 0) ? (Na > 0 && n < Na) : !(n <= N - Na - 1);
   const C *Ew = P.expw[useA ? 0 : 1] + zoff;
-  C *work = reinterpret_cast<C *>(P.work[p]) + zoff;
   load_tw<double>(twx, twbuf, g.ax[0]);
   load_tw<double>(twy, twbuf, g.ax[1]);
   if (n == 0) {
     for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = Ew[e];
   } else {
-    for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = work[e];
+    if (!GM)
+      for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = work[e];
     __syncthreads();
     fft_plane<double, +1, MAXV>(plane, g, twx, twy);
     for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = cmul(plane[e], Ew[e]);
@@ -126,7 +129,8 @@ __global__ void __launch_bounds__(512) k_prop_plane_f64(const PropJob *__restric
   }
   __syncthreads();
   fft_plane<double, -1, MAXV>(plane, g, twx, twy);
-  for (int e = threadIdx.x; e < E; e += blockDim.x) work[e] = plane[e];
+  if (!GM)
+    for (int e = threadIdx.x; e < E; e += blockDim.x) work[e] = plane[e];
 }
 
 // Graft sweeps (code/grafted_nanoparticle.cpp:15-42 and :44-100), one CTA per
@@ -135,7 +139,7 @@ __global__ void __launch_bounds__(512) k_prop_plane_f64(const PropJob *__restric
 //            every step kept (the density needs all of them);
 //   sweep 1: qdag_g[0] = grafts * e^{-w_G} / q_g[Ng-1]; same recurrence, and
 //            the density term q_g[Ng-1-n] * qdag_g[n] is added at step n.
-template <int MAXV>
+template <int MAXV, bool GM>
 __global__ void __launch_bounds__(512) k_graft_plane_f64(const PropJob *__restrict__ jobs,
                                                         const PropInst *__restrict__ insts,
                                                         const DevGeom *__restrict__ geoms,
@@ -148,13 +152,13 @@ __global__ void __launch_bounds__(512) k_graft_plane_f64(const PropJob *__restri
   const int Ng = P.Ng;
   if (n >= Ng) return;
   const int E = g.nx * g.ny;
-  C *plane = reinterpret_cast<C *>(smem_raw);
-  C *twx = plane + E;
-  C *twy = twx + g.nx;
   const long long zoff = (long long)jb.z * E;
   const long long M = g.M;
   const C *Ew = P.gexpw + zoff;
   C *work = reinterpret_cast<C *>(P.gwork) + zoff;
+  C *plane = GM ? work : reinterpret_cast<C *>(smem_raw);
+  C *twx = GM ? reinterpret_cast<C *>(smem_raw) : plane + E;
+  C *twy = twx + g.nx;
   const C *hist = reinterpret_cast<const C *>(P.ghist);
   load_tw<double>(twx, twbuf, g.ax[0]);
   load_tw<double>(twy, twbuf, g.ax[1]);
@@ -180,7 +184,8 @@ __global__ void __launch_bounds__(512) k_graft_plane_f64(const PropJob *__restri
       }
     }
   } else {
-    for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = work[e];
+    if (!GM)
+      for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = work[e];
     __syncthreads();
     fft_plane<double, +1, MAXV>(plane, g, twx, twy);
     for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = cmul(plane[e], Ew[e]);
@@ -196,14 +201,15 @@ __global__ void __launch_bounds__(512) k_graft_plane_f64(const PropJob *__restri
   if (n == Ng - 1) return;
   __syncthreads();
   fft_plane<double, -1, MAXV>(plane, g, twx, twy);
-  for (int e = threadIdx.x; e < E; e += blockDim.x) work[e] = plane[e];
+  if (!GM)
+    for (int e = threadIdx.x; e < E; e += blockDim.x) work[e] = plane[e];
 }
 
 template <int MAXV>
 static cudaError_t launch_graft_plane_t(const LaunchShape &ls, const PropJob *jobs, int njobs,
                                         const PropInst *insts, const DevGeom *geoms, const void *tw, int sweep,
                                         int n, cudaStream_t st) {
-  auto kfn = k_graft_plane_f64<MAXV>;
+  auto kfn = ls.gm ? k_graft_plane_f64<MAXV, true> : k_graft_plane_f64<MAXV, false>;
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, ls.smem);
   if (e != cudaSuccess) return e;
   kfn<<<njobs, ls.threads, ls.smem, st>>>(jobs, insts, geoms, reinterpret_cast<const double2 *>(tw), sweep, n);
@@ -222,7 +228,7 @@ template <int MAXV>
 static cudaError_t launch_prop_plane_t(const LaunchShape &ls, const PropJob *jobs, int njobs,
                                        const PropInst *insts, const DevGeom *geoms, const void *tw, int n,
                                        cudaStream_t st) {
-  auto kfn = k_prop_plane_f64<MAXV>;
+  auto kfn = ls.gm ? k_prop_plane_f64<MAXV, true> : k_prop_plane_f64<MAXV, false>;
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, ls.smem);
   if (e != cudaSuccess) return e;
   kfn<<<njobs, ls.threads, ls.smem, st>>>(jobs, insts, geoms, reinterpret_cast<const double2 *>(tw), n);

@@ -7,10 +7,15 @@ namespace scft {
 
 // Block size, dynamic shared memory and per-thread value bound (MAXV) of a
 // launch; MAXV * threads must cover the largest plane or tile of the batch.
+// gm: the plane does not fit in shared memory (FP64 planes above ~227 KB, e.g.
+// 128 x 128): the plane kernels then transform it in place in its own array
+// in global memory (L2-resident while the CTA works on it) and shared memory
+// holds only the twiddles; smem is then that smaller size.
 struct LaunchShape {
   int threads;
   int smem;
   int maxv;
+  int gm;
 };
 
 template <typename T>

@@ -68,6 +68,7 @@ LaunchShape shape_for(int E, size_t extra) {
   s.threads = t;
   s.maxv = maxv;
   s.smem = (int)(E * sizeof(double2) + extra);
+  s.gm = 0;  // larger planes are rejected below
   return s;
 }
 

@@ -43,11 +43,13 @@ def plate_params(theta_deg: float, N: int = 100, fA: float = 0.5, chiN: float = 
                        shell_lambda=(-1.0 / N if shell else 0.0), shell_width=(0.1 * R if shell else 0.0))
 
 
-def seeded_fields(p, seed: int) -> dict:
+def seeded_fields(p, seed: int, periods: int = 1) -> dict:
+    """w_AB^- = 0.5 chi cos(2 pi periods x / L_x) + N(0, 0.01^2) per segment."""
     nx, ny, nz = p.Nx[0], p.Nx[1], p.Nx[2]
     rng = np.random.default_rng(seed)
     x = np.arange(nx) * p.L[0] / nx
-    wabm = 0.5 * p.chi_ab * np.cos(2 * np.pi * x / p.L[0])[None, None, :] + 0.01 * rng.standard_normal((nz, ny, nx))
+    wabm = 0.5 * p.chi_ab * np.cos(2 * np.pi * periods * x / p.L[0])[None, None, :] + \
+        0.01 * rng.standard_normal((nz, ny, nx))
     return {"wabm": wabm.astype(np.complex128)}
 
 
@@ -70,10 +72,53 @@ def sweep15_mixed_sizes(precision=PREC_MIXED):
     return out
 
 
+SEPARATIONS = tuple(round(0.14 + 0.04 * k, 2) for k in range(9))
+
+
+def separation9(precision=PREC_MIXED):
+    """Config 3: two parallel plates (theta = 0) at centre separations
+    d = 0.14 .. 0.46 of the long box side, N = 100, chiN = 20.  The long axis
+    is y, as in the reference's particle-separation sweep (separation along
+    L_y): grid 64 x 128 x 64, box 6.4 x 12.8 x 6.4 Rg."""
+    return [plate_params(0.0, grid=(64, 128, 64), box_rg=(6.4, 12.8, 6.4), precision=precision,
+                         centers=((0.5, 0.5 - d / 2, 0.5), (0.5, 0.5 + d / 2, 0.5))) for d in SEPARATIONS]
+
+
+def large_grafted8(precision=PREC_MIXED):
+    """Config 4: 128 x 128 x 256 grid, box 12.8 x 12.8 x 25.6 Rg, N = 200,
+    f_A = 0.4, chiN = 30, two plates rotated by 20 degrees at d = 0.25 L_z,
+    each grafted with chains of Ng = 20 at sigma = 0.5 / Rg^2 (graft species
+    A-like: chi_AC = 0, chi_BC = chi_AB); 8 instances that differ in the seed
+    of their initial fields (seeded_fields with 1000 + k and 3 lamellar
+    periods across L_x in the bench).  Step sizes 0.0005 / 0.0002: both the
+    FP64 method and the mixed form diverge at 0.0015 / 0.0004 here (graft
+    propagator q_g <= 0 after ~10 iterations)."""
+    N = 200
+    out = []
+    for _ in range(8):
+        p = plate_params(20.0, N=N, fA=0.4, chiN=30.0, grid=(128, 128, 256), box_rg=(12.8, 12.8, 25.6),
+                         precision=precision, lam_pl=0.0005, lam_mi=0.0002,
+                         centers=((0.5, 0.5, 0.375), (0.5, 0.5, 0.625)), sigma=0.5 / rg(N) ** 2, Ng=20)
+        p.chi_bc = p.chi_ab
+        out.append(p)
+    return out
+
+
 WORKLOADS = {
     "plate64_N100": lambda prec: [plate_params(10.0, precision=prec)],
     "plate64_N100_shell": lambda prec: [plate_params(10.0, precision=prec, shell=True)],
     "sweep15_64_N100_shell": lambda prec: [plate_params(t, precision=prec, shell=True) for t in SWEEP_ANGLES],
     "sweep15_64_N100": lambda prec: sweep15(precision=prec),
     "sweep15_mixed_sizes": lambda prec: sweep15_mixed_sizes(precision=prec),
+    "sep9_64x128x64_N100": lambda prec: separation9(precision=prec),
+    "graft8_128x128x256_N200": lambda prec: large_grafted8(precision=prec),
+}
+
+# per-workload defaults of the bench: relaxation iterations, how many
+# instances the FP64 comparison runs (the FP64 method needs ~16 GB per
+# instance of the large grafted workload) and the lamellar periods of the
+# seeded fields (one period across a 12.8 Rg box at chiN = 30, N = 200 makes q
+# span ~e^15 across the box, far from any saddle point)
+BENCH_DEFAULTS = {
+    "graft8_128x128x256_N200": {"relax": 30, "plain_max": 2, "periods": 3},
 }

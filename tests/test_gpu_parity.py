@@ -49,7 +49,8 @@ def load_golden(name):
     return c, z
 
 
-@pytest.mark.parametrize("shape", [(8, 8, 8), (6, 10, 12), (16, 24, 48), (4, 9, 96), (64, 64, 64), (3, 32, 8)])
+@pytest.mark.parametrize("shape", [(8, 8, 8), (6, 10, 12), (16, 24, 48), (4, 9, 96), (64, 64, 64), (3, 32, 8),
+                                   (4, 128, 128)])
 def test_fft3d_matches_numpy(scft, shape):
     nz, ny, nx = shape
     p = scft.make_params(Nx=(nx, ny, nz), L=(1.0, 1.0, 1.0))
@@ -186,3 +187,24 @@ def test_config0_full_size_trace(scft):
     assert np.abs(rows[:, 0] - tr[:, 1]).max() <= H_TOL * np.abs(tr[:, 1]).max()
     for k, a in (("rhoda", ra), ("rhodb", rb), ("wpl", f["wpl"]), ("wabm", f["wabm"])):
         assert rel(digest(a), z["digest_" + k]) < RHO_TOL, k
+
+
+def test_large_plane_in_global_memory_matches_restatement(scft):
+    """A 128 x 128 FP64 plane (256 KB) does not fit in shared memory: the plane
+    kernels then work on it in place in global memory.  Propagators and
+    densities against the restatement (code/diblock_discrete.cpp:4-95)."""
+    import scft_oracle as O
+
+    Nx, L = (128, 128, 4), (8.0, 8.0, 1.0)
+    s = O.System(Nda=4, Ndb=5, a_smear=0.2, rho0=5.0, chi_ab=0.5, chi_bc=0.0, chi_ac=0.0, kappa=50.0, Nx=Nx, L=L,
+                 lam_pl=0.005, lam_mi=0.005)
+    rng = np.random.default_rng(17)
+    WA = 0.3 * rng.standard_normal(s.g.shape) + 0j
+    WB = 0.3 * rng.standard_normal(s.g.shape) + 0j
+    Qr, q, qd = O.diblock_discrete(s, WA, WB)
+    ra_r, rb_r = O.integrate_diblock_discrete(s, q, qd, Qr, s.nD, WA, WB)
+    with scft.Context(scft.make_params(Nda=4, Ndb=5, Nx=Nx, L=L)) as ctx:
+        ra, rb, Q = ctx.diblock_density(0, WA, WB)
+    assert abs(Q - Qr) <= RHO_TOL * abs(Qr)
+    assert rel(ra, ra_r) < RHO_TOL
+    assert rel(rb, rb_r) < RHO_TOL
