@@ -341,6 +341,8 @@ void validate(const scft_params &p) {
     if (!make_axis_plan(p.Nx[d], ap)) throw ScftError(SCFT_ERR_UNSUPPORTED, "grid sizes must be 2^a 3^b 5^c");
   }
   if (p.update_scheme != SCFT_UPDATE_1S && p.update_scheme != SCFT_UPDATE_EULER) bad("unknown update_scheme");
+  if (p.do_cl && p.precision == SCFT_PREC_MIXED)
+    throw ScftError(SCFT_ERR_UNSUPPORTED, "complex-Langevin noise makes the fields complex: FP64 method only");
   if (p.update_scheme == SCFT_UPDATE_1S && !(p.kappa > 0))
     bad("kappa must be > 0 with the 1S update (code/1s_update.cpp:72-78 leaves B unset otherwise)");
   if (!(p.rho0 > 0)) bad("rho0 must be positive");
@@ -442,6 +444,18 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
   I.mixed = (p.precision == SCFT_PREC_MIXED);
   for (int f = 0; f < 7; f++) I.w[f] = dalloc<double2>(c, M);
   for (int f = 0; f < 3; f++) I.rho[f] = dalloc<double2>(c, M);
+  if (p.do_cl) {
+    // noise arrays of code/1s_update.cpp:54-319: w+, then (+, -) of each pair with chi != 0
+    I.eta[0] = dalloc<double2>(c, M);
+    const double chis[3] = {p.chi_ab, p.chi_bc, p.chi_ac};
+    for (int k = 0; k < 3; k++)
+      if (chis[k] != 0.0) {
+        I.eta[1 + 2 * k] = dalloc<double2>(c, M);
+        I.eta[2 + 2 * k] = dalloc<double2>(c, M);
+      }
+    CK(cudaMallocHost(&I.eta_host, sizeof(double2) * 7 * (size_t)M));
+    I.rng.reseed(p.cl_seed);
+  }
   if (!I.mixed) {
     for (int f = 0; f < 3; f++) {
       I.sm[f] = dalloc<double2>(c, M);
@@ -813,6 +827,26 @@ void build_jobs(scft_ctx *c) {
     F.grafts = I.grafts;
     F.nx = I.p.Nx[0];
     F.ny = I.p.Nx[1];
+    for (int f = 0; f < 7; f++) F.eta[f] = nullptr;
+    if (I.p.do_cl) {
+      // which noise array enters which field's update (code/1s_update.cpp:81-319,
+      // code/Euler_update.cpp:65-172): with the 1S scheme and a negative chi the
+      // + field of AB gets none and both BC (AC) fields get the + array
+      const bool eul = I.p.update_scheme == SCFT_UPDATE_EULER;
+      F.eta[0] = I.eta[0];
+      const int negs[3] = {I.neg_ab, I.neg_bc, I.neg_ac};
+      for (int k = 0; k < 3; k++) {
+        double2 *ep = I.eta[1 + 2 * k], *em = I.eta[2 + 2 * k];
+        if (!ep) continue;
+        if (eul || !negs[k]) {
+          F.eta[1 + 2 * k] = ep;
+          F.eta[2 + 2 * k] = em;
+        } else {
+          F.eta[1 + 2 * k] = (k == 0) ? nullptr : ep;
+          F.eta[2 + 2 * k] = ep;
+        }
+      }
+    }
     F.zr = I.zr;
     F.zs = I.zs;
     F.zg = I.zg;
@@ -914,6 +948,8 @@ void build_jobs(scft_ctx *c) {
     if (I.cbc != 0.0) { fld.push_back(I.w[4]); fld.push_back(I.w[3]); }
     if (I.cac != 0.0) { fld.push_back(I.w[6]); fld.push_back(I.w[5]); }
     for (double2 *a : fld) upd.push_back(a);
+    for (int g = 0; g < 7; g++)
+      if (I.eta[g]) upd.push_back(I.eta[g]);  // complex-Langevin noise, forward with the densities
     std::vector<double2 *> smr = {I.sm[0], I.sm[1]};
     if (I.graft) smr.push_back(I.sm[2]);
     auto add = [&](std::vector<double2 *> &arrs, std::vector<PlaneJob> &pj, std::vector<ColJob> &cj,
@@ -1191,9 +1227,38 @@ void seq_poly_density(scft_ctx *c) {
 }
 
 // update_1s for every instance (code/1s_update.cpp:7-352)
+// Complex-Langevin noise of one update (code/1s_update.cpp:356-368,
+// generate_1s_noise): per array, sqrt(2 lambda) / sqrt(dx) / sqrt(dy) / sqrt(dz)
+// times one Gaussian deviate of the reference's stream per grid point (stack
+// order), real; the arrays are drawn in the reference's order (w+, then + and
+// - of AB, BC, AC for the pairs with chi != 0) and forward-transformed with
+// the densities.  Step sizes: 1S draws w+ with lam_pl and every pair's + and
+// - arrays with lam_mi and lam_pl; Euler draws BC's with lam_pl and lam_mi.
+void cl_generate(scft_ctx *c) {
+  bool any = false;
+  for (auto &I : c->inst) any = any || I.p.do_cl;
+  if (!any) return;
+  CK(cudaStreamSynchronize(c->st));  // the staging buffers of the last step are free
+  for (auto &I : c->inst) {
+    if (!I.p.do_cl) continue;
+    const bool eul = I.p.update_scheme == SCFT_UPDATE_EULER;
+    const double li = I.p.lam_pl, lr = I.p.lam_mi;
+    const double lam[7] = {li, lr, li, eul ? li : lr, eul ? lr : li, lr, li};
+    for (int g = 0; g < 7; g++) {
+      if (!I.eta[g]) continue;
+      double scale = std::sqrt(2.0 * lam[g]);
+      for (int d = 0; d < 3; d++) scale /= std::sqrt(I.info.dx[d]);
+      double2 *h = I.eta_host + (size_t)g * I.M;
+      for (long long i = 0; i < I.M; i++) h[i] = make_double2(scale * I.rng.gauss(), 0.0);
+      CK(cudaMemcpyAsync(I.eta[g], h, sizeof(double2) * I.M, cudaMemcpyHostToDevice, c->st));
+    }
+  }
+}
+
 void seq_update_1s(scft_ctx *c) {
   const int n = (int)c->inst.size();
   cudaStream_t st = c->st;
+  cl_generate(c);
   LK(launch_plane_fft<double>(c->shp_plane, c->d_pj_upd, c->n_pj_upd, c->d_geoms, c->d_tw64, -1, 0, st));
   LK(launch_col_fft<double>(c->shp_col, c->d_cj_upd, c->n_cj_upd, c->d_geoms, c->d_tw64, 0, 1, st));
   LK(launch_update_1s(c->d_fi, n, c->eblocks, st));
@@ -1356,6 +1421,8 @@ void ctx_destroy(scft_ctx *c) {
   if (c->g_update) cudaGraphExecDestroy(c->g_update);
   for (void *p : c->allocs) cudaFree(p);
   for (cudaStream_t sst : c->side) cudaStreamDestroy(sst);
+  for (auto &I : c->inst)
+    if (I.eta_host) cudaFreeHost(I.eta_host);
   for (cudaEvent_t ev : c->ev_join) cudaEventDestroy(ev);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->st) cudaStreamDestroy(c->st);
@@ -1374,6 +1441,13 @@ void ctx_update(scft_ctx *c, int n_iter) {
   if (n_iter <= 0) return;
   if (c->dirty_density) ctx_poly_density(c);
   int k = 0;
+  bool cl = false;
+  for (auto &I : c->inst) cl = cl || I.p.do_cl;
+  if (cl) {  // the noise is drawn on the host every step: no captured graph
+    for (; k < n_iter; k++) seq_update_1s(c);
+    CK(cudaStreamSynchronize(c->st));
+    return;
+  }
   if (!c->g_update) {
     // first iteration runs eagerly (kernel attributes get set), then capture
     (c->mixed ? seq_mix_update(c) : seq_update_1s(c));

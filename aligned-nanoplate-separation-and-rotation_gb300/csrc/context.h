@@ -9,6 +9,7 @@
 #include "common.h"
 #include "inst.h"
 #include "launch.h"
+#include "refrng.h"
 
 namespace scft {
 
@@ -16,6 +17,11 @@ typedef std::complex<double> cd;
 
 struct Instance {
   scft_params p;
+  // complex Langevin: the reference's random stream and the noise arrays in
+  // the order the reference draws them (w+, then + and - of AB, BC, AC)
+  scft::RefRng rng;
+  double2 *eta[7] = {};        // device, real space then k-space
+  double2 *eta_host = nullptr;  // pinned staging, 7 x M
   scft_info info;
   int N, Na, Ng;
   double fD, Rg2, cab, cbc, cac;

@@ -110,6 +110,9 @@ struct FieldInst {
   float *gacc32;         // graft density sum (true scale)
   const float *ghist32_last;  // q_g[Ng-1], scaled by 2^-gK[Ng-1]
   const int *gK;
+  // complex Langevin: k-space noise added to the update numerator of field f
+  // (NULL: none); several fields may share one array, as in the reference
+  const double2 *eta[7];
   // mixed precision: the 1S update of field f is w <- alpha_f(k) w - beta_f(k) F_f(k)
   // (NULL for fields whose chi is zero)
   const double *alpha[7], *beta[7];

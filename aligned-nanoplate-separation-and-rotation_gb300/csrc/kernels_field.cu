@@ -195,6 +195,11 @@ __global__ void k_qga_finalize(const FieldInst *__restrict__ fi, int ninst, int 
   F.scal[kQg] = make_double2(cnt, 0.0);
 }
 
+// Complex-Langevin noise of field f at k-space point i (zero without).
+__device__ __forceinline__ double2 cl_noise(const FieldInst &F, int f, long long i) {
+  return F.eta[f] ? F.eta[f][i] : make_double2(0.0, 0.0);
+}
+
 // code/1s_update.cpp:58-329 at one k-space point (mean-field: no noise, no
 // film/channel, no field nanoparticles, no homopolymer).  ra, rb, rg are the
 // forward transforms (1/M scaled) of rhoda, rhodb, rhog_exp at this point and
@@ -219,7 +224,8 @@ __device__ __forceinline__ void update_1s_point(const FieldInst &F, long long i,
                      (F.phiG * Ng * gc) * rho0 * hh2;
     const double B = A - rho0 / F.kappa;
     const double2 wv = w[0];
-    const double2 num = make_double2(wv.x - li * (F1.x - B * wv.x), wv.y - li * (F1.y - B * wv.y));
+    const double2 e0 = cl_noise(F, 0, i);
+    const double2 num = make_double2(wv.x - li * (F1.x - B * wv.x) + e0.x, wv.y - li * (F1.y - B * wv.y) + e0.y);
     const double den = 1.0 + li * A;
     w[0] = make_double2(num.x / den, num.y / den);
   }
@@ -227,27 +233,28 @@ __device__ __forceinline__ void update_1s_point(const FieldInst &F, long long i,
   if (F.cab != 0.0) {
     const double c = F.cab;
     double2 wp = w[1], wm = w[2];
+    const double2 ep = cl_noise(F, 1, i), em = cl_noise(F, 2, i);
     if (!F.neg_ab) {
       double2 F1 = make_double2(-hh * (ra.y + rb.y), hh * (ra.x + rb.x));  // I*hhat*(ra+rb)
       if (F.np_chem == 1) F1 = make_double2(F1.x - rho0 * enh.x, F1.y - rho0 * enh.y);
       const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * (gaa + 2.0 * gab + gbb);
       const double B = A - 2.0 * rho0 / c;
       const double den = 1.0 + li * A;
-      wp = make_double2((wp.x - li * (F1.x - B * wp.x)) / den, (wp.y - li * (F1.y - B * wp.y)) / den);
+      wp = make_double2((wp.x - li * (F1.x - B * wp.x) + ep.x) / den, (wp.y - li * (F1.y - B * wp.y) + ep.y) / den);
       double2 F2 = make_double2(hh * (rb.x - ra.x), hh * (rb.y - ra.y));
       if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
       const double den2 = 1.0 + lr * 2.0 * rho0 / c;
-      wm = make_double2((wm.x - lr * F2.x) / den2, (wm.y - lr * F2.y) / den2);
+      wm = make_double2((wm.x - lr * F2.x + em.x) / den2, (wm.y - lr * F2.y + em.y) / den2);
     } else {
       const double2 F1 = make_double2(-hh * (ra.x + rb.x), -hh * (ra.y + rb.y));
       const double den1 = 1.0 + lr * 2.0 * rho0 / c;
-      wp = make_double2((wp.x - lr * F1.x) / den1, (wp.y - lr * F1.y) / den1);
+      wp = make_double2((wp.x - lr * F1.x + ep.x) / den1, (wp.y - lr * F1.y + ep.y) / den1);
       double2 F2 = make_double2(-hh * (ra.y - rb.y), hh * (ra.x - rb.x));  // I*hhat*(ra-rb)
       if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
       const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * (gaa - gbb);
       const double B = A - 2.0 * rho0 / c;
       const double den = 1.0 + li * A;
-      wm = make_double2((wm.x - li * (F2.x - B * wm.x)) / den, (wm.y - li * (F2.y - B * wm.y)) / den);
+      wm = make_double2((wm.x - li * (F2.x - B * wm.x) + em.x) / den, (wm.y - li * (F2.y - B * wm.y) + em.y) / den);
     }
     w[1] = wp;
     w[2] = wm;
@@ -259,27 +266,28 @@ __device__ __forceinline__ void update_1s_point(const FieldInst &F, long long i,
   if (F.cbc != 0.0) {
     const double c = F.cbc;
     double2 wp = w[3], wm = w[4];
+    const double2 ep = cl_noise(F, 3, i), em = cl_noise(F, 4, i);
     if (!F.neg_bc) {
       const double2 F1 = make_double2(-hh * (rg.y + rb.y), hh * (rg.x + rb.x));
       const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * (+gbb) + F.phiG * rho0 * Ng * hh2 * gc;
       const double B = A - 2.0 * rho0 / c;
       const double den = 1.0 + li * A;
-      wp = make_double2((wp.x - li * (F1.x - B * wp.x)) / den, (wp.y - li * (F1.y - B * wp.y)) / den);
+      wp = make_double2((wp.x - li * (F1.x - B * wp.x) + ep.x) / den, (wp.y - li * (F1.y - B * wp.y) + ep.y) / den);
       double2 F2 = make_double2(hh * (rg.x - rb.x), hh * (rg.y - rb.y));
       if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
       const double den2 = 1.0 + lr * 2.0 * rho0 / c;
-      wm = make_double2((wm.x - lr * F2.x) / den2, (wm.y - lr * F2.y) / den2);
+      wm = make_double2((wm.x - lr * F2.x + em.x) / den2, (wm.y - lr * F2.y + em.y) / den2);
     } else {
       const double2 F1 = make_double2(-hh * (rb.x + rg.x), -hh * (rb.y + rg.y));
       const double den1 = 1.0 + lr * 2.0 * rho0 / c;
-      wp = make_double2((wp.x - lr * F1.x) / den1, (wp.y - lr * F1.y) / den1);
+      wp = make_double2((wp.x - lr * F1.x + ep.x) / den1, (wp.y - lr * F1.y + ep.y) / den1);
       // -I*hhat*(rg - rb) = (hh*(rg-rb).y, -hh*(rg-rb).x)
       double2 F2 = make_double2(hh * (rg.y - rb.y), -hh * (rg.x - rb.x));
       if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
       const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * gbb - F.phiG * Ng * hh2 * rho0 * gc;
       const double B = A - 2.0 * rho0 / c;
       const double den = 1.0 + li * A;
-      wm = make_double2((wm.x - li * (F2.x - B * wm.x)) / den, (wm.y - li * (F2.y - B * wm.y)) / den);
+      wm = make_double2((wm.x - li * (F2.x - B * wm.x) + em.x) / den, (wm.y - li * (F2.y - B * wm.y) + em.y) / den);
     }
     w[3] = wp;
     w[4] = wm;
@@ -291,26 +299,27 @@ __device__ __forceinline__ void update_1s_point(const FieldInst &F, long long i,
   if (F.cac != 0.0) {
     const double c = F.cac;
     double2 wp = w[5], wm = w[6];
+    const double2 ep = cl_noise(F, 5, i), em = cl_noise(F, 6, i);
     if (!F.neg_ac) {
       const double2 F1 = make_double2(-hh * (rg.y + ra.y), hh * (rg.x + ra.x));
       const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * gaa + F.phiG * Ng * hh2 * rho0 * gc;
       const double B = A - 2.0 * rho0 / c;
       const double den = 1.0 + li * A;
-      wp = make_double2((wp.x - li * (F1.x - B * wp.x)) / den, (wp.y - li * (F1.y - B * wp.y)) / den);
+      wp = make_double2((wp.x - li * (F1.x - B * wp.x) + ep.x) / den, (wp.y - li * (F1.y - B * wp.y) + ep.y) / den);
       double2 F2 = make_double2(hh * (rg.x - ra.x), hh * (rg.y - ra.y));
       if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.y, F2.y + rho0 * enh.x);
       const double den2 = 1.0 + lr * 2.0 * rho0 / c;
-      wm = make_double2((wm.x - lr * F2.x) / den2, (wm.y - lr * F2.y) / den2);
+      wm = make_double2((wm.x - lr * F2.x + em.x) / den2, (wm.y - lr * F2.y + em.y) / den2);
     } else {
       const double2 F1 = make_double2(-hh * (ra.x + rg.x), -hh * (ra.y + rg.y));
       const double den1 = 1.0 + lr * 2.0 * rho0 / c;
-      wp = make_double2((wp.x - lr * F1.x) / den1, (wp.y - lr * F1.y) / den1);
+      wp = make_double2((wp.x - lr * F1.x + ep.x) / den1, (wp.y - lr * F1.y + ep.y) / den1);
       double2 F2 = make_double2(hh * (rg.y - ra.y), -hh * (rg.x - ra.x));
       if (F.np_chem == 1) F2 = make_double2(F2.x - rho0 * enh.x, F2.y - rho0 * enh.y);
       const double A = 2.0 * rho0 / c + F.phiD * rho0 * N * hh2 * gaa - F.phiG * Ng * hh2 * rho0 * gc;
       const double B = A - 2.0 * rho0 / c;
       const double den = 1.0 + li * A;
-      wm = make_double2((wm.x - li * (F2.x - B * wm.x)) / den, (wm.y - li * (F2.y - B * wm.y)) / den);
+      wm = make_double2((wm.x - li * (F2.x - B * wm.x) + em.x) / den, (wm.y - li * (F2.y - B * wm.y) + em.y) / den);
     }
     w[5] = wp;
     w[6] = wm;
@@ -325,7 +334,7 @@ __device__ __forceinline__ void update_1s_point(const FieldInst &F, long long i,
 // for the - fields, no Debye terms and no np_chem terms.  Arguments as
 // update_1s_point.
 __device__ __forceinline__ void euler_pair(const FieldInst &F, double c, int neg, double2 X, double2 Y, double hh,
-                                           double2 &wp, double2 &wm) {
+                                           double2 ep, double2 em, double2 &wp, double2 &wm) {
   const double rho0 = F.rho0, li = F.lam_pl, lr = F.lam_mi;
   const double2 s = cadd(X, Y), d = csub(X, Y);
   // + : 2 rho0 wp / c + hhat (X + Y) (neg ? -1 : I)
@@ -334,8 +343,8 @@ __device__ __forceinline__ void euler_pair(const FieldInst &F, double c, int neg
   // - : 2 rho0 wm / c + (neg ? I hhat (X - Y) : hhat (Y - X))
   const double2 Fm = neg ? make_double2(2.0 * rho0 * wm.x / c - hh * d.y, 2.0 * rho0 * wm.y / c + hh * d.x)
                          : make_double2(2.0 * rho0 * wm.x / c - hh * d.x, 2.0 * rho0 * wm.y / c - hh * d.y);
-  wp = make_double2(wp.x - li * Fp.x, wp.y - li * Fp.y);
-  wm = make_double2(wm.x - lr * Fm.x, wm.y - lr * Fm.y);
+  wp = make_double2(wp.x - li * Fp.x + ep.x, wp.y - li * Fp.y + ep.y);
+  wm = make_double2(wm.x - lr * Fm.x + em.x, wm.y - lr * Fm.y + em.y);
 }
 
 __device__ __forceinline__ void euler_point(const FieldInst &F, long long i, double2 ra, double2 rb, double2 rg,
@@ -350,14 +359,15 @@ __device__ __forceinline__ void euler_point(const FieldInst &F, long long i, dou
     // rho0 w+ / kappa + I rho0 (exp_nrH - evar) + I hhat s
     const double2 Fv = make_double2(rho0 * F.ikappa * wv.x - rho0 * enh.y - hh * s.y,
                                     rho0 * F.ikappa * wv.y + rho0 * (enh.x - evar) + hh * s.x);
-    w[0] = make_double2(wv.x - F.lam_pl * Fv.x, wv.y - F.lam_pl * Fv.y);
+    const double2 e0 = cl_noise(F, 0, i);
+    w[0] = make_double2(wv.x - F.lam_pl * Fv.x + e0.x, wv.y - F.lam_pl * Fv.y + e0.y);
   }
   const double2 z = make_double2(0.0, 0.0);
-  if (F.cab != 0.0) euler_pair(F, F.cab, F.neg_ab, ra, rb, hh, w[1], w[2]);
+  if (F.cab != 0.0) euler_pair(F, F.cab, F.neg_ab, ra, rb, hh, cl_noise(F, 1, i), cl_noise(F, 2, i), w[1], w[2]);
   else w[1] = w[2] = z;
-  if (F.cbc != 0.0) euler_pair(F, F.cbc, F.neg_bc, rb, rg, hh, w[3], w[4]);
+  if (F.cbc != 0.0) euler_pair(F, F.cbc, F.neg_bc, rb, rg, hh, cl_noise(F, 3, i), cl_noise(F, 4, i), w[3], w[4]);
   else w[3] = w[4] = z;
-  if (F.cac != 0.0) euler_pair(F, F.cac, F.neg_ac, ra, rg, hh, w[5], w[6]);
+  if (F.cac != 0.0) euler_pair(F, F.cac, F.neg_ac, ra, rg, hh, cl_noise(F, 5, i), cl_noise(F, 6, i), w[5], w[6]);
   else w[5] = w[6] = z;
 }
 

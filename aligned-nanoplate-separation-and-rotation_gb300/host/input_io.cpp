@@ -91,7 +91,6 @@ std::string read_input(const std::string &path, Input &in) {
   if (in.do_fld_np) return "No field-based nanoparticles (code/read_input.cpp:184-189)";
   if (in.do_film && in.do_channel) return "Can't do film and channel in same simulation";
   if (in.do_film || in.do_channel) return "films and channels are not built here";
-  if (in.do_CL) return "complex Langevin sampling (do_CL = 1) is not built here";
   if (in.n_exp_nr > 0 && in.np_type != 2) return "explicit particles must be nanorods/plates (np_type = 2)";
   for (int j = 0; j < in.n_exp_nr; j++)
     for (int d = 0; d < 3; d++)
@@ -134,6 +133,8 @@ scft_params to_params(const Input &in, int precision) {
   p.precision = precision;
   // code/simulate.cpp:86-89: update_scheme 0 runs update_Euler, anything else update_1s
   p.update_scheme = in.update_scheme == 0 ? SCFT_UPDATE_EULER : SCFT_UPDATE_1S;
+  p.do_cl = in.do_CL != 0;
+  p.cl_seed = 1;  // the driver sets the run's seed
   p.plate_shape = SCFT_PLATE_REFERENCE;
   return p;
 }

@@ -12,6 +12,7 @@
 #include <cmath>
 #include <complex>
 #include <cstdio>
+#include <ctime>
 #include <cstdlib>
 #include <random>
 #include <string>
@@ -36,6 +37,9 @@ struct Run {
   int close_to_tol = 0;
   bool done = false;
   FILE *dat = nullptr;
+  // complex-Langevin averages (code/array_utils.cpp:13-45)
+  std::vector<std::complex<double>> avg_a, avg_b, avg_g;
+  double n_samples = 0.0;
 };
 
 int check(int st, const char *what) {
@@ -122,8 +126,10 @@ std::vector<std::complex<double>> initial_fields(scft_ctx *ctx, int k, const Run
   return w;
 }
 
-// write_outputs (code/io_utils.cpp:11-104): smeared and raw densities, fields.
-void write_outputs(scft_ctx *ctx, int k, const Run &r) {
+// write_outputs (code/io_utils.cpp:11-104): smeared and raw densities, fields,
+// and with complex Langevin the running averages divided by the sample count
+// once iter >= sample_wait (avg_rhog of free grafted particles stays zero).
+void write_outputs(scft_ctx *ctx, int k, const Run &r, int iter) {
   typedef std::complex<double> cd;
   const Input &in = r.in;
   const long M = r.M;
@@ -163,6 +169,17 @@ void write_outputs(scft_ctx *ctx, int k, const Run &r) {
     write_bin(d + "rhog_exp.p0.bin", in.Nx, in.L, t.data(), M);
     write_bin(d + "rhog_exp_c.p0.bin", in.Nx, in.L, rg.data(), M);
   }
+  if (in.do_CL && iter >= in.sample_wait) {
+    auto write_avg = [&](const char *name, const std::vector<cd> &acc) {
+      std::vector<cd> a(M);
+      for (long i = 0; i < M; i++) a[i] = (acc.empty() ? cd(0.0) : acc[i]) / r.n_samples;
+      write_bin(d + name + ".p0.bin", in.Nx, in.L, a.data(), M);
+    };
+    write_avg("avg_rhoda", r.avg_a);
+    write_avg("avg_rhodb", r.avg_b);
+    write_avg("avg_rhog", std::vector<cd>());
+    write_avg("avg_rhog_exp", r.avg_g);
+  }
   std::vector<cd> w(7 * M);
   check(scft_get_fields(ctx, k, reinterpret_cast<double *>(w.data())), "scft_get_fields");
   write_bin(d + "wpl.p0.bin", in.Nx, in.L, w.data(), M);
@@ -179,12 +196,16 @@ void write_outputs(scft_ctx *ctx, int k, const Run &r) {
 
 int main(int argc, char **argv) {
   int precision = SCFT_PREC_FP64;
+  // complex-Langevin seed: the reference seeds ran2 with idum = -time(0)
+  // (code/main.cpp:20); --seed S reproduces a run seeded with idum = -S
+  long long seed = (long long)time(nullptr);
   bool quiet = false;
   std::vector<std::string> dirs;
   for (int a = 1; a < argc; a++) {
     const std::string s = argv[a];
     if (s == "--mixed") precision = SCFT_PREC_MIXED;
     else if (s == "--quiet") quiet = true;
+    else if (s == "--seed" && a + 1 < argc) seed = atoll(argv[++a]);
     else dirs.push_back(s);
   }
   if (dirs.empty()) dirs.push_back(".");
@@ -198,6 +219,7 @@ int main(int argc, char **argv) {
       return 1;
     }
     params.push_back(to_params(runs[k].in, precision));
+    params.back().cl_seed = seed;
   }
   scft_ctx *ctx = nullptr;
   check(scft_create(params.data(), (int)params.size(), &ctx), "scft_create");
@@ -223,7 +245,7 @@ int main(int argc, char **argv) {
   int st = scft_calc_H(ctx, h.data());
   for (int k = 0; k < n; k++) {
     if (!quiet) printf("%s: Starting H: %lf\n", runs[k].dir.c_str(), h[5 * k]);
-    write_outputs(ctx, k, runs[k]);
+    write_outputs(ctx, k, runs[k], 0);
   }
   int itermax = 0;
   for (auto &r : runs) itermax = std::max(itermax, r.in.itermax);
@@ -234,6 +256,28 @@ int main(int argc, char **argv) {
     for (auto &r : runs) all_done = all_done && (r.done || iter > r.in.itermax);
     if (all_done) break;
     check(scft_update_1s(ctx, 1), "scft_update_1s");
+    // complex-Langevin sampling (code/simulate.cpp:91-92)
+    for (int k = 0; k < n; k++) {
+      Run &r = runs[k];
+      if (r.done || iter > r.in.itermax || !r.in.do_CL || iter < r.in.sample_wait || r.in.sample_freq <= 0 ||
+          iter % r.in.sample_freq != 0)
+        continue;
+      std::vector<std::complex<double>> ra(r.M), rb(r.M), rg(r.M);
+      check(scft_get_density(ctx, k, reinterpret_cast<double *>(ra.data()), reinterpret_cast<double *>(rb.data()),
+                             reinterpret_cast<double *>(rg.data())),
+            "scft_get_density");
+      if (r.avg_a.empty()) {
+        r.avg_a.assign(r.M, 0.0);
+        r.avg_b.assign(r.M, 0.0);
+        r.avg_g.assign(r.M, 0.0);
+      }
+      for (long i = 0; i < r.M; i++) {
+        r.avg_a[i] += ra[i];
+        r.avg_b[i] += rb[i];
+        r.avg_g[i] += rg[i];
+      }
+      r.n_samples += 1.0;
+    }
     bool need_h = false;
     for (auto &r : runs)
       if (!r.done && iter <= r.in.itermax && iter % r.in.print_freq == 0) need_h = true;
@@ -266,9 +310,9 @@ int main(int argc, char **argv) {
         fprintf(r.dat, "%d %5.6lf %1.3e %5.6lf %1.3e %5.6lf %1.3e %5.6lf %1.3e %1.3e\n", iter, H.real(), H.imag(),
                 mlq.real(), mlq.imag(), mlqh.real(), mlqh.imag(), mlqp.real(), mlqp.imag(), r.error);
         fflush(r.dat);
-        write_outputs(ctx, k, r);
+        write_outputs(ctx, k, r, iter);
       }
-      if (iter > 25 && r.error < r.in.error_tol && r.close_to_tol > 10) {
+      if (!r.in.do_CL && iter > 25 && r.error < r.in.error_tol && r.close_to_tol > 10) {
         r.done = true;
         if (!quiet) printf("%s: Tolerance reached. Error = %.4e\n", r.dir.c_str(), r.error);
       }

@@ -49,6 +49,7 @@ class Params(ctypes.Structure):
         ("center", (ctypes.c_double * 3) * 2), ("orient", (ctypes.c_double * 3) * 2),
         ("precision", ctypes.c_int), ("plate_shape", ctypes.c_int),
         ("shell_lambda", ctypes.c_double), ("shell_width", ctypes.c_double), ("update_scheme", ctypes.c_int),
+        ("do_cl", ctypes.c_int), ("cl_seed", ctypes.c_longlong),
     ]
 
 
@@ -128,7 +129,7 @@ def make_params(**kw) -> Params:
                     sigma=0.0, Ng=0, L_nr=1.0, R_nr=1.0, xi_nr=0.2,
                     center=((0.5, 0.5, 0.5), (0.5, 0.5, 0.5)), orient=((1.0, 0.0, 0.0), (1.0, 0.0, 0.0)),
                     precision=PREC_FP64, plate_shape=PLATE_REFERENCE, shell_lambda=0.0, shell_width=0.0,
-                    update_scheme=UPDATE_1S)
+                    update_scheme=UPDATE_1S, do_cl=0, cl_seed=1)
     defaults.update(kw)
     for k, v in defaults.items():
         if k in ("Nx", "L"):

@@ -99,6 +99,12 @@ typedef struct scft_params {
    * update_scheme 1 (update_1s, code/1s_update.cpp) and 0 (update_Euler,
    * code/Euler_update.cpp).  kappa <= 0 (no w+^2 term) is allowed with Euler. */
   int update_scheme;
+  /* Complex-Langevin noise in the field update (do_CL, code/1s_update.cpp:
+   * 54-319, code/Euler_update.cpp:49-172), FP64 method only.  The noise is
+   * the reference's own stream: its ran2/Gaussian deviates seeded like
+   * idum = -cl_seed, so a run with the same seed adds the same noise. */
+  int do_cl;
+  long long cl_seed;
 } scft_params;
 
 /* Derived per-instance quantities (code/initialize.cpp:249-386). */

@@ -125,11 +125,26 @@ def driver_cases() -> dict:
     c = Case(update_scheme=0, **dict(base, chi_ab=-0.5))
     c.fields = seeded_fields(c, 3, 0.3, 0.01, False)
     cases["driver_euler_negab"] = c
+    # complex Langevin (do_CL = 1, the harness seeds ran2 with idum = -12345),
+    # averages sampled every 2 iterations from iteration 4
+    cl = dict(do_CL=1, sample_freq=2, sample_wait=4)
+    c = Case(**cl, **base)
+    c.fields = seeded_fields(c, 4, 0.3, 0.01, False)
+    cases["driver_cl"] = c
+    c = Case(**cl, **dict(base, chi_ab=-0.5))
+    c.fields = seeded_fields(c, 5, 0.3, 0.01, False)
+    cases["driver_cl_negab"] = c
+    c = Case(update_scheme=0, **cl, **base)
+    c.fields = seeded_fields(c, 6, 0.3, 0.01, False)
+    cases["driver_cl_euler"] = c
     return cases
 
 
 DRIVER_OUTPUTS = ["data.dat", "wpl.p0.bin", "wabp.p0.bin", "wabm.p0.bin", "rhoda.p0.bin", "rhodb.p0.bin",
                   "rhoda_c.p0.bin", "rhodb_c.p0.bin"]
+
+
+CL_OUTPUTS = ["avg_rhoda.p0.bin", "avg_rhodb.p0.bin"]
 
 
 def make_driver_fixtures(tmp):
@@ -146,7 +161,8 @@ def make_driver_fixtures(tmp):
             raise RuntimeError(r.stderr)
         out = os.path.join(HERE, name)
         os.makedirs(out, exist_ok=True)
-        for f in ["bcp.input"] + [n + ".res" for n in c.fields] + DRIVER_OUTPUTS:
+        extra = CL_OUTPUTS if c.do_CL else []
+        for f in ["bcp.input"] + [n + ".res" for n in c.fields] + DRIVER_OUTPUTS + extra:
             shutil.copy(os.path.join(run, f), os.path.join(out, f if f == "bcp.input" or f.endswith(".res")
                                                            else f + ".ref"))
         print(name, open(os.path.join(run, "data.dat")).read().splitlines()[-1])

@@ -90,6 +90,34 @@ def test_driver_mixed_precision(tmp_path, name):
     assert np.abs(got[:, 1] - ref[:, 1]).max() <= 2e-5 * np.abs(ref[:, 1]).max()
 
 
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["driver_cl", "driver_cl_negab", "driver_cl_euler"])
+def test_driver_complex_langevin_matches_reference(tmp_path, name):
+    """do_CL = 1: the noise is the reference's own random stream (the fixture
+    was written with idum = -12345), so fields, densities and the running
+    averages match the reference run (code/1s_update.cpp:54-368,
+    code/Euler_update.cpp:49-172, code/array_utils.cpp:13-45)."""
+    run = stage(str(tmp_path), name)
+    r = subprocess.run([DRIVER, "--quiet", "--seed", "12345", run], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr
+    compare_run(run, name)
+    for f in ("avg_rhoda.p0.bin", "avg_rhodb.p0.bin"):
+        _, _, _, _, a = read_bin(os.path.join(run, f))
+        _, _, _, _, b = read_bin(os.path.join(GOLDEN, name, f + ".ref"))
+        assert np.abs(a - b).max() <= 1e-10 * np.abs(b).max(), f
+
+
+@pytest.mark.gpu
+def test_complex_langevin_seed_changes_the_noise(tmp_path):
+    runs = []
+    for seed in ("12345", "777"):
+        run = stage(str(tmp_path / seed), "driver_cl")
+        r = subprocess.run([DRIVER, "--quiet", "--seed", seed, run], capture_output=True, text=True, timeout=600)
+        assert r.returncode == 0, r.stderr
+        runs.append(read_bin(os.path.join(run, "wpl.p0.bin"))[4])
+    assert np.abs(runs[0] - runs[1]).max() > 1e-3 * np.abs(runs[0]).max()
+
+
 def _driver_or_skip():
     if not os.path.exists(DRIVER):
         from scft.build import build
@@ -101,7 +129,7 @@ def _driver_or_skip():
 @pytest.mark.parametrize("edit,message", [
     (lambda s: s.replace("0.0 0  phiAH, Nah", "0.1 10  phiAH, Nah"), "homopolymer"),
     (lambda s: s.replace("0  do_fld_np", "1  do_fld_np"), "field-based"),
-    (lambda s: s.replace("0  do_CL", "1  do_CL"), "complex Langevin"),
+    (lambda s: s.replace("0  do_film", "1  do_film"), "films"),
 ])
 def test_driver_rejects_inputs_like_the_reference(tmp_path, edit, message):
     """Input errors are reported before any GPU work (code/read_input.cpp:40-45,

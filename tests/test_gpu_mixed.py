@@ -211,3 +211,9 @@ def test_mixed_grafted_plates_match_fp64(scft):
         assert rel(a, b) < RHO_TOL
     for k in ("wpl", "wbcp", "wbcm"):
         assert rel(f32[k], f64[k]) < RHO_TOL, k
+
+
+def test_complex_langevin_is_fp64_only(scft):
+    p = scft.make_params(precision=scft.PREC_MIXED, do_cl=1, cl_seed=3)
+    with pytest.raises(scft.ScftError):
+        scft.Context(p)
