@@ -887,6 +887,7 @@ void build_jobs(scft_ctx *c) {
     P.grafts = I.grafts;
   }
   c->d_fi = dupload(c, fi);
+  c->h_fi = fi;
   c->d_pi = dupload(c, pi);
   c->mixed = c->inst[0].mixed;
   for (auto &I : c->inst)
@@ -1041,6 +1042,41 @@ void build_jobs(scft_ctx *c) {
     c->job_order = order;
     c->inst_pj_end = inst_pj_end;
     c->inst_cj_end = inst_cj_end;
+    // field-level data in job order, so that a sweep group's instances are a
+    // contiguous range for the field kernels and the FP64 field transforms too
+    std::vector<FieldInst> fio;
+    std::vector<PlaneJob> fpj, ipj;
+    std::vector<ColJob> fcj, icj;
+    c->fld_end.assign(4 * n, 0);
+    for (int oi = 0; oi < n; oi++) {
+      Instance &I = c->inst[order[oi]];
+      const DevGeom &g = c->geoms[I.geom];
+      fio.push_back(c->h_fi[order[oi]]);
+      std::vector<double2 *> fw = {I.zr}, iv = {I.zs};
+      if (I.graft) {
+        fw.push_back(I.zg);
+        iv.push_back(I.zg);
+      }
+      for (double2 *a : fw) {
+        for (int z = 0; z < g.nz; z++) fpj.push_back(PlaneJob{a, I.geom, z});
+        for (int y = 0; y < g.ny; y++)
+          for (int x0 = 0; x0 < g.nx; x0 += g.tx) fcj.push_back(ColJob{a, nullptr, I.geom, x0, y});
+      }
+      for (double2 *a : iv) {
+        for (int z = 0; z < g.nz; z++) ipj.push_back(PlaneJob{a, I.geom, z});
+        for (int y = 0; y < g.ny; y++)
+          for (int x0 = 0; x0 < g.nx; x0 += g.tx) icj.push_back(ColJob{a, nullptr, I.geom, x0, y});
+      }
+      c->fld_end[4 * oi + 0] = (int)fpj.size();
+      c->fld_end[4 * oi + 1] = (int)fcj.size();
+      c->fld_end[4 * oi + 2] = (int)ipj.size();
+      c->fld_end[4 * oi + 3] = (int)icj.size();
+    }
+    c->d_fi_ord = dupload(c, fio);
+    c->d_fpj_ord = dupload(c, fpj);
+    c->d_fcj_ord = dupload(c, fcj);
+    c->d_ipj_ord = dupload(c, ipj);
+    c->d_icj_ord = dupload(c, icj);
     build_groups(c);
     c->shp_mix = choose_shape(emax_plane, sizeof(float2), (nxy_max + 32) * sizeof(float2));
     c->all64 = 1;
@@ -1267,44 +1303,74 @@ void seq_update_1s(scft_ctx *c) {
   seq_poly_density(c);
 }
 
-// Mixed form: FP32 packed propagator sweep over all instances (after E32),
-// as one chain of launches per sweep group, each on its own side stream.
-void seq_mix_sweep(scft_ctx *c) {
-  const int n = (int)c->inst.size();
-  cudaStream_t st = c->st;
-  for (auto &I : c->inst) {
-    CK(cudaMemsetAsync(I.acc32[0], 0, sizeof(float) * I.M, st));
-    CK(cudaMemsetAsync(I.acc32[1], 0, sizeof(float) * I.M, st));
+// Mixed form, one sweep group on stream sg: the work of one update_1s (or of
+// calc_poly_density when `update` is false) for the group's instances, from
+// the densities of the last sweep to the densities of this one:
+//   update:  density pack -> forward FP64 transform -> k-space update (which
+//            also forms the smeared pair) ->
+//   density: (smeared pair from the fields) ->
+//   both:    inverse FP64 transform -> Boltzmann factors -> FP32 sweep -> Q.
+// Each group is an independent chain, so one group's FP64-bound field work
+// runs beside another group's bandwidth-bound sweep.
+void mix_group_chain(scft_ctx *c, int g, cudaStream_t sg, bool update) {
+  const scft_ctx::SweepGroup &gr = c->groups[g];
+  const int i0 = gr.inst_begin, cnt_i = gr.inst_end - gr.inst_begin;
+  const FieldInst *fi = c->d_fi_ord + i0;
+  auto range = [&](int kind, int &b0, int &n0) {
+    b0 = i0 ? c->fld_end[4 * (i0 - 1) + kind] : 0;
+    n0 = c->fld_end[4 * (gr.inst_end - 1) + kind] - b0;
+  };
+  int b, m;
+  if (update) {
+    LK(launch_mix_rho_pack(fi, cnt_i, c->eblocks, 0, sg));
+    range(0, b, m);
+    LK(launch_plane_fft<double>(c->shp_plane, c->d_fpj_ord + b, m, c->d_geoms, c->d_tw64, -1, 0, sg));
+    range(1, b, m);
+    LK(launch_col_fft<double>(c->shp_col, c->d_fcj_ord + b, m, c->d_geoms, c->d_tw64, 0, 1, sg));
+    LK(launch_mix_update(fi, cnt_i, c->eblocks, sg));
+  } else {
+    LK(launch_mix_smear(fi, cnt_i, c->eblocks, sg));
   }
-  const int G = (int)c->groups.size();
-  const bool fork = G > 1;
+  range(3, b, m);
+  LK(launch_col_fft<double>(c->shp_col, c->d_icj_ord + b, m, c->d_geoms, c->d_tw64, 1, 0, sg));
+  range(2, b, m);
+  LK(launch_plane_fft<double>(c->shp_plane, c->d_ipj_ord + b, m, c->d_geoms, c->d_tw64, +1, 0, sg));
+  LK(launch_mix_boltzmann(fi, cnt_i, c->eblocks, sg));
+  for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) {
+    Instance &I = c->inst[c->job_order[oi]];
+    CK(cudaMemsetAsync(I.acc32[0], 0, sizeof(float) * I.M, sg));
+    CK(cudaMemsetAsync(I.acc32[1], 0, sizeof(float) * I.M, sg));
+  }
   auto clampc = [](int v, int lo, int hi) { return std::min(std::max(v, lo), hi) - lo; };
-  auto plane = [&](int g, int s) {
-    const scft_ctx::SweepGroup &gr = c->groups[g];
-    cudaStream_t sg = fork ? c->side[g] : st;
+  for (int s = 0; s < c->nmax; s++) {
     const int cnt = clampc(c->prop_pj_count[s], gr.pj_begin, gr.pj_end);
-    if (cnt <= 0) return;
+    if (cnt <= 0) break;
+    if (s > 0) {
+      if (c->all64) {
+        const int per = 64 * (64 / c->col64_tx);  // z-pass jobs per instance
+        LK(launch_mix_col64(col64_jobs(c) + (size_t)gr.inst_begin * per, (cnt / 64) * per, c->d_tw32_64, 64, 64,
+                            c->col64_tx, sg));
+      } else {
+        const int cc = clampc(c->prop_cj_count[s], gr.cj_begin, gr.cj_end);
+        LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cc, c->d_geoms, c->d_tw32, 3, 1, sg));
+      }
+    }
     if (c->all64)
       LK(launch_mix_plane64(c->mix64_tab.data() + gr.inst_begin, cnt / 64, c->d_tw32_64, s, sg));
     else
       LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj + gr.pj_begin, cnt, c->d_mi, c->d_geoms, c->d_tw32, s, sg));
-  };
-  auto column = [&](int g, int s) {
-    const scft_ctx::SweepGroup &gr = c->groups[g];
-    cudaStream_t sg = fork ? c->side[g] : st;
-    if (c->all64) {
-      // 64 * 64 / tx jobs per instance, in job order
-      const int per = 64 * (64 / c->col64_tx);
-      const int act = clampc(c->prop_pj_count[s], gr.pj_begin, gr.pj_end) / 64;
-      if (act > 0)
-        LK(launch_mix_col64(col64_jobs(c) + (size_t)gr.inst_begin * per, act * per, c->d_tw32_64, 64, 64,
-                            c->col64_tx, sg));
-    } else {
-      const int cnt = clampc(c->prop_cj_count[s], gr.cj_begin, gr.cj_end);
-      if (cnt > 0)
-        LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cnt, c->d_geoms, c->d_tw32, 3, 1, sg));
-    }
-  };
+  }
+  LK(launch_mix_q_finalize(fi, cnt_i, sg));
+}
+
+// The groups of each phase forked onto side streams and joined back; then
+// the grafted chains of every instance (code/calc_poly_density.cpp:131-133,
+// 155-159) on the context stream.
+void seq_mix(scft_ctx *c, bool update) {
+  const int n = (int)c->inst.size();
+  cudaStream_t st = c->st;
+  const int G = (int)c->groups.size();
+  const bool fork = G > 1;
   for (int g0 = 0; g0 < G;) {
     int g1 = g0;
     while (g1 < G && c->groups[g1].phase == c->groups[g0].phase) g1++;
@@ -1312,12 +1378,7 @@ void seq_mix_sweep(scft_ctx *c) {
       CK(cudaEventRecord(c->ev_fork, st));
       for (int g = g0; g < g1; g++) CK(cudaStreamWaitEvent(c->side[g], c->ev_fork, 0));
     }
-    for (int g = g0; g < g1; g++) plane(g, 0);
-    for (int s = 1; s < c->nmax; s++)
-      for (int g = g0; g < g1; g++) {
-        column(g, s);
-        plane(g, s);
-      }
+    for (int g = g0; g < g1; g++) mix_group_chain(c, g, fork ? c->side[g] : st, update);
     if (fork)
       for (int g = g0; g < g1; g++) {
         CK(cudaEventRecord(c->ev_join[g], c->side[g]));
@@ -1325,8 +1386,6 @@ void seq_mix_sweep(scft_ctx *c) {
       }
     g0 = g1;
   }
-  LK(launch_mix_q_finalize(c->d_fi, n, st));
-  // grafted chains (code/calc_poly_density.cpp:131-133,155-159)
   if (c->ngmax > 0) {
     for (auto &I : c->inst)
       if (I.graft) CK(cudaMemsetAsync(I.gacc32, 0, sizeof(float) * I.M, st));
@@ -1345,33 +1404,11 @@ void seq_mix_sweep(scft_ctx *c) {
   }
 }
 
-// Mixed form: inverse transform of the packed smeared pair, Boltzmann factors, sweep.
-void seq_mix_from_zs(scft_ctx *c) {
-  const int n = (int)c->inst.size();
-  cudaStream_t st = c->st;
-  LK(launch_col_fft<double>(c->shp_col, c->d_cj_fld, c->n_cj_fld, c->d_geoms, c->d_tw64, 1, 0, st));
-  LK(launch_plane_fft<double>(c->shp_plane, c->d_pj_fld, c->n_pj_fld, c->d_geoms, c->d_tw64, +1, 0, st));
-  LK(launch_mix_boltzmann(c->d_fi, n, c->eblocks, st));
-  seq_mix_sweep(c);
-}
-
 // Mixed calc_poly_density from the k-space fields.
-void seq_mix_density(scft_ctx *c) {
-  LK(launch_mix_smear(c->d_fi, (int)c->inst.size(), c->eblocks, c->st));
-  seq_mix_from_zs(c);
-}
+void seq_mix_density(scft_ctx *c) { seq_mix(c, false); }
 
-// Mixed update_1s: densities -> packed forward transform -> k-space update
-// (which also forms the packed smeared pair) -> inverse -> sweep.
-void seq_mix_update(scft_ctx *c) {
-  const int n = (int)c->inst.size();
-  cudaStream_t st = c->st;
-  LK(launch_mix_rho_pack(c->d_fi, n, c->eblocks, 0, st));
-  LK(launch_plane_fft<double>(c->shp_plane, c->d_pj_upd, c->n_pj_upd, c->d_geoms, c->d_tw64, -1, 0, st));
-  LK(launch_col_fft<double>(c->shp_col, c->d_cj_upd, c->n_cj_upd, c->d_geoms, c->d_tw64, 0, 1, st));
-  LK(launch_mix_update(c->d_fi, n, c->eblocks, st));
-  seq_mix_from_zs(c);
-}
+// Mixed update_1s.
+void seq_mix_update(scft_ctx *c) { seq_mix(c, true); }
 
 }  // namespace
 
@@ -1489,11 +1526,14 @@ void ctx_set_sweep_groups(scft_ctx *c, int groups, int phases) {
   }
 }
 
-// Autotuner of the mixed sweep's launch schedule: for every candidate
-// (number of sweep groups, z-pass columns per CTA of the 64-point kernels)
-// it times `reps` complete propagator sweeps of the batch with CUDA events on
-// the context stream, after one untimed sweep, and keeps the fastest.  The
-// sweeps recompute the current densities, so the state is unchanged.
+// Autotuner of the mixed form's launch schedule: for every candidate
+// (sequential phases x concurrent groups x z-pass columns per CTA of the
+// 64-point kernels) it times `reps` density builds of the batch (smeared
+// pair, inverse FP64 transform, Boltzmann factors, FP32 sweep: the chain of
+// an update without its k-space step) with CUDA events on the context
+// stream, after one untimed build, and keeps the fastest.  The builds
+// recompute the current densities from the current fields, so the state is
+// unchanged.
 void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *tx_out, double *ms_out) {
   *groups_out = 1;
   *phases_out = 1;
@@ -1525,9 +1565,9 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
       c->sweep_streams = g;
       c->col64_tx = tx;
       build_groups(c);
-      seq_mix_sweep(c);
+      seq_mix_density(c);
       CK(cudaEventRecord(e0, c->st));
-      for (int r = 0; r < reps; r++) seq_mix_sweep(c);
+      for (int r = 0; r < reps; r++) seq_mix_density(c);
       CK(cudaEventRecord(e1, c->st));
       CK(cudaEventSynchronize(e1));
       float ms = 0.f;
@@ -1875,6 +1915,10 @@ void ctx_override_nD(scft_ctx *c, int k, double nD) {
   c->inst[k].info.nD = nD;
   CK(cudaMemcpyAsync(reinterpret_cast<char *>(c->d_fi + k) + offsetof(FieldInst, nD), &nD, sizeof(double),
                      cudaMemcpyHostToDevice, c->st));
+  for (size_t oi = 0; c->d_fi_ord && oi < c->job_order.size(); oi++)
+    if (c->job_order[oi] == k)
+      CK(cudaMemcpyAsync(reinterpret_cast<char *>(c->d_fi_ord + oi) + offsetof(FieldInst, nD), &nD, sizeof(double),
+                         cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
 }
 }  // namespace scft

@@ -123,6 +123,15 @@ struct scft_ctx {
   std::vector<SweepGroup> groups;
   int sweep_phases = 1;  // requested number of sequential phases
   std::vector<int> job_order, inst_pj_end, inst_cj_end;  // mixed job lists, by instance
+  // mixed field-level data in job order: FieldInst table, forward (rho pack)
+  // and inverse (smeared pair) FP64 transform jobs; fld_end[4 oi + k] = end of
+  // instance oi's jobs in list k (forward plane, forward column, inverse
+  // plane, inverse column)
+  std::vector<scft::FieldInst> h_fi;
+  scft::FieldInst *d_fi_ord = nullptr;
+  scft::PlaneJob *d_fpj_ord = nullptr, *d_ipj_ord = nullptr;
+  scft::ColJob *d_fcj_ord = nullptr, *d_icj_ord = nullptr;
+  std::vector<int> fld_end;
   int sweep_streams = 2;  // requested number of groups (1 = a single chain)
   std::vector<cudaStream_t> side;
   std::vector<cudaEvent_t> ev_join;
