@@ -722,6 +722,46 @@ void setup_plates(scft_ctx *c, Instance &I) {
   CK(cudaStreamSynchronize(c->st));
 }
 
+// TMA descriptor of a float2 array seen as `rows` rows of 64 float2 (128
+// floats), boxes of 64 rows x 32 floats with the 128-byte swizzle; the entry
+// point comes from the driver (cuTensorMapEncodeTiled) through the runtime.
+CUtensorMap tensor_map_rows(const float2 *base, unsigned long long rows) {
+  typedef CUresult (*EncodeFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                               const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                               CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+  static EncodeFn encode = nullptr;
+  if (!encode) {
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    CK(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !fn)
+      throw ScftError(SCFT_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    encode = reinterpret_cast<EncodeFn>(fn);
+  }
+  CUtensorMap m;
+  const cuuint64_t dims[2] = {128, rows};
+  const cuuint64_t strides[1] = {128 * sizeof(float)};
+  const cuuint32_t box[2] = {32, 64};
+  const cuuint32_t estr[2] = {1, 1};
+  const CUresult r = encode(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2 *>(base), dims, strides, box, estr,
+                            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                            CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) throw ScftError(SCFT_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+  return m;
+}
+
+// Raises the plane pass's error word (an mbarrier wait that ran out) as an error.
+void check_device_error(scft_ctx *c) {
+  if (!c->d_err) return;
+  int h = 0;
+  CK(cudaMemcpyAsync(&h, c->d_err, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  if (h) {
+    CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+    throw ScftError(SCFT_ERR_CUDA, "a TMA wait of the plane pass ran out (results of that call are invalid)");
+  }
+}
+
 ColJob *col64_jobs(scft_ctx *c) { return c->d_mix64_cj_tx[c->col64_tx == 8 ? 0 : (c->col64_tx == 16 ? 1 : 2)]; }
 
 // Sweep groups: the job order is cut into `sweep_phases` contiguous phases and
@@ -1094,7 +1134,15 @@ void build_jobs(scft_ctx *c) {
         c->d_mix64_cj_tx[t] = dupload(c, cj64);
       }
       c->mix64_tab.clear();
-      for (int oi = 0; oi < n; oi++) c->mix64_tab.push_back(c->h_mi[order[oi]]);
+      c->tmE.clear();
+      c->tmH.clear();
+      for (int oi = 0; oi < n; oi++) {
+        c->mix64_tab.push_back(c->h_mi[order[oi]]);
+        Instance &I = c->inst[order[oi]];
+        c->tmE.push_back(tensor_map_rows(I.E32, 4096ULL));
+        c->tmH.push_back(tensor_map_rows(I.hist32, 4096ULL * (unsigned long long)(I.hmax + 1)));
+      }
+      if (!c->d_err) c->d_err = dalloc<int>(c, 1);
     }
     c->shp_col32 = choose_shape(emax_col, sizeof(float2), (nz_max + 32) * sizeof(float2));
     if (c->shp_mix.gm)
@@ -1356,7 +1404,8 @@ void mix_group_chain(scft_ctx *c, int g, cudaStream_t sg, bool update) {
       }
     }
     if (c->all64)
-      LK(launch_mix_plane64(c->mix64_tab.data() + gr.inst_begin, cnt / 64, c->d_tw32_64, s, sg));
+      LK(launch_mix_plane64(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
+                            c->tmH.data() + gr.inst_begin, cnt / 64, c->d_tw32_64, s, c->d_err, sg));
     else
       LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj + gr.pj_begin, cnt, c->d_mi, c->d_geoms, c->d_tw32, s, sg));
   }
@@ -1471,6 +1520,7 @@ void ctx_poly_density(scft_ctx *c) {
   else
     seq_poly_density(c);
   CK(cudaStreamSynchronize(c->st));
+  check_device_error(c);
   c->dirty_density = 0;
 }
 
@@ -1511,6 +1561,7 @@ void ctx_update(scft_ctx *c, int n_iter) {
     c->launches += c->launches_per_update;
   }
   CK(cudaStreamSynchronize(c->st));
+  check_device_error(c);
 }
 
 // Number of independent launch chains of the mixed sweep (1 = one chain).
@@ -1606,7 +1657,8 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   CK(cudaEventRecord(e0, c->st));
   for (int r = 0; r < reps; r++) {
     if (c->mixed && c->all64)
-      LK(launch_mix_plane64(c->mix64_tab.data(), c->prop_pj_count[s] / 64, c->d_tw32_64, s, c->st));
+      LK(launch_mix_plane64(c->mix64_tab.data(), c->tmE.data(), c->tmH.data(), c->prop_pj_count[s] / 64, c->d_tw32_64,
+                            s, c->d_err, c->st));
     else if (c->mixed)
       LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_geoms, c->d_tw32, s,
                                c->st));

@@ -1,6 +1,8 @@
 // context.h -- host-side state of an scft_ctx.
 #pragma once
 
+#include <cuda.h>
+
 #include <complex>
 #include <string>
 #include <vector>
@@ -111,6 +113,8 @@ struct scft_ctx {
   scft::GraftMixInst *d_gmi = nullptr;  // per instance (zero for instances without grafts)
   std::vector<scft::MixInst> h_mi;       // host copy of d_mi
   std::vector<scft::MixInst> mix64_tab;  // instances in job order (64^3 plane pass)
+  std::vector<CUtensorMap> tmE, tmH;      // their TMA descriptors (Boltzmann, history)
+  int *d_err = nullptr;                   // error word of the plane pass
   // The mixed sweep of a batch runs as `groups` independent chains of
   // launches on side streams (contiguous instance ranges in job order), so
   // that one group's column passes fill the last wave of another group's

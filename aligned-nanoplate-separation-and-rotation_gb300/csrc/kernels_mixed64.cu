@@ -14,9 +14,14 @@
 // stay inside a warp (warp barrier); exchanges along y cross warps (block
 // barrier).
 //
-// The plane pass prefetches, with cp.async at kernel start, the Boltzmann
-// factors and the stored history plane it will need after the inverse
-// transforms, so that their memory latency overlaps the transform work.
+// The plane pass stages the Boltzmann factors and the stored history plane it
+// needs after the inverse transforms with TMA tensor loads issued at kernel
+// start (cp.async.bulk.tensor, completion on an mbarrier), so that their
+// memory latency overlaps the transform work.  Each 64 x 64 float2 plane
+// arrives as four 64-row x 128-byte boxes with the 128-byte swizzle (16-byte
+// chunk c of row r stored at chunk c ^ (r & 7)), which keeps the row-phase
+// reads free of bank conflicts without padding.  The mbarrier wait is
+// bounded; a wait that runs out sets the context's error word.
 // Plane sums are formed with error-free FP32 two-sums per thread and across
 // the warp (FP64 only for the 16 warp results): GB300 issues FP64 at a small
 // fraction of its FP32 rate.
@@ -77,25 +82,48 @@ __device__ __forceinline__ uint64_t l2_policy_last() {
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
   return p;
 }
-__device__ __forceinline__ void cp_async16(void *smem, const void *gmem, uint64_t pol) {
-  const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-  asm volatile("cp.async.cg.shared.global.L2::cache_hint [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gmem), "l"(pol));
-}
 __device__ __forceinline__ void st_stream(float2 *g, float2 v, uint64_t pol) {
   asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;\n" ::"l"(g), "f"(v.x), "f"(v.y), "l"(pol)
                : "memory");
 }
-__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
-__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::); }
 
-// Copies one 64 x 64 float2 plane into a padded shared plane (16 B per copy).
-__device__ __forceinline__ void prefetch_plane(float2 *dst, const float2 *src, uint64_t pol) {
-#pragma unroll
-  for (int k = 0; k < 4; k++) {
-    const int c = threadIdx.x + 512 * k;  // 16-byte chunk: two float2
-    const int row = c >> 5, x = (2 * c) & 63;
-    cp_async16(dst + row * kRowPad + x, src + 2 * c, pol);
-  }
+// mbarrier and TMA (tensor) helpers; addresses are shared-window offsets.
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count));
+  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false if the phase did not complete within `limit` polls
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int limit) {
+  for (int k = 0; k < limit; k++)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar,
+                                            uint64_t policy) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint "
+      "[%0], [%1, {%2, %3}], [%4], %5;\n" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(policy)
+      : "memory");
+}
+// Element (row, x) of a plane staged by four 64 x 128 B boxes with the
+// 128-byte swizzle: box x / 16, 16-byte chunk ((x % 16) / 2) ^ (row % 8).
+__device__ __forceinline__ float2 swz(const float2 *plane, int row, int x) {
+  return plane[(x >> 4) * 1024 + row * 16 + ((((x & 15) >> 1) ^ (row & 7)) << 1) + (x & 1)];
 }
 
 }  // namespace
@@ -104,19 +132,22 @@ __device__ __forceinline__ void prefetch_plane(float2 *dst, const float2 *src, u
 // (instance, z plane): CTA b works on plane b % 64 of T.inst[b / 64].  The
 // instance table is a kernel parameter, so the first global loads (the
 // working plane, the prefetches) depend on nothing loaded before them.
-// Dynamic shared memory: exchange/transpose plane, prefetched Boltzmann
-// plane, prefetched history plane (3 padded planes, 110.6 KB; two CTAs per SM).
+// Dynamic shared memory (1024-byte aligned for the swizzle): staged Boltzmann
+// plane and history plane (32 KB each), then the padded exchange/transpose
+// plane (36.9 KB); 101 KB, two CTAs per SM.
 __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ Mix64Table T,
                                                         const float2 *__restrict__ tw_g, int n) {
-  extern __shared__ __align__(16) float2 dsm[];
-  float2 *buf = dsm;
-  float2 *Es = dsm + kPlanePad;
-  float2 *Hs = dsm + 2 * kPlanePad;
+  extern __shared__ __align__(16) unsigned char dsm_raw[];
+  float2 *Es = reinterpret_cast<float2 *>(dsm_raw + ((1024 - (smem_u32(dsm_raw) & 1023)) & 1023));
+  float2 *Hs = Es + 4096;
+  float2 *buf = Hs + 4096;
   __shared__ float2 tw[64];
+  __shared__ __align__(8) uint64_t s_bar;
   __shared__ double s_red[2][16];
   __shared__ double s_mu[2];
   __shared__ int s_exp[2];
-  const MixInst &P = T.inst[blockIdx.x >> 6];
+  const int ii = blockIdx.x >> 6;
+  const MixInst &P = T.inst[ii];
   const int zz = blockIdx.x & 63;
   const int N = P.N, Na = P.Na;
   if (n >= N) return;
@@ -137,9 +168,16 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
   const int m2 = N - 1 - n;
   const bool pair = (m2 < n);  // a stored partner plane is needed
   const uint64_t pol_first = l2_policy_first();
-  prefetch_plane(Es, P.E + zoff, l2_policy_last());
-  if (pair) prefetch_plane(Hs, P.hist + (long long)m2 * M + zoff, pol_first);
-  cp_async_commit();
+  if (tid == 0) {
+    // E rows z*64 + y of a 4096-row tensor; history rows (m2*64 + z)*64 + y
+    mbar_init(&s_bar, 1);
+    mbar_expect_tx(&s_bar, pair ? 65536u : 32768u);
+    const uint64_t pol_last = l2_policy_last();
+    for (int b = 0; b < 4; b++) tma_load_2d(Es + b * 1024, &T.tmE[ii], 32 * b, zz * 64, &s_bar, pol_last);
+    if (pair)
+      for (int b = 0; b < 4; b++)
+        tma_load_2d(Hs + b * 1024, &T.tmH[ii], 32 * b, (m2 * 64 + zz) * 64, &s_bar, pol_first);
+  }
   // accumulators of a paired step, loaded now so that their latency overlaps
   // the inverse transforms (row-phase ownership, as they are used)
   const int gi = row * 64 + tr;  // global index of element d = 0 in this plane
@@ -187,13 +225,16 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
     // inverse x transform (row phase, inside one warp)
     fft64_group<+1, true>(v, tr, buf + row * kRowPad, 9, 1, tw);
   }
-  cp_async_wait_all();
-  __syncthreads();  // prefetched planes visible
-  const float2 *Er = Es + row * kRowPad + tr;
+  if (!mbar_wait(&s_bar, 0, 1 << 22)) {
+    atomicExch(T.err, 1);
+    mbar_wait(&s_bar, 0, 1 << 22);  // let copies in flight land before the CTA moves on
+  }
+  __syncthreads();
+
   if (n == 0) {
 #pragma unroll
     for (int d = 0; d < 8; d++) {
-      const float2 e = Er[8 * d];
+      const float2 e = swz(Es, row, tr + 8 * d);
       v[d] = make_float2(useA_q ? e.x : e.y, useA_d ? e.x : e.y);
     }
   } else {
@@ -205,7 +246,7 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
     const float md_hi = (float)md, md_lo = (float)(md - (double)md_hi);
 #pragma unroll
     for (int d = 0; d < 8; d++) {
-      const float2 e = Er[8 * d];
+      const float2 e = swz(Es, row, tr + 8 * d);
       const float eq_ = useA_q ? e.x : e.y, ed_ = useA_d ? e.x : e.y;
       const float uq = fmaf(v[d].x, eq_, fmaf(mq_hi, eq_, mq_lo * eq_));
       const float ud = fmaf(v[d].y, ed_, fmaf(md_hi, ed_, md_lo * ed_));
@@ -229,19 +270,18 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
     const int Kref = (n == n0) ? Kq + (m2 == n ? Kd : P.K[N + m2]) : P.K[2 * N];
     if (n == n0 && zz == 0 && tid == 0) P.K[2 * N] = Kref;
     if (pair) {
-      const float2 *Hr = Hs + row * kRowPad + tr;
       const float f1 = ldexpf(1.0f, Kq + P.K[N + m2] - Kref);
       const float f2 = ldexpf(1.0f, P.K[m2] + Kd - Kref);
       if (same_acc) {
 #pragma unroll
         for (int d = 0; d < 8; d++) {
-          const float2 h = Hr[8 * d];
+          const float2 h = swz(Hs, row, tr + 8 * d);
           a1[8 * d] = acc1[d] + fmaf(v[d].x * h.y, f1, (h.x * v[d].y) * f2);
         }
       } else {
 #pragma unroll
         for (int d = 0; d < 8; d++) {
-          const float2 h = Hr[8 * d];
+          const float2 h = swz(Hs, row, tr + 8 * d);
           a1[8 * d] = acc1[d] + (v[d].x * h.y) * f1;
           a2[8 * d] = acc2[d] + (h.x * v[d].y) * f2;
         }
@@ -345,9 +385,10 @@ __global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__
   for (int j = 0; j < 8; j++) a[(t + 8 * j) * plane + base] = v[j];
 }
 
-cudaError_t launch_mix_plane64(const MixInst *insts, int ninst, const void *tw64, int n, cudaStream_t st) {
+cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
+                               const void *tw64, int n, int *err, cudaStream_t st) {
   if (ninst <= 0) return cudaSuccess;
-  const int smem = 3 * kPlanePad * (int)sizeof(float2);
+  const int smem = 1024 + 2 * 4096 * (int)sizeof(float2) + kPlanePad * (int)sizeof(float2);
   cudaError_t e = cudaFuncSetAttribute(k_mix_plane64, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(k_mix_plane64, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
@@ -356,7 +397,12 @@ cudaError_t launch_mix_plane64(const MixInst *insts, int ninst, const void *tw64
     const int cnt = ninst - i0 < kMix64MaxInst ? ninst - i0 : kMix64MaxInst;
     Mix64Table T;
     memset(&T, 0, sizeof T);
-    for (int k = 0; k < cnt; k++) T.inst[k] = insts[i0 + k];
+    for (int k = 0; k < cnt; k++) {
+      T.inst[k] = insts[i0 + k];
+      T.tmE[k] = tmE[i0 + k];
+      T.tmH[k] = tmH[i0 + k];
+    }
+    T.err = err;
     k_mix_plane64<<<64 * cnt, 512, smem, st>>>(T, reinterpret_cast<const float2 *>(tw64), n);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;

@@ -1,6 +1,8 @@
 // prop_launch.h -- launchers of the propagator and field kernels.
 #pragma once
 
+#include <cuda.h>
+
 #include "inst.h"
 #include "launch.h"
 
@@ -24,13 +26,19 @@ cudaError_t launch_h_partials(const FieldInst *fi, int ninst, int blocks, double
 cudaError_t launch_mix_prop_plane(const LaunchShape &ls, const PropJob *jobs, int njobs, const MixInst *insts,
                                   const DevGeom *geoms, const void *tw, int n, cudaStream_t st);
 // Instances of one 64^3 plane-pass launch, passed by value as the kernel
-// parameter (3.5 KB); larger batches are launched in chunks.
+// parameter (15.4 KB: TMA descriptors of each instance's Boltzmann and
+// history arrays, the instance views, the error word); larger batches are
+// launched in chunks.
 constexpr int kMix64MaxInst = 48;
 struct Mix64Table {
+  CUtensorMap tmE[kMix64MaxInst];  // E32 as 4096 rows x 128 floats, boxes of 64 rows x 32 floats, 128B swizzle
+  CUtensorMap tmH[kMix64MaxInst];  // hist32 as 4096 (hmax + 1) rows x 128 floats, same boxes
   MixInst inst[kMix64MaxInst];
+  int *err;                        // set to 1 when an mbarrier wait runs out
 };
-// insts: host array of the active instances in job order (64 CTAs each)
-cudaError_t launch_mix_plane64(const MixInst *insts, int ninst, const void *tw64, int n, cudaStream_t st);
+// insts, tmE, tmH: host arrays of the active instances in job order (64 CTAs each)
+cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
+                               const void *tw64, int n, int *err, cudaStream_t st);
 // tx: x columns per CTA (8, 16 or 32); jobs must be built for that width
 cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw64, int nx, int ny, int tx,
                              cudaStream_t st);
