@@ -605,8 +605,9 @@ __global__ void k_mix_q_finalize(const FieldInst *__restrict__ fi, int ninst) {
 // rho_A, rho_B = acc * e^{+smw} * factor packed into zr (and optionally kept
 // as complex arrays for scft_get_density).
 __global__ void k_mix_rho_pack(const FieldInst *__restrict__ fi, int keep) {
+  const FieldInst &F0 = fi[blockIdx.y];
+  const double f = ldexp(F0.scal[kFactor].x, F0.K[2 * F0.N]);  // accumulators are scaled by 2^-Kref
   FOR_POINTS(F) {
-    const double f = ldexp(F.scal[kFactor].x, F.K[2 * F.N]);  // accumulators are scaled by 2^-Kref
     // e^{+smw} = 1 / e^{-smw}: the FP32 reciprocal of the Boltzmann factor
     const float2 E = F.E32[i];
     const double ra = (double)(F.acc32[0][i] * __frcp_rn(E.x)) * f;

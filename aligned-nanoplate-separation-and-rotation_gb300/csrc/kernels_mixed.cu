@@ -57,7 +57,7 @@ __global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restric
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   // previous step's means (FP64, same summation order in every CTA) and the
   // power-of-two exponents chosen from them
-  __shared__ double s_mu[2];
+  __shared__ float s_mh[2], s_ml[2];  // the step means as two-float pairs (split once)
   if (warp == 0) {
     double a = 0.0, b = 0.0;
     if (n > 0) {
@@ -79,8 +79,10 @@ __global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restric
       if (n > 0 && isfinite(mb) && mb > 0.0) frexp(mb, &eb);
       s_exp[0] = ea;
       s_exp[1] = eb;
-      s_mu[0] = ma;
-      s_mu[1] = mb;
+      s_mh[0] = (float)ma;
+      s_ml[0] = (float)(ma - (double)s_mh[0]);
+      s_mh[1] = (float)mb;
+      s_ml[1] = (float)(mb - (double)s_mh[1]);
     }
   }
   load_tw<float>(twx, twbuf, g.ax[0]);
@@ -106,9 +108,8 @@ __global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restric
   if (n > 0) {
     // q = (conv + mean) * e^{-w} * 2^{-e}, the mean as a two-float constant
     const float sq = ldexpf(1.0f, -eq), sd = ldexpf(1.0f, -ed);
-    const double mq = s_mu[0], md = s_mu[1];
-    const float mq_hi = (float)mq, mq_lo = (float)(mq - (double)mq_hi);
-    const float md_hi = (float)md, md_lo = (float)(md - (double)md_hi);
+    const float mq_hi = s_mh[0], mq_lo = s_ml[0];
+    const float md_hi = s_mh[1], md_lo = s_ml[1];
     for (int e = threadIdx.x; e < E; e += blockDim.x) {
       const C v = Ew[e];
       const C z = plane[e];
@@ -210,7 +211,7 @@ __global__ void __launch_bounds__(512) k_mix_graft_plane(const PropJob *__restri
   typedef float2 C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_red[32];
-  __shared__ double s_mu;
+  __shared__ float s_mh, s_ml;
   __shared__ int s_exp;
   const PropJob jb = jobs[blockIdx.x];
   const GraftMixInst &P = insts[jb.inst];
@@ -237,7 +238,8 @@ __global__ void __launch_bounds__(512) k_mix_graft_plane(const PropJob *__restri
       int ea = 0;
       if (n > 0 && isfinite(ma) && ma > 0.0) frexp(ma, &ea);
       s_exp = ea;
-      s_mu = ma;
+      s_mh = (float)ma;
+      s_ml = (float)(ma - (double)s_mh);
     }
   }
   load_tw<float>(twx, twbuf, g.ax[0]);
@@ -262,8 +264,7 @@ __global__ void __launch_bounds__(512) k_mix_graft_plane(const PropJob *__restri
   const int Kn = (n > 0) ? K[n - 1] + ex : (sweep == 0 ? 0 : -P.K[Ng - 1]);
   if (n > 0) {
     const float sc = ldexpf(1.0f, -ex);
-    const double m = s_mu;
-    const float m_hi = (float)m, m_lo = (float)(m - (double)m_hi);
+    const float m_hi = s_mh, m_lo = s_ml;
     for (int e = threadIdx.x; e < E; e += blockDim.x) {
       const float eg = Eg[e];
       plane[e] = make_float2(fmaf(plane[e].x, eg, fmaf(m_hi, eg, m_lo * eg)) * sc, 0.f);

@@ -144,7 +144,7 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
   __shared__ float2 tw[64];
   __shared__ __align__(8) uint64_t s_bar;
   __shared__ double s_red[2][16];
-  __shared__ double s_mu[2];
+  __shared__ float s_mh[2], s_ml[2];  // step means as two-float pairs
   __shared__ int s_exp[2];
   const int ii = blockIdx.x >> 6;
   const MixInst &P = T.inst[ii];
@@ -207,12 +207,16 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
       int ea = 0;
       if (n > 0 && isfinite(ma) && ma > 0.0) frexp(ma, &ea);
       s_exp[warp] = ea;
-      s_mu[warp] = ma;
+      // split once here: GB300 runs FP64 (conversions included) at a small
+      // fraction of the FP32 rate, so no thread of the plane does it
+      const float hi = (float)ma;
+      s_mh[warp] = hi;
+      s_ml[warp] = (float)(ma - (double)hi);
     }
   }
   const bool useA_q = (Na > 0 && n < Na);
   const bool useA_d = !(n <= N - Na - 1);
-  __syncthreads();  // tw, s_mu, s_exp
+  __syncthreads();  // tw, means, exponents
   if (n > 0) {
     // inverse y transform (column phase)
     fft64_group<+1, false>(v, tc, buf + col, 8 * 64, 64, tw);
@@ -241,9 +245,8 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
     // q = (conv + mean) * e^{-w} * 2^{-e}, the mean as a two-float constant
     const int eq = s_exp[0], ed = s_exp[1];
     const float sq = ldexpf(1.0f, -eq), sd = ldexpf(1.0f, -ed);
-    const double mq = s_mu[0], md = s_mu[1];
-    const float mq_hi = (float)mq, mq_lo = (float)(mq - (double)mq_hi);
-    const float md_hi = (float)md, md_lo = (float)(md - (double)md_hi);
+    const float mq_hi = s_mh[0], mq_lo = s_ml[0];
+    const float md_hi = s_mh[1], md_lo = s_ml[1];
 #pragma unroll
     for (int d = 0; d < 8; d++) {
       const float2 e = swz(Es, row, tr + 8 * d);
