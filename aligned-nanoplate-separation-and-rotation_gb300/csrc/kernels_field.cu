@@ -489,9 +489,31 @@ __global__ void k_mix_update(const FieldInst *__restrict__ fi) {
 // w <- (w - lam (F - B w)) / (1 + lam A) = alpha w - beta F, alpha, beta
 // functions of k alone.  No division per iteration; only fields with
 // nonzero chi are read and written.
+// Sign s_f with w_f(-k) = s_f conj(w_f(k)) under the mean-field phase
+// convention (the one scft_set_fields checks): -1 for the fields that are
+// imaginary in real space (w+, and the + field of a pair with positive chi or
+// the - field of a pair with negative chi), +1 for the real ones.
+__device__ __forceinline__ double field_parity(const FieldInst &F, int f) {
+  if (f == 0) return -1.0;
+  const int neg = (f <= 2) ? F.neg_ab : (f <= 4 ? F.neg_bc : F.neg_ac);
+  return (f & 1) ? (neg ? 1.0 : -1.0) : (neg ? -1.0 : 1.0);
+}
+
+// One thread per pair (k, -k): every field and density is Hermitian or
+// anti-Hermitian in k-space, so the update at -k follows from the one at k by
+// conjugation; this halves the FP64 work, which bounds this kernel on GB300.
+// Threads run over the planes z = 0..nz/2; within the self-conjugate planes
+// (z = 0 and, for even nz, nz/2) only the member with the smaller index of
+// each pair works.
 __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
-  FOR_POINTS(F) {
-    const double2 Z = F.zr[i], Zm = F.zr[neg_k(F, i)];
+  const FieldInst &F = fi[blockIdx.y];
+  const long long plane = (long long)F.nx * F.ny;
+  const long long Mh = plane * (F.nz / 2 + 1);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < Mh;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long j = neg_k(F, i);
+    if (j < i) continue;
+    const double2 Z = F.zr[i], Zm = F.zr[j];
     const double2 ra = make_double2(0.5 * (Z.x + Zm.x), 0.5 * (Z.y - Zm.y));
     const double2 rb = make_double2(0.5 * (Z.y + Zm.y), 0.5 * (Zm.x - Z.x));
     const double rho0 = F.rho0, hh = F.hhat[i];
@@ -557,12 +579,24 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
         step(6, F2);
       }
     }
+    const bool pair = (j != i);
     for (int f = 0; f < 7; f++)
-      if (F.alpha[f]) F.w[f][i] = w[f];
+      if (F.alpha[f]) {
+        F.w[f][i] = w[f];
+        if (pair) {
+          const double sf = field_parity(F, f);
+          F.w[f][j] = make_double2(sf * w[f].x, -sf * w[f].y);
+        }
+      }
     double2 wa, wb, wg;
     assemble_point(F, w, wa, wb, wg);
+    // zs = hhat (w_A + i w_B) at k and, with w_A(-k) = conj w_A(k), at -k
     F.zs[i] = make_double2(hh * (wa.x - wb.y), hh * (wa.y + wb.x));
-    if (F.graft) F.zg[i] = make_double2(hh * wg.x, hh * wg.y);
+    if (pair) F.zs[j] = make_double2(hh * (wa.x + wb.y), hh * (wb.x - wa.y));
+    if (F.graft) {
+      F.zg[i] = make_double2(hh * wg.x, hh * wg.y);
+      if (pair) F.zg[j] = make_double2(hh * wg.x, -hh * wg.y);
+    }
   }
 }
 
