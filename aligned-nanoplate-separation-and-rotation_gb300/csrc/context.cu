@@ -1119,9 +1119,10 @@ void build_jobs(scft_ctx *c) {
     c->d_icj_ord = dupload(c, icj);
     build_groups(c);
     c->shp_mix = choose_shape(emax_plane, sizeof(float2), (nxy_max + 32) * sizeof(float2));
-    c->all64 = 1;
+    c->xy64 = 1;
     for (auto &I : c->inst)
-      if (I.p.Nx[0] != 64 || I.p.Nx[1] != 64 || I.p.Nx[2] != 64) c->all64 = 0;
+      if (I.p.Nx[0] != 64 || I.p.Nx[1] != 64 || I.p.Nx[2] != c->inst[0].p.Nx[2]) c->xy64 = 0;
+    c->all64 = c->xy64 && c->inst[0].p.Nx[2] == 64;
     if (c->all64) {
       for (int t = 0; t < 3; t++) {
         const int tx = 8 << t;
@@ -1133,14 +1134,18 @@ void build_jobs(scft_ctx *c) {
         }
         c->d_mix64_cj_tx[t] = dupload(c, cj64);
       }
+
+    }
+    if (c->xy64) {
       c->mix64_tab.clear();
       c->tmE.clear();
       c->tmH.clear();
       for (int oi = 0; oi < n; oi++) {
         c->mix64_tab.push_back(c->h_mi[order[oi]]);
         Instance &I = c->inst[order[oi]];
-        c->tmE.push_back(tensor_map_rows(I.E32, 4096ULL));
-        c->tmH.push_back(tensor_map_rows(I.hist32, 4096ULL * (unsigned long long)(I.hmax + 1)));
+        const unsigned long long rows = 64ULL * (unsigned long long)I.p.Nx[2];
+        c->tmE.push_back(tensor_map_rows(I.E32, rows));
+        c->tmH.push_back(tensor_map_rows(I.hist32, rows * (unsigned long long)(I.hmax + 1)));
       }
       if (!c->d_err) c->d_err = dalloc<int>(c, 1);
     }
@@ -1403,9 +1408,11 @@ void mix_group_chain(scft_ctx *c, int g, cudaStream_t sg, bool update) {
         LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cc, c->d_geoms, c->d_tw32, 3, 1, sg));
       }
     }
-    if (c->all64)
+    if (c->xy64) {
+      const int nzi = c->inst[0].p.Nx[2];
       LK(launch_mix_plane64(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
-                            c->tmH.data() + gr.inst_begin, cnt / 64, c->d_tw32_64, s, c->d_err, sg));
+                            c->tmH.data() + gr.inst_begin, cnt / nzi, nzi, c->d_tw32_64, s, c->d_err, sg));
+    }
     else
       LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj + gr.pj_begin, cnt, c->d_mi, c->d_geoms, c->d_tw32, s, sg));
   }
@@ -1656,9 +1663,10 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   CK(cudaEventCreate(&e2));
   CK(cudaEventRecord(e0, c->st));
   for (int r = 0; r < reps; r++) {
-    if (c->mixed && c->all64)
-      LK(launch_mix_plane64(c->mix64_tab.data(), c->tmE.data(), c->tmH.data(), c->prop_pj_count[s] / 64, c->d_tw32_64,
-                            s, c->d_err, c->st));
+    if (c->mixed && c->xy64)
+      LK(launch_mix_plane64(c->mix64_tab.data(), c->tmE.data(), c->tmH.data(),
+                            c->prop_pj_count[s] / c->inst[0].p.Nx[2], c->inst[0].p.Nx[2], c->d_tw32_64, s, c->d_err,
+                            c->st));
     else if (c->mixed)
       LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_geoms, c->d_tw32, s,
                                c->st));

@@ -128,13 +128,16 @@ __device__ __forceinline__ float2 swz(const float2 *plane, int row, int x) {
 
 }  // namespace
 
-// Plane pass of step n for 64 x 64 xy planes, 512 threads, one CTA per
-// (instance, z plane): CTA b works on plane b % 64 of T.inst[b / 64].  The
+// Plane pass of step n for 64 x 64 xy planes (any nz, the same for every
+// instance of the launch), 512 threads, one CTA per (instance, z plane): CTA b
+// works on plane b % nz of T.inst[b / nz].  The
 // instance table is a kernel parameter, so the first global loads (the
 // working plane, the prefetches) depend on nothing loaded before them.
 // Dynamic shared memory (1024-byte aligned for the swizzle): staged Boltzmann
 // plane and history plane (32 KB each), then the padded exchange/transpose
 // plane (36.9 KB); 101 KB, two CTAs per SM.
+// NZ: nz known at compile time (64), or 0 to read it from the table.
+template <int NZ>
 __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ Mix64Table T,
                                                         const float2 *__restrict__ tw_g, int n) {
   extern __shared__ __align__(16) unsigned char dsm_raw[];
@@ -146,13 +149,13 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
   __shared__ double s_red[2][16];
   __shared__ float s_mh[2], s_ml[2];  // step means as two-float pairs
   __shared__ int s_exp[2];
-  const int ii = blockIdx.x >> 6;
+  const int nz = NZ ? NZ : T.nz;
+  const int ii = blockIdx.x / nz;
   const MixInst &P = T.inst[ii];
-  const int zz = blockIdx.x & 63;
+  const int zz = blockIdx.x - ii * nz;
   const int N = P.N, Na = P.Na;
   if (n >= N) return;
-  const int nz = 64;
-  const long long M = 64LL * 64 * 64;
+  const long long M = 4096LL * nz;
   const long long zoff = (long long)zz * 4096;
   const int tid = threadIdx.x;
   const int lane = tid & 31, warp = tid >> 5;
@@ -169,14 +172,14 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
   const bool pair = (m2 < n);  // a stored partner plane is needed
   const uint64_t pol_first = l2_policy_first();
   if (tid == 0) {
-    // E rows z*64 + y of a 4096-row tensor; history rows (m2*64 + z)*64 + y
+    // E rows z*64 + y of a 64 nz-row tensor; history rows (m2*nz + z)*64 + y
     mbar_init(&s_bar, 1);
     mbar_expect_tx(&s_bar, pair ? 65536u : 32768u);
     const uint64_t pol_last = l2_policy_last();
     for (int b = 0; b < 4; b++) tma_load_2d(Es + b * 1024, &T.tmE[ii], 32 * b, zz * 64, &s_bar, pol_last);
     if (pair)
       for (int b = 0; b < 4; b++)
-        tma_load_2d(Hs + b * 1024, &T.tmH[ii], 32 * b, (m2 * 64 + zz) * 64, &s_bar, pol_first);
+        tma_load_2d(Hs + b * 1024, &T.tmH[ii], 32 * b, (m2 * nz + zz) * 64, &s_bar, pol_first);
   }
   // accumulators of a paired step, loaded now so that their latency overlaps
   // the inverse transforms (row-phase ownership, as they are used)
@@ -199,11 +202,11 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
     double a = 0.0;
     if (n > 0) {
       const double *pp = P.part + (long long)(warp * N + n - 1) * nz;
-      a = pp[lane] + pp[lane + 32];
+      for (int z = lane; z < nz; z += 32) a += pp[z];
     }
     for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
     if (lane == 0) {
-      const double ma = a * (1.0 / (double)M);  // M = 2^18: exact
+      const double ma = NZ ? a * (1.0 / (double)M) : a / (double)M;  // 2^18 when NZ = 64: exact
       int ea = 0;
       if (n > 0 && isfinite(ma) && ma > 0.0) frexp(ma, &ea);
       s_exp[warp] = ea;
@@ -389,12 +392,13 @@ __global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__
 }
 
 cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
-                               const void *tw64, int n, int *err, cudaStream_t st) {
+                               int nz, const void *tw64, int n, int *err, cudaStream_t st) {
   if (ninst <= 0) return cudaSuccess;
   const int smem = 1024 + 2 * 4096 * (int)sizeof(float2) + kPlanePad * (int)sizeof(float2);
-  cudaError_t e = cudaFuncSetAttribute(k_mix_plane64, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  auto kfn = (nz == 64) ? k_mix_plane64<64> : k_mix_plane64<0>;
+  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(k_mix_plane64, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  e = cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e != cudaSuccess) return e;
   for (int i0 = 0; i0 < ninst; i0 += kMix64MaxInst) {
     const int cnt = ninst - i0 < kMix64MaxInst ? ninst - i0 : kMix64MaxInst;
@@ -406,7 +410,8 @@ cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, con
       T.tmH[k] = tmH[i0 + k];
     }
     T.err = err;
-    k_mix_plane64<<<64 * cnt, 512, smem, st>>>(T, reinterpret_cast<const float2 *>(tw64), n);
+    T.nz = nz;
+    kfn<<<nz * cnt, 512, smem, st>>>(T, reinterpret_cast<const float2 *>(tw64), n);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
   }

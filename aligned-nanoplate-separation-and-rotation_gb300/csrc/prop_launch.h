@@ -35,10 +35,11 @@ struct Mix64Table {
   CUtensorMap tmH[kMix64MaxInst];  // hist32 as 4096 (hmax + 1) rows x 128 floats, same boxes
   MixInst inst[kMix64MaxInst];
   int *err;                        // set to 1 when an mbarrier wait runs out
+  int nz;                          // z planes per instance (64 x 64 xy planes)
 };
-// insts, tmE, tmH: host arrays of the active instances in job order (64 CTAs each)
+// insts, tmE, tmH: host arrays of the active instances in job order (nz CTAs each)
 cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
-                               const void *tw64, int n, int *err, cudaStream_t st);
+                               int nz, const void *tw64, int n, int *err, cudaStream_t st);
 // tx: x columns per CTA (8, 16 or 32); jobs must be built for that width
 cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw64, int nx, int ny, int tx,
                              cudaStream_t st);

@@ -76,12 +76,14 @@ SEPARATIONS = tuple(round(0.14 + 0.04 * k, 2) for k in range(9))
 
 
 def separation9(precision=PREC_MIXED):
-    """Config 3: two parallel plates (theta = 0) at centre separations
-    d = 0.14 .. 0.46 of the long box side, N = 100, chiN = 20.  The long axis
-    is y, as in the reference's particle-separation sweep (separation along
-    L_y): grid 64 x 128 x 64, box 6.4 x 12.8 x 6.4 Rg."""
-    return [plate_params(0.0, grid=(64, 128, 64), box_rg=(6.4, 12.8, 6.4), precision=precision,
-                         centers=((0.5, 0.5 - d / 2, 0.5), (0.5, 0.5 + d / 2, 0.5))) for d in SEPARATIONS]
+    """Config 3: two parallel plates (theta = 0, normal along x) at centre
+    separations d = 0.14 .. 0.46 of the long box side, N = 100, chiN = 20, on
+    a 64 x 64 x 128 grid (box 6.4 x 6.4 x 12.8 Rg) with the separation along
+    the long axis z, perpendicular to the plate normal as in the reference's
+    particle-separation sweep (there along L_y; the disc is symmetric about
+    its normal, so the two set-ups are the same up to a rotation)."""
+    return [plate_params(0.0, grid=(64, 64, 128), box_rg=(6.4, 6.4, 12.8), precision=precision,
+                         centers=((0.5, 0.5, 0.5 - d / 2), (0.5, 0.5, 0.5 + d / 2))) for d in SEPARATIONS]
 
 
 def large_grafted8(precision=PREC_MIXED):
@@ -110,7 +112,7 @@ WORKLOADS = {
     "sweep15_64_N100_shell": lambda prec: [plate_params(t, precision=prec, shell=True) for t in SWEEP_ANGLES],
     "sweep15_64_N100": lambda prec: sweep15(precision=prec),
     "sweep15_mixed_sizes": lambda prec: sweep15_mixed_sizes(precision=prec),
-    "sep9_64x128x64_N100": lambda prec: separation9(precision=prec),
+    "sep9_64x64x128_N100": lambda prec: separation9(precision=prec),
     "graft8_128x128x256_N200": lambda prec: large_grafted8(precision=prec),
 }
 

@@ -128,11 +128,15 @@ def test_mixed_range_normalisation_long_chain(scft):
     assert rel(d32[0][0].real, d64[0][0].real) < 1e-3
 
 
-def test_mixed_64cubed_specialised_kernels_match_fp64(scft):
-    """All-64^3 batches take the specialised 64-point kernels; uneven N."""
+@pytest.mark.parametrize("nz", [64, 32, 128])
+def test_mixed_64cubed_specialised_kernels_match_fp64(scft, nz):
+    """Batches of 64 x 64 xy planes take the specialised 64-point plane pass
+    (and, for nz = 64, the 64-point z pass); uneven N."""
     from scft.workloads import plate_params, seeded_fields
 
-    params = [plate_params(10.0, N=20), plate_params(45.0, N=13)]
+    box = (6.4, 6.4, 6.4 * nz / 64)
+    params = [plate_params(10.0, N=20, grid=(64, 64, nz), box_rg=box),
+              plate_params(45.0, N=13, grid=(64, 64, nz), box_rg=box)]
     fields = [seeded_fields(p, 20 + k) for k, p in enumerate(params)]
     (H64, d64, _), (H32, d32, _) = run_pair(scft, params, fields, 3)
     for k in range(len(params)):
