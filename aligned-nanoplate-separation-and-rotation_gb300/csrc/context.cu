@@ -1123,7 +1123,8 @@ void build_jobs(scft_ctx *c) {
     for (auto &I : c->inst)
       if (I.p.Nx[0] != 64 || I.p.Nx[1] != 64 || I.p.Nx[2] != c->inst[0].p.Nx[2]) c->xy64 = 0;
     c->all64 = c->xy64 && c->inst[0].p.Nx[2] == 64;
-    if (c->all64) {
+    c->colfast = c->xy64 && (c->inst[0].p.Nx[2] == 64 || c->inst[0].p.Nx[2] == 128);
+    if (c->colfast) {
       for (int t = 0; t < 3; t++) {
         const int tx = 8 << t;
         std::vector<ColJob> cj64;
@@ -1399,9 +1400,10 @@ void mix_group_chain(scft_ctx *c, int g, cudaStream_t sg, bool update) {
     const int cnt = clampc(c->prop_pj_count[s], gr.pj_begin, gr.pj_end);
     if (cnt <= 0) break;
     if (s > 0) {
-      if (c->all64) {
+      if (c->colfast) {
+        const int nzi = c->inst[0].p.Nx[2];
         const int per = 64 * (64 / c->col64_tx);  // z-pass jobs per instance
-        LK(launch_mix_col64(col64_jobs(c) + (size_t)gr.inst_begin * per, (cnt / 64) * per, c->d_tw32_64, 64, 64,
+        LK(launch_mix_col64(col64_jobs(c) + (size_t)gr.inst_begin * per, (cnt / nzi) * per, c->d_tw32_z, 64, 64, nzi,
                             c->col64_tx, sg));
       } else {
         const int cc = clampc(c->prop_cj_count[s], gr.cj_begin, gr.cj_end);
@@ -1504,6 +1506,10 @@ void ctx_create(scft_ctx *c, const scft_params *params, int n_inst) {
   for (size_t t = 0; t < tw.size(); t++) tw32[t] = make_float2((float)tw[t].x, (float)tw[t].y);
   c->d_tw32 = dupload(c, tw32);
   if (off.count(64)) c->d_tw32_64 = static_cast<float2 *>(c->d_tw32) + off[64];
+  {
+    const int nz0 = c->inst.empty() ? 0 : c->inst[0].p.Nx[2];
+    if (off.count(nz0)) c->d_tw32_z = static_cast<float2 *>(c->d_tw32) + off[nz0];
+  }
   c->d_geoms = dupload(c, c->geoms);
   for (auto &I : c->inst) setup_plates(c, I);
   build_jobs(c);
@@ -1603,7 +1609,7 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
   std::vector<int> gs, txs;
   for (int g : {1, 2, 3, 4, 5, 6, 8})
     if (g <= n) gs.push_back(g);
-  if (c->all64)
+  if (c->colfast)
     txs = {8, 16, 32};
   else
     txs = {c->col64_tx};
@@ -1647,7 +1653,7 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
   }
   *groups_out = bg;
   *phases_out = bp;
-  *tx_out = c->all64 ? bt : 0;
+  *tx_out = c->colfast ? bt : 0;
   *ms_out = best;
 }
 
@@ -1676,9 +1682,9 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   }
   CK(cudaEventRecord(e1, c->st));
   for (int r = 0; r < reps; r++) {
-    if (c->mixed && c->all64)
-      LK(launch_mix_col64(col64_jobs(c), c->prop_pj_count[s] * (64 / c->col64_tx), c->d_tw32_64, 64, 64,
-                          c->col64_tx, c->st));
+    if (c->mixed && c->colfast)
+      LK(launch_mix_col64(col64_jobs(c), (c->prop_pj_count[s] / c->inst[0].p.Nx[2]) * 64 * (64 / c->col64_tx),
+                          c->d_tw32_z, 64, 64, c->inst[0].p.Nx[2], c->col64_tx, c->st));
     else if (c->mixed)
       LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw32, 3, 1, c->st));
     else
@@ -1701,7 +1707,7 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
       // the FP32 accumulators A and B (2 x 8 B); column: read + write z, plus
       // the h table in the generic pass (the 64-point pass forms h on the fly)
       bp += I.M * (4.0 * sizeof(float2) + 4.0 * sizeof(float));
-      bc += I.M * (2.0 * sizeof(float2) + (c->all64 ? 0.0 : sizeof(float)));
+      bc += I.M * (2.0 * sizeof(float2) + (c->colfast ? 0.0 : sizeof(float)));
     } else {
       const double props = I.single ? 1.0 : 2.0;
       bp += props * I.M * 6.0 * sizeof(double2);

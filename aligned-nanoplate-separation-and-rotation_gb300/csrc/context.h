@@ -106,6 +106,8 @@ struct scft_ctx {
   int mixed = 0;
   int all64 = 0;         // every instance is 64^3: specialised plane and z passes
   int xy64 = 0;          // every instance has 64 x 64 xy planes and the same nz: specialised plane pass
+  int colfast = 0;       // xy64 with nz = 64 or 128: specialised z pass
+  void *d_tw32_z = nullptr;  // twiddles of that nz
   void *d_tw32_64 = nullptr;  // the 64-point twiddle table inside d_tw32
   void *d_tw32 = nullptr;
   scft::ColJob *d_mix64_cj_tx[3] = {};  // z-pass jobs of the 64^3 kernels for 8, 16, 32 columns per CTA

@@ -391,6 +391,96 @@ __global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__
   for (int j = 0; j < 8; j++) a[(t + 8 * j) * plane + base] = v[j];
 }
 
+// z pass for nz = 128, same contract as k_mix_col64: 8 threads per column,
+// thread t holding the 16 values x[t + 8a].  128 = 8 x 16:
+//   Y[t][c]  = sum_a x[t + 8a] w16^(a c)          (DFT16 in registers, 4 x 4)
+//   Y[t][c] *= w128^(t c)
+//   exchange through shared memory: thread t takes c = t and c = t + 8
+//   X[c + 16 d] = sum_b Y[b][c] w8^(b d)          (two DFT8)
+// which returns X[t + 8m] in v[m], the input order, so the same routine runs
+// both directions.
+template <int SIGN> __device__ __forceinline__ void dft16f(float2 *v, const float2 *tw128) {
+  // n = a + 4b, k = c + 4d: DFT4 over b, twiddle w16^(a c) = w128^(8 a c), DFT4 over a
+  float2 z[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+#pragma unroll
+    for (int b = 0; b < 4; b++) z[a][b] = v[a + 4 * b];
+    Dft<4, SIGN, float2>::run(z[a]);
+  }
+#pragma unroll
+  for (int a = 1; a < 4; a++)
+#pragma unroll
+    for (int c = 1; c < 4; c++) z[a][c] = ctw<SIGN>(z[a][c], tw128[8 * a * c]);
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    float2 u[4] = {z[0][c], z[1][c], z[2][c], z[3][c]};
+    Dft<4, SIGN, float2>::run(u);
+#pragma unroll
+    for (int d = 0; d < 4; d++) v[c + 4 * d] = u[d];
+  }
+}
+
+template <int SIGN>
+__device__ __forceinline__ void fft128_group(float2 *v, int t, float2 *xch, int sb, int sc, const float2 *tw) {
+  dft16f<SIGN>(v, tw);
+#pragma unroll
+  for (int c = 1; c < 16; c++) v[c] = ctw<SIGN>(v[c], tw[t * c]);
+#pragma unroll
+  for (int c = 0; c < 16; c++) xch[t * sb + c * sc] = v[c];
+  __syncthreads();
+  float2 p[8], q[8];
+#pragma unroll
+  for (int b = 0; b < 8; b++) {
+    p[b] = xch[b * sb + t * sc];
+    q[b] = xch[b * sb + (t + 8) * sc];
+  }
+  __syncthreads();
+  dft8f<SIGN>(p);
+  dft8f<SIGN>(q);
+#pragma unroll
+  for (int d = 0; d < 8; d++) {
+    v[2 * d] = p[d];
+    v[2 * d + 1] = q[d];
+  }
+}
+
+template <int TX>
+__global__ void __launch_bounds__(8 * TX) k_mix_col128(const ColJob *__restrict__ jobs,
+                                                       const float2 *__restrict__ tw_g, int nx, int ny, float s_hi,
+                                                       float s_lo) {
+  __shared__ __align__(16) float2 buf[128 * TX];
+  __shared__ float2 tw[128];
+  const ColJob jb = jobs[blockIdx.x];
+  const int tid = threadIdx.x;
+  const int col = tid % TX, t = tid / TX;
+  for (int k = tid; k < 128; k += 8 * TX) tw[k] = tw_g[k];
+  const long long plane = (long long)nx * ny;
+  const long long base = (long long)jb.y * nx + jb.x0 + col;
+  float2 *a = reinterpret_cast<float2 *>(jb.ptr);
+  const float *ht = reinterpret_cast<const float *>(jb.kern);
+  const float hx = ht[jb.x0 + col], hy = ht[nx + jb.y];
+  const float hxy = fmaf(-hx, hy, hx + hy);
+  float2 v[16];
+#pragma unroll
+  for (int j = 0; j < 16; j++) v[j] = a[(t + 8 * j) * plane + base];
+  __syncthreads();  // tw
+  fft128_group<-1>(v, t, buf + col, 16 * TX, TX, tw);
+#pragma unroll
+  for (int d = 0; d < 16; d++) {
+    const int kz = t + 8 * d;
+    const float hz = ht[nx + ny + kz];
+    const float hv = fmaf(-hxy, hz, hxy + hz);
+    float2 u = make_float2(fmaf(v[d].x, s_hi, v[d].x * s_lo), fmaf(v[d].y, s_hi, v[d].y * s_lo));
+    u = make_float2(fmaf(-hv, u.x, u.x), fmaf(-hv, u.y, u.y));
+    if (kz == 0 && jb.y == 0 && jb.x0 + col == 0) u = make_float2(0.f, 0.f);
+    v[d] = u;
+  }
+  fft128_group<+1>(v, t, buf + col, 16 * TX, TX, tw);
+#pragma unroll
+  for (int j = 0; j < 16; j++) a[(t + 8 * j) * plane + base] = v[j];
+}
+
 cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
                                int nz, const void *tw64, int n, int *err, cudaStream_t st) {
   if (ninst <= 0) return cudaSuccess;
@@ -418,16 +508,26 @@ cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, con
   return cudaSuccess;
 }
 
-cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw64, int nx, int ny, int tx,
+cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw, int nx, int ny, int nz, int tx,
                              cudaStream_t st) {
   if (njobs <= 0) return cudaSuccess;
-  const double s = 1.0 / ((double)nx * ny * 64);
+  const double s = 1.0 / ((double)nx * ny * nz);
   const float s_hi = (float)s, s_lo = (float)(s - (double)s_hi);
-  const float2 *tw = reinterpret_cast<const float2 *>(tw64);
+  const float2 *t2 = reinterpret_cast<const float2 *>(tw);
+  if (nz == 128) {
+    switch (tx) {
+      case 8: k_mix_col128<8><<<njobs, 64, 0, st>>>(jobs, t2, nx, ny, s_hi, s_lo); break;
+      case 16: k_mix_col128<16><<<njobs, 128, 0, st>>>(jobs, t2, nx, ny, s_hi, s_lo); break;
+      case 32: k_mix_col128<32><<<njobs, 256, 0, st>>>(jobs, t2, nx, ny, s_hi, s_lo); break;
+      default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+  }
+  if (nz != 64) return cudaErrorInvalidValue;
   switch (tx) {
-    case 8: k_mix_col64<8><<<njobs, 64, 0, st>>>(jobs, tw, nx, ny, s_hi, s_lo); break;
-    case 16: k_mix_col64<16><<<njobs, 128, 0, st>>>(jobs, tw, nx, ny, s_hi, s_lo); break;
-    case 32: k_mix_col64<32><<<njobs, 256, 0, st>>>(jobs, tw, nx, ny, s_hi, s_lo); break;
+    case 8: k_mix_col64<8><<<njobs, 64, 0, st>>>(jobs, t2, nx, ny, s_hi, s_lo); break;
+    case 16: k_mix_col64<16><<<njobs, 128, 0, st>>>(jobs, t2, nx, ny, s_hi, s_lo); break;
+    case 32: k_mix_col64<32><<<njobs, 256, 0, st>>>(jobs, t2, nx, ny, s_hi, s_lo); break;
     default: return cudaErrorInvalidValue;
   }
   return cudaGetLastError();

@@ -40,8 +40,9 @@ struct Mix64Table {
 // insts, tmE, tmH: host arrays of the active instances in job order (nz CTAs each)
 cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
                                int nz, const void *tw64, int n, int *err, cudaStream_t st);
-// tx: x columns per CTA (8, 16 or 32); jobs must be built for that width
-cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw64, int nx, int ny, int tx,
+// z pass of the 64 x 64-plane instances for nz = 64 or 128 (tw: the nz-point
+// twiddles); tx: x columns per CTA (8, 16 or 32); jobs built for that width
+cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw, int nx, int ny, int nz, int tx,
                              cudaStream_t st);
 cudaError_t launch_mix_graft_plane(const LaunchShape &ls, const PropJob *jobs, int njobs, const GraftMixInst *insts,
                                    const DevGeom *geoms, const void *tw, int sweep, int n, cudaStream_t st);

@@ -376,8 +376,10 @@ def main():
 
     # ---- dominant kernel, isolated (after the timed regions)
     prof = ctx.profile_step(20)
-    all64 = all(tuple(p.Nx) == (64, 64, 64) for p in params)
-    kernel_names = {"mixed": ("k_mix_plane64", "k_mix_col64") if all64 else ("k_mix_prop_plane", "k_col_fft<float>"),
+    nz0 = params[0].Nx[2]
+    xy64 = all(p.Nx[0] == 64 and p.Nx[1] == 64 and p.Nx[2] == nz0 for p in params)
+    col_fast = {64: "k_mix_col64", 128: "k_mix_col128"}.get(nz0) if xy64 else None
+    kernel_names = {"mixed": ("k_mix_plane64" if xy64 else "k_mix_prop_plane", col_fast or "k_col_fft<float>"),
                     "plain": ("k_prop_plane_f64", "k_col_fft<double> (bond kernel)")}
     hbm, peak_kind = peaks()
     dom = "plane" if prof["ms_plane"] >= prof["ms_col"] else "col"
