@@ -23,6 +23,7 @@ void ctx_diblock_density(scft_ctx *c, int k, const double *smwa, const double *s
 void ctx_override_nD(scft_ctx *c, int k, double nD);
 int ctx_grad_geom(scft_ctx *c, double *out);
 void ctx_set_sweep_groups(scft_ctx *c, int groups, int phases);
+void ctx_set_fields_all(scft_ctx *c, const double *const *w);
 void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *tx_out, double *ms_out);
 void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
                       double *bytes_col);
@@ -95,6 +96,15 @@ int scft_set_fields(scft_ctx *c, int inst, const double *w) {
   if (int s = check_ctx(c, inst)) return s;
   if (!w) return fail(SCFT_ERR_ARG, "null field buffer");
   API_BODY(scft::ctx_set_fields(c, inst, w));
+  return SCFT_OK;
+}
+
+int scft_set_fields_all(scft_ctx *c, const double *const *w) {
+  if (int s = check_ctx(c, 0)) return s;
+  if (!w) return fail(SCFT_ERR_ARG, "null field buffers");
+  for (size_t k = 0; k < c->inst.size(); k++)
+    if (!w[k]) return fail(SCFT_ERR_ARG, "null field buffer");
+  API_BODY(scft::ctx_set_fields_all(c, w));
   return SCFT_OK;
 }
 

@@ -442,7 +442,9 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
 
   // device arrays
   I.mixed = (p.precision == SCFT_PREC_MIXED);
-  for (int f = 0; f < 7; f++) I.w[f] = dalloc<double2>(c, M);
+  // the seven fields in one allocation, in scft_set_fields' order: one copy per instance
+  I.w[0] = dalloc<double2>(c, 7 * (size_t)M);
+  for (int f = 1; f < 7; f++) I.w[f] = I.w[0] + (size_t)f * M;
   for (int f = 0; f < 3; f++) I.rho[f] = dalloc<double2>(c, M);
   if (p.do_cl) {
     // noise arrays of code/1s_update.cpp:54-319: w+, then (+, -) of each pair with chi != 0
@@ -928,6 +930,22 @@ void build_jobs(scft_ctx *c) {
   }
   c->d_fi = dupload(c, fi);
   c->h_fi = fi;
+  if (c->inst[0].mixed) {  // (c->mixed is set further down)
+    // scft_set_fields: check results, instance mask, job staging for the
+    // forward transforms of up to all seven fields of every instance
+    c->d_realout = dalloc<double>(c, 128 * (size_t)n);
+    c->d_skip = dalloc<int>(c, n);
+    size_t jobs = 0;
+    for (auto &I : c->inst) {
+      const DevGeom &g = c->geoms[I.geom];
+      jobs += 7 * (size_t)std::max(g.nz, g.ny * (g.nx / g.tx));
+    }
+    c->jobs_cap = 2 * jobs * std::max(sizeof(PlaneJob), sizeof(ColJob));
+    c->d_jobs = dalloc<char>(c, c->jobs_cap);
+    CK(cudaMallocHost(&c->h_jobs, c->jobs_cap));
+    CK(cudaMallocHost(&c->h_skip, sizeof(int) * (size_t)n));
+  }
+  if (!c->h_pin) CK(cudaMallocHost(&c->h_pin, 128 * sizeof(double) * (size_t)std::max(1, n)));
   c->d_pi = dupload(c, pi);
   c->mixed = c->inst[0].mixed;
   for (auto &I : c->inst)
@@ -1200,73 +1218,53 @@ void build_jobs(scft_ctx *c) {
 }
 
 // Largest |Im| and |Re| of w_A and w_B over the grid (mixed form input check).
-__global__ void k_real_check(const double2 *const *w, long long M, int neg_ab, int neg_bc, int neg_ac, int graft,
-                             double *out) {
-  __shared__ double ri[32], rr[32];
-  double mi = 0.0, mr = 0.0;
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
-    const double2 pl = w[0][i], abp = w[1][i], abm = w[2][i], bcp = w[3][i], bcm = w[4][i], acp = w[5][i],
-                  acm = w[6][i];
-    // imaginary parts of w_A, w_B (code/calc_poly_density.cpp:45-50)
+// Realness check of the mixed form's fields of every instance (blockIdx.y),
+// from its FieldInst (code/calc_poly_density.cpp:45-54): per block, out[9 b] =
+// max |Im w_A|, |Im w_B| (and |Im w_G| with grafts), out[9 b + 1] = the
+// largest real part, out[9 b + 2 + f] = max |w_f|; out advances by 128 per
+// instance.  Instances with skip[inst] = 0 are checked.
+__global__ void k_real_check_all(const FieldInst *__restrict__ fi, const int *__restrict__ skip, double *out) {
+  const FieldInst &F = fi[blockIdx.y];
+  if (skip && skip[blockIdx.y]) return;
+  __shared__ double red[9][32];
+  double m[9];
+  for (int k = 0; k < 9; k++) m[k] = 0.0;
+  const int neg_ab = F.neg_ab, neg_bc = F.neg_bc, neg_ac = F.neg_ac;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < F.M; i += (long long)gridDim.x * blockDim.x) {
+    const double2 pl = F.w[0][i], abp = F.w[1][i], abm = F.w[2][i], bcp = F.w[3][i], bcm = F.w[4][i],
+                  acp = F.w[5][i], acm = F.w[6][i];
     const double ia = pl.x + (neg_ab ? abm.x - abp.y : abp.x - abm.y) + (neg_ac ? acm.x - acp.y : acp.x - acm.y);
     const double ib = pl.x + (neg_ab ? -abm.x - abp.y : abp.x + abm.y) + (neg_bc ? bcm.x - bcp.y : bcp.x - bcm.y);
     const double ra = -pl.y + (neg_ab ? -abm.y - abp.x : -abp.y - abm.x) + (neg_ac ? -acm.y - acp.x : -acp.y - acm.x);
     const double rb = -pl.y + (neg_ab ? abm.y - abp.x : -abp.y + abm.x) + (neg_bc ? -bcm.y - bcp.x : -bcp.y - bcm.x);
-    mi = fmax(mi, fmax(fabs(ia), fabs(ib)));
-    mr = fmax(mr, fmax(fabs(ra), fabs(rb)));
-    if (graft) {  // w_G (code/calc_poly_density.cpp:51-54)
+    m[0] = fmax(m[0], fmax(fabs(ia), fabs(ib)));
+    m[1] = fmax(m[1], fmax(fabs(ra), fabs(rb)));
+    if (F.graft) {  // w_G (code/calc_poly_density.cpp:51-54)
       const double ig = pl.x + (neg_ac ? -acm.x - acp.y : acp.x + acm.y) + (neg_bc ? -bcm.x - bcp.y : bcp.x + bcm.y);
       const double rg = -pl.y + (neg_ac ? acm.y - acp.x : -acp.y + acm.x) + (neg_bc ? bcm.y - bcp.x : -bcp.y + bcm.x);
-      mi = fmax(mi, fabs(ig));
-      mr = fmax(mr, fabs(rg));
+      m[0] = fmax(m[0], fabs(ig));
+      m[1] = fmax(m[1], fabs(rg));
     }
-  }
-  for (int o = 16; o > 0; o >>= 1) {
-    mi = fmax(mi, __shfl_down_sync(0xffffffffu, mi, o));
-    mr = fmax(mr, __shfl_down_sync(0xffffffffu, mr, o));
+    const double2 all[7] = {pl, abp, abm, bcp, bcm, acp, acm};
+    for (int f = 0; f < 7; f++) m[2 + f] = fmax(m[2 + f], fmax(fabs(all[f].x), fabs(all[f].y)));
   }
   const int wp = threadIdx.x >> 5, l = threadIdx.x & 31;
-  if (l == 0) { ri[wp] = mi; rr[wp] = mr; }
+  for (int k = 0; k < 9; k++) {
+    double v = m[k];
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    if (l == 0) red[k][wp] = v;
+  }
   __syncthreads();
   if (wp == 0) {
-    mi = l < (int)(blockDim.x >> 5) ? ri[l] : 0.0;
-    mr = l < (int)(blockDim.x >> 5) ? rr[l] : 0.0;
-    for (int o = 16; o > 0; o >>= 1) {
-      mi = fmax(mi, __shfl_down_sync(0xffffffffu, mi, o));
-      mr = fmax(mr, __shfl_down_sync(0xffffffffu, mr, o));
-    }
-    if (l == 0) {
-      out[2 * blockIdx.x] = mi;
-      out[2 * blockIdx.x + 1] = mr;
+    for (int k = 0; k < 9; k++) {
+      double v = l < (int)(blockDim.x >> 5) ? red[k][l] : 0.0;
+      for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+      if (l == 0) out[128 * (size_t)blockIdx.y + 9 * blockIdx.x + k] = v;
     }
   }
 }
 
-void check_real_fields(scft_ctx *c, int k) {
-  Instance &I = c->inst[k];
-  const double2 **dw = nullptr;
-  double *dout = nullptr;
-  const int nb = 64;
-  CK(cudaMalloc(&dw, sizeof(double2 *) * 7));
-  CK(cudaMalloc(&dout, sizeof(double) * 2 * nb));
-  CK(cudaMemcpyAsync(dw, I.w, sizeof(double2 *) * 7, cudaMemcpyHostToDevice, c->st));
-  k_real_check<<<nb, 256, 0, c->st>>>(dw, I.M, I.neg_ab, I.neg_bc, I.neg_ac, I.graft, dout);
-  std::vector<double> h(2 * nb);
-  cudaError_t e = cudaGetLastError();
-  if (e == cudaSuccess) e = cudaMemcpyAsync(h.data(), dout, sizeof(double) * 2 * nb, cudaMemcpyDeviceToHost, c->st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(c->st);
-  cudaFree(dw);
-  cudaFree(dout);
-  CK(e);
-  double mi = 0.0, mr = 0.0;
-  for (int b = 0; b < nb; b++) {
-    mi = std::max(mi, h[2 * b]);
-    mr = std::max(mr, h[2 * b + 1]);
-  }
-  if (mi > 1e-12 * std::max(1.0, mr))
-    throw ScftError(SCFT_ERR_COMPLEX, "mixed precision needs real w_A, w_B (and w_G with grafts): the mean-field "
-                                      "phase convention");
-}
+
 
 // CK plus one kernel launch on the context's counter
 #define LK(x)        \
@@ -1518,20 +1516,54 @@ void ctx_create(scft_ctx *c, const scft_params *params, int n_inst) {
 
 void ctx_destroy(scft_ctx *c) {
   if (c->g_update) cudaGraphExecDestroy(c->g_update);
+  if (c->g_density) cudaGraphExecDestroy(c->g_density);
   for (void *p : c->allocs) cudaFree(p);
   for (cudaStream_t sst : c->side) cudaStreamDestroy(sst);
   for (auto &I : c->inst)
     if (I.eta_host) cudaFreeHost(I.eta_host);
+  if (c->h_pin) cudaFreeHost(c->h_pin);
+  if (c->h_jobs) cudaFreeHost(c->h_jobs);
+  if (c->h_skip) cudaFreeHost(c->h_skip);
   for (cudaEvent_t ev : c->ev_join) cudaEventDestroy(ev);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->st) cudaStreamDestroy(c->st);
 }
 
+// calc_poly_density of every instance.  The first build runs eagerly (kernel
+// attributes get set); later builds replay a captured graph, as update_1s
+// does: a batch's density build is over a thousand launches.
 void ctx_poly_density(scft_ctx *c) {
-  if (c->mixed)
-    seq_mix_density(c);
-  else
-    seq_poly_density(c);
+  auto body = [c]() {
+    if (c->mixed)
+      seq_mix_density(c);
+    else
+      seq_poly_density(c);
+  };
+  if (c->g_density) {
+    CK(cudaGraphLaunch(c->g_density, c->st));
+    c->launches += c->launches_per_density;
+  } else if (!c->density_runs) {
+    body();
+  } else {
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+    const long long before = c->launches;
+    try {
+      body();
+      c->launches_per_density = c->launches - before;
+      c->launches = before;
+    } catch (...) {
+      cudaGraph_t g2;
+      cudaStreamEndCapture(c->st, &g2);
+      throw;
+    }
+    CK(cudaStreamEndCapture(c->st, &graph));
+    CK(cudaGraphInstantiate(&c->g_density, graph, 0));
+    cudaGraphDestroy(graph);
+    CK(cudaGraphLaunch(c->g_density, c->st));
+    c->launches += c->launches_per_density;
+  }
+  c->density_runs++;
   CK(cudaStreamSynchronize(c->st));
   check_device_error(c);
   c->dirty_density = 0;
@@ -1587,6 +1619,10 @@ void ctx_set_sweep_groups(scft_ctx *c, int groups, int phases) {
   if (c->g_update) {  // the captured iteration holds the old launch chains
     CK(cudaGraphExecDestroy(c->g_update));
     c->g_update = nullptr;
+  }
+  if (c->g_density) {
+    CK(cudaGraphExecDestroy(c->g_density));
+    c->g_density = nullptr;
   }
 }
 
@@ -1650,6 +1686,10 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
   if (c->g_update) {
     CK(cudaGraphExecDestroy(c->g_update));
     c->g_update = nullptr;
+  }
+  if (c->g_density) {
+    CK(cudaGraphExecDestroy(c->g_density));
+    c->g_density = nullptr;
   }
   *groups_out = bg;
   *phases_out = bp;
@@ -1772,17 +1812,87 @@ int ctx_calc_H(scft_ctx *c, double *out) {
   return status;
 }
 
-void ctx_set_fields(scft_ctx *c, int k, const double *w) {
-  Instance &I = c->inst[k];
-  for (int f = 0; f < 7; f++)
-    CK(cudaMemcpyAsync(I.w[f], w + (size_t)f * 2 * I.M, sizeof(double2) * I.M, cudaMemcpyHostToDevice, c->st));
-  if (I.mixed) {
-    // the packed transforms need real w_A, w_B (the mean-field phase convention)
-    check_real_fields(c, k);
-    fft3d_arrays(c, I, std::vector<double2 *>(I.w, I.w + 7), -1);
-  }
-  CK(cudaStreamSynchronize(c->st));
+// scft_set_fields of one instance or of all: one copy per instance (the seven
+// fields are contiguous on both sides), one realness check launch over the
+// instances, one synchronisation (the caller may reuse its buffers, the check
+// result is on the host), then one batched forward transform of the nonzero
+// fields (zero fields are transforms of themselves), left to run on the
+// stream.  SCFT_ERR_COMPLEX leaves the instance's fields undefined until its
+// next successful call.
+static constexpr int kCheckBlocks = 14;
+
+static void set_fields_ks(scft_ctx *c, const std::vector<int> &ks, const double *const *w) {
+  const int n = (int)c->inst.size();
   c->dirty_density = 1;
+  bool mixed = false;
+  for (size_t q = 0; q < ks.size(); q++) {
+    Instance &I = c->inst[ks[q]];
+    CK(cudaMemcpyAsync(I.w[0], w[q], sizeof(double2) * 7 * (size_t)I.M, cudaMemcpyHostToDevice, c->st));
+    mixed = mixed || I.mixed;
+  }
+  if (!mixed) {
+    CK(cudaStreamSynchronize(c->st));
+    return;
+  }
+  if (!c->h_skip || !c->h_jobs || !c->d_realout || !c->h_pin)
+    throw ScftError(SCFT_ERR_CUDA, "scft_set_fields: staging buffers missing");
+  // check only the instances in ks
+  for (int k = 0; k < n; k++) c->h_skip[k] = 1;
+  for (int k : ks) c->h_skip[k] = 0;
+  CK(cudaMemcpyAsync(c->d_skip, c->h_skip, sizeof(int) * n, cudaMemcpyHostToDevice, c->st));
+  k_real_check_all<<<dim3(kCheckBlocks, n), 256, 0, c->st>>>(c->d_fi, c->d_skip, c->d_realout);
+  CK(cudaGetLastError());
+  for (int k : ks)
+    CK(cudaMemcpyAsync(c->h_pin + 128 * (size_t)k, c->d_realout + 128 * (size_t)k, sizeof(double) * 9 * kCheckBlocks,
+                       cudaMemcpyDeviceToHost, c->st));
+  CK(cudaStreamSynchronize(c->st));
+  std::vector<PlaneJob> pj;
+  std::vector<ColJob> cj;
+  std::string bad;
+  for (int k : ks) {
+    Instance &I = c->inst[k];
+    double m[9] = {};
+    for (int b = 0; b < kCheckBlocks; b++)
+      for (int q = 0; q < 9; q++) m[q] = std::max(m[q], c->h_pin[128 * (size_t)k + 9 * b + q]);
+    if (m[0] > 1e-12 * std::max(1.0, m[1])) {
+      if (bad.empty()) bad = std::to_string(k);
+      continue;
+    }
+    const DevGeom &g = c->geoms[I.geom];
+    for (int f = 0; f < 7; f++) {
+      if (m[2 + f] == 0.0) continue;
+      for (int z = 0; z < g.nz; z++) pj.push_back(PlaneJob{I.w[f], I.geom, z});
+      for (int y = 0; y < g.ny; y++)
+        for (int x0 = 0; x0 < g.nx; x0 += g.tx) cj.push_back(ColJob{I.w[f], nullptr, I.geom, x0, y});
+    }
+  }
+  if (!pj.empty()) {
+    // the job lists go through pinned staging (no synchronisation needed:
+    // the next call's writes to the staging come after a synchronisation)
+    memcpy(c->h_jobs, pj.data(), sizeof(PlaneJob) * pj.size());
+    memcpy(reinterpret_cast<char *>(c->h_jobs) + c->jobs_cap / 2, cj.data(), sizeof(ColJob) * cj.size());
+    CK(cudaMemcpyAsync(c->d_jobs, c->h_jobs, sizeof(PlaneJob) * pj.size(), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(reinterpret_cast<char *>(c->d_jobs) + c->jobs_cap / 2,
+                       reinterpret_cast<char *>(c->h_jobs) + c->jobs_cap / 2, sizeof(ColJob) * cj.size(),
+                       cudaMemcpyHostToDevice, c->st));
+    CK(launch_plane_fft<double>(c->shp_plane, reinterpret_cast<PlaneJob *>(c->d_jobs), (int)pj.size(), c->d_geoms,
+                                c->d_tw64, -1, 0, c->st));
+    CK(launch_col_fft<double>(c->shp_col,
+                              reinterpret_cast<ColJob *>(reinterpret_cast<char *>(c->d_jobs) + c->jobs_cap / 2),
+                              (int)cj.size(), c->d_geoms, c->d_tw64, 0, 1, c->st));
+  }
+  if (!bad.empty())
+    throw ScftError(SCFT_ERR_COMPLEX, "instance " + bad +
+                                          ": mixed precision needs real w_A, w_B (and w_G with grafts): the "
+                                          "mean-field phase convention");
+}
+
+void ctx_set_fields(scft_ctx *c, int k, const double *w) { set_fields_ks(c, {k}, &w); }
+
+void ctx_set_fields_all(scft_ctx *c, const double *const *w) {
+  std::vector<int> ks(c->inst.size());
+  for (size_t k = 0; k < ks.size(); k++) ks[k] = (int)k;
+  set_fields_ks(c, ks, w);
 }
 
 void ctx_get_fields(scft_ctx *c, int k, double *w) {

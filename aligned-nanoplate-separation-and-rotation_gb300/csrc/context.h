@@ -118,6 +118,13 @@ struct scft_ctx {
   std::vector<scft::MixInst> mix64_tab;  // instances in job order (64^3 plane pass)
   std::vector<CUtensorMap> tmE, tmH;      // their TMA descriptors (Boltzmann, history)
   int *d_err = nullptr;                   // error word of the plane pass
+  double *h_pin = nullptr;                // pinned read-back of the field checks (128 doubles per instance)
+  // scft_set_fields (mixed form): check results, instance mask, job staging
+  double *d_realout = nullptr;
+  int *d_skip = nullptr, *h_skip = nullptr;
+  char *d_jobs = nullptr;
+  void *h_jobs = nullptr;
+  size_t jobs_cap = 0;
   // The mixed sweep of a batch runs as `groups` independent chains of
   // launches on side streams (contiguous instance ranges in job order), so
   // that one group's column passes fill the last wave of another group's
@@ -154,6 +161,9 @@ struct scft_ctx {
   double2 *d_hpart = nullptr;
   int hblocks = 0;
   cudaGraphExec_t g_update = nullptr;
+  cudaGraphExec_t g_density = nullptr;  // captured density build (after the first, eager one)
+  long long launches_per_density = 0;
+  int density_runs = 0;
   long long launches = 0;            // kernel launches issued (graph replays included)
   long long launches_per_update = 0;  // kernels in one captured update_1s iteration
   int update_runs = 0;

@@ -26,7 +26,8 @@ EXPORTS = ("scft_last_error", "scft_version", "scft_create", "scft_destroy", "sc
            "scft_set_fields", "scft_get_fields", "scft_calc_poly_density", "scft_update_1s",
            "scft_calc_H", "scft_grad_geom", "scft_get_density", "scft_get_plate_density", "scft_get_smeared", "scft_diblock_density",
            "scft_homopolymer_density", "scft_fft3d", "scft_sync", "scft_get_stream", "scft_launch_count",
-           "scft_profile_step", "scft_diblock_density_noalloc", "scft_set_sweep_groups", "scft_autotune")
+           "scft_profile_step", "scft_diblock_density_noalloc", "scft_set_sweep_groups", "scft_autotune",
+           "scft_set_fields_all")
 
 
 class ScftError(RuntimeError):
@@ -102,6 +103,7 @@ def load(path: str | None = None):
     lib.scft_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
     lib.scft_profile_step.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
     lib.scft_set_sweep_groups.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    lib.scft_set_fields_all.argtypes = [vp, ctypes.POINTER(ctypes.c_void_p)]
     ip = ctypes.POINTER(ctypes.c_int)
     lib.scft_autotune.argtypes = [vp, ctypes.c_int, ip, ip, ip, dp]
     lib.scft_diblock_density_noalloc.argtypes = [ctypes.POINTER(ctypes.c_int), dp, ctypes.c_int, ctypes.c_int,
@@ -285,6 +287,11 @@ class Context:
         v = [ctypes.c_double() for _ in range(4)]
         _check(load().scft_profile_step(self._h, int(reps), *[ctypes.byref(x) for x in v]))
         return {"ms_plane": v[0].value, "bytes_plane": v[1].value, "ms_col": v[2].value, "bytes_col": v[3].value}
+
+    def set_fields_all_raw(self, ptrs):
+        """scft_set_fields_all from device-visible host pointers (one per instance)."""
+        arr = (ctypes.c_void_p * self.n)(*ptrs)
+        _check(load().scft_set_fields_all(self._h, arr))
 
     def set_fields_raw(self, inst, ptr: int):
         """set_fields from a host buffer given by address (7*M complex, e.g. pinned memory)."""

@@ -127,6 +127,12 @@ void scft_destroy(scft_ctx *ctx);
 
 int scft_get_info(scft_ctx *ctx, int inst, scft_info *info);
 
+/* scft_set_fields for every instance of the context in one call: w[inst]
+ * as for scft_set_fields.  The copies and checks of all instances are issued
+ * back to back with one synchronisation (the per-instance call waits once
+ * per instance).  No counterpart in the reference (one process per run). */
+int scft_set_fields_all(scft_ctx *ctx, const double *const *w);
+
 /* Sets/gets the seven fields of one instance: w[f*2*M + 2*i + {0,1}]. */
 int scft_set_fields(scft_ctx *ctx, int inst, const double *w);
 int scft_get_fields(scft_ctx *ctx, int inst, double *w);

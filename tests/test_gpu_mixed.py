@@ -221,3 +221,40 @@ def test_complex_langevin_is_fp64_only(scft):
     p = scft.make_params(precision=scft.PREC_MIXED, do_cl=1, cl_seed=3)
     with pytest.raises(scft.ScftError):
         scft.Context(p)
+
+
+def test_set_fields_all_matches_per_instance_calls(scft):
+    """scft_set_fields_all is the per-instance call for every instance at once:
+    identical densities and H; a complex field is reported with its instance."""
+    import torch
+
+    from scft.workloads import plate_params, seeded_fields
+
+    params = [plate_params(t, N=16, grid=(32, 32, 32), box_rg=(4.0, 4.0, 4.0), precision=scft.PREC_MIXED)
+              for t in (0.0, 30.0, 60.0)]
+    fields = [seeded_fields(p, 60 + k) for k, p in enumerate(params)]
+    bufs = []
+    for f in fields:
+        arr = np.stack([np.asarray(f.get(n, np.zeros((32, 32, 32))), np.complex128) for n in scft.FIELD_NAMES])
+        t = torch.zeros(arr.size * 2, dtype=torch.float64, pin_memory=True)
+        t.numpy()[:] = arr.view(np.float64).ravel()
+        bufs.append(t)
+    res = []
+    for batched in (False, True):
+        with scft.Context(params) as ctx:
+            if batched:
+                ctx.set_fields_all_raw([b.data_ptr() for b in bufs])
+            else:
+                for k, f in enumerate(fields):
+                    ctx.set_fields(k, f)
+            ctx.update_1s(2)
+            res.append((ctx.calc_H(), [ctx.density(k)[0] for k in range(3)]))
+    assert np.array_equal(res[0][0], res[1][0])
+    for a, b in zip(res[0][1], res[1][1]):
+        assert np.array_equal(a, b)
+    bad = bufs[1].numpy().copy()
+    bad[0] = 0.5  # real part of w+ at one point: w_A, w_B get an imaginary part
+    bt = torch.from_numpy(bad).pin_memory()
+    with scft.Context(params) as ctx:
+        with pytest.raises(scft.ScftError, match="instance 1"):
+            ctx.set_fields_all_raw([bufs[0].data_ptr(), bt.data_ptr(), bufs[2].data_ptr()])
