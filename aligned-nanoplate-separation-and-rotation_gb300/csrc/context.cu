@@ -1140,7 +1140,6 @@ void build_jobs(scft_ctx *c) {
     c->xy64 = 1;
     for (auto &I : c->inst)
       if (I.p.Nx[0] != 64 || I.p.Nx[1] != 64 || I.p.Nx[2] != c->inst[0].p.Nx[2]) c->xy64 = 0;
-    c->all64 = c->xy64 && c->inst[0].p.Nx[2] == 64;
     c->colfast = c->xy64 && (c->inst[0].p.Nx[2] == 64 || c->inst[0].p.Nx[2] == 128);
     if (c->colfast) {
       for (int t = 0; t < 3; t++) {

@@ -104,7 +104,6 @@ struct scft_ctx {
   int gblocks = 0;
   // mixed precision
   int mixed = 0;
-  int all64 = 0;         // every instance is 64^3: specialised plane and z passes
   int xy64 = 0;          // every instance has 64 x 64 xy planes and the same nz: specialised plane pass
   int colfast = 0;       // xy64 with nz = 64 or 128: specialised z pass
   void *d_tw32_z = nullptr;  // twiddles of that nz
