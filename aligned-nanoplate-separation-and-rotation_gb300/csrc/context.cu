@@ -475,8 +475,7 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
       I.hist[q] = dalloc<double2>(c, (size_t)M * (I.hmax + 1));
     }
   } else {
-    I.zr = dalloc<double2>(c, M);
-    I.zs = dalloc<double2>(c, M);
+    I.z32 = dalloc<float2>(c, M);
     I.E32 = dalloc<float2>(c, M);
     I.work32 = dalloc<float2>(c, M);
     I.hist32 = dalloc<float2>(c, (size_t)M * (I.hmax + 1));
@@ -889,8 +888,7 @@ void build_jobs(scft_ctx *c) {
         }
       }
     }
-    F.zr = I.zr;
-    F.zs = I.zs;
+    F.z32 = I.z32;
     F.zg = I.zg;
     F.Eg32 = I.Eg32;
     F.gacc32 = I.gacc32;
@@ -1019,18 +1017,10 @@ void build_jobs(scft_ctx *c) {
           for (int x0 = 0; x0 < g.nx; x0 += g.tx) cj.push_back(ColJob{a, kern, I.geom, x0, y});
       }
     };
-    if (!I.mixed) {
+    if (!I.mixed) {  // the mixed form builds its field-transform lists in job order below
       add(upd, pj_upd, cj_upd, nullptr);
       add(fld, pj_fld, cj_fld, nullptr);
       add(smr, pj_sm, cj_sm, I.hhat);
-    } else {
-      std::vector<double2 *> zr = {I.zr}, zs = {I.zs};
-      if (I.graft) {  // rho_g forward, hhat w_G inverse
-        zr.push_back(I.zg);
-        zs.push_back(I.zg);
-      }
-      add(zr, pj_upd, cj_upd, nullptr);  // forward transform of rho_A + i rho_B
-      add(zs, pj_fld, cj_fld, nullptr);  // inverse transform of the smeared pair
     }
   }
   c->shp_plane = choose_shape(emax_plane, sizeof(double2), (nxy_max + 32) * sizeof(double2));
@@ -1101,42 +1091,36 @@ void build_jobs(scft_ctx *c) {
     c->inst_pj_end = inst_pj_end;
     c->inst_cj_end = inst_cj_end;
     // field-level data in job order, so that a sweep group's instances are a
-    // contiguous range for the field kernels and the FP64 field transforms too
+    // contiguous range for the field kernels and the field transforms too:
+    // FP32 jobs of z32 (every instance), FP64 jobs of zg (grafted instances)
     std::vector<FieldInst> fio;
-    std::vector<PlaneJob> fpj, ipj;
-    std::vector<ColJob> fcj, icj;
+    std::vector<PlaneJob> zpj, gpj;
+    std::vector<ColJob> zcj, gcj;
     c->fld_end.assign(4 * n, 0);
     for (int oi = 0; oi < n; oi++) {
       Instance &I = c->inst[order[oi]];
       const DevGeom &g = c->geoms[I.geom];
       fio.push_back(c->h_fi[order[oi]]);
-      std::vector<double2 *> fw = {I.zr}, iv = {I.zs};
-      if (I.graft) {
-        fw.push_back(I.zg);
-        iv.push_back(I.zg);
-      }
-      for (double2 *a : fw) {
-        for (int z = 0; z < g.nz; z++) fpj.push_back(PlaneJob{a, I.geom, z});
+      auto add_ord = [&](void *a, std::vector<PlaneJob> &pj, std::vector<ColJob> &cj) {
+        for (int z = 0; z < g.nz; z++) pj.push_back(PlaneJob{a, I.geom, z});
         for (int y = 0; y < g.ny; y++)
-          for (int x0 = 0; x0 < g.nx; x0 += g.tx) fcj.push_back(ColJob{a, nullptr, I.geom, x0, y});
-      }
-      for (double2 *a : iv) {
-        for (int z = 0; z < g.nz; z++) ipj.push_back(PlaneJob{a, I.geom, z});
-        for (int y = 0; y < g.ny; y++)
-          for (int x0 = 0; x0 < g.nx; x0 += g.tx) icj.push_back(ColJob{a, nullptr, I.geom, x0, y});
-      }
-      c->fld_end[4 * oi + 0] = (int)fpj.size();
-      c->fld_end[4 * oi + 1] = (int)fcj.size();
-      c->fld_end[4 * oi + 2] = (int)ipj.size();
-      c->fld_end[4 * oi + 3] = (int)icj.size();
+          for (int x0 = 0; x0 < g.nx; x0 += g.tx) cj.push_back(ColJob{a, nullptr, I.geom, x0, y});
+      };
+      add_ord(I.z32, zpj, zcj);
+      if (I.graft) add_ord(I.zg, gpj, gcj);
+      c->fld_end[4 * oi + 0] = (int)zpj.size();
+      c->fld_end[4 * oi + 1] = (int)zcj.size();
+      c->fld_end[4 * oi + 2] = (int)gpj.size();
+      c->fld_end[4 * oi + 3] = (int)gcj.size();
     }
     c->d_fi_ord = dupload(c, fio);
-    c->d_fpj_ord = dupload(c, fpj);
-    c->d_fcj_ord = dupload(c, fcj);
-    c->d_ipj_ord = dupload(c, ipj);
-    c->d_icj_ord = dupload(c, icj);
+    c->d_zpj_ord = dupload(c, zpj);
+    c->d_zcj_ord = dupload(c, zcj);
+    c->d_gpj_ord = dupload(c, gpj);
+    c->d_gcj_ord = dupload(c, gcj);
     build_groups(c);
     c->shp_mix = choose_shape(emax_plane, sizeof(float2), (nxy_max + 32) * sizeof(float2));
+    c->shp_plane32 = c->shp_mix;  // same plane and twiddle footprint
     c->xy64 = 1;
     for (auto &I : c->inst)
       if (I.p.Nx[0] != 64 || I.p.Nx[1] != 64 || I.p.Nx[2] != c->inst[0].p.Nx[2]) c->xy64 = 0;
@@ -1357,35 +1341,47 @@ void seq_update_1s(scft_ctx *c) {
 // Mixed form, one sweep group on stream sg: the work of one update_1s (or of
 // calc_poly_density when `update` is false) for the group's instances, from
 // the densities of the last sweep to the densities of this one:
-//   update:  density pack -> forward FP64 transform -> k-space update (which
-//            also forms the smeared pair) ->
+//   update:  density pack -> forward FP32 transform (FP64 for the graft
+//            density) -> k-space update (which also forms the smeared pair) ->
 //   density: (smeared pair from the fields) ->
-//   both:    inverse FP64 transform -> Boltzmann factors -> FP32 sweep -> Q.
-// Each group is an independent chain, so one group's FP64-bound field work
-// runs beside another group's bandwidth-bound sweep.
+//   both:    inverse FP32 transform (FP64 for the graft field) -> Boltzmann
+//            factors -> FP32 sweep -> Q.
+// The fields stay in FP64 in k-space; only the densities going in and the
+// mean-free smeared fields coming out pass through FP32 transforms, whose
+// error (~1e-7 of the fluctuation) is below that of the FP32 sweep.
+// Each group is an independent chain, so one group's field work runs beside
+// another group's bandwidth-bound sweep.
 void mix_group_chain(scft_ctx *c, int g, cudaStream_t sg, bool update) {
   const scft_ctx::SweepGroup &gr = c->groups[g];
   const int i0 = gr.inst_begin, cnt_i = gr.inst_end - gr.inst_begin;
   const FieldInst *fi = c->d_fi_ord + i0;
+  int pb, pm, cb, cm, gpb, gpm, gcb, gcm;
   auto range = [&](int kind, int &b0, int &n0) {
     b0 = i0 ? c->fld_end[4 * (i0 - 1) + kind] : 0;
     n0 = c->fld_end[4 * (gr.inst_end - 1) + kind] - b0;
   };
-  int b, m;
+  range(0, pb, pm);
+  range(1, cb, cm);
+  range(2, gpb, gpm);
+  range(3, gcb, gcm);
   if (update) {
     LK(launch_mix_rho_pack(fi, cnt_i, c->eblocks, 0, sg));
-    range(0, b, m);
-    LK(launch_plane_fft<double>(c->shp_plane, c->d_fpj_ord + b, m, c->d_geoms, c->d_tw64, -1, 0, sg));
-    range(1, b, m);
-    LK(launch_col_fft<double>(c->shp_col, c->d_fcj_ord + b, m, c->d_geoms, c->d_tw64, 0, 1, sg));
+    LK(launch_plane_fft<float>(c->shp_plane32, c->d_zpj_ord + pb, pm, c->d_geoms, c->d_tw32, -1, 0, sg));
+    LK(launch_col_fft<float>(c->shp_col32, c->d_zcj_ord + cb, cm, c->d_geoms, c->d_tw32, 0, 1, sg));
+    if (gpm > 0) {
+      LK(launch_plane_fft<double>(c->shp_plane, c->d_gpj_ord + gpb, gpm, c->d_geoms, c->d_tw64, -1, 0, sg));
+      LK(launch_col_fft<double>(c->shp_col, c->d_gcj_ord + gcb, gcm, c->d_geoms, c->d_tw64, 0, 1, sg));
+    }
     LK(launch_mix_update(fi, cnt_i, c->eblocks, sg));
   } else {
     LK(launch_mix_smear(fi, cnt_i, c->eblocks, sg));
   }
-  range(3, b, m);
-  LK(launch_col_fft<double>(c->shp_col, c->d_icj_ord + b, m, c->d_geoms, c->d_tw64, 1, 0, sg));
-  range(2, b, m);
-  LK(launch_plane_fft<double>(c->shp_plane, c->d_ipj_ord + b, m, c->d_geoms, c->d_tw64, +1, 0, sg));
+  LK(launch_col_fft<float>(c->shp_col32, c->d_zcj_ord + cb, cm, c->d_geoms, c->d_tw32, 1, 0, sg));
+  LK(launch_plane_fft<float>(c->shp_plane32, c->d_zpj_ord + pb, pm, c->d_geoms, c->d_tw32, +1, 0, sg));
+  if (gpm > 0) {
+    LK(launch_col_fft<double>(c->shp_col, c->d_gcj_ord + gcb, gcm, c->d_geoms, c->d_tw64, 1, 0, sg));
+    LK(launch_plane_fft<double>(c->shp_plane, c->d_gpj_ord + gpb, gpm, c->d_geoms, c->d_tw64, +1, 0, sg));
+  }
   LK(launch_mix_boltzmann(fi, cnt_i, c->eblocks, sg));
   for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) {
     Instance &I = c->inst[c->job_order[oi]];
@@ -1916,7 +1912,7 @@ void ctx_get_density(scft_ctx *c, int k, double *ra, double *rb, double *rg) {
   if (c->dirty_density) ctx_poly_density(c);
   Instance &I = c->inst[k];
   if (I.mixed) {
-    // zr is rebuilt from the accumulators by the next update, so this is safe
+    // FP64 densities from the accumulators (the sweep state is not touched)
     CK(launch_mix_rho_pack(c->d_fi, (int)c->inst.size(), c->eblocks, 1, c->st));
     if (!I.graft) CK(cudaMemsetAsync(I.rho[2], 0, sizeof(double2) * I.M, c->st));
   }
@@ -1930,13 +1926,17 @@ void ctx_get_smeared(scft_ctx *c, int k, double *a, double *b, double *g) {
   if (c->dirty_density) ctx_poly_density(c);
   Instance &I = c->inst[k];
   if (I.mixed) {
-    // zs holds smwa + i smwb (both real) in real space
-    std::vector<double2> h(I.M);
-    CK(cudaMemcpyAsync(h.data(), I.zs, sizeof(double2) * I.M, cudaMemcpyDeviceToHost, c->st));
+    // z32 holds smwa + i smwb minus their means (real space, FP32); the means
+    // are in scal[kSmean]
+    std::vector<float2> h(I.M);
+    std::vector<double2> sc(kNumScalars);
+    CK(cudaMemcpyAsync(h.data(), I.z32, sizeof(float2) * I.M, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(sc.data(), I.scal, sizeof(double2) * kNumScalars, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
+    const double2 m = sc[kSmean];
     for (long long i = 0; i < I.M; i++) {
-      if (a) { a[2 * i] = h[i].x; a[2 * i + 1] = 0.0; }
-      if (b) { b[2 * i] = h[i].y; b[2 * i + 1] = 0.0; }
+      if (a) { a[2 * i] = m.x + h[i].x; a[2 * i + 1] = 0.0; }
+      if (b) { b[2 * i] = m.y + h[i].y; b[2 * i + 1] = 0.0; }
       if (g) { g[2 * i] = 0.0; g[2 * i + 1] = 0.0; }
     }
     if (g && I.graft) CK(cudaMemcpy(g, I.sm[2], sizeof(double2) * I.M, cudaMemcpyDeviceToHost));
@@ -2016,7 +2016,7 @@ int ctx_grad_geom(scft_ctx *c, double *out) {
   try {
     bool any_shell = false;
     for (auto &I : c->inst) any_shell = any_shell || (I.shellU != nullptr);
-    if (c->mixed && any_shell)  // real-space rho_A of every instance (zr is rebuilt by the next update)
+    if (c->mixed && any_shell)  // real-space FP64 rho_A of every instance
       CK(launch_mix_rho_pack(c->d_fi, n, c->eblocks, 1, c->st));
     for (int k = 0; k < n; k++) {
       Instance &I = c->inst[k];

@@ -50,7 +50,7 @@ struct Instance {
   double2 *gwork = nullptr, *ghist = nullptr, *gacc = nullptr;  // graft sweeps
   // mixed precision
   int mixed = 0;
-  double2 *zr = nullptr, *zs = nullptr;
+  float2 *z32 = nullptr;  // FP32 field-transform array (FieldInst::z32)
   // mixed form with grafts
   double2 *zg = nullptr;
   float *Eg32 = nullptr, *ghist32 = nullptr, *gacc32 = nullptr;
@@ -136,25 +136,20 @@ struct scft_ctx {
   std::vector<SweepGroup> groups;
   int sweep_phases = 1;  // requested number of sequential phases
   std::vector<int> job_order, inst_pj_end, inst_cj_end;  // mixed job lists, by instance
-  // mixed field-level data in job order: FieldInst table, forward (rho pack)
-  // and inverse (smeared pair) FP64 transform jobs; fld_end[4 oi + k] = end of
-  // instance oi's jobs in list k (forward plane, forward column, inverse
-  // plane, inverse column)
+  // mixed field-level data in job order: FieldInst table, the FP32 transform
+  // jobs of z32 and the FP64 ones of zg (grafted instances); fld_end[4 oi + k]
+  // = end of instance oi's jobs in list k (z32 plane, z32 column, zg plane,
+  // zg column); the same lists serve both directions
   std::vector<scft::FieldInst> h_fi;
   scft::FieldInst *d_fi_ord = nullptr;
-  scft::PlaneJob *d_fpj_ord = nullptr, *d_ipj_ord = nullptr;
-  scft::ColJob *d_fcj_ord = nullptr, *d_icj_ord = nullptr;
+  scft::PlaneJob *d_zpj_ord = nullptr, *d_gpj_ord = nullptr;
+  scft::ColJob *d_zcj_ord = nullptr, *d_gcj_ord = nullptr;
   std::vector<int> fld_end;
   int sweep_streams = 2;  // requested number of groups (1 = a single chain)
   std::vector<cudaStream_t> side;
   std::vector<cudaEvent_t> ev_join;
   cudaEvent_t ev_fork = nullptr;
-  scft::PropJob *d_mix_pj = nullptr;
-  scft::ColJob *d_mix_cj = nullptr;
-  scft::PlaneJob *d_pj_zr = nullptr, *d_pj_zs = nullptr;
-  scft::ColJob *d_cj_zr = nullptr, *d_cj_zs = nullptr;
-  int n_pj_zr = 0, n_cj_zr = 0;
-  scft::LaunchShape shp_mix{}, shp_col32{};
+  scft::LaunchShape shp_mix{}, shp_col32{}, shp_plane32{};
   scft::LaunchShape shp_plane{}, shp_col{}, shp_prop{};
   int eblocks = 0;  // blocks per instance for pointwise kernels
   double2 *d_hpart = nullptr;

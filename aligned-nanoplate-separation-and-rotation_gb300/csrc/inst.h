@@ -11,7 +11,8 @@ enum ScalarSlot {
   kFactor = 1,   // nD / Q / V (code/calc_poly_density.cpp:176)
   kQga = 2,      // Qga_exp (code/grafted_nanoparticle.cpp:112)
   kQg = 3,       // graft propagator check: count of points with Re q_g[Ng-1] <= 0 in .x
-  kNumScalars = 4
+  kSmean = 4,    // mixed form: means of smwa (.x) and smwb (.y), kept out of the FP32 transform
+  kNumScalars = 5
 };
 
 // View of one instance for the propagator sweeps.  Propagator p = 0 is q
@@ -97,8 +98,10 @@ struct FieldInst {
   const double2 *grafts;
   // mixed precision: w[] hold the k-space (1/M scaled) fields
   int nx, ny;
-  double2 *zr;         // rho_A + i rho_B (real space), then its transform
-  double2 *zs;         // hhat*(w_A + i w_B) (k-space), then smwa + i smwb (real space)
+  // FP32 field-transform array: rho_A + i rho_B (real space), then its
+  // transform; then hhat*(w_A + i w_B) (k-space) with the k = 0 term moved to
+  // scal[kSmean] in FP64, then smwa + i smwb minus their means (real space)
+  float2 *z32;
   float2 *E32;         // (e^{-smwa}, e^{-smwb})
   float *acc32[2];     // density sums, scaled by 2^-K[2N]
   int *K;              // [2][N] + 1

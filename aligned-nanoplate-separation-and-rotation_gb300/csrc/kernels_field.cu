@@ -459,33 +459,30 @@ __device__ __forceinline__ double2 smear_pack(const FieldInst &F, long long i, c
   return make_double2(hh * (wa.x - wb.y), hh * (wa.y + wb.x));
 }
 
+// Stores zs(k) = hhat (w_A + i w_B) for the FP32 inverse transform: the
+// k = 0 term (the means of smwa and smwb, which can be large) goes to
+// scal[kSmean] in FP64 and is added back by the Boltzmann kernel, so the
+// FP32 transform carries only the fluctuating part.
+__device__ __forceinline__ void store_zs(const FieldInst &F, long long i, double2 zs) {
+  if (i == 0) {
+    F.scal[kSmean] = zs;
+    F.z32[0] = make_float2(0.0f, 0.0f);
+  } else {
+    F.z32[i] = make_float2((float)zs.x, (float)zs.y);
+  }
+}
+
 __global__ void k_mix_smear(const FieldInst *__restrict__ fi) {
   FOR_POINTS(F) {
     double2 w[7];
     for (int f = 0; f < 7; f++) w[f] = F.w[f][i];
-    F.zs[i] = smear_pack(F, i, w);
+    store_zs(F, i, smear_pack(F, i, w));
     if (F.graft) F.zg[i] = smear_graft(F, i, w);
   }
 }
 
-// 1S update on the k-space fields; the two density transforms come from one
-// packed transform Z of rho_A + i rho_B:
-//   rho_A(k) = (Z(k) + conj Z(-k)) / 2,  rho_B(k) = (Z(k) - conj Z(-k)) / (2i).
-__global__ void k_mix_update(const FieldInst *__restrict__ fi) {
-  FOR_POINTS(F) {
-    const double2 Z = F.zr[i], Zm = F.zr[neg_k(F, i)];
-    const double2 ra = make_double2(0.5 * (Z.x + Zm.x), 0.5 * (Z.y - Zm.y));
-    const double2 rb = make_double2(0.5 * (Z.y + Zm.y), 0.5 * (Zm.x - Z.x));
-    double2 w[7];
-    for (int f = 0; f < 7; f++) w[f] = F.w[f][i];
-    update_1s_point(F, i, ra, rb, make_double2(0.0, 0.0), w);
-    for (int f = 0; f < 7; f++) F.w[f][i] = w[f];
-    F.zs[i] = smear_pack(F, i, w);
-  }
-}
-
-// The same update with the k-only coefficients tabulated at set-up: for
-// every field and sign branch of code/1s_update.cpp:58-329 the step is
+// 1S update on the k-space fields, with the k-only coefficients tabulated at
+// set-up: for every field and sign branch of code/1s_update.cpp:58-329 the step is
 // w <- (w - lam (F - B w)) / (1 + lam A) = alpha w - beta F, alpha, beta
 // functions of k alone.  No division per iteration; only fields with
 // nonzero chi are read and written.
@@ -499,6 +496,11 @@ __device__ __forceinline__ double field_parity(const FieldInst &F, int f) {
   return (f & 1) ? (neg ? 1.0 : -1.0) : (neg ? -1.0 : 1.0);
 }
 
+// The two density transforms come from one packed FP32 transform Z of
+// rho_A + i rho_B:
+//   rho_A(k) = (Z(k) + conj Z(-k)) / 2,  rho_B(k) = (Z(k) - conj Z(-k)) / (2i),
+// and zs(k) is written back into the same array (each thread reads and writes
+// only its own pair).
 // One thread per pair (k, -k): every field and density is Hermitian or
 // anti-Hermitian in k-space, so the update at -k follows from the one at k by
 // conjugation; this halves the FP64 work, which bounds this kernel on GB300.
@@ -513,7 +515,8 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
        i += (long long)gridDim.x * blockDim.x) {
     const long long j = neg_k(F, i);
     if (j < i) continue;
-    const double2 Z = F.zr[i], Zm = F.zr[j];
+    const float2 Zf = F.z32[i], Zmf = F.z32[j];
+    const double2 Z = make_double2(Zf.x, Zf.y), Zm = make_double2(Zmf.x, Zmf.y);
     const double2 ra = make_double2(0.5 * (Z.x + Zm.x), 0.5 * (Z.y - Zm.y));
     const double2 rb = make_double2(0.5 * (Z.y + Zm.y), 0.5 * (Zm.x - Z.x));
     const double rho0 = F.rho0, hh = F.hhat[i];
@@ -591,8 +594,8 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
     double2 wa, wb, wg;
     assemble_point(F, w, wa, wb, wg);
     // zs = hhat (w_A + i w_B) at k and, with w_A(-k) = conj w_A(k), at -k
-    F.zs[i] = make_double2(hh * (wa.x - wb.y), hh * (wa.y + wb.x));
-    if (pair) F.zs[j] = make_double2(hh * (wa.x + wb.y), hh * (wb.x - wa.y));
+    store_zs(F, i, make_double2(hh * (wa.x - wb.y), hh * (wa.y + wb.x)));
+    if (pair) F.z32[j] = make_float2((float)(hh * (wa.x + wb.y)), (float)(hh * (wb.x - wa.y)));
     if (F.graft) {
       F.zg[i] = make_double2(hh * wg.x, hh * wg.y);
       if (pair) F.zg[j] = make_double2(hh * wg.x, -hh * wg.y);
@@ -600,12 +603,23 @@ __global__ void k_mix_update_tab(const FieldInst *__restrict__ fi) {
   }
 }
 
-// After the inverse transform zs = smwa + i smwb (real space): Boltzmann
-// factors for the FP32 sweep.  exp(-s) is evaluated in FP32 from a two-float
-// split s = s_hi + s_lo: exp(-s) = expf(-s_hi) (1 - s_lo), the neglected term
-// being O(s_lo^2) ~ 1e-14 relative, so the result carries expf's accuracy
-// without an FP64 exponential.
+// After the inverse transform z32 = smwa + i smwb minus their means (real
+// space): Boltzmann factors for the FP32 sweep.  s = mean + d with the mean
+// as a two-float (m_hi, m_lo) and d the FP32 transform value:
+// t = fl(m_hi + d) with its rounding error e (two-sum), and
+// exp(-s) = expf(-t) (1 - (m_lo + e)), the neglected term being
+// O((m_lo + e)^2) ~ 1e-14 relative, so the result carries expf's accuracy
+// without an FP64 exponential however large the mean is.
+__device__ __forceinline__ float boltz_two_float(float mh, float ml, float d) {
+  const float t = mh + d, v = t - mh;
+  const float e = (mh - (t - v)) + (d - v);
+  return expf(-t) * (1.0f - (ml + e));
+}
+
 __global__ void k_mix_boltzmann(const FieldInst *__restrict__ fi) {
+  const double2 m = fi[blockIdx.y].scal[kSmean];
+  const float ah = (float)m.x, al = (float)(m.x - (double)ah);
+  const float bh = (float)m.y, bl = (float)(m.y - (double)bh);
   FOR_POINTS(F) {
     if (F.graft) {
       const double sg = F.zg[i].x;
@@ -613,11 +627,9 @@ __global__ void k_mix_boltzmann(const FieldInst *__restrict__ fi) {
       F.Eg32[i] = expf(-gh) * (1.0f - gl);
       F.sm[2][i] = make_double2(sg, F.zg[i].y);
     }
-    double2 s = F.zs[i];
-    if (F.shellU) s.x += F.shellU[i];
-    const float ah = (float)s.x, al = (float)(s.x - (double)ah);
-    const float bh = (float)s.y, bl = (float)(s.y - (double)bh);
-    F.E32[i] = make_float2(expf(-ah) * (1.0f - al), expf(-bh) * (1.0f - bl));
+    const float2 d = F.z32[i];
+    const float da = F.shellU ? d.x + (float)F.shellU[i] : d.x;
+    F.E32[i] = make_float2(boltz_two_float(ah, al, da), boltz_two_float(bh, bl, d.y));
   }
 }
 
@@ -636,20 +648,25 @@ __global__ void k_mix_q_finalize(const FieldInst *__restrict__ fi, int ninst) {
   F.scal[kFactor] = make_double2(F.nD / Q / F.V, 0.0);
 }
 
-// rho_A, rho_B = acc * e^{+smw} * factor packed into zr (and optionally kept
-// as complex arrays for scft_get_density).
+// rho_A, rho_B = acc * e^{+smw} * factor, packed into z32 for the FP32
+// forward transform (keep = 0) or stored as FP64 complex arrays for
+// scft_get_density and the gradient (keep = 1).  The factor carries the
+// accumulators' exponent and can lie outside the FP32 range: it is applied as
+// an FP32 mantissa and an ldexpf.
 __global__ void k_mix_rho_pack(const FieldInst *__restrict__ fi, int keep) {
   const FieldInst &F0 = fi[blockIdx.y];
   const double f = ldexp(F0.scal[kFactor].x, F0.K[2 * F0.N]);  // accumulators are scaled by 2^-Kref
+  int fe;
+  const float fm = (float)frexp(f, &fe);
   FOR_POINTS(F) {
     // e^{+smw} = 1 / e^{-smw}: the FP32 reciprocal of the Boltzmann factor
     const float2 E = F.E32[i];
-    const double ra = (double)(F.acc32[0][i] * __frcp_rn(E.x)) * f;
-    const double rb = (double)(F.acc32[1][i] * __frcp_rn(E.y)) * f;
-    F.zr[i] = make_double2(ra, rb);
+    const float xa = F.acc32[0][i] * __frcp_rn(E.x), xb = F.acc32[1][i] * __frcp_rn(E.y);
     if (keep) {
-      F.rho[0][i] = make_double2(ra, 0.0);
-      F.rho[1][i] = make_double2(rb, 0.0);
+      F.rho[0][i] = make_double2((double)xa * f, 0.0);
+      F.rho[1][i] = make_double2((double)xb * f, 0.0);
+    } else {
+      F.z32[i] = make_float2(ldexpf(xa * fm, fe), ldexpf(xb * fm, fe));
     }
   }
 }
