@@ -802,15 +802,23 @@ void build_groups(scft_ctx *c) {
     const int G = std::max(1, std::min(c->sweep_streams, pe - p0));
     int i0 = p0;
     for (int i1 : cut(p0, pe, G)) {
-      scft_ctx::SweepGroup gr;
-      gr.inst_begin = i0;
-      gr.inst_end = i1;
-      gr.pj_begin = i0 ? c->inst_pj_end[i0 - 1] : 0;
-      gr.pj_end = c->inst_pj_end[i1 - 1];
-      gr.cj_begin = i0 ? c->inst_cj_end[i0 - 1] : 0;
-      gr.cj_end = c->inst_cj_end[i1 - 1];
-      gr.phase = ph;
-      c->groups.push_back(gr);
+      // a group never straddles the 64^3 instances and the others of a
+      // batch of mixed grids: split at that boundary
+      for (int a = i0; a < i1;) {
+        int b = a + 1;
+        while (b < i1 && (c->fast64.empty() || c->fast64[b] == c->fast64[a])) b++;
+        scft_ctx::SweepGroup gr;
+        gr.inst_begin = a;
+        gr.inst_end = b;
+        gr.pj_begin = a ? c->inst_pj_end[a - 1] : 0;
+        gr.pj_end = c->inst_pj_end[b - 1];
+        gr.cj_begin = a ? c->inst_cj_end[a - 1] : 0;
+        gr.cj_end = c->inst_cj_end[b - 1];
+        gr.phase = ph;
+        gr.fast = c->fast64.empty() ? 0 : c->fast64[a];
+        c->groups.push_back(gr);
+        a = b;
+      }
       i0 = i1;
     }
     p0 = pe;
@@ -1068,6 +1076,30 @@ void build_jobs(scft_ctx *c) {
     }
   }
   if (c->mixed) {
+    // Kernel classes: a batch of 64 x 64 planes with one nz runs the 64-point
+    // plane kernel throughout (xy64; and the 64- or 128-point z kernel,
+    // colfast).  In a batch of mixed grids the 64^3 instances run the 64-point
+    // kernels and the rest the generic ones: the 64^3 instances come first in
+    // job order (each class still by decreasing N, so the instances active at
+    // a step are a prefix of every sweep group), and the sweep groups never
+    // straddle the two classes.
+    c->xy64 = 1;
+    for (auto &I : c->inst)
+      if (I.p.Nx[0] != 64 || I.p.Nx[1] != 64 || I.p.Nx[2] != c->inst[0].p.Nx[2]) c->xy64 = 0;
+    c->colfast = c->xy64 && (c->inst[0].p.Nx[2] == 64 || c->inst[0].p.Nx[2] == 128);
+    auto is64 = [&](int k) {
+      const int *X = c->inst[k].p.Nx;
+      return X[0] == 64 && X[1] == 64 && X[2] == 64;
+    };
+    c->fast64.assign(n, 0);
+    c->anyfast = 0;
+    if (!c->xy64) {
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return is64(a) && !is64(b); });
+      for (int oi = 0; oi < n; oi++) {
+        c->fast64[oi] = is64(order[oi]) ? 1 : 0;
+        c->anyfast = c->anyfast || c->fast64[oi];
+      }
+    }
     // one plane job per z (q and qdag packed), FP32 column jobs
     ppj.clear();
     pcj.clear();
@@ -1121,33 +1153,38 @@ void build_jobs(scft_ctx *c) {
     build_groups(c);
     c->shp_mix = choose_shape(emax_plane, sizeof(float2), (nxy_max + 32) * sizeof(float2));
     c->shp_plane32 = c->shp_mix;  // same plane and twiddle footprint
-    c->xy64 = 1;
-    for (auto &I : c->inst)
-      if (I.p.Nx[0] != 64 || I.p.Nx[1] != 64 || I.p.Nx[2] != c->inst[0].p.Nx[2]) c->xy64 = 0;
-    c->colfast = c->xy64 && (c->inst[0].p.Nx[2] == 64 || c->inst[0].p.Nx[2] == 128);
-    if (c->colfast) {
+    // 64-point kernel tables, indexed by job-order position (64 x (64 / tx)
+    // z-pass jobs per instance); entries of generic-class instances are
+    // placeholders that no launch reads
+    if (c->colfast || c->anyfast) {
       for (int t = 0; t < 3; t++) {
         const int tx = 8 << t;
         std::vector<ColJob> cj64;
         for (int oi = 0; oi < n; oi++) {
           Instance &I = c->inst[order[oi]];
+          const bool use = c->colfast || c->fast64[oi];
           for (int y = 0; y < 64; y++)
-            for (int x0 = 0; x0 < 64; x0 += tx) cj64.push_back(ColJob{I.work32, I.htab32, I.geom, x0, y});
+            for (int x0 = 0; x0 < 64; x0 += tx)
+              cj64.push_back(ColJob{I.work32, I.htab32, I.geom, use ? x0 : 0, use ? y : 0});
         }
         c->d_mix64_cj_tx[t] = dupload(c, cj64);
       }
-
     }
-    if (c->xy64) {
+    if (c->xy64 || c->anyfast) {
       c->mix64_tab.clear();
       c->tmE.clear();
       c->tmH.clear();
       for (int oi = 0; oi < n; oi++) {
         c->mix64_tab.push_back(c->h_mi[order[oi]]);
         Instance &I = c->inst[order[oi]];
-        const unsigned long long rows = 64ULL * (unsigned long long)I.p.Nx[2];
-        c->tmE.push_back(tensor_map_rows(I.E32, rows));
-        c->tmH.push_back(tensor_map_rows(I.hist32, rows * (unsigned long long)(I.hmax + 1)));
+        if (c->xy64 || c->fast64[oi]) {
+          const unsigned long long rows = 64ULL * (unsigned long long)I.p.Nx[2];
+          c->tmE.push_back(tensor_map_rows(I.E32, rows));
+          c->tmH.push_back(tensor_map_rows(I.hist32, rows * (unsigned long long)(I.hmax + 1)));
+        } else {
+          c->tmE.push_back(CUtensorMap{});
+          c->tmH.push_back(CUtensorMap{});
+        }
       }
       if (!c->d_err) c->d_err = dalloc<int>(c, 1);
     }
@@ -1388,26 +1425,29 @@ void mix_group_chain(scft_ctx *c, int g, cudaStream_t sg, bool update) {
     CK(cudaMemsetAsync(I.acc32[0], 0, sizeof(float) * I.M, sg));
     CK(cudaMemsetAsync(I.acc32[1], 0, sizeof(float) * I.M, sg));
   }
-  auto clampc = [](int v, int lo, int hi) { return std::min(std::max(v, lo), hi) - lo; };
+  const bool p64 = c->xy64 || gr.fast, z64 = c->colfast || gr.fast;
+  const int nzi = gr.fast ? 64 : c->inst[0].p.Nx[2];
+  const void *twz = gr.fast ? c->d_tw32_64 : c->d_tw32_z;
+  const int per = 64 * (64 / c->col64_tx);  // z-pass jobs per instance of the 64-point kernels
   for (int s = 0; s < c->nmax; s++) {
-    const int cnt = clampc(c->prop_pj_count[s], gr.pj_begin, gr.pj_end);
-    if (cnt <= 0) break;
+    // instances of the group still active at step s: a prefix (decreasing N)
+    int act = 0;
+    for (int oi = gr.inst_begin; oi < gr.inst_end; oi++)
+      if (c->inst[c->job_order[oi]].N > s) act = oi + 1 - gr.inst_begin;
+    if (act == 0) break;
+    const int last = gr.inst_begin + act - 1;
+    const int cnt = c->inst_pj_end[last] - gr.pj_begin;
+    const int cc = c->inst_cj_end[last] - gr.cj_begin;
     if (s > 0) {
-      if (c->colfast) {
-        const int nzi = c->inst[0].p.Nx[2];
-        const int per = 64 * (64 / c->col64_tx);  // z-pass jobs per instance
-        LK(launch_mix_col64(col64_jobs(c) + (size_t)gr.inst_begin * per, (cnt / nzi) * per, c->d_tw32_z, 64, 64, nzi,
-                            c->col64_tx, sg));
-      } else {
-        const int cc = clampc(c->prop_cj_count[s], gr.cj_begin, gr.cj_end);
+      if (z64)
+        LK(launch_mix_col64(col64_jobs(c) + (size_t)gr.inst_begin * per, act * per, twz, 64, 64, nzi, c->col64_tx,
+                            sg));
+      else
         LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cc, c->d_geoms, c->d_tw32, 3, 1, sg));
-      }
     }
-    if (c->xy64) {
-      const int nzi = c->inst[0].p.Nx[2];
+    if (p64)
       LK(launch_mix_plane64(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
-                            c->tmH.data() + gr.inst_begin, cnt / nzi, nzi, c->d_tw32_64, s, c->d_err, sg));
-    }
+                            c->tmH.data() + gr.inst_begin, act, nzi, c->d_tw32_64, s, c->d_err, sg));
     else
       LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj + gr.pj_begin, cnt, c->d_mi, c->d_geoms, c->d_tw32, s, sg));
   }
@@ -1640,7 +1680,7 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
   std::vector<int> gs, txs;
   for (int g : {1, 2, 3, 4, 5, 6, 8})
     if (g <= n) gs.push_back(g);
-  if (c->colfast)
+  if (c->colfast || c->anyfast)
     txs = {8, 16, 32};
   else
     txs = {c->col64_tx};
@@ -1688,7 +1728,7 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
   }
   *groups_out = bg;
   *phases_out = bp;
-  *tx_out = c->colfast ? bt : 0;
+  *tx_out = (c->colfast || c->anyfast) ? bt : 0;
   *ms_out = best;
 }
 

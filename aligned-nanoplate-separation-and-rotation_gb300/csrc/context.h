@@ -130,12 +130,19 @@ struct scft_ctx {
   // plane pass; all of it sits in one captured graph.
   // Phases run one after another (each phase's working set can stay in L2);
   // the groups of one phase run concurrently.
+  // fast: the group's instances are 64^3 grids of a batch of mixed grids and
+  // run on the 64-point plane and z kernels (a batch of 64 x 64 planes only
+  // uses them throughout: xy64)
   struct SweepGroup {
-    int inst_begin, inst_end, pj_begin, pj_end, cj_begin, cj_end, phase;
+    int inst_begin, inst_end, pj_begin, pj_end, cj_begin, cj_end, phase, fast;
   };
   std::vector<SweepGroup> groups;
   int sweep_phases = 1;  // requested number of sequential phases
   std::vector<int> job_order, inst_pj_end, inst_cj_end;  // mixed job lists, by instance
+  // batch of mixed grids: fast64[oi] = 1 for the 64^3 instances (job-order
+  // position oi), which come first in job order; anyfast = some instance is one
+  std::vector<char> fast64;
+  int anyfast = 0;
   // mixed field-level data in job order: FieldInst table, the FP32 transform
   // jobs of z32 and the FP64 ones of zg (grafted instances); fld_end[4 oi + k]
   // = end of instance oi's jobs in list k (z32 plane, z32 column, zg plane,

@@ -617,9 +617,18 @@ __device__ __forceinline__ float boltz_two_float(float mh, float ml, float d) {
 }
 
 __global__ void k_mix_boltzmann(const FieldInst *__restrict__ fi) {
-  const double2 m = fi[blockIdx.y].scal[kSmean];
-  const float ah = (float)m.x, al = (float)(m.x - (double)ah);
-  const float bh = (float)m.y, bl = (float)(m.y - (double)bh);
+  // the means split once per block: GB300 runs FP64 (conversions included)
+  // at a small fraction of the FP32 rate, so no per-point FP64 work here
+  __shared__ float s_m[4];
+  if (threadIdx.x == 0) {
+    const double2 m = fi[blockIdx.y].scal[kSmean];
+    s_m[0] = (float)m.x;
+    s_m[1] = (float)(m.x - (double)s_m[0]);
+    s_m[2] = (float)m.y;
+    s_m[3] = (float)(m.y - (double)s_m[2]);
+  }
+  __syncthreads();
+  const float ah = s_m[0], al = s_m[1], bh = s_m[2], bl = s_m[3];
   FOR_POINTS(F) {
     if (F.graft) {
       const double sg = F.zg[i].x;
@@ -654,10 +663,22 @@ __global__ void k_mix_q_finalize(const FieldInst *__restrict__ fi, int ninst) {
 // accumulators' exponent and can lie outside the FP32 range: it is applied as
 // an FP32 mantissa and an ldexpf.
 __global__ void k_mix_rho_pack(const FieldInst *__restrict__ fi, int keep) {
-  const FieldInst &F0 = fi[blockIdx.y];
-  const double f = ldexp(F0.scal[kFactor].x, F0.K[2 * F0.N]);  // accumulators are scaled by 2^-Kref
-  int fe;
-  const float fm = (float)frexp(f, &fe);
+  // the factor (accumulators are scaled by 2^-Kref) formed once per block
+  __shared__ double s_f;
+  __shared__ float s_fm;
+  __shared__ int s_fe;
+  if (threadIdx.x == 0) {
+    const FieldInst &F0 = fi[blockIdx.y];
+    const double f = ldexp(F0.scal[kFactor].x, F0.K[2 * F0.N]);
+    int fe;
+    s_fm = (float)frexp(f, &fe);
+    s_fe = fe;
+    s_f = f;
+  }
+  __syncthreads();
+  const double f = s_f;
+  const float fm = s_fm;
+  const int fe = s_fe;
   FOR_POINTS(F) {
     // e^{+smw} = 1 / e^{-smw}: the FP32 reciprocal of the Boltzmann factor
     const float2 E = F.E32[i];

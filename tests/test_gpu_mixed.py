@@ -146,7 +146,8 @@ def test_mixed_64cubed_specialised_kernels_match_fp64(scft, nz):
         assert rel(d32[k][1].real, d64[k][1].real) < RHO_TOL
 
 
-@pytest.mark.parametrize("grids", [((64, 64, 64),) * 5, ((48, 48, 48), (32, 32, 32), (48, 48, 48))])
+@pytest.mark.parametrize("grids", [((64, 64, 64),) * 5, ((48, 48, 48), (32, 32, 32), (48, 48, 48)),
+                                   ((48, 48, 48), (64, 64, 64), (32, 32, 32), (64, 64, 64))])
 def test_sweep_schedule_does_not_change_results(scft, grids):
     """Sweep groups and z-pass tile widths only regroup independent work:
     every schedule gives bit-identical H, Q and densities; the autotuner
@@ -171,13 +172,45 @@ def test_sweep_schedule_does_not_change_results(scft, grids):
             else:
                 t = ctx.autotune(2)
                 assert 1 <= t["groups"] <= len(params) and t["ms_per_sweep"] > 0
-                assert t["col_tile"] in ((8, 16, 32) if grids[0] == (64, 64, 64) else (0,))
+                assert t["col_tile"] in ((8, 16, 32) if (64, 64, 64) in grids else (0,))
             ctx.update_1s(3)
             res.append((ctx.calc_H(), [ctx.density(k)[0] for k in range(len(params))]))
     for H, d in res[1:]:
         assert np.array_equal(H, res[0][0])
         for a, b in zip(d, res[0][1]):
             assert np.array_equal(a, b)
+
+
+def test_mixed_grid_batch_runs_64cubed_on_the_64_point_kernels(scft):
+    """In a batch of mixed grids the 64^3 instances run the 64-point plane and
+    z kernels and the others the generic ones, and the batch matches the FP64
+    method.  The 64-point kernels have one launch shape, so a 64^3 instance's
+    H, Q and densities are bit-identical to those of a context holding it
+    alone; the generic kernels size their blocks for the largest grid of the
+    batch, which reorders FP32 plane sums, so the others agree to the FP32
+    tolerance."""
+    from scft.workloads import plate_params, seeded_fields
+
+    params = [plate_params(0.0, N=21, grid=(48, 48, 48), box_rg=(4.8, 4.8, 4.8)),
+              plate_params(30.0, N=24, grid=(64, 64, 64)),
+              plate_params(90.0, N=16, grid=(32, 32, 32), box_rg=(4.0, 4.0, 4.0)),
+              plate_params(60.0, N=13, grid=(64, 64, 64))]
+    fields = [seeded_fields(p, 60 + k) for k, p in enumerate(params)]
+    (H64, d64, _), (H32, d32, _) = run_pair(scft, params, fields, 4)
+    for k in range(len(params)):
+        assert np.abs(H32[:, k, 0] - H64[:, k, 0]).max() <= H_TOL * np.abs(H64[:, k, 0]).max()
+        assert np.abs(H32[:, k, 2] - H64[:, k, 2]).max() <= Q_TOL * np.abs(H64[:, k, 2]).max()
+        assert rel(d32[k][0].real, d64[k][0].real) < RHO_TOL
+        assert rel(d32[k][1].real, d64[k][1].real) < RHO_TOL
+    for k, p in enumerate(params):
+        (_, _, _), (H1, d1, _) = run_pair(scft, [p], [fields[k]], 4)
+        if tuple(p.Nx) == (64, 64, 64):
+            assert np.array_equal(H1[:, 0], H32[:, k])
+            assert np.array_equal(d1[0][0], d32[k][0])
+            assert np.array_equal(d1[0][1], d32[k][1])
+        else:
+            assert np.abs(H1[:, 0, 0] - H32[:, k, 0]).max() <= H_TOL * np.abs(H32[:, k, 0]).max()
+            assert rel(d1[0][0].real, d32[k][0].real) < RHO_TOL
 
 
 def grafted_params(scft, prec, theta=20.0):
