@@ -25,7 +25,18 @@ struct DevGeom {
   int tx;  // x-columns per z-pass tile (divides nx)
   long long M;
   AxisPlan ax[3];
+  // 1/M in FP64 and as an FP32 two-float pair, formed once on the host: the
+  // transform kernels scale by it and GB300 runs FP64 division (and FP64 in
+  // general) at a small fraction of the FP32 rate
+  double inv_m;
+  float inv_m_hi, inv_m_lo;
 };
+
+inline void set_inv_m(DevGeom &g) {
+  g.inv_m = 1.0 / (double)g.M;
+  g.inv_m_hi = (float)g.inv_m;
+  g.inv_m_lo = (float)(g.inv_m - (double)g.inv_m_hi);
+}
 
 // One CTA of an xy-plane pass: array base pointer (complex, M entries),
 // geometry index, z plane.

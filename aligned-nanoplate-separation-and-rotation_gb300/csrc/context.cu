@@ -405,6 +405,7 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
   g.ny = p.Nx[1];
   g.nz = p.Nx[2];
   g.M = M;
+  set_inv_m(g);
   g.tx = 16;
   while (g.nx % g.tx) g.tx /= 2;
   for (int d = 0; d < 3; d++) make_axis_plan(p.Nx[d], g.ax[d]);
@@ -1188,7 +1189,30 @@ void build_jobs(scft_ctx *c) {
       }
       if (!c->d_err) c->d_err = dalloc<int>(c, 1);
     }
+    // generic plane pass: out-of-place transforms when a second plane buffer
+    // fits; then bulk-copy staging of the planes when every plane is 16-byte
+    // aligned (nx ny even) and a third buffer still leaves room for two CTAs
+    // per SM
+    c->shp_mixp = c->shp_mix;
+    {
+      const int pbytes = emax_plane * (int)sizeof(float2) + 16;
+      bool even = true;
+      for (auto &I : c->inst) even = even && ((I.p.Nx[0] * I.p.Nx[1]) % 2 == 0);
+      if (!c->shp_mix.gm && c->shp_mix.smem + pbytes <= 227 * 1024) {
+        c->shp_mixp.pp = 1;
+        c->shp_mixp.smem += pbytes;
+        if (even && c->shp_mixp.smem + pbytes <= 113 * 1024) {
+          c->shp_mixp.stage = 1;
+          c->shp_mixp.smem += pbytes;
+        }
+      }
+    }
+    if (!c->d_err) c->d_err = dalloc<int>(c, 1);
     c->shp_col32 = choose_shape(emax_col, sizeof(float2), (nz_max + 32) * sizeof(float2));
+    if (!c->shp_col32.gm && c->shp_col32.smem + emax_col * (int)sizeof(float2) <= 227 * 1024) {
+      c->shp_col32.pp = 1;  // out-of-place z transforms: second tile buffer
+      c->shp_col32.smem += emax_col * (int)sizeof(float2);
+    }
     if (c->shp_mix.gm)
       throw ScftError(SCFT_ERR_UNSUPPORTED, "xy plane too large for the mixed plane pass (nx*ny*8 B > 227 KB)");
     if (c->shp_col32.gm) throw ScftError(SCFT_ERR_UNSUPPORTED, "z columns too long for the mixed z pass");
@@ -1449,7 +1473,8 @@ void mix_group_chain(scft_ctx *c, int g, cudaStream_t sg, bool update) {
       LK(launch_mix_plane64(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
                             c->tmH.data() + gr.inst_begin, act, nzi, c->d_tw32_64, s, c->d_err, sg));
     else
-      LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj + gr.pj_begin, cnt, c->d_mi, c->d_geoms, c->d_tw32, s, sg));
+      LK(launch_mix_prop_plane(c->shp_mixp, c->d_prop_pj + gr.pj_begin, cnt, c->d_mi, c->d_geoms, c->d_tw32, s,
+                               c->d_err, sg));
   }
   LK(launch_mix_q_finalize(fi, cnt_i, sg));
 }
@@ -1749,7 +1774,8 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
                             c->prop_pj_count[s] / c->inst[0].p.Nx[2], c->inst[0].p.Nx[2], c->d_tw32_64, s, c->d_err,
                             c->st));
     else if (c->mixed)
-      LK(launch_mix_prop_plane(c->shp_mix, c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_geoms, c->d_tw32, s,
+      LK(launch_mix_prop_plane(c->shp_mixp, c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_geoms, c->d_tw32, s,
+                               c->d_err,
                                c->st));
     else
       LK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[s], c->d_pi, c->d_geoms, c->d_tw64, s,

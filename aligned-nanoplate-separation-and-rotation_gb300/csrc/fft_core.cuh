@@ -194,6 +194,68 @@ __device__ __forceinline__ void fft_plane(cx<T> *plane, const DevGeom &g, const 
   fft_lines<T, SIGN, MAXV>(plane, g.ax[1], g.nx, 1, g.nx, twy);  // columns along y
 }
 
+// Out-of-place ("ping-pong") Stockham stage, src -> dst: each thread reads,
+// transforms and writes one butterfly at a time, so it holds only R values
+// and the stage needs a single barrier (after the writes).  For the FP32
+// kernels of the mixed form, whose planes leave room for a second buffer: the
+// in-place form above keeps all MAXV values of a thread in registers across
+// its barrier, which spills for MAXV >= 16.
+template <typename T, int R, int SIGN>
+__device__ __forceinline__ void fft_stage_pp(const cx<T> *__restrict__ src, cx<T> *__restrict__ dst, int n,
+                                             int nlines, int ls, int es, int Ns, const cx<T> *tw, bool lines_fast) {
+  typedef cx<T> C;
+  const int nb = n / R;
+  const int total = nb * nlines;
+  const int tstep = n / (Ns * R);
+  for (int b = threadIdx.x; b < total; b += blockDim.x) {
+    int l, j;
+    if (lines_fast) { l = b % nlines; j = b / nlines; } else { j = b % nb; l = b / nb; }
+    const int k = j % Ns;
+    const C *sp = src + l * ls + j * es;
+    C v[R];
+    v[0] = sp[0];
+#pragma unroll
+    for (int r = 1; r < R; r++) v[r] = ctw<SIGN>(sp[r * nb * es], tw[r * k * tstep]);
+    Dft<R, SIGN, C>::run(v);
+    C *dp = dst + l * ls + ((j - k) * R + k) * es;
+#pragma unroll
+    for (int r = 0; r < R; r++) dp[r * Ns * es] = v[r];
+  }
+  __syncthreads();
+}
+
+// All stages of plan `ap` alternating between buffers a and b (the data
+// starts in a and must be visible to the whole block); returns the buffer
+// holding the result.
+template <typename T, int SIGN>
+__device__ __forceinline__ cx<T> *fft_lines_pp(cx<T> *a, cx<T> *b, const AxisPlan &ap, int nlines, int ls, int es,
+                                               const cx<T> *tw) {
+  const bool lf = (ls == 1 && es != 1);
+  int Ns = 1;
+  for (int s = 0; s < ap.nst; s++) {
+    const int R = ap.radix[s];
+    if (R == 8) fft_stage_pp<T, 8, SIGN>(a, b, ap.n, nlines, ls, es, Ns, tw, lf);
+    else if (R == 4) fft_stage_pp<T, 4, SIGN>(a, b, ap.n, nlines, ls, es, Ns, tw, lf);
+    else if (R == 3) fft_stage_pp<T, 3, SIGN>(a, b, ap.n, nlines, ls, es, Ns, tw, lf);
+    else if (R == 5) fft_stage_pp<T, 5, SIGN>(a, b, ap.n, nlines, ls, es, Ns, tw, lf);
+    else fft_stage_pp<T, 2, SIGN>(a, b, ap.n, nlines, ls, es, Ns, tw, lf);
+    cx<T> *t = a;
+    a = b;
+    b = t;
+    Ns *= R;
+  }
+  return a;
+}
+
+// 2-D FFT of an nx-by-ny plane held in buffer a (other: a second buffer of
+// the same size); returns the buffer holding the result.
+template <typename T, int SIGN>
+__device__ __forceinline__ cx<T> *fft_plane_pp(cx<T> *a, cx<T> *other, const DevGeom &g, const cx<T> *twx,
+                                               const cx<T> *twy) {
+  cx<T> *r = fft_lines_pp<T, SIGN>(a, other, g.ax[0], g.ny, g.nx, 1, twx);
+  return fft_lines_pp<T, SIGN>(r, r == a ? other : a, g.ax[1], g.nx, 1, g.nx, twy);
+}
+
 // Copies a twiddle table (n entries) from global to shared memory.
 template <typename T>
 __device__ __forceinline__ void load_tw(cx<T> *dst, const cx<T> *twbuf, const AxisPlan &ap) {

@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(512) k_plane_fft(const PlaneJob *__restrict__ 
   __syncthreads();
   fft_plane<T, SIGN, MAXV>(plane, g, twx, twy);
   if (scale_by_M) {
-    const T s = (T)(1.0 / (double)g.M);
+    const T s = (T)g.inv_m;
     for (int e = threadIdx.x; e < E; e += blockDim.x) a[e] = cscale(plane[e], s);
   } else if (!GM) {
     for (int e = threadIdx.x; e < E; e += blockDim.x) a[e] = plane[e];
@@ -48,7 +48,9 @@ __global__ void __launch_bounds__(512) k_plane_fft(const PlaneJob *__restrict__ 
 // the plane pass), multiply by (1 - h) / M with h = 1 - g(k) tabulated and 1/M
 // applied as a two-float product, inverse.  Writing g = 1 - h keeps the
 // low-k bond factors, which decide Q, exact to eps*h instead of eps.
-template <typename T, int MODE, int MAXV>
+// PP: out-of-place stages between two tile buffers (fft_lines_pp; the FP32
+// passes, whose tiles leave room for the second buffer).
+template <typename T, int MODE, int MAXV, bool PP>
 __global__ void __launch_bounds__(512) k_col_fft(const ColJob *__restrict__ jobs, const DevGeom *__restrict__ geoms,
                           const cx<T> *__restrict__ twbuf, int scale_by_M) {
   typedef cx<T> C;
@@ -57,8 +59,10 @@ __global__ void __launch_bounds__(512) k_col_fft(const ColJob *__restrict__ jobs
   const DevGeom g = geoms[jb.geom];
   const int tx = g.tx, nz = g.nz;
   const int E = tx * nz;
-  C *tile = reinterpret_cast<C *>(smem_raw);
-  C *twz = tile + E;
+  C *tile0 = reinterpret_cast<C *>(smem_raw);
+  C *tile1 = tile0 + E;  // second buffer (PP)
+  C *twz = tile0 + (PP ? 2 : 1) * E;
+  C *tile = tile0;       // buffer holding the tile
   load_tw<T>(twz, twbuf, g.ax[2]);
   C *a = reinterpret_cast<C *>(jb.ptr);
   const long long plane = (long long)g.nx * g.ny;
@@ -68,26 +72,31 @@ __global__ void __launch_bounds__(512) k_col_fft(const ColJob *__restrict__ jobs
     tile[e] = a[z * plane + base + x];
   }
   __syncthreads();
-  if (MODE == 1) {
+  if (PP) {
+    tile = (MODE == 1) ? fft_lines_pp<T, +1>(tile0, tile1, g.ax[2], tx, 1, tx, twz)
+                       : fft_lines_pp<T, -1>(tile0, tile1, g.ax[2], tx, 1, tx, twz);
+  } else if (MODE == 1) {
     fft_lines<T, +1, MAXV>(tile, g.ax[2], tx, 1, tx, twz);
   } else {
     fft_lines<T, -1, MAXV>(tile, g.ax[2], tx, 1, tx, twz);
   }
   if (MODE == 2) {
     const T *kern = reinterpret_cast<const T *>(jb.kern);
-    const T s = scale_by_M ? (T)(1.0 / (double)g.M) : (T)1;
+    const T s = scale_by_M ? (T)g.inv_m : (T)1;
     for (int e = threadIdx.x; e < E; e += blockDim.x) {
       const int z = e / tx, x = e - z * tx;
       const T kv = kern[z * plane + base + x];
       tile[e] = cscale(cscale(tile[e], s), kv);
     }
     __syncthreads();
-    fft_lines<T, +1, MAXV>(tile, g.ax[2], tx, 1, tx, twz);
+    if (PP)
+      tile = fft_lines_pp<T, +1>(tile, tile == tile0 ? tile1 : tile0, g.ax[2], tx, 1, tx, twz);
+    else
+      fft_lines<T, +1, MAXV>(tile, g.ax[2], tx, 1, tx, twz);
   }
   if (MODE == 3) {
     const T *kern = reinterpret_cast<const T *>(jb.kern);
-    const double sd = 1.0 / (double)g.M;
-    const T s_hi = (T)sd, s_lo = (T)(sd - (double)s_hi);
+    const T s_hi = (T)g.inv_m_hi, s_lo = (T)g.inv_m_lo;
     for (int e = threadIdx.x; e < E; e += blockDim.x) {
       const int z = e / tx, x = e - z * tx;
       const T h = kern[z * plane + base + x];
@@ -98,9 +107,12 @@ __global__ void __launch_bounds__(512) k_col_fft(const ColJob *__restrict__ jobs
       tile[e] = t;
     }
     __syncthreads();
-    fft_lines<T, +1, MAXV>(tile, g.ax[2], tx, 1, tx, twz);
+    if (PP)
+      tile = fft_lines_pp<T, +1>(tile, tile == tile0 ? tile1 : tile0, g.ax[2], tx, 1, tx, twz);
+    else
+      fft_lines<T, +1, MAXV>(tile, g.ax[2], tx, 1, tx, twz);
   }
-  const T s = (MODE == 0 && scale_by_M) ? (T)(1.0 / (double)g.M) : (T)1;
+  const T s = (MODE == 0 && scale_by_M) ? (T)g.inv_m : (T)1;
   for (int e = threadIdx.x; e < E; e += blockDim.x) {
     const int z = e / tx, x = e - z * tx;
     a[z * plane + base + x] = (MODE == 0 && scale_by_M) ? cscale(tile[e], s) : tile[e];
@@ -134,10 +146,10 @@ cudaError_t launch_plane_fft(const LaunchShape &ls, const PlaneJob *jobs, int nj
   return launch_plane_t<T, 1, 32>(ls, jobs, njobs, geoms, tw, scale, st);
 }
 
-template <typename T, int MODE, int MAXV>
+template <typename T, int MODE, int MAXV, bool PP = false>
 static cudaError_t launch_col_t(const LaunchShape &ls, const ColJob *jobs, int njobs, const DevGeom *geoms,
                                 const void *tw, int scale, cudaStream_t st) {
-  auto kfn = k_col_fft<T, MODE, MAXV>;
+  auto kfn = k_col_fft<T, MODE, MAXV, PP>;
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, ls.smem);
   if (e != cudaSuccess) return e;
   kfn<<<njobs, ls.threads, ls.smem, st>>>(jobs, geoms, reinterpret_cast<const cx<T> *>(tw), scale);
@@ -148,6 +160,16 @@ template <typename T>
 cudaError_t launch_col_fft(const LaunchShape &ls, const ColJob *jobs, int njobs, const DevGeom *geoms,
                            const void *tw, int mode, int scale, cudaStream_t st) {
   if (njobs <= 0) return cudaSuccess;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (ls.pp) {  // the value bound does not apply out of place
+      if (mode == 0) return launch_col_t<T, 0, 8, true>(ls, jobs, njobs, geoms, tw, scale, st);
+      if (mode == 1) return launch_col_t<T, 1, 8, true>(ls, jobs, njobs, geoms, tw, scale, st);
+      if (mode == 3) return launch_col_t<T, 3, 8, true>(ls, jobs, njobs, geoms, tw, scale, st);
+      return launch_col_t<T, 2, 8, true>(ls, jobs, njobs, geoms, tw, scale, st);
+    }
+  } else {
+    if (ls.pp) return cudaErrorInvalidValue;  // FP32 only
+  }
 #define SCFT_COL(MODE)                                                                          \
   do {                                                                                          \
     if (ls.maxv <= 8) return launch_col_t<T, MODE, 8>(ls, jobs, njobs, geoms, tw, scale, st);   \

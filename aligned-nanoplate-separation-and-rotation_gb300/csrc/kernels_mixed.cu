@@ -26,6 +26,7 @@
 // Density terms are accumulated as in the FP64 kernel: for n > (N-1)/2 the
 // terms j = n and j = N-1-n pair the current step with the stored half of
 // the history; the middle term of odd N is formed in place at n = (N-1)/2.
+#include "async_copy.cuh"
 #include "fft_core.cuh"
 #include "inst.h"
 #include "launch.h"
@@ -33,15 +34,27 @@
 
 namespace scft {
 
-template <int MAXV>
+// PP: the transforms run out of place between two plane buffers
+// (fft_plane_pp), which needs E * 8 bytes more shared memory but keeps the
+// registers free of the in-place form's per-thread value arrays.
+// STAGE: the plane arrives by bulk copy (cp.async.bulk) into shared memory,
+// and so do the Boltzmann plane (issued at kernel start, so that its latency
+// overlaps the inverse transforms) and, on a paired step, the stored partner
+// plane (issued into the Boltzmann buffer once that is consumed, overlapping
+// the history store).  It needs E * 8 bytes more shared memory and 16-byte
+// aligned planes (E even); the host picks it when every plane of the batch
+// qualifies and the total fits.  Waits are bounded and set *err when they
+// run out.
+template <int MAXV, bool STAGE, bool PP>
 __global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restrict__ jobs,
                                                        const MixInst *__restrict__ insts,
                                                        const DevGeom *__restrict__ geoms,
-                                                       const float2 *__restrict__ twbuf, int n) {
+                                                       const float2 *__restrict__ twbuf, int n, int *err) {
   typedef float2 C;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ double s_red[2][32];
   __shared__ int s_exp[2];
+  __shared__ __align__(8) uint64_t s_bar[2];  // [0] working plane, [1] Boltzmann then partner plane
   const PropJob jb = jobs[blockIdx.x];
   const MixInst &P = insts[jb.inst];
   const int N = P.N, Na = P.Na;
@@ -49,12 +62,36 @@ __global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restric
   const DevGeom g = geoms[P.geom];
   const int E = g.nx * g.ny;
   const int nz = g.nz;
+  const int nbuf = PP ? 2 : 1;
   C *plane = reinterpret_cast<C *>(smem_raw);
-  C *twx = plane + E;
+  C *plane2 = plane + E;  // second buffer (PP)
+  C *twx = plane + nbuf * E;
   C *twy = twx + g.nx;
+  C *Es = reinterpret_cast<C *>(smem_raw + (((size_t)(nbuf * E + g.nx + g.ny) * sizeof(C) + 15) & ~(size_t)15));
   const long long zoff = (long long)jb.z * E;
   const long long M = g.M;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int m2 = N - 1 - n;
+  C *cur = plane;  // buffer holding the plane
+  const uint32_t pbytes = (uint32_t)E * (uint32_t)sizeof(C);
+  if (STAGE && threadIdx.x == 0) {
+    mbar_init(&s_bar[0], 1);
+    mbar_init(&s_bar[1], 1);
+    const uint64_t pol = l2_policy_last();
+    if (n > 0) {
+      mbar_expect_tx(&s_bar[0], pbytes);
+      bulk_load_1d(plane, P.work + zoff, pbytes, &s_bar[0], pol);
+    }
+    mbar_expect_tx(&s_bar[1], pbytes);
+    bulk_load_1d(Es, P.E + zoff, pbytes, &s_bar[1], pol);
+  }
+  // bounded wait on stage barrier b, phase ph (all threads)
+  auto stage_wait = [&](int b, uint32_t ph) {
+    if (!mbar_wait(&s_bar[b], ph, 1 << 22)) {
+      atomicExch(err, 1);
+      mbar_wait(&s_bar[b], ph, 1 << 22);  // let copies in flight land before the CTA moves on
+    }
+  };
   // previous step's means (FP64, same summation order in every CTA) and the
   // power-of-two exponents chosen from them
   __shared__ float s_mh[2], s_ml[2];  // the step means as two-float pairs (split once)
@@ -87,20 +124,29 @@ __global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restric
   }
   load_tw<float>(twx, twbuf, g.ax[0]);
   load_tw<float>(twy, twbuf, g.ax[1]);
-  const C *Ew = P.E + zoff;
+  const C *Ew = STAGE ? Es : P.E + zoff;
   C *work = P.work + zoff;
   const bool useA_q = (Na > 0 && n < Na);
   const bool useA_d = !(n <= N - Na - 1);
+  if (STAGE) __syncthreads();  // barriers initialised
   if (n == 0) {
+    if (STAGE) stage_wait(1, 0);
     for (int e = threadIdx.x; e < E; e += blockDim.x) {
       const C v = Ew[e];
       plane[e] = make_float2(useA_q ? v.x : v.y, useA_d ? v.x : v.y);
     }
     __syncthreads();
   } else {
-    for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = work[e];
+    if (STAGE)
+      stage_wait(0, 0);
+    else
+      for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = work[e];
     __syncthreads();
-    fft_plane<float, +1, MAXV>(plane, g, twx, twy);
+    if (PP)
+      cur = fft_plane_pp<float, +1>(plane, plane2, g, twx, twy);
+    else
+      fft_plane<float, +1, MAXV>(plane, g, twx, twy);
+    if (STAGE) stage_wait(1, 0);
   }
   const int eq = s_exp[0], ed = s_exp[1];
   const int Kq = (n == 0) ? 0 : P.K[n - 1] + eq;
@@ -112,49 +158,60 @@ __global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restric
     const float md_hi = s_mh[1], md_lo = s_ml[1];
     for (int e = threadIdx.x; e < E; e += blockDim.x) {
       const C v = Ew[e];
-      const C z = plane[e];
+      const C z = cur[e];
       const float eq_ = useA_q ? v.x : v.y, ed_ = useA_d ? v.x : v.y;
       const float uq = fmaf(z.x, eq_, fmaf(mq_hi, eq_, mq_lo * eq_));
       const float ud = fmaf(z.y, ed_, fmaf(md_hi, ed_, md_lo * ed_));
-      plane[e] = make_float2(uq * sq, ud * sd);
+      cur[e] = make_float2(uq * sq, ud * sd);
     }
   }
   if (jb.z == 0 && threadIdx.x == 0) {
     P.K[n] = Kq;
     P.K[N + n] = Kd;
   }
+  if (STAGE && m2 < n) {
+    // every thread is done with the Boltzmann buffer: reuse it for the
+    // stored partner plane, which arrives while the history is stored
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      fence_proxy_async_smem();
+      mbar_expect_tx(&s_bar[1], pbytes);
+      bulk_load_1d(Es, P.hist + (long long)m2 * M + zoff, pbytes, &s_bar[1], l2_policy_first());
+    }
+  }
   // history (first half) and plane sums (mean of the next step, Q): each
-  // thread sums its few values in FP32, the block in FP64
+  // thread sums its few values in FP32, the warp with error-free FP32
+  // two-sums, the block in FP64 (one value per warp: GB300 runs FP64 at a
+  // small fraction of the FP32 rate)
   float aqf = 0.f, adf = 0.f;
   C *hst = P.hist + (long long)n * M + zoff;
   const bool keep = (n <= P.hmax);
   for (int e = threadIdx.x; e < E; e += blockDim.x) {
-    const C z = plane[e];
+    const C z = cur[e];
     aqf += z.x;
     adf += z.y;
     if (keep) hst[e] = z;
   }
-  double aq = (double)aqf, ad = (double)adf;
   // density terms, relative to the reference exponent Kref
-  const int m2 = N - 1 - n;
   const int n0 = N / 2;  // first step that adds a term
   if (m2 <= n) {
     const int Kref = (n == n0) ? Kq + (m2 == n ? Kd : P.K[N + m2]) : P.K[2 * N];
     if (n == n0 && jb.z == 0 && threadIdx.x == 0) P.K[2 * N] = Kref;
     if (m2 < n) {
-      const C *o = P.hist + (long long)m2 * M + zoff;
+      if (STAGE) stage_wait(1, 1);
+      const C *o = STAGE ? Es : P.hist + (long long)m2 * M + zoff;
       const float f1 = ldexpf(1.0f, Kq + P.K[N + m2] - Kref);  // q_n * qdag_{m2}
       const float f2 = ldexpf(1.0f, P.K[m2] + Kd - Kref);      // q_{m2} * qdag_n
       float *a1 = P.acc[n < Na ? 0 : 1] + zoff;
       float *a2 = P.acc[m2 < Na ? 0 : 1] + zoff;
       if (a1 == a2) {
         for (int e = threadIdx.x; e < E; e += blockDim.x) {
-          const C z = plane[e], h = o[e];
+          const C z = cur[e], h = o[e];
           a1[e] += fmaf(z.x * h.y, f1, (h.x * z.y) * f2);
         }
       } else {
         for (int e = threadIdx.x; e < E; e += blockDim.x) {
-          const C z = plane[e], h = o[e];
+          const C z = cur[e], h = o[e];
           a1[e] += (z.x * h.y) * f1;
           a2[e] += (h.x * z.y) * f2;
         }
@@ -163,24 +220,33 @@ __global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restric
       const float f = ldexpf(1.0f, Kq + Kd - Kref);
       float *a1 = P.acc[n < Na ? 0 : 1] + zoff;
       for (int e = threadIdx.x; e < E; e += blockDim.x) {
-        const C z = plane[e];
+        const C z = cur[e];
         a1[e] += (z.x * z.y) * f;
       }
     }
   }
-  for (int o = 16; o > 0; o >>= 1) {
-    aq += __shfl_down_sync(0xffffffffu, aq, o);
-    ad += __shfl_down_sync(0xffffffffu, ad, o);
-  }
-  if (lane == 0) {
-    s_red[0][warp] = aq;
-    s_red[1][warp] = ad;
+  {
+    float cq = 0.f, cd = 0.f;
+    for (int o = 16; o > 0; o >>= 1) {
+      const float s2 = __shfl_down_sync(0xffffffffu, aqf, o), c2 = __shfl_down_sync(0xffffffffu, cq, o);
+      const float t2 = __shfl_down_sync(0xffffffffu, adf, o), d2 = __shfl_down_sync(0xffffffffu, cd, o);
+      float sa = aqf + s2, va = sa - aqf;
+      cq += c2 + ((aqf - (sa - va)) + (s2 - va));
+      aqf = sa;
+      float sb = adf + t2, vb = sb - adf;
+      cd += d2 + ((adf - (sb - vb)) + (t2 - vb));
+      adf = sb;
+    }
+    if (lane == 0) {
+      s_red[0][warp] = (double)aqf + (double)cq;
+      s_red[1][warp] = (double)adf + (double)cd;
+    }
   }
   __syncthreads();
   if (warp == 0) {
     const int nw = (blockDim.x + 31) >> 5;
-    aq = lane < nw ? s_red[0][lane] : 0.0;
-    ad = lane < nw ? s_red[1][lane] : 0.0;
+    double aq = lane < nw ? s_red[0][lane] : 0.0;
+    double ad = lane < nw ? s_red[1][lane] : 0.0;
     for (int o = 16; o > 0; o >>= 1) {
       aq += __shfl_down_sync(0xffffffffu, aq, o);
       ad += __shfl_down_sync(0xffffffffu, ad, o);
@@ -192,8 +258,12 @@ __global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restric
   }
   if (n == N - 1) return;
   __syncthreads();
-  fft_plane<float, -1, MAXV>(plane, g, twx, twy);
-  for (int e = threadIdx.x; e < E; e += blockDim.x) work[e] = plane[e];
+  if (PP) {
+    cur = fft_plane_pp<float, -1>(cur, cur == plane ? plane2 : plane, g, twx, twy);
+  } else {
+    fft_plane<float, -1, MAXV>(plane, g, twx, twy);
+  }
+  for (int e = threadIdx.x; e < E; e += blockDim.x) work[e] = cur[e];
 }
 
 // Graft sweeps of the mixed form (code/grafted_nanoparticle.cpp:15-117), one
@@ -324,22 +394,30 @@ cudaError_t launch_mix_graft_plane(const LaunchShape &ls, const PropJob *jobs, i
   return launch_mix_graft_t<32>(ls, jobs, njobs, insts, geoms, tw, sweep, n, st);
 }
 
-template <int MAXV>
+template <int MAXV, bool STAGE, bool PP>
 static cudaError_t launch_mix_t(const LaunchShape &ls, const PropJob *jobs, int njobs, const MixInst *insts,
-                                const DevGeom *geoms, const void *tw, int n, cudaStream_t st) {
-  auto kfn = k_mix_prop_plane<MAXV>;
+                                const DevGeom *geoms, const void *tw, int n, int *err, cudaStream_t st) {
+  auto kfn = k_mix_prop_plane<MAXV, STAGE, PP>;
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, ls.smem);
   if (e != cudaSuccess) return e;
-  kfn<<<njobs, ls.threads, ls.smem, st>>>(jobs, insts, geoms, reinterpret_cast<const float2 *>(tw), n);
+  kfn<<<njobs, ls.threads, ls.smem, st>>>(jobs, insts, geoms, reinterpret_cast<const float2 *>(tw), n, err);
   return cudaGetLastError();
 }
 
 cudaError_t launch_mix_prop_plane(const LaunchShape &ls, const PropJob *jobs, int njobs, const MixInst *insts,
-                                  const DevGeom *geoms, const void *tw, int n, cudaStream_t st) {
+                                  const DevGeom *geoms, const void *tw, int n, int *err, cudaStream_t st) {
   if (njobs <= 0) return cudaSuccess;
-  if (ls.maxv <= 8) return launch_mix_t<8>(ls, jobs, njobs, insts, geoms, tw, n, st);
-  if (ls.maxv <= 16) return launch_mix_t<16>(ls, jobs, njobs, insts, geoms, tw, n, st);
-  return launch_mix_t<32>(ls, jobs, njobs, insts, geoms, tw, n, st);
+  if (ls.pp) {  // the value bound does not apply out of place
+    if (ls.stage) {
+      if (!err) return cudaErrorInvalidValue;
+      return launch_mix_t<8, true, true>(ls, jobs, njobs, insts, geoms, tw, n, err, st);
+    }
+    return launch_mix_t<8, false, true>(ls, jobs, njobs, insts, geoms, tw, n, err, st);
+  }
+  if (ls.stage) return cudaErrorInvalidValue;  // staging is laid out for the out-of-place form
+  if (ls.maxv <= 8) return launch_mix_t<8, false, false>(ls, jobs, njobs, insts, geoms, tw, n, err, st);
+  if (ls.maxv <= 16) return launch_mix_t<16, false, false>(ls, jobs, njobs, insts, geoms, tw, n, err, st);
+  return launch_mix_t<32, false, false>(ls, jobs, njobs, insts, geoms, tw, n, err, st);
 }
 
 }  // namespace scft

@@ -25,6 +25,7 @@
 // Plane sums are formed with error-free FP32 two-sums per thread and across
 // the warp (FP64 only for the 16 warp results): GB300 issues FP64 at a small
 // fraction of its FP32 rate.
+#include "async_copy.cuh"
 #include "fft_core.cuh"
 #include "inst.h"
 #include "launch.h"
@@ -68,58 +69,13 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
   e = (a - (s - bb)) + (b - bb);
 }
 
-// L2 policies: the history is written once and read once about N/2 steps
-// later, so it is streamed with evict-first; the Boltzmann factors are read by
-// every step and kept with evict-last.  The per-step arrays (propagator,
-// factors, accumulators) then stay in L2 while the history streams past.
-__device__ __forceinline__ uint64_t l2_policy_first() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;\n" : "=l"(p));
-  return p;
-}
-__device__ __forceinline__ uint64_t l2_policy_last() {
-  uint64_t p;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;\n" : "=l"(p));
-  return p;
-}
+// The per-step arrays (propagator, factors, accumulators) stay in L2 while
+// the history streams past with evict-first (async_copy.cuh).
 __device__ __forceinline__ void st_stream(float2 *g, float2 v, uint64_t pol) {
   asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;\n" ::"l"(g), "f"(v.x), "f"(v.y), "l"(pol)
                : "memory");
 }
 
-// mbarrier and TMA (tensor) helpers; addresses are shared-window offsets.
-__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
-  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count));
-  asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
-               : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
-  uint32_t ok;
-  asm volatile(
-      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
-      : "=r"(ok)
-      : "r"(smem_u32(bar)), "r"(parity)
-      : "memory");
-  return ok != 0;
-}
-// bounded wait: false if the phase did not complete within `limit` polls
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, int limit) {
-  for (int k = 0; k < limit; k++)
-    if (mbar_try_wait(bar, parity)) return true;
-  return false;
-}
-__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar,
-                                            uint64_t policy) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint "
-      "[%0], [%1, {%2, %3}], [%4], %5;\n" ::"r"(smem_u32(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_u32(bar)), "l"(policy)
-      : "memory");
-}
 // Element (row, x) of a plane staged by four 64 x 128 B boxes with the
 // 128-byte swizzle: box x / 16, 16-byte chunk ((x % 16) / 2) ^ (row % 8).
 __device__ __forceinline__ float2 swz(const float2 *plane, int row, int x) {

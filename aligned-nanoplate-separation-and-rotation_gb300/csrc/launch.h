@@ -16,6 +16,8 @@ struct LaunchShape {
   int smem;
   int maxv;
   int gm;
+  int pp = 0;     // FP32 transforms out of place between two buffers (smem includes the second one)
+  int stage = 0;  // mixed plane pass: planes staged by bulk copy (smem includes that buffer too; needs pp)
 };
 
 template <typename T>

@@ -169,6 +169,7 @@ int noalloc_diblock(const int *Nx, const double *L, int Nda, int Ndb, double nD,
     }
   }
   g.M = (long long)g.nx * g.ny * g.nz;
+  set_inv_m(g);
   g.tx = 16;
   while (g.nx % g.tx) g.tx /= 2;
   g.ax[0].tw = 0;

@@ -23,8 +23,9 @@ cudaError_t launch_density(const FieldInst *fi, int ninst, int blocks, cudaStrea
 cudaError_t launch_update_1s(const FieldInst *fi, int ninst, int blocks, cudaStream_t st);
 cudaError_t launch_h_partials(const FieldInst *fi, int ninst, int blocks, double2 *out, cudaStream_t st);
 
+// err: error word set when a bounded wait of the staged form runs out (needed when ls.stage)
 cudaError_t launch_mix_prop_plane(const LaunchShape &ls, const PropJob *jobs, int njobs, const MixInst *insts,
-                                  const DevGeom *geoms, const void *tw, int n, cudaStream_t st);
+                                  const DevGeom *geoms, const void *tw, int n, int *err, cudaStream_t st);
 // Instances of one 64^3 plane-pass launch, passed by value as the kernel
 // parameter (15.4 KB: TMA descriptors of each instance's Boltzmann and
 // history arrays, the instance views, the error word); larger batches are
