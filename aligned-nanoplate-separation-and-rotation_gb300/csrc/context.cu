@@ -1189,16 +1189,27 @@ void build_jobs(scft_ctx *c) {
       }
       if (!c->d_err) c->d_err = dalloc<int>(c, 1);
     }
-    // generic plane pass: out-of-place transforms when a second plane buffer
-    // fits; then bulk-copy staging of the planes when every plane is 16-byte
-    // aligned (nx ny even) and a third buffer still leaves room for two CTAs
-    // per SM
-    c->shp_mixp = c->shp_mix;
+    // Mixed plane passes in place (graft sweeps; the diblock sweep when a
+    // second buffer does not fit): planes above 8192 points (128 x 128) run
+    // with 16 values per thread on up to 1024 threads -- one CTA per SM by
+    // shared memory either way, and half the per-thread values (and spills)
+    // of the 512-thread shape.
+    c->shp_mixg = c->shp_mix;
+    if (emax_plane > 8192 && (emax_plane + 15) / 16 <= 1024) {
+      c->shp_mixg.maxv = 16;
+      c->shp_mixg.threads = ((emax_plane + 15) / 16 + 31) / 32 * 32;
+    }
+    // Diblock plane pass: out-of-place transforms (at most 512 threads) when a
+    // second plane buffer fits; then bulk-copy staging of the planes when
+    // every plane is 16-byte aligned (nx ny even) and a third buffer still
+    // leaves room for two CTAs per SM.
+    c->shp_mixp = c->shp_mixg;
     {
       const int pbytes = emax_plane * (int)sizeof(float2) + 16;
       bool even = true;
       for (auto &I : c->inst) even = even && ((I.p.Nx[0] * I.p.Nx[1]) % 2 == 0);
       if (!c->shp_mix.gm && c->shp_mix.smem + pbytes <= 227 * 1024) {
+        c->shp_mixp = c->shp_mix;
         c->shp_mixp.pp = 1;
         c->shp_mixp.smem += pbytes;
         if (even && c->shp_mixp.smem + pbytes <= 113 * 1024) {
@@ -1506,12 +1517,12 @@ void seq_mix(scft_ctx *c, bool update) {
     for (auto &I : c->inst)
       if (I.graft) CK(cudaMemsetAsync(I.gacc32, 0, sizeof(float) * I.M, st));
     for (int sweep = 0; sweep < 2; sweep++) {
-      LK(launch_mix_graft_plane(c->shp_mix, c->d_graft_pj, c->graft_pj_count[0], c->d_gmi, c->d_geoms, c->d_tw32,
+      LK(launch_mix_graft_plane(c->shp_mixg, c->d_graft_pj, c->graft_pj_count[0], c->d_gmi, c->d_geoms, c->d_tw32,
                                 sweep, 0, st));
       for (int s = 1; s < c->ngmax; s++) {
         LK(launch_col_fft<float>(c->shp_col32, c->d_graft_cj, c->graft_cj_count[s], c->d_geoms, c->d_tw32, 3, 1,
                                  st));
-        LK(launch_mix_graft_plane(c->shp_mix, c->d_graft_pj, c->graft_pj_count[s], c->d_gmi, c->d_geoms, c->d_tw32,
+        LK(launch_mix_graft_plane(c->shp_mixg, c->d_graft_pj, c->graft_pj_count[s], c->d_gmi, c->d_geoms, c->d_tw32,
                                   sweep, s, st));
       }
     }

@@ -157,7 +157,8 @@ struct scft_ctx {
   std::vector<cudaEvent_t> ev_join;
   cudaEvent_t ev_fork = nullptr;
   scft::LaunchShape shp_mix{}, shp_col32{}, shp_plane32{};
-  scft::LaunchShape shp_mixp{};  // generic mixed plane pass (shp_mix, plus bulk-copy staging where it fits)
+  scft::LaunchShape shp_mixg{};  // mixed plane passes in place (shp_mix; 1024 threads for the largest planes)
+  scft::LaunchShape shp_mixp{};  // generic mixed plane pass (out of place and staged where it fits, else shp_mixg)
   scft::LaunchShape shp_plane{}, shp_col{}, shp_prop{};
   int eblocks = 0;  // blocks per instance for pointwise kernels
   double2 *d_hpart = nullptr;

@@ -45,8 +45,13 @@ namespace scft {
 // aligned planes (E even); the host picks it when every plane of the batch
 // qualifies and the total fits.  Waits are bounded and set *err when they
 // run out.
+// Launch bounds: the out-of-place form runs up to 512 threads, two CTAs per
+// SM (64 registers); the in-place form keeps a thread's MAXV values live
+// across its barriers and runs one CTA per SM (its plane fills shared
+// memory), with MAXV = 16 on up to 1024 threads for planes too large for a
+// second buffer (128 x 128).
 template <int MAXV, bool STAGE, bool PP>
-__global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restrict__ jobs,
+__global__ void __launch_bounds__(PP ? 512 : (MAXV == 16 ? 1024 : 512), PP ? 2 : 1) k_mix_prop_plane(const PropJob *__restrict__ jobs,
                                                        const MixInst *__restrict__ insts,
                                                        const DevGeom *__restrict__ geoms,
                                                        const float2 *__restrict__ twbuf, int n, int *err) {
@@ -274,7 +279,7 @@ __global__ void __launch_bounds__(512) k_mix_prop_plane(const PropJob *__restric
 // power-of-two rescaling exactly as in the diblock sweep; with qdag_g[0]
 // scaled by 2^-K[0][Ng-1] the products need no reference exponent.
 template <int MAXV>
-__global__ void __launch_bounds__(512) k_mix_graft_plane(const PropJob *__restrict__ jobs,
+__global__ void __launch_bounds__(MAXV == 16 ? 1024 : 512, 1) k_mix_graft_plane(const PropJob *__restrict__ jobs,
                                                         const GraftMixInst *__restrict__ insts,
                                                         const DevGeom *__restrict__ geoms,
                                                         const float2 *__restrict__ twbuf, int sweep, int n) {

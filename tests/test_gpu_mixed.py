@@ -213,26 +213,34 @@ def test_mixed_grid_batch_runs_64cubed_on_the_64_point_kernels(scft):
             assert rel(d1[0][0].real, d32[k][0].real) < RHO_TOL
 
 
-def grafted_params(scft, prec, theta=20.0):
-    """Config 4's chemistry at a small size: two rotated plates grafted with
+GRAFT_GEOMS = {
+    "two_plates_32": dict(grid=(32, 32, 32), box_rg=(4.0, 4.0, 4.0),
+                          centers=((0.5, 0.5, 0.375), (0.5, 0.5, 0.625))),
+    # 128 x 128 planes: the in-place plane passes with 1024 threads
+    "one_plate_128x128x16": dict(grid=(128, 128, 16), box_rg=(4.0, 4.0, 2.0), centers=((0.5, 0.5, 0.5),)),
+}
+
+
+def grafted_params(scft, prec, theta=20.0, geom="two_plates_32"):
+    """Config 4's chemistry at a small size: rotated plates grafted with
     chains of the A-like species C (chi_AC = 0, chi_BC = chi_AB)."""
     from scft.workloads import plate_params, rg
 
     N = 32
-    p = plate_params(theta, N=N, fA=0.4, chiN=30.0, grid=(32, 32, 32), box_rg=(4.0, 4.0, 4.0), precision=prec,
-                     centers=((0.5, 0.5, 0.375), (0.5, 0.5, 0.625)), thickness_rg=0.3, radius_rg=0.8, xi_rg=0.2,
-                     sigma=0.5 / rg(N) ** 2, Ng=8, lam_pl=0.002, lam_mi=0.001)
+    p = plate_params(theta, N=N, fA=0.4, chiN=30.0, precision=prec, thickness_rg=0.3, radius_rg=0.8, xi_rg=0.2,
+                     sigma=0.5 / rg(N) ** 2, Ng=8, lam_pl=0.002, lam_mi=0.001, **GRAFT_GEOMS[geom])
     p.chi_bc = p.chi_ab
     return p
 
 
-def test_mixed_grafted_plates_match_fp64(scft):
+@pytest.mark.parametrize("geom", sorted(GRAFT_GEOMS))
+def test_mixed_grafted_plates_match_fp64(scft, geom):
     from scft.workloads import seeded_fields
 
-    f = seeded_fields(grafted_params(scft, scft.PREC_FP64), 21)
+    f = seeded_fields(grafted_params(scft, scft.PREC_FP64, geom=geom), 21)
     out = {}
     for prec in (scft.PREC_FP64, scft.PREC_MIXED):
-        with scft.Context(grafted_params(scft, prec)) as ctx:
+        with scft.Context(grafted_params(scft, prec, geom=geom)) as ctx:
             assert ctx.info(0)["phiG"] > 0
             ctx.set_fields(0, f)
             ctx.calc_poly_density()
