@@ -1154,6 +1154,10 @@ void build_jobs(scft_ctx *c) {
     build_groups(c);
     c->shp_mix = choose_shape(emax_plane, sizeof(float2), (nxy_max + 32) * sizeof(float2));
     c->shp_plane32 = c->shp_mix;  // same plane and twiddle footprint
+    if (!c->shp_mix.gm && c->shp_mix.smem + emax_plane * (int)sizeof(float2) <= 227 * 1024) {
+      c->shp_plane32.pp = 1;  // FP32 field transforms out of place: second plane buffer
+      c->shp_plane32.smem += emax_plane * (int)sizeof(float2);
+    }
     // 64-point kernel tables, indexed by job-order position (64 x (64 / tx)
     // z-pass jobs per instance); entries of generic-class instances are
     // placeholders that no launch reads

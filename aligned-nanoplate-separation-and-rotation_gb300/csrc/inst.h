@@ -12,7 +12,9 @@ enum ScalarSlot {
   kQga = 2,      // Qga_exp (code/grafted_nanoparticle.cpp:112)
   kQg = 3,       // graft propagator check: count of points with Re q_g[Ng-1] <= 0 in .x
   kSmean = 4,    // mixed form: means of smwa (.x) and smwb (.y), kept out of the FP32 transform
-  kNumScalars = 5
+  kSmean32 = 5,  // the same as two-float pairs (hi, lo of smwa, hi, lo of smwb) in the slot's 16 bytes
+  kFactor32 = 6, // mixed form: nD / Q / V * 2^Kref as an FP32 mantissa (bytes 0-3) and exponent (int, bytes 4-7)
+  kNumScalars = 7
 };
 
 // View of one instance for the propagator sweeps.  Propagator p = 0 is q

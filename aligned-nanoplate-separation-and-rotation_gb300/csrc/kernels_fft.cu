@@ -16,7 +16,9 @@
 namespace scft {
 
 // GM: the plane is transformed in place in global memory (see LaunchShape).
-template <typename T, int SIGN, int MAXV, bool GM>
+// PP: out-of-place stages between two shared buffers (FP32 planes that leave
+// room for the second one).
+template <typename T, int SIGN, int MAXV, bool GM, bool PP>
 __global__ void __launch_bounds__(512) k_plane_fft(const PlaneJob *__restrict__ jobs, const DevGeom *__restrict__ geoms,
                             const cx<T> *__restrict__ twbuf, int scale_by_M) {
   typedef cx<T> C;
@@ -26,14 +28,17 @@ __global__ void __launch_bounds__(512) k_plane_fft(const PlaneJob *__restrict__ 
   const int E = g.nx * g.ny;
   C *a = reinterpret_cast<C *>(jb.ptr) + (long long)jb.z * E;
   C *plane = GM ? a : reinterpret_cast<C *>(smem_raw);
-  C *twx = GM ? reinterpret_cast<C *>(smem_raw) : plane + E;
+  C *twx = GM ? reinterpret_cast<C *>(smem_raw) : plane + (PP ? 2 : 1) * E;
   C *twy = twx + g.nx;
   load_tw<T>(twx, twbuf, g.ax[0]);
   load_tw<T>(twy, twbuf, g.ax[1]);
   if (!GM)
     for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = a[e];
   __syncthreads();
-  fft_plane<T, SIGN, MAXV>(plane, g, twx, twy);
+  if (PP)
+    plane = fft_plane_pp<T, SIGN>(plane, plane + E, g, twx, twy);
+  else
+    fft_plane<T, SIGN, MAXV>(plane, g, twx, twy);
   if (scale_by_M) {
     const T s = (T)g.inv_m;
     for (int e = threadIdx.x; e < E; e += blockDim.x) a[e] = cscale(plane[e], s);
@@ -67,9 +72,21 @@ __global__ void __launch_bounds__(512) k_col_fft(const ColJob *__restrict__ jobs
   C *a = reinterpret_cast<C *>(jb.ptr);
   const long long plane = (long long)g.nx * g.ny;
   const long long base = (long long)jb.y * g.nx + jb.x0;
-  for (int e = threadIdx.x; e < E; e += blockDim.x) {
-    const int z = e / tx, x = e - z * tx;
-    tile[e] = a[z * plane + base + x];
+  // tx is a power of two (16 halved until it divides nx); four independent
+  // loads in flight per thread and round
+  const int ltx = __ffs(tx) - 1;
+  for (int e0 = threadIdx.x; e0 < E; e0 += 4 * blockDim.x) {
+    C t4[4];
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int e = e0 + u * blockDim.x;
+      if (e < E) t4[u] = a[(e >> ltx) * plane + base + (e & (tx - 1))];
+    }
+#pragma unroll
+    for (int u = 0; u < 4; u++) {
+      const int e = e0 + u * blockDim.x;
+      if (e < E) tile[e] = t4[u];
+    }
   }
   __syncthreads();
   if (PP) {
@@ -84,7 +101,7 @@ __global__ void __launch_bounds__(512) k_col_fft(const ColJob *__restrict__ jobs
     const T *kern = reinterpret_cast<const T *>(jb.kern);
     const T s = scale_by_M ? (T)g.inv_m : (T)1;
     for (int e = threadIdx.x; e < E; e += blockDim.x) {
-      const int z = e / tx, x = e - z * tx;
+      const int z = e >> ltx, x = e & (tx - 1);
       const T kv = kern[z * plane + base + x];
       tile[e] = cscale(cscale(tile[e], s), kv);
     }
@@ -98,7 +115,7 @@ __global__ void __launch_bounds__(512) k_col_fft(const ColJob *__restrict__ jobs
     const T *kern = reinterpret_cast<const T *>(jb.kern);
     const T s_hi = (T)g.inv_m_hi, s_lo = (T)g.inv_m_lo;
     for (int e = threadIdx.x; e < E; e += blockDim.x) {
-      const int z = e / tx, x = e - z * tx;
+      const int z = e >> ltx, x = e & (tx - 1);
       const T h = kern[z * plane + base + x];
       const C v = tile[e];
       C t = mkc(fma(v.x, s_hi, v.x * s_lo), fma(v.y, s_hi, v.y * s_lo));
@@ -114,7 +131,7 @@ __global__ void __launch_bounds__(512) k_col_fft(const ColJob *__restrict__ jobs
   }
   const T s = (MODE == 0 && scale_by_M) ? (T)g.inv_m : (T)1;
   for (int e = threadIdx.x; e < E; e += blockDim.x) {
-    const int z = e / tx, x = e - z * tx;
+    const int z = e >> ltx, x = e & (tx - 1);
     a[z * plane + base + x] = (MODE == 0 && scale_by_M) ? cscale(tile[e], s) : tile[e];
   }
 }
@@ -125,7 +142,12 @@ __global__ void __launch_bounds__(512) k_col_fft(const ColJob *__restrict__ jobs
 template <typename T, int SIGN, int MAXV>
 static cudaError_t launch_plane_t(const LaunchShape &ls, const PlaneJob *jobs, int njobs, const DevGeom *geoms,
                                   const void *tw, int scale, cudaStream_t st) {
-  auto kfn = ls.gm ? k_plane_fft<T, SIGN, MAXV, true> : k_plane_fft<T, SIGN, MAXV, false>;
+  auto kfn = ls.gm ? k_plane_fft<T, SIGN, MAXV, true, false> : k_plane_fft<T, SIGN, MAXV, false, false>;
+  if constexpr (sizeof(T) == sizeof(float)) {
+    if (ls.pp) kfn = k_plane_fft<T, SIGN, 8, false, true>;  // the value bound does not apply out of place
+  } else {
+    if (ls.pp) return cudaErrorInvalidValue;  // FP32 only
+  }
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, ls.smem);
   if (e != cudaSuccess) return e;
   kfn<<<njobs, ls.threads, ls.smem, st>>>(jobs, geoms, reinterpret_cast<const cx<T> *>(tw), scale);

@@ -466,6 +466,10 @@ __device__ __forceinline__ double2 smear_pack(const FieldInst &F, long long i, c
 __device__ __forceinline__ void store_zs(const FieldInst &F, long long i, double2 zs) {
   if (i == 0) {
     F.scal[kSmean] = zs;
+    // the two-float pairs the Boltzmann kernel needs, formed once here
+    const float ah = (float)zs.x, bh = (float)zs.y;
+    *reinterpret_cast<float4 *>(&F.scal[kSmean32]) =
+        make_float4(ah, (float)(zs.x - (double)ah), bh, (float)(zs.y - (double)bh));
     F.z32[0] = make_float2(0.0f, 0.0f);
   } else {
     F.z32[i] = make_float2((float)zs.x, (float)zs.y);
@@ -617,18 +621,11 @@ __device__ __forceinline__ float boltz_two_float(float mh, float ml, float d) {
 }
 
 __global__ void k_mix_boltzmann(const FieldInst *__restrict__ fi) {
-  // the means split once per block: GB300 runs FP64 (conversions included)
-  // at a small fraction of the FP32 rate, so no per-point FP64 work here
-  __shared__ float s_m[4];
-  if (threadIdx.x == 0) {
-    const double2 m = fi[blockIdx.y].scal[kSmean];
-    s_m[0] = (float)m.x;
-    s_m[1] = (float)(m.x - (double)s_m[0]);
-    s_m[2] = (float)m.y;
-    s_m[3] = (float)(m.y - (double)s_m[2]);
-  }
-  __syncthreads();
-  const float ah = s_m[0], al = s_m[1], bh = s_m[2], bl = s_m[3];
+  // the means as two-float pairs, split once by the kernel that formed them:
+  // GB300 runs FP64 (conversions included) at a small fraction of the FP32
+  // rate, so no per-point or per-block FP64 work here
+  const float4 m = *reinterpret_cast<const float4 *>(&fi[blockIdx.y].scal[kSmean32]);
+  const float ah = m.x, al = m.y, bh = m.z, bl = m.w;
   FOR_POINTS(F) {
     if (F.graft) {
       const double sg = F.zg[i].x;
@@ -655,6 +652,9 @@ __global__ void k_mix_q_finalize(const FieldInst *__restrict__ fi, int ninst) {
   const double Q = s / F.V;
   F.scal[kQd] = make_double2(Q, 0.0);
   F.scal[kFactor] = make_double2(F.nD / Q / F.V, 0.0);
+  int fe;
+  const float fm = (float)frexp(ldexp(F.nD / Q / F.V, F.K[2 * F.N]), &fe);
+  *reinterpret_cast<float2 *>(&F.scal[kFactor32]) = make_float2(fm, __int_as_float(fe));
 }
 
 // rho_A, rho_B = acc * e^{+smw} * factor, packed into z32 for the FP32
@@ -663,22 +663,16 @@ __global__ void k_mix_q_finalize(const FieldInst *__restrict__ fi, int ninst) {
 // accumulators' exponent and can lie outside the FP32 range: it is applied as
 // an FP32 mantissa and an ldexpf.
 __global__ void k_mix_rho_pack(const FieldInst *__restrict__ fi, int keep) {
-  // the factor (accumulators are scaled by 2^-Kref) formed once per block
-  __shared__ double s_f;
-  __shared__ float s_fm;
-  __shared__ int s_fe;
-  if (threadIdx.x == 0) {
+  // the factor (accumulators are scaled by 2^-Kref): FP32 mantissa and
+  // exponent from k_mix_q_finalize; FP64 (formed here) only for keep
+  const float2 fx = *reinterpret_cast<const float2 *>(&fi[blockIdx.y].scal[kFactor32]);
+  const float fm = fx.x;
+  const int fe = __float_as_int(fx.y);
+  double f = 0.0;
+  if (keep) {
     const FieldInst &F0 = fi[blockIdx.y];
-    const double f = ldexp(F0.scal[kFactor].x, F0.K[2 * F0.N]);
-    int fe;
-    s_fm = (float)frexp(f, &fe);
-    s_fe = fe;
-    s_f = f;
+    f = ldexp(F0.scal[kFactor].x, F0.K[2 * F0.N]);
   }
-  __syncthreads();
-  const double f = s_f;
-  const float fm = s_fm;
-  const int fe = s_fe;
   FOR_POINTS(F) {
     // e^{+smw} = 1 / e^{-smw}: the FP32 reciprocal of the Boltzmann factor
     const float2 E = F.E32[i];

@@ -142,10 +142,24 @@ __global__ void __launch_bounds__(PP ? 512 : (MAXV == 16 ? 1024 : 512), PP ? 2 :
     }
     __syncthreads();
   } else {
-    if (STAGE)
+    if (STAGE) {
       stage_wait(0, 0);
-    else
-      for (int e = threadIdx.x; e < E; e += blockDim.x) plane[e] = work[e];
+    } else {
+      // four independent loads in flight per thread and round
+      for (int e0 = threadIdx.x; e0 < E; e0 += 4 * blockDim.x) {
+        C w4[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int e = e0 + u * blockDim.x;
+          if (e < E) w4[u] = work[e];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int e = e0 + u * blockDim.x;
+          if (e < E) plane[e] = w4[u];
+        }
+      }
+    }
     __syncthreads();
     if (PP)
       cur = fft_plane_pp<float, +1>(plane, plane2, g, twx, twy);
@@ -161,13 +175,24 @@ __global__ void __launch_bounds__(PP ? 512 : (MAXV == 16 ? 1024 : 512), PP ? 2 :
     const float sq = ldexpf(1.0f, -eq), sd = ldexpf(1.0f, -ed);
     const float mq_hi = s_mh[0], mq_lo = s_ml[0];
     const float md_hi = s_mh[1], md_lo = s_ml[1];
-    for (int e = threadIdx.x; e < E; e += blockDim.x) {
-      const C v = Ew[e];
-      const C z = cur[e];
-      const float eq_ = useA_q ? v.x : v.y, ed_ = useA_d ? v.x : v.y;
-      const float uq = fmaf(z.x, eq_, fmaf(mq_hi, eq_, mq_lo * eq_));
-      const float ud = fmaf(z.y, ed_, fmaf(md_hi, ed_, md_lo * ed_));
-      cur[e] = make_float2(uq * sq, ud * sd);
+    for (int e0 = threadIdx.x; e0 < E; e0 += 4 * blockDim.x) {
+      C v4[4];
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int e = e0 + u * blockDim.x;
+        if (e < E) v4[u] = Ew[e];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; u++) {
+        const int e = e0 + u * blockDim.x;
+        if (e >= E) break;
+        const C v = v4[u];
+        const C z = cur[e];
+        const float eq_ = useA_q ? v.x : v.y, ed_ = useA_d ? v.x : v.y;
+        const float uq = fmaf(z.x, eq_, fmaf(mq_hi, eq_, mq_lo * eq_));
+        const float ud = fmaf(z.y, ed_, fmaf(md_hi, ed_, md_lo * ed_));
+        cur[e] = make_float2(uq * sq, ud * sd);
+      }
     }
   }
   if (jb.z == 0 && threadIdx.x == 0) {
@@ -209,16 +234,30 @@ __global__ void __launch_bounds__(PP ? 512 : (MAXV == 16 ? 1024 : 512), PP ? 2 :
       const float f2 = ldexpf(1.0f, P.K[m2] + Kd - Kref);      // q_{m2} * qdag_n
       float *a1 = P.acc[n < Na ? 0 : 1] + zoff;
       float *a2 = P.acc[m2 < Na ? 0 : 1] + zoff;
-      if (a1 == a2) {
-        for (int e = threadIdx.x; e < E; e += blockDim.x) {
-          const C z = cur[e], h = o[e];
-          a1[e] += fmaf(z.x * h.y, f1, (h.x * z.y) * f2);
+      const bool same = (a1 == a2);
+      for (int e0 = threadIdx.x; e0 < E; e0 += 4 * blockDim.x) {
+        C h4[4];
+        float b1[4], b2[4];
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int e = e0 + u * blockDim.x;
+          if (e < E) {
+            h4[u] = o[e];
+            b1[u] = a1[e];
+            if (!same) b2[u] = a2[e];
+          }
         }
-      } else {
-        for (int e = threadIdx.x; e < E; e += blockDim.x) {
-          const C z = cur[e], h = o[e];
-          a1[e] += (z.x * h.y) * f1;
-          a2[e] += (h.x * z.y) * f2;
+#pragma unroll
+        for (int u = 0; u < 4; u++) {
+          const int e = e0 + u * blockDim.x;
+          if (e >= E) break;
+          const C z = cur[e], h = h4[u];
+          if (same) {
+            a1[e] = b1[u] + fmaf(z.x * h.y, f1, (h.x * z.y) * f2);
+          } else {
+            a1[e] = b1[u] + (z.x * h.y) * f1;
+            a2[e] = b2[u] + (h.x * z.y) * f2;
+          }
         }
       }
     } else {
