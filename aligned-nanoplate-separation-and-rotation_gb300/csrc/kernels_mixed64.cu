@@ -184,15 +184,20 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
     __syncthreads();
 #pragma unroll
     for (int a = 0; a < 8; a++) v[a] = buf[row * kRowPad + tr + 8 * a];
-    __syncthreads();
+    // a row's exchange area (row * kRowPad + 9b + c < (row + 1) * kRowPad)
+    // lies inside the padded row, and a warp owns whole rows: a warp
+    // barrier suffices before the exchange overwrites what was just read
+    __syncwarp();
     // inverse x transform (row phase, inside one warp)
     fft64_group<+1, true>(v, tr, buf + row * kRowPad, 9, 1, tw);
   }
+  // every thread waits on the mbarrier itself (acquiring the staged planes),
+  // and the shared plane is touched only in the thread's own rows until the
+  // barrier of the plane sums: no block barrier here
   if (!mbar_wait(&s_bar, 0, 1 << 22)) {
     atomicExch(T.err, 1);
     mbar_wait(&s_bar, 0, 1 << 22);  // let copies in flight land before the CTA moves on
   }
-  __syncthreads();
 
   if (n == 0) {
 #pragma unroll
