@@ -38,7 +38,7 @@ METRIC = "SCFT iters/s @64^3,N=100"
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant
 # kernel, from an ncu capture of the same workload (the paired plane-pass step;
 # profiles/mixed_kernels_sweep15_64_N100_ncu.txt).  Only valid for that workload.
-NCU_TRAFFIC = {("sweep15_64_N100", "mixed"): 125.928704e6 + 15.102208e6}
+NCU_TRAFFIC = {("sweep15_64_N100", "mixed"): 125.905664e6 + 16.460032e6}
 UNIT = "iters/s"
 
 
