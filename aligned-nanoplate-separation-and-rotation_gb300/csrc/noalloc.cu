@@ -2,11 +2,11 @@
 // density (the same kernels as scft_diblock_density) for callers that must not
 // allocate device memory, with all scratch in one file-scope device array.
 //
-// Who needs it: code that runs while a CUDA stream is being captured into a
-// graph in global capture mode (cudaMalloc is refused there), code whose GPU
-// memory is owned by another framework's pool allocator (allocating behind its
-// back fragments or oversubscribes that pool), and services with a fixed
-// memory budget set at start-up.  They pass device buffers for the inputs and
+// Who needs it: code whose GPU memory is owned by another framework's pool
+// allocator (allocating behind its back fragments or oversubscribes that
+// pool), services with a fixed memory budget set at start-up, and code that
+// cannot accept the device-wide wait of cudaFree (it waits for all work
+// queued on the device, other streams included).  They pass device buffers for the inputs and
 // outputs; everything else lives in g_noalloc_scratch.
 //
 // The array is g_noalloc_scratch (kNoAllocScratchBytes = 64 MiB); every GPU

@@ -183,10 +183,10 @@ int scft_homopolymer_density(scft_ctx *ctx, int inst, const double *W, int N, do
                              double *rho, double *Q);
 
 /* The same computation as scft_diblock_density (FP64 method) for callers that
- * cannot allocate GPU memory: code running while a stream is captured into a
- * CUDA graph in global capture mode (cudaMalloc is refused there), code whose
- * device memory belongs to another framework's pool allocator, and services
- * with a fixed memory budget.  No counterpart in the reference.
+ * cannot allocate GPU memory: code whose device memory belongs to another
+ * framework's pool allocator, services with a fixed memory budget, and code
+ * that cannot accept the device-wide wait of cudaFree.  No counterpart in the
+ * reference.
  *
  * All pointers except Nx and L are DEVICE pointers owned by the caller:
  * smwa, smwb (inputs) and rhoda, rhodb (outputs) hold M complex values each,

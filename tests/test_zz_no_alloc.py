@@ -1,6 +1,7 @@
 """scft_diblock_density_noalloc: the propagator-density entry point for
-callers that cannot allocate GPU memory (inside a global-mode stream capture,
-under another framework's pool allocator, or with a fixed memory budget).
+callers that cannot allocate GPU memory (under another framework's pool
+allocator, with a fixed memory budget, or unable to accept the device-wide
+wait of cudaFree).
 
 It is called through the C ABI with device buffers that the caller owns and
 must agree with the allocating entry point scft_diblock_density within the
