@@ -86,7 +86,7 @@ std::string read_input(const std::string &path, Input &in) {
   }
   fclose(f);
   if (!r.ok) return path + ": truncated or malformed";
-  // the reference's own rejections and what this build does not cover
+  // the reference's own rejections and what this library does not cover
   if (in.phiH > 0) return "No homopolymer allowed unless it's a diblock homopolymer (code/read_input.cpp:40-45)";
   if (in.do_fld_np) return "No field-based nanoparticles (code/read_input.cpp:184-189)";
   if (in.do_film && in.do_channel) return "Can't do film and channel in same simulation";

@@ -1,4 +1,4 @@
-"""Workload definitions: the BASELINE configurations in the reference's b-units.
+"""Workload definitions: the benchmark configurations in the reference's b-units.
 
 Conversions (code/initialize.cpp:53-55): N = Nda + Ndb beads, bond length
 b = 1, Rg^2 = (N-1)/6.  chiN is per chain, so chi = chiN/N per segment;

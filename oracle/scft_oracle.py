@@ -1,7 +1,8 @@
 """CPU restatement (numpy, FP64 complex) of the reference SCFT hot path.
 
 TEST INFRASTRUCTURE ONLY.  tests/, __graft_entry__.smoke() and bench.py's CPU
-baseline use this module as the checker; the product (libscft) never calls it.
+baseline use this module to check results against; the product (libscft) never
+calls it.
 
 Parity is pinned: tests/test_oracle.py runs this restatement against the
 reference's own code compiled here (oracle/_ref/scft_ref, built by

@@ -2,7 +2,7 @@
 
 Tests marked `gpu` need a CUDA device and the CUDA library (libscft.so) built
 for sm_103a; everything else runs on the CPU.  The oracle under oracle/ is
-the checker only.
+used only to check results against.
 """
 import os
 import sys
