@@ -145,6 +145,47 @@ def time_reference(params, fields, iters, max_procs):
 
 
 # ---------------------------------------------------------------------------
+class Ranks:
+    """One process per GPU, launched by torchrun (RANK, WORLD_SIZE, MASTER_*
+    from the environment).  Instances are independent SCFT solves, so ranks
+    exchange nothing but the barrier around the timed region and the maximum
+    of their timings; with one rank both are no-ops."""
+
+    def __init__(self, world: int, backend: str, device: str):
+        self.world = world
+        self.device = device
+        self.dist = None
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group(backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def allmax(self, x: float) -> float:
+        if self.dist is None:
+            return x
+        import torch
+
+        t = torch.tensor([x], dtype=torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.dist is not None:
+            self.dist.destroy_process_group()
+            self.dist = None
+
+
+def job_rate(units_per_rank: float, world: int, seconds_max: float) -> float:
+    """Whole-job rate: the units every rank processed (the same batch on each
+    rank, weak scaling) over the slowest rank's time."""
+    return units_per_rank * world / seconds_max
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -218,22 +259,8 @@ def main():
     import torch
 
     torch.cuda.set_device(local)
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def allmax(x):
-        if dist is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    ranks = Ranks(world, "nccl", "cuda")
+    barrier, allmax = ranks.barrier, ranks.allmax
 
     if args.relax > 0 and scft.mixed_available():
         # near-saddle start: relax the seeded fields with the mixed form
@@ -277,11 +304,12 @@ def main():
     launches = ctx.launch_count() - l0
     ms = allmax(e0.elapsed_time(e1))
     H = ctx.calc_H()
-    value = n_inst * args.steps * world / (ms / 1e3)
+    value = job_rate(n_inst * args.steps, world, ms / 1e3)
     if args.iterations_only:
         ctx.close()
         if rank == 0:
             print(json.dumps({"metric": METRIC, "value": value, "unit": UNIT, "iterations_only": True}))
+        ranks.close()
         return
 
     # ---- end to end through the C ABI with pinned host buffers
@@ -307,7 +335,7 @@ def main():
         ctx.calc_H_raw(host_out.data_ptr())
     torch.cuda.synchronize()
     t_e2e = allmax(time.perf_counter() - t0)
-    e2e = {"value": n_inst * e2e_steps * world / t_e2e, "unit": UNIT,
+    e2e = {"value": job_rate(n_inst * e2e_steps, world, t_e2e), "unit": UNIT,
            "h2d_bytes_per_step": int(sum(7 * 16 * m for m in M)), "d2h_bytes_per_step": int(5 * 8 * n_inst)}
 
     # ---- the plain FP64 method on the same batch, same iteration count:
@@ -414,8 +442,7 @@ def main():
                 "cpu_baseline": cpu, "clocks": ck, "gpu_launches": launches,
                 "plain_fp64": plain, "H_first_instance": float(H[0, 0])}
         print(json.dumps(line))
-    if dist is not None:
-        dist.destroy_process_group()
+    ranks.close()
 
 
 if __name__ == "__main__":
