@@ -1,4 +1,8 @@
-// kernels_fft.cu -- batched 3-D complex FFTs on per-instance grids.
+// kernels_fft.cuh -- batched 3-D complex FFTs on per-instance grids.
+//
+// Kernel and launcher templates only: each (pass, precision) pair is
+// instantiated in its own translation unit (kernels_fft_{plane,col}_f{32,64}.cu)
+// so that the library's units compile in parallel.
 //
 // A 3-D transform is two passes over the array:
 //   plane pass : one CTA per (array, z) loads the nx*ny plane into shared
@@ -10,6 +14,7 @@
 // The reference's fft_fwd_wrapper/fft_bck_wrapper (code/fft_wrappers.cpp:4-67)
 // are forward scaled by 1/M and backward unscaled; the scale is folded into
 // the last pass of a forward transform or into the multiplier.
+#pragma once
 #include "fft_core.cuh"
 #include "launch.h"
 
@@ -204,14 +209,5 @@ cudaError_t launch_col_fft(const LaunchShape &ls, const ColJob *jobs, int njobs,
   SCFT_COL(2);
 #undef SCFT_COL
 }
-
-template cudaError_t launch_plane_fft<double>(const LaunchShape &, const PlaneJob *, int, const DevGeom *,
-                                              const void *, int, int, cudaStream_t);
-template cudaError_t launch_plane_fft<float>(const LaunchShape &, const PlaneJob *, int, const DevGeom *,
-                                             const void *, int, int, cudaStream_t);
-template cudaError_t launch_col_fft<double>(const LaunchShape &, const ColJob *, int, const DevGeom *,
-                                            const void *, int, int, cudaStream_t);
-template cudaError_t launch_col_fft<float>(const LaunchShape &, const ColJob *, int, const DevGeom *,
-                                           const void *, int, int, cudaStream_t);
 
 }  // namespace scft

@@ -1,4 +1,8 @@
-// kernels_prop.cu -- the chain-propagator sweep of the plain FP64 method.
+// kernels_prop.cuh -- the chain-propagator sweep of the plain FP64 method.
+//
+// Kernels only: the diblock and graft plane passes are launched from their
+// own translation units (kernels_prop_f64.cu, kernels_graft_f64.cu) so that
+// the library's units compile in parallel.
 //
 // Reference: diblock_discrete (code/diblock_discrete.cpp:4-95) computes
 //   q_0 = e^{-W},  q_n = e^{-w(n)} * IFFT[ g(k) * FFT[q_{n-1}] ] / M,
@@ -7,7 +11,7 @@
 // forms rho_A, rho_B = e^{+W} nD/(Q V) sum_j q_j qdag_{N-1-j}.
 //
 // Here one step n is two launches over all instances and both propagators:
-//   z-column pass (kernels_fft.cu, mode 2): forward-z, * g(k)/M, inverse-z;
+//   z-column pass (kernels_fft.cuh, mode 2): forward-z, * g(k)/M, inverse-z;
 //   xy-plane pass (k_prop_plane below): inverse-xy, * e^{-w(n)} -> q_n, then
 //     - q_n kept only for n <= (N-1)/2 (half history);
 //     - for n > (N-1)/2 the density terms j = n and j = N-1-n are added
@@ -18,6 +22,7 @@
 //     - at n = N-1 the plane sums of q_{N-1} (for Q) are written;
 //     - forward-xy for the next step.
 // Step 0 starts from e^{-W}.
+#pragma once
 #include "fft_core.cuh"
 #include "inst.h"
 #include "launch.h"
@@ -203,44 +208,6 @@ __global__ void __launch_bounds__(512) k_graft_plane_f64(const PropJob *__restri
   fft_plane<double, -1, MAXV>(plane, g, twx, twy);
   if (!GM)
     for (int e = threadIdx.x; e < E; e += blockDim.x) work[e] = plane[e];
-}
-
-template <int MAXV>
-static cudaError_t launch_graft_plane_t(const LaunchShape &ls, const PropJob *jobs, int njobs,
-                                        const PropInst *insts, const DevGeom *geoms, const void *tw, int sweep,
-                                        int n, cudaStream_t st) {
-  auto kfn = ls.gm ? k_graft_plane_f64<MAXV, true> : k_graft_plane_f64<MAXV, false>;
-  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, ls.smem);
-  if (e != cudaSuccess) return e;
-  kfn<<<njobs, ls.threads, ls.smem, st>>>(jobs, insts, geoms, reinterpret_cast<const double2 *>(tw), sweep, n);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_graft_plane_f64(const LaunchShape &ls, const PropJob *jobs, int njobs, const PropInst *insts,
-                                   const DevGeom *geoms, const void *tw, int sweep, int n, cudaStream_t st) {
-  if (njobs <= 0) return cudaSuccess;
-  if (ls.maxv <= 8) return launch_graft_plane_t<8>(ls, jobs, njobs, insts, geoms, tw, sweep, n, st);
-  if (ls.maxv <= 16) return launch_graft_plane_t<16>(ls, jobs, njobs, insts, geoms, tw, sweep, n, st);
-  return launch_graft_plane_t<32>(ls, jobs, njobs, insts, geoms, tw, sweep, n, st);
-}
-
-template <int MAXV>
-static cudaError_t launch_prop_plane_t(const LaunchShape &ls, const PropJob *jobs, int njobs,
-                                       const PropInst *insts, const DevGeom *geoms, const void *tw, int n,
-                                       cudaStream_t st) {
-  auto kfn = ls.gm ? k_prop_plane_f64<MAXV, true> : k_prop_plane_f64<MAXV, false>;
-  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, ls.smem);
-  if (e != cudaSuccess) return e;
-  kfn<<<njobs, ls.threads, ls.smem, st>>>(jobs, insts, geoms, reinterpret_cast<const double2 *>(tw), n);
-  return cudaGetLastError();
-}
-
-cudaError_t launch_prop_plane_f64(const LaunchShape &ls, const PropJob *jobs, int njobs, const PropInst *insts,
-                                  const DevGeom *geoms, const void *tw, int n, cudaStream_t st) {
-  if (njobs <= 0) return cudaSuccess;
-  if (ls.maxv <= 8) return launch_prop_plane_t<8>(ls, jobs, njobs, insts, geoms, tw, n, st);
-  if (ls.maxv <= 16) return launch_prop_plane_t<16>(ls, jobs, njobs, insts, geoms, tw, n, st);
-  return launch_prop_plane_t<32>(ls, jobs, njobs, insts, geoms, tw, n, st);
 }
 
 }  // namespace scft
