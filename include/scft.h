@@ -117,14 +117,19 @@ typedef struct scft_info {
 
 typedef struct scft_ctx scft_ctx;
 
+/* Message of the last failed call on this host thread, and the ABI version
+ * (2: with the mixed form).  No counterpart in the reference, which prints
+ * and exits on errors. */
 const char *scft_last_error(void);
 int scft_version(void);
 
 /* Creates n_inst instances (sizes may differ) on the current CUDA device.
- * Fields start at zero. */
+ * Fields start at zero.  scft_destroy frees everything the context holds (the
+ * reference frees its globals only at process exit). */
 int scft_create(const scft_params *params, int n_inst, scft_ctx **out);
 void scft_destroy(scft_ctx *ctx);
 
+/* The derived quantities of one instance (see scft_info above). */
 int scft_get_info(scft_ctx *ctx, int inst, scft_info *info);
 
 /* scft_set_fields for every instance of the context in one call: w[inst]
@@ -133,7 +138,9 @@ int scft_get_info(scft_ctx *ctx, int inst, scft_info *info);
  * per instance).  No counterpart in the reference (one process per run). */
 int scft_set_fields_all(scft_ctx *ctx, const double *const *w);
 
-/* Sets/gets the seven fields of one instance: w[f*2*M + 2*i + {0,1}]. */
+/* Sets/gets the seven fields of one instance: w[f*2*M + 2*i + {0,1}]
+ * (read_resume_files(), code/io_utils.cpp:183-240; the get side feeds the
+ * field files of write_outputs(), code/io_utils.cpp:11-105). */
 int scft_set_fields(scft_ctx *ctx, int inst, const double *w);
 int scft_get_fields(scft_ctx *ctx, int inst, double *w);
 
@@ -170,7 +177,8 @@ int scft_grad_geom(scft_ctx *ctx, double *out);
  * as built at set-up (code/initialize.cpp:210-239). */
 int scft_get_plate_density(scft_ctx *ctx, int inst, double *rho_exp_nr);
 
-/* Smeared fields of one instance (smwa, smwb, smwg; any may be NULL). */
+/* Smeared fields of one instance (smwa, smwb, smwg; any may be NULL): the
+ * globals calc_poly_density() forms, code/calc_poly_density.cpp:92-104. */
 int scft_get_smeared(scft_ctx *ctx, int inst, double *smwa, double *smwb, double *smwg);
 
 /* diblock_discrete + integrate_diblock_discrete on given smeared fields of
@@ -207,7 +215,9 @@ int scft_diblock_density_noalloc(const int Nx[3], const double L[3], int Nda, in
  * sign -1 forward (scaled 1/M), +1 backward (unscaled). */
 int scft_fft3d(scft_ctx *ctx, int inst, double *data, int count, int sign);
 
-/* Synchronises the context's stream; returns the first asynchronous error. */
+/* Synchronises the context's stream; returns the first asynchronous error.
+ * This and the next four entry points have no counterpart in the reference:
+ * they expose the GPU context (stream, launch count, schedule, timing). */
 int scft_sync(scft_ctx *ctx);
 
 /* The cudaStream_t on which every kernel of this context runs (for callers
