@@ -23,6 +23,7 @@ void ctx_diblock_density(scft_ctx *c, int k, const double *smwa, const double *s
 void ctx_override_nD(scft_ctx *c, int k, double nD);
 int ctx_grad_geom(scft_ctx *c, double *out);
 void ctx_set_sweep_groups(scft_ctx *c, int groups, int phases);
+void ctx_set_wait_limit(scft_ctx *c, int polls);
 void ctx_set_fields_all(scft_ctx *c, const double *const *w);
 void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *tx_out, double *ms_out);
 void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
@@ -242,6 +243,13 @@ int scft_set_sweep_groups(scft_ctx *c, int groups, int phases) {
   if (int s = check_ctx(c, 0)) return s;
   if (groups < 1 || phases < 1) return fail(SCFT_ERR_ARG, "groups and phases must be >= 1");
   API_BODY(scft::ctx_set_sweep_groups(c, groups, phases));
+  return SCFT_OK;
+}
+
+int scft_set_wait_limit(scft_ctx *c, int polls) {
+  if (int s = check_ctx(c, 0)) return s;
+  if (polls < 0) return fail(SCFT_ERR_ARG, "polls must be >= 0");
+  API_BODY(scft::ctx_set_wait_limit(c, polls));
   return SCFT_OK;
 }
 

@@ -8,6 +8,11 @@ namespace scft {
 
 constexpr int kMaxStages = 8;
 
+// Polls of a bounded mbarrier wait before the kernel records a timeout in the
+// context's error word (each poll is one mbarrier.try_wait, which itself
+// suspends the thread for a hardware-chosen interval).
+constexpr int kWaitPolls = 1 << 22;
+
 // Stage plan of a 1-D FFT of length n along one grid axis: radices applied in
 // order (Stockham autosort, decimation in time) and the offset of this
 // length's twiddle table exp(-2*pi*i*t/n), t = 0..n-1, in the context's

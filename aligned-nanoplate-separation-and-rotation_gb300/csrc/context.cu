@@ -752,6 +752,15 @@ CUtensorMap tensor_map_rows(const float2 *base, unsigned long long rows) {
   return m;
 }
 
+// The plane passes' error word and first-wait poll limit (see context.h).
+void ensure_err(scft_ctx *c) {
+  if (c->d_err) return;
+  c->d_err = dalloc<int>(c, 2);
+  const int init[2] = {0, kWaitPolls};
+  CK(cudaMemcpyAsync(c->d_err, init, sizeof init, cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+}
+
 // Raises the plane pass's error word (an mbarrier wait that ran out) as an error.
 void check_device_error(scft_ctx *c) {
   if (!c->d_err) return;
@@ -1191,7 +1200,7 @@ void build_jobs(scft_ctx *c) {
           c->tmH.push_back(CUtensorMap{});
         }
       }
-      if (!c->d_err) c->d_err = dalloc<int>(c, 1);
+      ensure_err(c);
     }
     // Mixed plane passes in place (graft sweeps; the diblock sweep when a
     // second buffer does not fit): planes above 8192 points (128 x 128) run
@@ -1222,7 +1231,7 @@ void build_jobs(scft_ctx *c) {
         }
       }
     }
-    if (!c->d_err) c->d_err = dalloc<int>(c, 1);
+    ensure_err(c);
     c->shp_col32 = choose_shape(emax_col, sizeof(float2), (nz_max + 32) * sizeof(float2));
     if (!c->shp_col32.gm && c->shp_col32.smem + emax_col * (int)sizeof(float2) <= 227 * 1024) {
       c->shp_col32.pp = 1;  // out-of-place z transforms: second tile buffer
@@ -1684,6 +1693,16 @@ void ctx_update(scft_ctx *c, int n_iter) {
   check_device_error(c);
 }
 
+// Poll limit of the first bounded mbarrier wait of every mixed plane-pass CTA
+// (read by the kernels from d_err[1] at run time, so captured graphs need no
+// re-capture).
+void ctx_set_wait_limit(scft_ctx *c, int polls) {
+  if (polls < 0) throw ScftError(SCFT_ERR_ARG, "polls must be >= 0");
+  ensure_err(c);
+  CK(cudaMemcpyAsync(c->d_err + 1, &polls, sizeof(int), cudaMemcpyHostToDevice, c->st));
+  CK(cudaStreamSynchronize(c->st));
+}
+
 // Number of independent launch chains of the mixed sweep (1 = one chain).
 void ctx_set_sweep_groups(scft_ctx *c, int groups, int phases) {
   if (groups < 1 || phases < 1) throw ScftError(SCFT_ERR_ARG, "groups and phases must be >= 1");
@@ -1882,7 +1901,7 @@ int ctx_calc_H(scft_ctx *c, double *out) {
     out[5 * k + 3] = Qd.imag();
     out[5 * k + 4] = Qga.real();
     if (H != H) status = SCFT_ERR_NAN;
-    // the reference exits once 5 points have Re q_g[Ng-1] <= 0 (code/grafted_nanoparticle.cpp:313-334)
+    // the reference exits once 5 points have Re q_g[Ng-1] <= 0 (code/grafted_nanoparticle.cpp:82-107)
     if (I.graft && sc[(size_t)k * kNumScalars + kQg].x >= 5.0 && status == SCFT_OK) status = SCFT_ERR_QNONPOS;
   }
   return status;

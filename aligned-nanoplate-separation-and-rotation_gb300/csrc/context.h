@@ -116,7 +116,10 @@ struct scft_ctx {
   std::vector<scft::MixInst> h_mi;       // host copy of d_mi
   std::vector<scft::MixInst> mix64_tab;  // instances in job order (64^3 plane pass)
   std::vector<CUtensorMap> tmE, tmH;      // their TMA descriptors (Boltzmann, history)
-  int *d_err = nullptr;                   // error word of the plane pass
+  // d_err[0]: error word of the plane passes (a bounded wait ran out);
+  // d_err[1]: polls of each plane-pass CTA's first mbarrier wait before it
+  // records a timeout (kWaitPolls; scft_set_wait_limit lowers it)
+  int *d_err = nullptr;
   double *h_pin = nullptr;                // pinned read-back of the field checks (128 doubles per instance)
   // scft_set_fields (mixed form): check results, instance mask, job staging
   double *d_realout = nullptr;

@@ -91,10 +91,13 @@ __global__ void __launch_bounds__(PP ? 512 : (MAXV == 16 ? 1024 : 512), PP ? 2 :
     bulk_load_1d(Es, P.E + zoff, pbytes, &s_bar[1], pol);
   }
   // bounded wait on stage barrier b, phase ph (all threads)
+  // (err[1] is the poll limit of the first try: kWaitPolls unless lowered
+  // with scft_set_wait_limit)
+  const int first_polls = STAGE ? err[1] : 0;
   auto stage_wait = [&](int b, uint32_t ph) {
-    if (!mbar_wait(&s_bar[b], ph, 1 << 22)) {
+    if (!mbar_wait(&s_bar[b], ph, first_polls)) {
       atomicExch(err, 1);
-      mbar_wait(&s_bar[b], ph, 1 << 22);  // let copies in flight land before the CTA moves on
+      mbar_wait(&s_bar[b], ph, kWaitPolls);  // let copies in flight land before the CTA moves on
     }
   };
   // previous step's means (FP64, same summation order in every CTA) and the

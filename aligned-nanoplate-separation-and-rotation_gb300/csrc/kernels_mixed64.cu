@@ -194,9 +194,9 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
   // every thread waits on the mbarrier itself (acquiring the staged planes),
   // and the shared plane is touched only in the thread's own rows until the
   // barrier of the plane sums: no block barrier here
-  if (!mbar_wait(&s_bar, 0, 1 << 22)) {
+  if (!mbar_wait(&s_bar, 0, T.err[1])) {
     atomicExch(T.err, 1);
-    mbar_wait(&s_bar, 0, 1 << 22);  // let copies in flight land before the CTA moves on
+    mbar_wait(&s_bar, 0, kWaitPolls);  // let copies in flight land before the CTA moves on
   }
 
   if (n == 0) {

@@ -14,10 +14,13 @@
 // the symbol's name as a device address, so on the first call on each device
 // (with that device current) the address is fetched once with
 // cudaGetSymbolAddress and cached; that first call should come before any
-// stream capture.  All calls share the array and it keeps the last call's
-// contents: the density accumulators are cleared on every call, the tables
-// and job lists rewritten; calls that overlap on the GPU (different streams,
-// or different host threads) race on it.
+// stream capture.  The cache is keyed by device ordinal and does not survive
+// cudaDeviceReset (or any teardown of the device's primary context): the
+// module is loaded again there, possibly at another address.  All calls
+// share the array and it keeps the last call's contents: the density
+// accumulators are cleared on every call, the tables and job lists
+// rewritten; calls that overlap on the GPU (different streams, or different
+// host threads) race on it.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -204,13 +207,17 @@ int noalloc_diblock(const int *Nx, const double *L, int Nda, int Ndb, double nD,
   if (off > kNoAllocScratchBytes) {
     msg = "grid x chain length needs " + std::to_string(off >> 20) +
           " MiB of scratch; scft_diblock_density_noalloc is limited to 64 MiB "
-          "(about M * (200 + 32 * ((N - 1) / 2 + 1)) bytes)";
+          "(about M * (136 + 32 * ((N - 1) / 2 + 1)) bytes for a diblock)";
     return SCFT_ERR_ARG;
   }
   const LaunchShape sp = shape_for(g.nx * g.ny, (g.nx + g.ny + 32) * sizeof(double2));
   const LaunchShape sc = shape_for(g.tx * g.nz, (g.nz + 32) * sizeof(double2));
   if (sp.smem > 227 * 1024) {
     msg = "xy plane too large for the FP64 plane pass";
+    return SCFT_ERR_UNSUPPORTED;
+  }
+  if (sc.smem > 227 * 1024) {
+    msg = "z columns too long for the FP64 column pass";
     return SCFT_ERR_UNSUPPORTED;
   }
   void *basev = nullptr;

@@ -96,6 +96,8 @@ std::string read_input(const std::string &path, Input &in) {
     for (int d = 0; d < 3; d++)
       if (in.center[j][d] < 0.0 || in.center[j][d] > 1.0)
         return "Nanorod center isn't valid. Must be between 0 and 1";
+  for (int d = 0; d < 3; d++)
+    if (in.Nx[d] < 1 || !(in.L[d] > 0.0)) return "grid sizes and box lengths must be positive";
   if (in.Ng == 0) in.sigma = 0;  // code/read_input.cpp:200
   if (in.print_freq < 1) return "print_freq must be >= 1";
   return "";

@@ -40,6 +40,8 @@ struct Run {
   // complex-Langevin averages (code/array_utils.cpp:13-45)
   std::vector<std::complex<double>> avg_a, avg_b, avg_g;
   double n_samples = 0.0;
+  // resume fields read (and checked) before the GPU is touched; empty: absent
+  std::vector<std::complex<double>> res[7];
 };
 
 int check(int st, const char *what) {
@@ -111,18 +113,11 @@ std::vector<std::complex<double>> initial_fields(scft_ctx *ctx, int k, const Run
       w[i] = pre * (u(gen) - 0.5) * I;
     }
   }
-  for (int f = 0; f < 7; f++) {
-    std::vector<cd> res;
-    std::string err;
-    const std::string path = r.dir + "/" + kFieldNames[f] + ".res";
-    if (read_res(path, M, res, err)) {
-      for (long i = 0; i < M; i++) w[f * M + i] = res[i];
+  for (int f = 0; f < 7; f++)
+    if ((long)r.res[f].size() == M) {
+      for (long i = 0; i < M; i++) w[f * M + i] = r.res[f][i];
       printf("Read %s.res\n", kFieldNames[f]);
-    } else if (!err.empty()) {
-      fprintf(stderr, "%s\n", err.c_str());
-      exit(1);
     }
-  }
   return w;
 }
 
@@ -220,6 +215,20 @@ int main(int argc, char **argv) {
     }
     params.push_back(to_params(runs[k].in, precision));
     params.back().cl_seed = seed;
+    // resume files (code/io_utils.cpp:138-177): read and checked here, before
+    // any GPU work, so that a short or malformed file ends the run cleanly
+    const long M = (long)runs[k].in.Nx[0] * runs[k].in.Nx[1] * runs[k].in.Nx[2];
+    for (int f = 0; f < 7; f++) {
+      std::string rerr;
+      const std::string path = dirs[k] + "/" + kFieldNames[f] + ".res";
+      if (!read_res(path, M, runs[k].res[f], rerr)) {
+        runs[k].res[f].clear();
+        if (!rerr.empty()) {
+          fprintf(stderr, "%s\n", rerr.c_str());
+          return 1;
+        }
+      }
+    }
   }
   scft_ctx *ctx = nullptr;
   check(scft_create(params.data(), (int)params.size(), &ctx), "scft_create");

@@ -27,7 +27,7 @@ EXPORTS = ("scft_last_error", "scft_version", "scft_create", "scft_destroy", "sc
            "scft_calc_H", "scft_grad_geom", "scft_get_density", "scft_get_plate_density", "scft_get_smeared", "scft_diblock_density",
            "scft_homopolymer_density", "scft_fft3d", "scft_sync", "scft_get_stream", "scft_launch_count",
            "scft_profile_step", "scft_diblock_density_noalloc", "scft_set_sweep_groups", "scft_autotune",
-           "scft_set_fields_all")
+           "scft_set_fields_all", "scft_set_wait_limit")
 
 
 class ScftError(RuntimeError):
@@ -103,6 +103,7 @@ def load(path: str | None = None):
     lib.scft_launch_count.argtypes = [vp, ctypes.POINTER(ctypes.c_longlong)]
     lib.scft_profile_step.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
     lib.scft_set_sweep_groups.argtypes = [vp, ctypes.c_int, ctypes.c_int]
+    lib.scft_set_wait_limit.argtypes = [vp, ctypes.c_int]
     lib.scft_set_fields_all.argtypes = [vp, ctypes.POINTER(ctypes.c_void_p)]
     ip = ctypes.POINTER(ctypes.c_int)
     lib.scft_autotune.argtypes = [vp, ctypes.c_int, ip, ip, ip, dp]
@@ -266,6 +267,9 @@ class Context:
 
     def set_sweep_groups(self, groups: int, phases: int = 1):
         _check(load().scft_set_sweep_groups(self._h, groups, phases))
+
+    def set_wait_limit(self, polls: int):
+        _check(load().scft_set_wait_limit(self._h, int(polls)))
 
     def autotune(self, reps=3) -> dict:
         g, ph, t, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()

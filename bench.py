@@ -110,24 +110,12 @@ class ClockSampler:
 # ---------------------------------------------------------------------------
 # the compiled reference on the host cores
 # ---------------------------------------------------------------------------
-def case_from_params(p, fields):
-    sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    from ref_case import Case
-
-    c = Case(Nda=p.Nda, Ndb=p.Ndb, a_smear=p.a_smear, rho0=p.rho0, chi_ab=p.chi_ab, chi_bc=p.chi_bc,
-             chi_ac=p.chi_ac, kappa=p.kappa, Nx=tuple(p.Nx), L=tuple(p.L), lam_pl=p.lam_pl, lam_mi=p.lam_mi,
-             n_exp_nr=p.n_exp_nr, np_chem=p.np_chem, sigma=p.sigma, Ng=p.Ng, L_nr=p.L_nr, R_nr=p.R_nr,
-             xi_nr=p.xi_nr, centers=tuple(tuple(p.center[j]) for j in range(2)),
-             orients=tuple(tuple(p.orient[j]) for j in range(2)))
-    c.fields = fields
-    return c
-
-
 def time_reference(params, fields, iters, max_procs):
     """Runs `iters` update_1s of each instance in its own process (up to
-    max_procs at once); returns (aggregate iters/s, processes, per-instance s/iter)."""
+    max_procs at once); returns (aggregate iters/s, processes, per-instance
+    s/iter, per-instance Re H after the updates)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    from ref_case import REF_BIN, time_reference as tref
+    from ref_case import REF_BIN, case_from_params, time_reference as tref
 
     if not os.path.exists(REF_BIN):
         raise FileNotFoundError(REF_BIN)
@@ -135,13 +123,53 @@ def time_reference(params, fields, iters, max_procs):
     cases = [case_from_params(p, f) for p, f in zip(params, fields)]
     procs = max(1, min(max_procs, len(cases)))
     with ThreadPoolExecutor(max_workers=procs) as ex:
-        secs = list(ex.map(lambda kc: tref(os.path.join(tmp, f"inst{kc[0]}"), kc[1], iters),
-                           list(enumerate(cases))))
+        res = list(ex.map(lambda kc: tref(os.path.join(tmp, f"inst{kc[0]}"), kc[1], iters, with_h=True),
+                          list(enumerate(cases))))
     shutil.rmtree(tmp, ignore_errors=True)
+    secs = [r[0] for r in res]
     waves = -(-len(cases) // procs)
     # instances run `procs` at a time; the batch takes `waves` rounds
     wall_per_iter = max(secs) * waves
-    return len(cases) / wall_per_iter, procs, secs
+    return len(cases) / wall_per_iter, procs, secs, [r[1] for r in res]
+
+
+def mapped_repo_libraries() -> list:
+    """Shared objects under the repository mapped into this process."""
+    try:
+        with open("/proc/self/maps") as f:
+            paths = {ln.split()[-1] for ln in f if ln.rstrip().endswith(".so") or ".so." in ln}
+    except OSError:
+        return []
+    return sorted(p for p in paths if p.startswith(ROOT))
+
+
+def reference_arm(args, rank, params, fields, config):
+    """--impl reference: the reference's own update_1s (oracle/_ref/scft_ref,
+    compiled from its sources) on the host cores, one process per instance.
+    Runs before anything loads libscft.so, so that this process maps none of
+    the repository's libraries."""
+    if rank != 0:
+        return
+    n_inst = len(params)
+    cores = os.cpu_count() or 1
+    iters = max(1, min(args.steps, 2))
+    try:
+        v, procs, secs, _ = time_reference(params, fields, iters, cores)
+    except Exception as e:  # noqa: BLE001
+        print(json.dumps({"impl": "reference", "unavailable": f"reference binary failed: {e}"}))
+        return
+    sample = (f"{n_inst} instances x {iters} update_1s each ({statistics.mean(secs):.2f} s per update per "
+              f"process), one process per instance ({procs} at a time); reference code/ with Dim=3, FFTs by "
+              f"the oracle shim; from the seeded fields (no relaxation)")
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": iters,
+            "warmup": 0, "ms_per_step": 1e3 * n_inst / v, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c128", "data": "synthetic seeded fields", "config": config,
+            "impl": "reference",
+            "steps_note": f"{iters} timed update_1s per instance (the GPU arm times --steps {args.steps})",
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "reference", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "repo_libraries_mapped": mapped_repo_libraries()}
+    print(json.dumps(line))
 
 
 # ---------------------------------------------------------------------------
@@ -213,6 +241,7 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
 
+    # parameter records and constants only: nothing here loads libscft.so
     import scft
     from scft.workloads import BENCH_DEFAULTS, WORKLOADS, seeded_fields
 
@@ -222,7 +251,7 @@ def main():
     if args.plain_max is None:
         args.plain_max = wd.get("plain_max", 0)
 
-    form = args.form or ("mixed" if scft.mixed_available() else "plain")
+    form = args.form or "mixed"
     prec = scft.PREC_MIXED if form == "mixed" else scft.PREC_FP64
     params = WORKLOADS[args.workload](prec)
     fields = [seeded_fields(p, 1000 + k, periods=wd.get("periods", 1)) for k, p in enumerate(params)]
@@ -236,25 +265,11 @@ def main():
               "l2": "working set per step larger than L2 (no flush)"}
 
     if args.impl == "reference":
-        if rank != 0:
-            return
-        cores = os.cpu_count() or 1
-        iters = max(1, min(args.steps, 2))
-        try:
-            v, procs, secs = time_reference(params, fields, iters, cores)
-        except Exception as e:  # noqa: BLE001
-            print(json.dumps({"impl": "reference", "unavailable": f"reference binary failed: {e}"}))
-            return
-        sample = (f"{n_inst} instances x {iters} update_1s each, one process per instance "
-                  f"({procs} at a time); reference code/ with Dim=3, FFTs by the oracle shim")
-        line = {"metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": iters,
-                "warmup": 0, "ms_per_step": 1e3 * n_inst / v, "higher_is_better": True, "scaling": "weak",
-                "vs_baseline": None, "dtype": "c128", "data": "synthetic seeded fields", "config": config,
-                "impl": "reference",
-                "cpu_baseline": {"value": v, "unit": UNIT, "cores": procs, "kind": "reference", "sample": sample},
-                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-        print(json.dumps(line))
+        reference_arm(args, rank, params, fields, config)
         return
+
+    if form == "mixed" and not scft.mixed_available():
+        raise SystemExit("libscft.so was built without the mixed form")
 
     import torch
 
@@ -426,10 +441,18 @@ def main():
         try:
             cores = os.cpu_count() or 1
             nb = min(n_inst, cores)
-            v, procs, secs = time_reference(params[:nb], fields[:nb], 1, cores)
+            v, procs, secs, h_ref = time_reference(params[:nb], fields[:nb], 1, cores)
             cpu = {"value": v, "unit": UNIT, "cores": procs, "kind": "reference",
                    "sample": f"{nb} instances x 1 update_1s, one process each; reference code/ (Dim=3, "
                              f"oracle FFT shim); {statistics.mean(secs):.2f} s/iter per process"}
+            # the same update on the GPU's FP64 method from the same fields: H against the reference's
+            with scft.Context(WORKLOADS[args.workload](scft.PREC_FP64)[:nb]) as c64:
+                for k in range(nb):
+                    c64.set_fields(k, fields[k])
+                c64.calc_poly_density()
+                c64.update_1s(1)
+                h_gpu = c64.calc_H()[:, 0]
+            cpu["H_fp64_gpu_vs_reference_rel_max"] = float(max(abs(a - b) / abs(b) for a, b in zip(h_gpu, h_ref)))
         except Exception as e:  # noqa: BLE001
             cpu = {"value": None, "unit": UNIT, "cores": 0, "kind": "reference", "sample": f"failed: {e}"}
 

@@ -202,11 +202,14 @@ int scft_homopolymer_density(scft_ctx *ctx, int inst, const double *W, int N, do
  * Work is queued on `stream` (a cudaStream_t, NULL for the default stream)
  * and the call returns without synchronising.  Nothing is allocated: the
  * scratch is one file-scope device array of 64 MiB that every GPU loading
- * libscft holds until exit, enough for about
- * M * (200 + 32 * ((Nda + Ndb - 1)/2 + 1)) bytes (32^3 grid up to N ~ 64);
- * larger problems are rejected with SCFT_ERR_ARG.  The first call on a device
- * looks up the array's device address (make that call before any stream
- * capture).  Calls share the array: calls that overlap on the GPU race. */
+ * libscft holds until exit; a diblock needs about
+ * M * (136 + 32 * ((Nda + Ndb - 1)/2 + 1)) bytes of it (32^3 grid up to
+ * N ~ 118); larger problems are rejected with SCFT_ERR_ARG.  The first call
+ * on a device looks up the array's device address (make that call before any
+ * stream capture); that cached address does not survive cudaDeviceReset.
+ * Calls share the array and it keeps the last call's contents (what must
+ * start at zero is cleared on every call): calls that overlap on the GPU
+ * race. */
 int scft_diblock_density_noalloc(const int Nx[3], const double L[3], int Nda, int Ndb, double nD,
                                  const double *smwa, const double *smwb, double *rhoda, double *rhodb,
                                  double *Q, void *stream);
@@ -236,6 +239,16 @@ int scft_launch_count(scft_ctx *ctx, long long *count);
  * that one chain's z passes fill the last wave of another chain's plane pass.
  * Default 2 groups, 1 phase. */
 int scft_set_sweep_groups(scft_ctx *ctx, int groups, int phases);
+
+/* Diagnostic (no counterpart in the reference, whose loops have no waits):
+ * the number of polls the first bounded mbarrier wait of each mixed
+ * plane-pass CTA makes before it records a timeout in the context's error
+ * word (default 4194304).  A CTA whose wait ran out still waits, bounded, for
+ * its copies to land, so its results are complete and the context stays
+ * usable; the next scft_calc_poly_density / scft_update_1s returns
+ * SCFT_ERR_CUDA ("a TMA wait ... ran out").  polls = 0 makes every such wait
+ * run out at once, which is how a test sees that path without a fault. */
+int scft_set_wait_limit(scft_ctx *ctx, int polls);
 
 /* Autotuner: times reps full propagator sweeps of the batch for every
  * candidate schedule (1-4 phases x 1-6 or 8 groups; for 64-point grids also

@@ -75,6 +75,19 @@ class Case:
         return (self.Nx[2], self.Nx[1], self.Nx[0])
 
 
+def case_from_params(p, fields=None) -> Case:
+    """Case from a library parameter record (any object with the scft_params
+    field names: Nda, Ndb, a_smear, rho0, chi_*, kappa, Nx, L, lam_*, n_exp_nr,
+    np_chem, sigma, Ng, L_nr, R_nr, xi_nr, center, orient)."""
+    c = Case(Nda=p.Nda, Ndb=p.Ndb, a_smear=p.a_smear, rho0=p.rho0, chi_ab=p.chi_ab, chi_bc=p.chi_bc,
+             chi_ac=p.chi_ac, kappa=p.kappa, Nx=tuple(p.Nx), L=tuple(p.L), lam_pl=p.lam_pl, lam_mi=p.lam_mi,
+             n_exp_nr=p.n_exp_nr, np_chem=p.np_chem, sigma=p.sigma, Ng=p.Ng, L_nr=p.L_nr, R_nr=p.R_nr,
+             xi_nr=p.xi_nr, centers=tuple(tuple(p.center[j]) for j in range(2)),
+             orients=tuple(tuple(p.orient[j]) for j in range(2)))
+    c.fields = dict(fields or {})
+    return c
+
+
 def _g(v: float) -> str:
     return repr(float(v))
 
@@ -211,14 +224,20 @@ def run_reference(dirpath: str, c: Case, iters: int, hist: bool = False, timeout
     return out
 
 
-def time_reference(dirpath: str, c: Case, iters: int, timeout: float = 3600) -> float:
-    """Seconds per update_1s() iteration of the compiled reference."""
+def time_reference(dirpath: str, c: Case, iters: int, timeout: float = 3600, with_h: bool = False):
+    """Seconds per update_1s() iteration of the compiled reference (and, with
+    with_h, Re H after the `iters` updates)."""
     write_case(dirpath, c)
     r = subprocess.run([REF_BIN, "time", str(iters)], cwd=dirpath, capture_output=True, text=True,
                        timeout=timeout)
     if r.returncode != 0:
         raise RuntimeError(f"reference timing failed: {r.stderr[-2000:]}")
+    secs = H = None
     for line in r.stdout.splitlines():
         if line.startswith("seconds_per_iter"):
-            return float(line.split()[1])
-    raise RuntimeError("no timing line in reference output")
+            secs = float(line.split()[1])
+        elif line.startswith("H "):
+            H = float(line.split()[1])
+    if secs is None:
+        raise RuntimeError("no timing line in reference output")
+    return (secs, H) if with_h else secs

@@ -3,6 +3,9 @@ reference SCFT code itself (compiled by oracle/Makefile into
 oracle/_ref/scft_ref, Dim=3, FFT via the oracle shim).
 
     make -C oracle && python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --large [name ...]   (configs 1, 3, 4;
+                                                             about 20 min and
+                                                             35 GB of host RAM)
 
 Each fixture <name>.npz holds
   case_json      the bcp.input parameters (json text)
@@ -93,11 +96,59 @@ def config0_case() -> Case:
     return c
 
 
-def digest(a: np.ndarray) -> np.ndarray:
-    """Size-independent summary: sum, sum of |.|^2, and 64 sampled points."""
+def digest(a: np.ndarray, samples: int = 64) -> np.ndarray:
+    """Size-independent summary: sum, sum of |.|^2, and `samples` sampled points."""
     a = a.ravel()
-    idx = np.random.default_rng(DIGEST_IDX_SEED).choice(a.size, 64, replace=False)
+    idx = np.random.default_rng(DIGEST_IDX_SEED).choice(a.size, samples, replace=False)
     return np.concatenate([[a.sum(), (np.abs(a) ** 2).sum()], a[idx]])
+
+
+# Benchmark configurations 1, 3 and 4 at full size, plain FP64 method: the
+# reference runs `iters` update_1s() from the seeded fields of the bench
+# workloads (scft/workloads.py); the fixtures hold the H/Q trace and digests
+# (LARGE_SAMPLES points each) of the initial and final densities, fields and
+# smeared fields, plus a digest of the seeded input so that a test can check
+# that it regenerated the same fields.
+LARGE_SAMPLES = 512
+LARGE_ARRAYS = ["rhoda0", "rhodb0", "smwa0", "smwb0", "rhoda", "rhodb", "wpl", "wabp", "wabm", "smwa", "smwb"]
+
+
+def large_cases() -> dict:
+    """name -> (workload name, instance index, seed, lamellar periods, iters)."""
+    return {
+        "config1_plate64_N100": ("plate64_N100", 0, 1001, 1, 3),
+        "config3_sep030_64x64x128_N100": ("sep9_64x64x128_N100", 4, 1004, 1, 3),
+        "config4_graft_128x128x256_N200": ("graft8_128x128x256_N200", 0, 1000, 3, 1),
+    }
+
+
+def large_case(name: str):
+    """(params, Case) of one large fixture, FP64 method, seeded fields included."""
+    sys.path.insert(0, os.path.join(ROOT, "aligned-nanoplate-separation-and-rotation_gb300"))
+    import scft
+    from scft.workloads import WORKLOADS, seeded_fields as ws
+    from ref_case import case_from_params
+
+    wl, k, seed, periods, iters = large_cases()[name]
+    p = WORKLOADS[wl](scft.PREC_FP64)[k]
+    return p, case_from_params(p, ws(p, seed, periods=periods)), iters
+
+
+def make_large_fixtures(tmp, names=None):
+    for name in (names or large_cases()):
+        p, c, iters = large_case(name)
+        out = run_reference(os.path.join(tmp, name), c, iters, hist=False, timeout=6 * 3600)
+        z = {"case_json": case_json(c), "trace": out["trace"], "scalars_json": json.dumps(out["scalars"]),
+             "digest_idx_seed": DIGEST_IDX_SEED, "samples": LARGE_SAMPLES,
+             "digest_in_wabm": digest(c.fields["wabm"], LARGE_SAMPLES)}
+        arrays = LARGE_ARRAYS + (["rhog_exp0", "rhog_exp"] if c.sigma > 0 and c.n_exp_nr > 0 else [])
+        for k in arrays:
+            z["digest_" + k] = digest(out[k], LARGE_SAMPLES)
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **z)
+        print(name, "H0", out["trace"][0, 1], "H_end", out["trace"][-1, 1], flush=True)
+        import shutil
+
+        shutil.rmtree(os.path.join(tmp, name), ignore_errors=True)
 
 
 def case_json(c: Case) -> str:
@@ -170,6 +221,10 @@ def make_driver_fixtures(tmp):
 
 def main():
     tmp = tempfile.mkdtemp(prefix="golden_")
+    if "--large" in sys.argv:
+        names = [a for a in sys.argv[1:] if not a.startswith("--")]
+        make_large_fixtures(tmp, names or None)
+        return
     make_driver_fixtures(tmp)
     if "--driver-only" in sys.argv:
         return

@@ -70,12 +70,12 @@ def mixed_sweep_model(s, wa, wb, rescale=True):
 
 
 def reference_case(grid, N, shift):
-    import bench
     import scft_oracle as O
+    from ref_case import case_from_params
     from scft.workloads import plate_params, seeded_fields
 
     p = plate_params(10.0, N=N, grid=grid)
-    c = bench.case_from_params(p, seeded_fields(p, 7))
+    c = case_from_params(p, seeded_fields(p, 7))
     s = O.System.from_case(c)
     o = O.calc_poly_density(s, O.State.from_fields(s.g, c.fields))
     wa = (o["smwa"] + s.tables["shellU"]).real - shift

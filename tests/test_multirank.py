@@ -71,3 +71,20 @@ def test_reference_arm_runs_on_rank_zero_only():
                         "--steps", "1", "--warmup", "3"], env=env, capture_output=True, text=True, timeout=300)
     assert p.returncode == 0, p.stderr
     assert p.stdout.strip() == ""
+
+
+def test_reference_arm_maps_no_repository_library():
+    """The reference arm times the compiled reference only: its process must
+    not load libscft.so (or any other shared object built in the repository)."""
+    from ref_case import REF_BIN
+
+    if not os.path.exists(REF_BIN):
+        pytest.skip("oracle binary not built")
+    env = dict(os.environ, RANK="0", WORLD_SIZE="1", LOCAL_RANK="0")
+    p = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), "--impl", "reference", "--workload",
+                        "plate64_N100", "--steps", "1", "--warmup", "3"], env=env, capture_output=True, text=True,
+                       timeout=600)
+    assert p.returncode == 0, p.stderr
+    line = json.loads(p.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0, line
+    assert line["repo_libraries_mapped"] == [], line["repo_libraries_mapped"]

@@ -79,6 +79,68 @@ def test_noalloc_matches_allocating_entry_point_twice():
         assert rel(ra, z["rhoda0"]) < RHO_TOL, name
 
 
+def test_noalloc_single_block_and_narrow_columns():
+    """The single-propagator path (Nda == N: one working array, q-dagger
+    equal to q) on the reference's own fixture, and a grid whose nx = 12 is
+    not a multiple of 16 (z-pass tiles of 4 columns), each against
+    scft_diblock_density."""
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.fail("gpu tests need a CUDA device")
+    import scft as S
+
+    c, z = load_golden("tiny_single_block")
+    with S.Context(S.params_from_case(c)) as ctx:
+        nD = ctx.info(0)["nD"]
+        ra_ref, rb_ref, Q_ref = ctx.diblock_density(0, z["smwa0"], z["smwb0"])
+    ra, rb, Q = call_noalloc(S, torch, c, nD, z["smwa0"], z["smwb0"])
+    assert abs(Q - Q_ref) <= RHO_TOL * abs(Q_ref)
+    assert rel(ra, ra_ref) < RHO_TOL
+    assert rel(ra, z["rhoda0"]) < RHO_TOL
+
+    from ref_case import Case
+
+    c = Case(Nda=4, Ndb=3, Nx=(12, 6, 10), L=(3.0, 2.0, 2.5))
+    rng = np.random.default_rng(31)
+    wa = 0.3 * rng.standard_normal(c.shape) + 0j
+    wb = 0.3 * rng.standard_normal(c.shape) + 0j
+    with S.Context(S.params_from_case(c)) as ctx:
+        nD = ctx.info(0)["nD"]
+        ra_ref, rb_ref, Q_ref = ctx.diblock_density(0, wa, wb)
+    for _ in range(2):
+        ra, rb, Q = call_noalloc(S, torch, c, nD, wa, wb)
+        assert abs(Q - Q_ref) <= RHO_TOL * abs(Q_ref)
+        assert rel(ra, ra_ref) < RHO_TOL and rel(rb, rb_ref) < RHO_TOL
+
+
+def test_noalloc_near_its_scratch_limit():
+    """32^3 with N = 110 uses about 59 of the 64 MiB: it matches the
+    allocating entry point; N = 130 at the same grid is rejected."""
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.fail("gpu tests need a CUDA device")
+    import scft as S
+    from ref_case import Case
+
+    c = Case(Nda=55, Ndb=55, Nx=(32, 32, 32), L=(10.0, 10.0, 10.0))
+    rng = np.random.default_rng(37)
+    wa = 0.05 * rng.standard_normal(c.shape) + 0j
+    wb = 0.05 * rng.standard_normal(c.shape) + 0j
+    with S.Context(S.params_from_case(c)) as ctx:
+        nD = ctx.info(0)["nD"]
+        ra_ref, rb_ref, Q_ref = ctx.diblock_density(0, wa, wb)
+    ra, rb, Q = call_noalloc(S, torch, c, nD, wa, wb)
+    assert abs(Q - Q_ref) <= RHO_TOL * abs(Q_ref)
+    assert rel(ra, ra_ref) < RHO_TOL and rel(rb, rb_ref) < RHO_TOL
+    lib = S.load()
+    nx = (ctypes.c_int * 3)(32, 32, 32)
+    L = (ctypes.c_double * 3)(10.0, 10.0, 10.0)
+    dummy = torch.zeros(2, dtype=torch.float64, device="cuda:0").data_ptr()
+    assert lib.scft_diblock_density_noalloc(nx, L, 65, 65, 1.0, dummy, dummy, dummy, dummy, dummy, None) == S.ERR_ARG
+
+
 def test_noalloc_rejects_problems_beyond_its_scratch():
     import torch
 
