@@ -56,10 +56,9 @@ def test_nonpositive_graft_propagator_gives_err_qnonpos(scft):
     with scft.Context(scft.params_from_case(c)) as ctx:
         ctx.set_fields(0, c.fields)
         ctx.calc_poly_density()
-        ctx.calc_H()
-        assert ctx.last_status == scft.ERR_QNONPOS
         with pytest.raises(scft.ScftError) as e:
-            scft._check(ctx.last_status)
+            ctx.calc_H()
+        assert e.value.code == scft.ERR_QNONPOS
         assert "q_g" in str(e.value)
 
 
