@@ -29,6 +29,7 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
 void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
                       double *bytes_col);
 int error_code(const std::exception &e);
+int fp64_fma_rate(int reps, double *gflops, std::string &msg);
 int noalloc_diblock(const int *Nx, const double *L, int Nda, int Ndb, double nD, const double *smwa,
                     const double *smwb, double *rhoda, double *rhodb, double *Q, void *stream, std::string &msg);
 }  // namespace scft
@@ -243,6 +244,14 @@ int scft_set_sweep_groups(scft_ctx *c, int groups, int phases) {
   if (int s = check_ctx(c, 0)) return s;
   if (groups < 1 || phases < 1) return fail(SCFT_ERR_ARG, "groups and phases must be >= 1");
   API_BODY(scft::ctx_set_sweep_groups(c, groups, phases));
+  return SCFT_OK;
+}
+
+int scft_fp64_fma_rate(int reps, double *gflops) {
+  if (!gflops || reps < 1) return fail(SCFT_ERR_ARG, "need reps >= 1 and an output pointer");
+  std::string msg;
+  const int st = scft::fp64_fma_rate(reps, gflops, msg);
+  if (st != SCFT_OK) return fail(st, msg);
   return SCFT_OK;
 }
 

@@ -27,7 +27,7 @@ EXPORTS = ("scft_last_error", "scft_version", "scft_create", "scft_destroy", "sc
            "scft_calc_H", "scft_grad_geom", "scft_get_density", "scft_get_plate_density", "scft_get_smeared", "scft_diblock_density",
            "scft_homopolymer_density", "scft_fft3d", "scft_sync", "scft_get_stream", "scft_launch_count",
            "scft_profile_step", "scft_diblock_density_noalloc", "scft_set_sweep_groups", "scft_autotune",
-           "scft_set_fields_all", "scft_set_wait_limit")
+           "scft_set_fields_all", "scft_set_wait_limit", "scft_fp64_fma_rate")
 
 
 class ScftError(RuntimeError):
@@ -104,6 +104,7 @@ def load(path: str | None = None):
     lib.scft_profile_step.argtypes = [vp, ctypes.c_int, dp, dp, dp, dp]
     lib.scft_set_sweep_groups.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     lib.scft_set_wait_limit.argtypes = [vp, ctypes.c_int]
+    lib.scft_fp64_fma_rate.argtypes = [ctypes.c_int, dp]
     lib.scft_set_fields_all.argtypes = [vp, ctypes.POINTER(ctypes.c_void_p)]
     ip = ctypes.POINTER(ctypes.c_int)
     lib.scft_autotune.argtypes = [vp, ctypes.c_int, ip, ip, ip, dp]
@@ -314,6 +315,13 @@ class Context:
         count = a.size // int(np.prod(sh))
         _check(load().scft_fft3d(self._h, inst, _ptr(a.view(np.float64)), count, int(sign)))
         return a
+
+
+def fp64_fma_rate(reps: int = 5) -> float:
+    """Measured FP64 FMA throughput of the current GPU, GFLOP/s."""
+    v = ctypes.c_double()
+    _check(load().scft_fp64_fma_rate(int(reps), ctypes.byref(v)))
+    return v.value
 
 
 def mixed_available() -> bool:

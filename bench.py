@@ -214,6 +214,94 @@ def job_rate(units_per_rank: float, world: int, seconds_max: float) -> float:
     return units_per_rank * world / seconds_max
 
 
+def converge_to_stop_rule(ctx, n, V, tol, itmax, print_freq=25):
+    """Iterates every instance of ctx until each has met the reference's stop
+    rule (code/simulate.cpp:97-155: every print_freq iterations
+    err = |H - H_previous| / V / print_freq, counted when below 10 tol; stop
+    after iteration 25 once err < tol with more than 10 such counts), or
+    until itmax.  Returns (iterations at which each instance met the rule or
+    None, the last err of each instance, total iterations run)."""
+    import numpy as np
+
+    Ho = np.zeros(n)
+    close = np.zeros(n, int)
+    done = [None] * n
+    err = np.full(n, np.inf)
+    it = 0
+    while it < itmax and any(d is None for d in done):
+        ctx.update_1s(print_freq)
+        it += print_freq
+        H = ctx.calc_H()[:, 0]
+        err = np.abs(H - Ho) / np.asarray(V) / print_freq
+        Ho = H.copy()
+        close += err < 10 * tol
+        for k in range(n):
+            if done[k] is None and it > 25 and err[k] < tol and close[k] > 10:
+                done[k] = it
+        if it % 1000 == 0:
+            print(f"  iteration {it}: max err {err.max():.3e}, stopped {sum(d is not None for d in done)}/{n}",
+                  file=sys.stderr, flush=True)
+    return done, err, it
+
+
+def converge_study(args):
+    """Converged accuracy of the mixed form at 64^3, N=100: angles 0, 10, 45
+    and 90 degrees from the same seeded start (seed 1000), each form run to
+    the reference's stop rule; then |dH| between the converged forms
+    (absolute, per volume as the stop rule measures, relative), and dH/dtheta
+    of the mixed form at 10 degrees against a central difference of the
+    converged FP64 H at 9.5 and 10.5 degrees (both converged from the same
+    start)."""
+    import math
+
+    import numpy as np
+    import torch
+
+    import scft
+    from scft.workloads import plate_params, seeded_fields
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    angles = [0.0, 10.0, 45.0, 90.0]
+    hdeg = 0.5
+    res = {}
+    t0 = time.time()
+    for form, prec, thetas in (("mixed", scft.PREC_MIXED, angles),
+                               ("fp64", scft.PREC_FP64, angles + [10.0 - hdeg, 10.0 + hdeg])):
+        ps = [plate_params(t, precision=prec) for t in thetas]
+        f0 = seeded_fields(ps[0], 1000)
+        with scft.Context(ps) as ctx:
+            for k in range(len(ps)):
+                ctx.set_fields(k, f0)
+            ctx.calc_poly_density()
+            V = [ctx.info(k)["V"] for k in range(len(ps))]
+            ts = time.time()
+            done, err, its = converge_to_stop_rule(ctx, len(ps), V, args.tol, args.itmax)
+            H = ctx.calc_H()[:, 0].copy()
+            g = ctx.grad_geom()
+            res[form] = {"H": H, "g": g, "done": done, "err": err, "its": its, "V": V, "thetas": thetas,
+                         "seconds": time.time() - ts}
+            print(f"{form}: stop at {done} after {its} iterations, {time.time() - ts:.1f} s, H {list(H)}",
+                  file=sys.stderr, flush=True)
+    m, d = res["mixed"], res["fp64"]
+    n = len(angles)
+    dH = np.abs(m["H"][:n] - d["H"][:n])
+    fd = (d["H"][n + 1] - d["H"][n]) / math.radians(2 * hdeg)
+    k10 = angles.index(10.0)
+    line = {"study": "converged accuracy, mixed vs FP64", "grid": [64, 64, 64], "N": 100, "angles": angles,
+            "stop_rule": {"error_tol": args.tol, "print_freq": 25, "itmax": args.itmax},
+            "iterations_to_stop": {"mixed": m["done"], "fp64": d["done"][:n]},
+            "last_err": {"mixed": [float(x) for x in m["err"]], "fp64": [float(x) for x in d["err"][:n]]},
+            "H": {"mixed": [float(x) for x in m["H"]], "fp64": [float(x) for x in d["H"][:n]]},
+            "dH_abs": [float(x) for x in dH], "dH_per_volume": [float(x / v) for x, v in zip(dH, d["V"][:n])],
+            "dH_rel": [float(x / abs(h)) for x, h in zip(dH, d["H"][:n])],
+            "dHdtheta_10deg": {"mixed_adjoint": float(m["g"][k10, 0, 0]), "fp64_adjoint": float(d["g"][k10, 0, 0]),
+                               "fp64_converged_central_difference": float(fd), "h_deg": hdeg,
+                               "fd_iterations_to_stop": d["done"][n:]},
+            "seconds": {"mixed": m["seconds"], "fp64": d["seconds"], "total": time.time() - t0}}
+    line["dHdtheta_10deg"]["mixed_vs_fd_rel"] = abs(line["dHdtheta_10deg"]["mixed_adjoint"] - fd) / abs(fd)
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -235,7 +323,16 @@ def main():
                     help="untimed mixed-form iterations from the seeded fields before anything is measured, so "
                          "that timing and the FP64 comparison start near the saddle point (0: seeded fields; "
                          "default 500, fewer for the large workload)")
+    ap.add_argument("--converge", action="store_true",
+                    help="convergence study instead of the timing: angles 0, 10, 45, 90 (and 10 +- 0.5 for the "
+                         "FP64 finite difference) at 64^3, N=100, both forms from the same seeded start to the "
+                         "reference's stop rule; prints one JSON line")
+    ap.add_argument("--tol", type=float, default=1e-8, help="error_tol of the stop rule (--converge)")
+    ap.add_argument("--itmax", type=int, default=20000, help="iteration cap (--converge)")
     args = ap.parse_args()
+    if args.converge:
+        converge_study(args)
+        return
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -392,6 +489,8 @@ def main():
                 g64 = c64.grad_geom()
             except scft.ScftError:
                 g64 = None
+            # the FP64 plane pass in isolation: HBM and FP64-FMA fractions
+            prof64 = c64.profile_step(5)
             drho = []
             for k in range(n_cmp):
                 a64, b64, _ = c64.density(k)
@@ -403,7 +502,24 @@ def main():
         # relative to its largest component
         dg = ([float(np.abs(a[0] - b[0]).max() / max(np.abs(b[0]).max(), 1e-300)) for a, b in zip(g_mixed, g64)]
               if g_mixed is not None and g64 is not None else [None] * n_cmp)
+        import math
+
+        hbm_peak, hbm_kind = peaks()
+        f64_peak = scft.fp64_fma_rate(5)
+        # conventional FFT count 5 E log2 E per 2-D transform of an E-point
+        # plane, two transforms (inverse, forward) per plane and propagator
+        flops = sum((1 if p.Nda in (0, p.Nda + p.Ndb) else 2) * p.Nx[2] * 2 * 5 * p.Nx[0] * p.Nx[1] *
+                    math.log2(p.Nx[0] * p.Nx[1]) for p in pp)
+        ach_b = prof64["bytes_plane"] / (prof64["ms_plane"] / 1e3) / 1e9
+        ach_f = flops / (prof64["ms_plane"] / 1e3) / 1e9
+        plain_roof = {"kernel": "k_prop_plane_f64", "ms_per_launch": prof64["ms_plane"],
+                      "hbm": {"achieved": ach_b, "peak": hbm_peak, "unit": "GB/s", "frac": ach_b / hbm_peak,
+                              "peak_kind": hbm_kind, "algorithmic_bytes_per_launch": prof64["bytes_plane"]},
+                      "fp64": {"achieved": ach_f, "peak": f64_peak, "unit": "GFLOP/s", "frac": ach_f / f64_peak,
+                               "peak_kind": "measured by scft_fp64_fma_rate (FMA chains over every SM)",
+                               "flops_per_launch": flops}}
         plain = {"value": n_cmp * psteps * world / (ms64 / 1e3), "unit": UNIT, "ms_per_step": ms64 / psteps,
+                 "roofline": plain_roof,
                  "instances": n_cmp, "steps": psteps,
                  "mixed_over_plain": (n_inst * args.steps * world / (ms / 1e3)) / (n_cmp * psteps * world /
                                                                                     (ms64 / 1e3)),

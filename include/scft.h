@@ -240,6 +240,12 @@ int scft_launch_count(scft_ctx *ctx, long long *count);
  * Default 2 groups, 1 phase. */
 int scft_set_sweep_groups(scft_ctx *ctx, int groups, int phases);
 
+/* Measurement (no counterpart in the reference): the FP64 FMA throughput of
+ * the current GPU in GFLOP/s (2 flops per FMA), from `reps` timed launches of
+ * a register-only FMA kernel over every SM (CUDA events).  The plain FP64
+ * method's kernels are placed against it as well as against HBM bandwidth. */
+int scft_fp64_fma_rate(int reps, double *gflops);
+
 /* Diagnostic (no counterpart in the reference, whose loops have no waits):
  * the number of polls the first bounded mbarrier wait of each mixed
  * plane-pass CTA makes before it records a timeout in the context's error

@@ -16,6 +16,13 @@
  * Usage (run inside a directory holding bcp.input and optional w*.res):
  *   scft_ref dump  <iters> [hist]   writes scalars.txt, trace.txt, *.f64
  *   scft_ref time  <iters>          prints "seconds_per_iter <t>"
+ *   scft_ref homopoly <Nh> <nK>     homopolymer_discrete(smwa, q, Nh) and
+ *                                   integrate_homopoly_discrete(q, Q, nK, rho,
+ *                                   smwa, Nh) on the smeared w_A after set-up
+ *                                   (code/homopolymer_discrete.cpp:3-55,
+ *                                   code/calc_poly_density.cpp:193-212; dead
+ *                                   in the shipped inputs, read_input.cpp:40-45):
+ *                                   writes homo_W.f64, homo_rho.f64, homo.txt
  *   scft_ref simulate 0             the reference's own main(): read_input,
  *                                   initialize_1, allocate, simulate
  *                                   (writes data.dat and *.p0.bin)
@@ -30,6 +37,9 @@
 
 void update_1s(void);
 double simulate(void);
+complex<double> homopolymer_discrete(complex<double> *, complex<double> **, int);
+void integrate_homopoly_discrete(complex<double> **, complex<double>, complex<double>, complex<double> *,
+                                 complex<double> *, int);
 
 // simulate() has no return statement (code/simulate.cpp:16-167).  Built at
 // -O0 (oracle/Makefile), GCC ends it with a trap instruction, which runs only
@@ -82,6 +92,23 @@ int main(int argc, char **argv) {
     initialize_1();
     allocate();
     simulate();
+    return 0;
+  }
+  if (!strcmp(argv[1], "homopoly")) {
+    if (argc < 4) return 2;
+    const int Nh = atoi(argv[2]);
+    const double nK = atof(argv[3]);
+    setup();
+    complex<double> **qh = new complex<double> *[Nh];
+    for (int s = 0; s < Nh; s++) qh[s] = new complex<double>[ML];
+    complex<double> *rh = new complex<double>[ML];
+    const complex<double> Qh = homopolymer_discrete(smwa, qh, Nh);
+    integrate_homopoly_discrete(qh, Qh, complex<double>(nK, 0.0), rh, smwa, Nh);
+    dump("homo_W", smwa);
+    dump("homo_rho", rh);
+    FILE *f = fopen("homo.txt", "w");
+    fprintf(f, "Q_re %.17g\nQ_im %.17g\n", real(Qh), imag(Qh));
+    fclose(f);
     return 0;
   }
   if (!strcmp(argv[1], "time")) {

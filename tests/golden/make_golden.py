@@ -219,8 +219,38 @@ def make_driver_fixtures(tmp):
         print(name, open(os.path.join(run, "data.dat")).read().splitlines()[-1])
 
 
+def make_homopolymer_fixture(tmp, Nh=7, nK=3.5):
+    """The reference's homopolymer_discrete + integrate_homopoly_discrete
+    (dead in its shipped inputs) on the smeared w_A of the tiny_plate case,
+    run through the oracle harness's homopoly mode."""
+    import subprocess
+
+    from ref_case import REF_BIN, load_f64, write_case
+
+    c, _, _ = tiny_cases()["tiny_plate"]
+    run = os.path.join(tmp, "homopoly")
+    write_case(run, c)
+    r = subprocess.run([REF_BIN, "homopoly", str(Nh), repr(nK)], cwd=run, capture_output=True, text=True,
+                       timeout=600)
+    if r.returncode != 0:
+        raise RuntimeError(r.stderr)
+    sc = {}
+    for line in open(os.path.join(run, "homo.txt")):
+        k, v = line.split()
+        sc[k] = float(v)
+    z = {"case_json": case_json(c), "Nh": Nh, "nK": nK, "W": load_f64(run, "homo_W", c),
+         "rho": load_f64(run, "homo_rho", c), "Q": complex(sc["Q_re"], sc["Q_im"])}
+    for k, v in c.fields.items():
+        z["in_" + k] = v
+    np.savez_compressed(os.path.join(HERE, "tiny_homopolymer.npz"), **z)
+    print("tiny_homopolymer Q", z["Q"])
+
+
 def main():
     tmp = tempfile.mkdtemp(prefix="golden_")
+    if "--homopolymer" in sys.argv:
+        make_homopolymer_fixture(tmp)
+        return
     if "--large" in sys.argv:
         names = [a for a in sys.argv[1:] if not a.startswith("--")]
         make_large_fixtures(tmp, names or None)

@@ -92,8 +92,10 @@ def test_fp64_matches_reference_at_full_size(scft, name):
         err = np.abs(rows[:, col_ours] - tr[:, col_ref]) / np.abs(tr[:, col_ref])
         assert err.max() <= H_TOL, (name, col_ref, err)
     if graft:
-        err = np.abs(rows[:, 4] - tr[:, 5]) / np.abs(tr[:, 5])
-        assert err.max() <= H_TOL, (name, "Qga", err)
+        # Qga before the first update is 0 on both sides (the set-up's
+        # density build does not form it)
+        d = np.abs(rows[:, 4] - tr[:, 5])
+        assert (d <= H_TOL * np.abs(tr[:, 5])).all(), (name, "Qga", rows[:, 4], tr[:, 5])
     for k, a in got.items():
         ok, parts = digest_close(digest(a, ns), z["digest_" + k], RHO_TOL, M)
         assert ok, (name, k, parts)

@@ -146,6 +146,19 @@ def test_batched_uneven_instances_match_reference(scft):
         assert rel(dens[k][1], st.out["rhodb"]) < RHO_TOL
 
 
+def test_homopolymer_matches_reference(scft):
+    """scft_homopolymer_density against the reference's own
+    homopolymer_discrete + integrate_homopoly_discrete (run by the oracle
+    harness on the smeared w_A of tiny_plate; tests/golden/tiny_homopolymer.npz)."""
+    c, _ = load_golden("tiny_plate")
+    z = np.load(os.path.join(GOLDEN, "tiny_homopolymer.npz"))
+    with scft.Context(scft.params_from_case(c)) as ctx:
+        r, Q = ctx.homopolymer_density(0, z["W"], int(z["Nh"]), float(z["nK"]))
+    Qr = complex(z["Q"])
+    assert abs(Q - Qr) <= RHO_TOL * abs(Qr)
+    assert rel(r, z["rho"]) < RHO_TOL
+
+
 def test_homopolymer_matches_restatement(scft):
     """homopolymer_discrete + integrate_homopoly_discrete (dead in the shipped
     inputs, code/read_input.cpp:40-45) against the restatement."""

@@ -132,6 +132,21 @@ def test_restatement_propagators_match_reference(name):
     assert rel(st.out["rhoda"], z["rhoda0"]) < 1e-12
 
 
+def test_restatement_homopolymer_matches_reference():
+    """homopolymer_discrete + integrate_homopoly_discrete (code/
+    homopolymer_discrete.cpp:3-55, code/calc_poly_density.cpp:193-212), dead
+    in the shipped inputs, run by the oracle harness on the smeared w_A of the
+    tiny_plate case (tests/golden/tiny_homopolymer.npz)."""
+    c, _ = load_golden("tiny_plate")
+    z = np.load(os.path.join(GOLDEN, "tiny_homopolymer.npz"))
+    s = O.System.from_case(c)
+    Nh, nK = int(z["Nh"]), float(z["nK"])
+    Q, q = O.homopolymer_discrete(s, z["W"], Nh)
+    rho = O.integrate_homopoly_discrete(s, q, Q, nK, z["W"], Nh)
+    assert abs(Q - complex(z["Q"])) <= 1e-13 * abs(complex(z["Q"]))
+    assert rel(rho, z["rho"]) < 1e-12
+
+
 def test_segment_count_invariant():
     """code/simulate.cpp:61-72: integral(rho_A + rho_B) = nD * N."""
     c, _ = load_golden("tiny_plate")
