@@ -24,6 +24,8 @@ void ctx_override_nD(scft_ctx *c, int k, double nD);
 int ctx_grad_geom(scft_ctx *c, double *out);
 void ctx_set_sweep_groups(scft_ctx *c, int groups, int phases);
 void ctx_set_wait_limit(scft_ctx *c, int polls);
+void ctx_set_persistent(scft_ctx *c, int on);
+void ctx_profile_sweep(scft_ctx *c, int reps, double *ms, double *bytes);
 void ctx_set_fields_all(scft_ctx *c, const double *const *w);
 void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *tx_out, double *ms_out);
 void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
@@ -257,8 +259,29 @@ int scft_fp64_fma_rate(int reps, double *gflops) {
 
 int scft_set_wait_limit(scft_ctx *c, int polls) {
   if (int s = check_ctx(c, 0)) return s;
-  if (polls < 0) return fail(SCFT_ERR_ARG, "polls must be >= 0");
   API_BODY(scft::ctx_set_wait_limit(c, polls));
+  return SCFT_OK;
+}
+
+int scft_set_persistent(scft_ctx *c, int on) {
+  if (int s = check_ctx(c, 0)) return s;
+  API_BODY(scft::ctx_set_persistent(c, on));
+  return SCFT_OK;
+}
+
+int scft_profile_sweep(scft_ctx *c, int reps, double *ms, double *bytes) {
+  if (int s = check_ctx(c, 0)) return s;
+  if (reps < 1 || !ms || !bytes) return fail(SCFT_ERR_ARG, "need reps >= 1 and output pointers");
+  API_BODY(scft::ctx_profile_sweep(c, reps, ms, bytes));
+  return SCFT_OK;
+}
+
+int scft_get_schedule(scft_ctx *c, int *groups, int *phases, int *col_tile, int *persistent) {
+  if (int s = check_ctx(c, 0)) return s;
+  if (groups) *groups = c->sweep_streams;
+  if (phases) *phases = c->sweep_phases;
+  if (col_tile) *col_tile = (c->colfast || c->anyfast) ? c->col64_tx : 0;
+  if (persistent) *persistent = c->sweep_persistent;
   return SCFT_OK;
 }
 

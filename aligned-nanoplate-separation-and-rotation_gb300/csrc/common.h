@@ -12,6 +12,9 @@ constexpr int kMaxStages = 8;
 // context's error word (each poll is one mbarrier.try_wait, which itself
 // suspends the thread for a hardware-chosen interval).
 constexpr int kWaitPolls = 1 << 22;
+// Polls (each followed by a ~64 ns sleep) of a dependency wait of the
+// persistent sweep before it gives up.
+constexpr int kSpinPolls = 1 << 24;
 
 // Stage plan of a 1-D FFT of length n along one grid axis: radices applied in
 // order (Stockham autosort, decimation in time) and the offset of this

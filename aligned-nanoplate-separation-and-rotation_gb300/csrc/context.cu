@@ -755,8 +755,8 @@ CUtensorMap tensor_map_rows(const float2 *base, unsigned long long rows) {
 // The plane passes' error word and first-wait poll limit (see context.h).
 void ensure_err(scft_ctx *c) {
   if (c->d_err) return;
-  c->d_err = dalloc<int>(c, 2);
-  const int init[2] = {0, kWaitPolls};
+  c->d_err = dalloc<int>(c, 3);
+  const int init[3] = {0, kWaitPolls, kSpinPolls};
   CK(cudaMemcpyAsync(c->d_err, init, sizeof init, cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
 }
@@ -769,6 +769,10 @@ void check_device_error(scft_ctx *c) {
   CK(cudaStreamSynchronize(c->st));
   if (h) {
     CK(cudaMemsetAsync(c->d_err, 0, sizeof(int), c->st));
+    if (h == 2)
+      throw ScftError(SCFT_ERR_CUDA,
+                      "a dependency wait of the persistent sweep ran out: the sweep stopped (results of that call "
+                      "are invalid; set the fields again)");
     throw ScftError(SCFT_ERR_CUDA, "a TMA wait of the plane pass ran out (results of that call are invalid)");
   }
 }
@@ -844,6 +848,11 @@ void build_groups(scft_ctx *c) {
     c->ev_join.push_back(ev);
   }
   if (!c->ev_fork) CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+  if (c->sweep_persistent && c->sweep_ctr_groups < ng) {
+    // counters are cleared by each launch; old arrays stay in c->allocs
+    c->d_sweep_ctr = dalloc<unsigned>(c, (size_t)ng * sweep64_counters(kMix64MaxInst));
+    c->sweep_ctr_groups = ng;
+  }
 }
 
 // Builds the device views and job lists once all instances exist.
@@ -1423,6 +1432,74 @@ void seq_update_1s(scft_ctx *c) {
   seq_poly_density(c);
 }
 
+// The group's sweep runs as one persistent launch: the context asks for it,
+// and the group's instances are 64 x 64 x 64 grids, at most kMix64MaxInst.
+bool persistent_group(const scft_ctx *c, const scft_ctx::SweepGroup &gr) {
+  if (!c->sweep_persistent) return false;
+  const bool p64 = c->xy64 || gr.fast, z64 = c->colfast || gr.fast;
+  const int nzi = gr.fast ? 64 : c->inst[0].p.Nx[2];
+  return p64 && z64 && nzi == 64 && gr.inst_end - gr.inst_begin <= kMix64MaxInst;
+}
+
+// The FP32 propagator sweep of group g on stream sg (accumulators cleared,
+// then every step), from the Boltzmann factors to the plane sums and the
+// density accumulators: one persistent launch (persistent_group) or a z pass
+// and a plane pass per step.
+void mix_group_sweep(scft_ctx *c, int g, cudaStream_t sg) {
+  const scft_ctx::SweepGroup &gr = c->groups[g];
+  const int cnt_i = gr.inst_end - gr.inst_begin;
+  for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) {
+    Instance &I = c->inst[c->job_order[oi]];
+    CK(cudaMemsetAsync(I.acc32[0], 0, sizeof(float) * I.M, sg));
+    CK(cudaMemsetAsync(I.acc32[1], 0, sizeof(float) * I.M, sg));
+  }
+  const bool p64 = c->xy64 || gr.fast, z64 = c->colfast || gr.fast;
+  const int nzi = gr.fast ? 64 : c->inst[0].p.Nx[2];
+  const void *twz = gr.fast ? c->d_tw32_64 : c->d_tw32_z;
+  if (persistent_group(c, gr)) {
+    // the whole sweep of the group in one launch; concurrent groups share the
+    // GPU's resident CTAs in proportion to their instances
+    std::vector<const float *> ht;
+    for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) ht.push_back(c->inst[c->job_order[oi]].htab32);
+    const int G = (int)c->groups.size();
+    int cap = 0;
+    if (G > 1) {
+      int in_phase = 0;
+      for (auto &o : c->groups)
+        if (o.phase == gr.phase) in_phase += o.inst_end - o.inst_begin;
+      cap = std::max(1, (int)((long long)c->sweep64_cap * cnt_i / std::max(1, in_phase)));
+    }
+    LK(launch_mix_sweep64(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
+                          c->tmH.data() + gr.inst_begin, ht.data(), cnt_i, c->d_tw32_64,
+                          c->d_sweep_ctr + (size_t)g * sweep64_counters(kMix64MaxInst), c->d_err, cap, sg));
+    return;
+  }
+  const int per = 64 * (64 / c->col64_tx);  // z-pass jobs per instance of the 64-point kernels
+  for (int s = 0; s < c->nmax; s++) {
+    // instances of the group still active at step s: a prefix (decreasing N)
+    int act = 0;
+    for (int oi = gr.inst_begin; oi < gr.inst_end; oi++)
+      if (c->inst[c->job_order[oi]].N > s) act = oi + 1 - gr.inst_begin;
+    if (act == 0) break;
+    const int last = gr.inst_begin + act - 1;
+    const int cnt = c->inst_pj_end[last] - gr.pj_begin;
+    const int cc = c->inst_cj_end[last] - gr.cj_begin;
+    if (s > 0) {
+      if (z64)
+        LK(launch_mix_col64(col64_jobs(c) + (size_t)gr.inst_begin * per, act * per, twz, 64, 64, nzi, c->col64_tx,
+                            sg));
+      else
+        LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cc, c->d_geoms, c->d_tw32, 3, 1, sg));
+    }
+    if (p64)
+      LK(launch_mix_plane64(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
+                            c->tmH.data() + gr.inst_begin, act, nzi, c->d_tw32_64, s, c->d_err, sg));
+    else
+      LK(launch_mix_prop_plane(c->shp_mixp, c->d_prop_pj + gr.pj_begin, cnt, c->d_mi, c->d_geoms, c->d_tw32, s,
+                               c->d_err, sg));
+  }
+}
+
 // Mixed form, one sweep group on stream sg: the work of one update_1s (or of
 // calc_poly_density when `update` is false) for the group's instances, from
 // the densities of the last sweep to the densities of this one:
@@ -1468,38 +1545,7 @@ void mix_group_chain(scft_ctx *c, int g, cudaStream_t sg, bool update) {
     LK(launch_plane_fft<double>(c->shp_plane, c->d_gpj_ord + gpb, gpm, c->d_geoms, c->d_tw64, +1, 0, sg));
   }
   LK(launch_mix_boltzmann(fi, cnt_i, c->eblocks, sg));
-  for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) {
-    Instance &I = c->inst[c->job_order[oi]];
-    CK(cudaMemsetAsync(I.acc32[0], 0, sizeof(float) * I.M, sg));
-    CK(cudaMemsetAsync(I.acc32[1], 0, sizeof(float) * I.M, sg));
-  }
-  const bool p64 = c->xy64 || gr.fast, z64 = c->colfast || gr.fast;
-  const int nzi = gr.fast ? 64 : c->inst[0].p.Nx[2];
-  const void *twz = gr.fast ? c->d_tw32_64 : c->d_tw32_z;
-  const int per = 64 * (64 / c->col64_tx);  // z-pass jobs per instance of the 64-point kernels
-  for (int s = 0; s < c->nmax; s++) {
-    // instances of the group still active at step s: a prefix (decreasing N)
-    int act = 0;
-    for (int oi = gr.inst_begin; oi < gr.inst_end; oi++)
-      if (c->inst[c->job_order[oi]].N > s) act = oi + 1 - gr.inst_begin;
-    if (act == 0) break;
-    const int last = gr.inst_begin + act - 1;
-    const int cnt = c->inst_pj_end[last] - gr.pj_begin;
-    const int cc = c->inst_cj_end[last] - gr.cj_begin;
-    if (s > 0) {
-      if (z64)
-        LK(launch_mix_col64(col64_jobs(c) + (size_t)gr.inst_begin * per, act * per, twz, 64, 64, nzi, c->col64_tx,
-                            sg));
-      else
-        LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cc, c->d_geoms, c->d_tw32, 3, 1, sg));
-    }
-    if (p64)
-      LK(launch_mix_plane64(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
-                            c->tmH.data() + gr.inst_begin, act, nzi, c->d_tw32_64, s, c->d_err, sg));
-    else
-      LK(launch_mix_prop_plane(c->shp_mixp, c->d_prop_pj + gr.pj_begin, cnt, c->d_mi, c->d_geoms, c->d_tw32, s,
-                               c->d_err, sg));
-  }
+  mix_group_sweep(c, g, sg);
   LK(launch_mix_q_finalize(fi, cnt_i, sg));
 }
 
@@ -1693,14 +1739,32 @@ void ctx_update(scft_ctx *c, int n_iter) {
   check_device_error(c);
 }
 
-// Poll limit of the first bounded mbarrier wait of every mixed plane-pass CTA
-// (read by the kernels from d_err[1] at run time, so captured graphs need no
-// re-capture).
+// Poll limits of the first bounded mbarrier wait of every mixed plane-pass
+// CTA (d_err[1]) and of the persistent sweep's dependency waits (d_err[2]),
+// read by the kernels at run time, so captured graphs need no re-capture;
+// polls < 0 restores the defaults.
 void ctx_set_wait_limit(scft_ctx *c, int polls) {
-  if (polls < 0) throw ScftError(SCFT_ERR_ARG, "polls must be >= 0");
   ensure_err(c);
-  CK(cudaMemcpyAsync(c->d_err + 1, &polls, sizeof(int), cudaMemcpyHostToDevice, c->st));
+  const int lim[2] = {polls < 0 ? kWaitPolls : polls, polls < 0 ? kSpinPolls : polls};
+  CK(cudaMemcpyAsync(c->d_err + 1, lim, sizeof lim, cudaMemcpyHostToDevice, c->st));
   CK(cudaStreamSynchronize(c->st));
+}
+
+// Persistent sweep on or off (64 x 64 x 64 groups only; others keep the
+// per-step launches).  The captured graphs hold the old launches.
+void ctx_set_persistent(scft_ctx *c, int on) {
+  if (on && (c->xy64 || c->anyfast) && !c->sweep64_cap) CK(sweep64_capacity(&c->sweep64_cap));
+  c->sweep_persistent = on ? 1 : 0;
+  if (!c->mixed) return;
+  build_groups(c);
+  if (c->g_update) {
+    CK(cudaGraphExecDestroy(c->g_update));
+    c->g_update = nullptr;
+  }
+  if (c->g_density) {
+    CK(cudaGraphExecDestroy(c->g_density));
+    c->g_density = nullptr;
+  }
 }
 
 // Number of independent launch chains of the mixed sweep (1 = one chain).
@@ -1750,11 +1814,18 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
   for (int ph : {1, 2, 3, 4})
     if (ph <= n) ps.push_back(ph);
   double best = 1e300;
-  int bg = c->sweep_streams, bt = c->col64_tx, bp = c->sweep_phases;
+  int bg = c->sweep_streams, bt = c->col64_tx, bp = c->sweep_phases, bpers = c->sweep_persistent;
+  // the persistent sweep applies to 64 x 64 x 64 instances
+  const bool can_persist = (c->xy64 && c->inst[0].p.Nx[2] == 64) || c->anyfast;
+  if (can_persist && !c->sweep64_cap) CK(sweep64_capacity(&c->sweep64_cap));
+  for (int pers = 0; pers <= (can_persist ? 1 : 0); pers++)
   for (int ph : ps)
   for (int g : gs)
     for (int tx : txs) {
       if (g * ph > n) continue;
+      // persistent: the z tasks take whole rows (tx unused); few groups, phases
+      if (pers && (tx != txs[0] || g > 3 || ph > 2)) continue;
+      c->sweep_persistent = pers;
       c->sweep_phases = ph;
       c->sweep_streams = g;
       c->col64_tx = tx;
@@ -1771,11 +1842,13 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
         bg = g;
         bt = tx;
         bp = ph;
+        bpers = pers;
       }
     }
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   c->col64_tx = bt;
+  c->sweep_persistent = bpers;
   ctx_set_sweep_groups(c, bg, bp);
   if (c->g_update) {
     CK(cudaGraphExecDestroy(c->g_update));
@@ -1789,6 +1862,67 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
   *phases_out = bp;
   *tx_out = (c->colfast || c->anyfast) ? bt : 0;
   *ms_out = best;
+}
+
+// Algorithmic bytes of one FP32 propagator sweep of a mixed instance (per
+// point: z pass 8 + 8 per step n >= 1; plane pass: working plane in (n >= 1)
+// and out (n < N - 1), Boltzmann pair, history plane out (n <= hmax) or
+// stored partner in (paired steps), FP32 accumulators read and written).
+static double mix_sweep_bytes(const Instance &I) {
+  const int N = I.N, Na = I.p.Nda;
+  double b = 0.0;
+  for (int n = 0; n < N; n++) {
+    const int m2 = N - 1 - n;
+    double pt = 8.0;  // Boltzmann pair
+    if (n >= 1) pt += 16.0 + 8.0;  // z pass in and out, plane in
+    if (n < N - 1) pt += 8.0;      // plane out
+    if (n <= I.hmax) pt += 8.0;    // history out
+    if (m2 < n) pt += 8.0 + ((n < Na) == (m2 < Na) ? 8.0 : 16.0);  // partner in, accumulators
+    else if (m2 == n) pt += 8.0;
+    b += pt;
+  }
+  return b * (double)I.M;
+}
+
+// Isolated timing of `reps` FP32 propagator sweeps of the whole batch with
+// the current schedule (groups of a phase concurrent, phases in order), no
+// field work, with their algorithmic bytes.  Leaves the densities invalid.
+void ctx_profile_sweep(scft_ctx *c, int reps, double *ms, double *bytes) {
+  if (!c->mixed) throw ScftError(SCFT_ERR_UNSUPPORTED, "the sweep profile is for the mixed form");
+  if (c->dirty_density) ctx_poly_density(c);
+  auto sweep = [c]() {
+    const int G = (int)c->groups.size();
+    for (int g0 = 0; g0 < G;) {
+      int g1 = g0;
+      while (g1 < G && c->groups[g1].phase == c->groups[g0].phase) g1++;
+      CK(cudaEventRecord(c->ev_fork, c->st));
+      for (int g = g0; g < g1; g++) {
+        CK(cudaStreamWaitEvent(c->side[g], c->ev_fork, 0));
+        mix_group_sweep(c, g, c->side[g]);
+        CK(cudaEventRecord(c->ev_join[g], c->side[g]));
+        CK(cudaStreamWaitEvent(c->st, c->ev_join[g], 0));
+      }
+      g0 = g1;
+    }
+  };
+  sweep();  // untimed
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, c->st));
+  for (int r = 0; r < reps; r++) sweep();
+  CK(cudaEventRecord(e1, c->st));
+  CK(cudaEventSynchronize(e1));
+  float t = 0.f;
+  CK(cudaEventElapsedTime(&t, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  check_device_error(c);
+  double b = 0.0;
+  for (auto &I : c->inst) b += mix_sweep_bytes(I);
+  *ms = t / reps;
+  *bytes = b;
+  c->dirty_density = 1;
 }
 
 // Isolated timing of the two kernels of one propagator step (step 3(N-1)/4,

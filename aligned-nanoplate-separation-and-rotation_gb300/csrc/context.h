@@ -111,14 +111,23 @@ struct scft_ctx {
   void *d_tw32 = nullptr;
   scft::ColJob *d_mix64_cj_tx[3] = {};  // z-pass jobs of the 64^3 kernels for 8, 16, 32 columns per CTA
   int col64_tx = 16;                      // columns per CTA of the 64^3 z pass
+  // the sweep of a group of 64 x 64 x 64 instances as one persistent launch
+  // (k_mix_sweep64) instead of two launches per step; its task counters
+  // (sweep64_counters(kMix64MaxInst) per group) and the CTAs resident at once
+  int sweep_persistent = 0;
+  unsigned *d_sweep_ctr = nullptr;
+  int sweep_ctr_groups = 0;
+  int sweep64_cap = 0;
   scft::MixInst *d_mi = nullptr;
   scft::GraftMixInst *d_gmi = nullptr;  // per instance (zero for instances without grafts)
   std::vector<scft::MixInst> h_mi;       // host copy of d_mi
   std::vector<scft::MixInst> mix64_tab;  // instances in job order (64^3 plane pass)
   std::vector<CUtensorMap> tmE, tmH;      // their TMA descriptors (Boltzmann, history)
-  // d_err[0]: error word of the plane passes (a bounded wait ran out);
+  // d_err[0]: error word of the plane passes (1: an mbarrier wait ran out;
+  // 2: a dependency wait of the persistent sweep ran out);
   // d_err[1]: polls of each plane-pass CTA's first mbarrier wait before it
-  // records a timeout (kWaitPolls; scft_set_wait_limit lowers it)
+  // records a timeout (kWaitPolls); d_err[2]: polls of a dependency wait
+  // (kSpinPolls); scft_set_wait_limit lowers both
   int *d_err = nullptr;
   double *h_pin = nullptr;                // pinned read-back of the field checks (128 doubles per instance)
   // scft_set_fields (mixed form): check results, instance mask, job staging

@@ -84,33 +84,45 @@ __device__ __forceinline__ float2 swz(const float2 *plane, int row, int x) {
 
 }  // namespace
 
-// Plane pass of step n for 64 x 64 xy planes (any nz, the same for every
-// instance of the launch), 512 threads, one CTA per (instance, z plane): CTA b
-// works on plane b % nz of T.inst[b / nz].  The
-// instance table is a kernel parameter, so the first global loads (the
-// working plane, the prefetches) depend on nothing loaded before them.
-// Dynamic shared memory (1024-byte aligned for the swizzle): staged Boltzmann
-// plane and history plane (32 KB each), then the padded exchange/transpose
-// plane (36.9 KB); 101 KB, two CTAs per SM.
-// NZ: nz known at compile time (64), or 0 to read it from the table.
-template <int NZ>
-__global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ Mix64Table T,
-                                                        const float2 *__restrict__ tw_g, int n) {
-  extern __shared__ __align__(16) unsigned char dsm_raw[];
-  float2 *Es = reinterpret_cast<float2 *>(dsm_raw + ((1024 - (smem_u32(dsm_raw) & 1023)) & 1023));
-  float2 *Hs = Es + 4096;
-  float2 *buf = Hs + 4096;
-  __shared__ float2 tw[64];
-  __shared__ __align__(8) uint64_t s_bar;
-  __shared__ double s_red[2][16];
-  __shared__ float s_mh[2], s_ml[2];  // step means as two-float pairs
-  __shared__ int s_exp[2];
-  const int nz = NZ ? NZ : T.nz;
-  const int ii = blockIdx.x / nz;
+// Static shared scratch of one plane task.
+struct Plane64Shared {
+  float2 tw[64];      // 64-point twiddles
+  double red[2][16];  // per-warp plane sums
+  float mh[2], ml[2]; // step means as two-float pairs
+  int exp[2];         // power-of-two exponents of the step
+};
+
+// Thread 0 of the CTA: TMA loads of the Boltzmann plane zz of instance ii
+// and, on a paired step n (partner step m2 = N - 1 - n < n), of the stored
+// history plane m2, into Es / Hs, completing on `bar` (E rows z*64 + y of a
+// 64 nz-row tensor; history rows (m2*nz + z)*64 + y).
+__device__ __forceinline__ void plane64_stage(const Mix64Table &T, int ii, int zz, int nz, int n, float2 *Es,
+                                              float2 *Hs, uint64_t *bar) {
   const MixInst &P = T.inst[ii];
-  const int zz = blockIdx.x - ii * nz;
+  const int m2 = P.N - 1 - n;
+  const bool pair = (m2 < n);
+  mbar_expect_tx(bar, pair ? 65536u : 32768u);
+  const uint64_t pol_last = l2_policy_last(), pol_first = l2_policy_first();
+  for (int b = 0; b < 4; b++) tma_load_2d(Es + b * 1024, &T.tmE[ii], 32 * b, zz * 64, bar, pol_last);
+  if (pair)
+    for (int b = 0; b < 4; b++) tma_load_2d(Hs + b * 1024, &T.tmH[ii], 32 * b, (m2 * nz + zz) * 64, bar, pol_first);
+}
+
+// One plane task: plane zz of instance ii at step n (n < N), 512 threads.
+// On entry S.tw holds the twiddles and plane64_stage has been issued on
+// `bar`, whose phase `parity` completes when the staged planes have landed;
+// both are ordered before the first wait by the body's first block barrier.
+// The CTA's shared planes Es, Hs (TMA, 128-byte swizzle) and buf (padded
+// exchange plane) are free again once the body returns and the caller has
+// passed a block barrier.
+// STAGE: thread 0 issues plane64_stage itself, right after its working-plane
+// loads (the one-launch-per-step kernel); otherwise the caller has issued it.
+template <int NZ, bool STAGE>
+__device__ __forceinline__ void plane64_body(const Mix64Table &T, int ii, int zz, int n, float2 *Es, float2 *Hs,
+                                             float2 *buf, Plane64Shared &S, uint64_t *bar, uint32_t parity) {
+  const int nz = NZ ? NZ : T.nz;
+  const MixInst &P = T.inst[ii];
   const int N = P.N, Na = P.Na;
-  if (n >= N) return;
   const long long M = 4096LL * nz;
   const long long zoff = (long long)zz * 4096;
   const int tid = threadIdx.x;
@@ -127,16 +139,7 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
   const int m2 = N - 1 - n;
   const bool pair = (m2 < n);  // a stored partner plane is needed
   const uint64_t pol_first = l2_policy_first();
-  if (tid == 0) {
-    // E rows z*64 + y of a 64 nz-row tensor; history rows (m2*nz + z)*64 + y
-    mbar_init(&s_bar, 1);
-    mbar_expect_tx(&s_bar, pair ? 65536u : 32768u);
-    const uint64_t pol_last = l2_policy_last();
-    for (int b = 0; b < 4; b++) tma_load_2d(Es + b * 1024, &T.tmE[ii], 32 * b, zz * 64, &s_bar, pol_last);
-    if (pair)
-      for (int b = 0; b < 4; b++)
-        tma_load_2d(Hs + b * 1024, &T.tmH[ii], 32 * b, (m2 * nz + zz) * 64, &s_bar, pol_first);
-  }
+  if (STAGE && tid == 0) plane64_stage(T, ii, zz, nz, n, Es, Hs, bar);
   // accumulators of a paired step, loaded now so that their latency overlaps
   // the inverse transforms (row-phase ownership, as they are used)
   const int gi = row * 64 + tr;  // global index of element d = 0 in this plane
@@ -152,7 +155,6 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
       for (int d = 0; d < 8; d++) acc2[d] = a2[8 * d];
     }
   }
-  if (tid < 64) tw[tid] = tw_g[tid];
   if (warp < 2) {
     // warp 0: mean of q_{n-1}; warp 1: mean of qdag_{n-1} (64 FP64 plane sums each)
     double a = 0.0;
@@ -165,20 +167,20 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
       const double ma = NZ ? a * (1.0 / (double)M) : a / (double)M;  // 2^18 when NZ = 64: exact
       int ea = 0;
       if (n > 0 && isfinite(ma) && ma > 0.0) frexp(ma, &ea);
-      s_exp[warp] = ea;
+      S.exp[warp] = ea;
       // split once here: GB300 runs FP64 (conversions included) at a small
       // fraction of the FP32 rate, so no thread of the plane does it
       const float hi = (float)ma;
-      s_mh[warp] = hi;
-      s_ml[warp] = (float)(ma - (double)hi);
+      S.mh[warp] = hi;
+      S.ml[warp] = (float)(ma - (double)hi);
     }
   }
   const bool useA_q = (Na > 0 && n < Na);
   const bool useA_d = !(n <= N - Na - 1);
-  __syncthreads();  // tw, means, exponents
+  __syncthreads();  // means, exponents (and, on entry, the twiddles and the barrier's initialisation)
   if (n > 0) {
     // inverse y transform (column phase)
-    fft64_group<+1, false>(v, tc, buf + col, 8 * 64, 64, tw);
+    fft64_group<+1, false>(v, tc, buf + col, 8 * 64, 64, S.tw);
 #pragma unroll
     for (int d = 0; d < 8; d++) buf[(tc + 8 * d) * kRowPad + col] = v[d];
     __syncthreads();
@@ -189,14 +191,14 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
     // barrier suffices before the exchange overwrites what was just read
     __syncwarp();
     // inverse x transform (row phase, inside one warp)
-    fft64_group<+1, true>(v, tr, buf + row * kRowPad, 9, 1, tw);
+    fft64_group<+1, true>(v, tr, buf + row * kRowPad, 9, 1, S.tw);
   }
   // every thread waits on the mbarrier itself (acquiring the staged planes),
   // and the shared plane is touched only in the thread's own rows until the
   // barrier of the plane sums: no block barrier here
-  if (!mbar_wait(&s_bar, 0, T.err[1])) {
+  if (!mbar_wait(bar, parity, T.err[1])) {
     atomicExch(T.err, 1);
-    mbar_wait(&s_bar, 0, kWaitPolls);  // let copies in flight land before the CTA moves on
+    mbar_wait(bar, parity, kWaitPolls);  // let copies in flight land before the CTA moves on
   }
 
   if (n == 0) {
@@ -207,10 +209,10 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
     }
   } else {
     // q = (conv + mean) * e^{-w} * 2^{-e}, the mean as a two-float constant
-    const int eq = s_exp[0], ed = s_exp[1];
+    const int eq = S.exp[0], ed = S.exp[1];
     const float sq = ldexpf(1.0f, -eq), sd = ldexpf(1.0f, -ed);
-    const float mq_hi = s_mh[0], mq_lo = s_ml[0];
-    const float md_hi = s_mh[1], md_lo = s_ml[1];
+    const float mq_hi = S.mh[0], mq_lo = S.ml[0];
+    const float md_hi = S.mh[1], md_lo = S.ml[1];
 #pragma unroll
     for (int d = 0; d < 8; d++) {
       const float2 e = swz(Es, row, tr + 8 * d);
@@ -220,8 +222,8 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
       v[d] = make_float2(uq * sq, ud * sd);
     }
   }
-  const int Kq = (n == 0) ? 0 : P.K[n - 1] + s_exp[0];
-  const int Kd = (n == 0) ? 0 : P.K[N + n - 1] + s_exp[1];
+  const int Kq = (n == 0) ? 0 : P.K[n - 1] + S.exp[0];
+  const int Kd = (n == 0) ? 0 : P.K[N + n - 1] + S.exp[1];
   if (zz == 0 && tid == 0) {
     P.K[n] = Kq;
     P.K[N + n] = Kd;
@@ -279,13 +281,13 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
     cd += d2 + e;
   }
   if (lane == 0) {
-    s_red[0][warp] = (double)sq_ + (double)cq;
-    s_red[1][warp] = (double)sd_ + (double)cd;
+    S.red[0][warp] = (double)sq_ + (double)cq;
+    S.red[1][warp] = (double)sd_ + (double)cd;
   }
   __syncthreads();
   if (warp == 0) {
-    double aq = lane < 16 ? s_red[0][lane] : 0.0;
-    double ad = lane < 16 ? s_red[1][lane] : 0.0;
+    double aq = lane < 16 ? S.red[0][lane] : 0.0;
+    double ad = lane < 16 ? S.red[1][lane] : 0.0;
     for (int o = 8; o > 0; o >>= 1) {
       aq += __shfl_down_sync(0xffffffffu, aq, o);
       ad += __shfl_down_sync(0xffffffffu, ad, o);
@@ -297,16 +299,44 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
   }
   if (n == N - 1) return;
   // forward x transform (row phase), then to the column phase, forward y
-  fft64_group<-1, true>(v, tr, buf + row * kRowPad, 9, 1, tw);
+  fft64_group<-1, true>(v, tr, buf + row * kRowPad, 9, 1, S.tw);
 #pragma unroll
   for (int d = 0; d < 8; d++) buf[row * kRowPad + tr + 8 * d] = v[d];
   __syncthreads();
 #pragma unroll
   for (int a = 0; a < 8; a++) v[a] = buf[(tc + 8 * a) * kRowPad + col];
   __syncthreads();
-  fft64_group<-1, false>(v, tc, buf + col, 8 * 64, 64, tw);
+  fft64_group<-1, false>(v, tc, buf + col, 8 * 64, 64, S.tw);
 #pragma unroll
   for (int d = 0; d < 8; d++) work[(tc + 8 * d) * 64 + col] = v[d];
+}
+
+
+// Plane pass of step n for 64 x 64 xy planes (any nz, the same for every
+// instance of the launch), 512 threads, one CTA per (instance, z plane): CTA b
+// works on plane b % nz of T.inst[b / nz].  The
+// instance table is a kernel parameter, so the first global loads (the
+// working plane, the prefetches) depend on nothing loaded before them.
+// Dynamic shared memory (1024-byte aligned for the swizzle): staged Boltzmann
+// plane and history plane (32 KB each), then the padded exchange/transpose
+// plane (36.9 KB); 101 KB, two CTAs per SM.
+// NZ: nz known at compile time (64), or 0 to read it from the table.
+template <int NZ>
+__global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ Mix64Table T,
+                                                        const float2 *__restrict__ tw_g, int n) {
+  extern __shared__ __align__(16) unsigned char dsm_raw[];
+  float2 *Es = reinterpret_cast<float2 *>(dsm_raw + ((1024 - (smem_u32(dsm_raw) & 1023)) & 1023));
+  float2 *Hs = Es + 4096;
+  float2 *buf = Hs + 4096;
+  __shared__ Plane64Shared S;
+  __shared__ __align__(8) uint64_t s_bar;
+  const int nz = NZ ? NZ : T.nz;
+  const int ii = blockIdx.x / nz;
+  const int zz = blockIdx.x - ii * nz;
+  if (n >= T.inst[ii].N) return;
+  if (threadIdx.x == 0) mbar_init(&s_bar, 1);
+  if (threadIdx.x < 64) S.tw[threadIdx.x] = tw_g[threadIdx.x];
+  plane64_body<NZ, true>(T, ii, zz, n, Es, Hs, buf, S, &s_bar, 0);
 }
 
 // z pass for nz = 64 (mode 3 of the generic column pass): tile of TX x columns
@@ -316,21 +346,18 @@ __global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ 
 // 1 - (1 - a)(1 - b) = a + b - a b, applied twice: every term is positive, so
 // h keeps its relative accuracy where it is small.  The pass moves only the
 // propagator itself.
+// One z-pass tile: TX columns x0 .. x0 + TX - 1 at row y of the array a, all
+// 64 z, 8 * TX threads; tw (64 twiddles) and buf (64 * TX float2) in shared
+// memory, the twiddles ready on entry (ordered by the block barrier after
+// the loads).
 template <int TX>
-__global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__ jobs,
-                                                      const float2 *__restrict__ tw_g, int nx, int ny, float s_hi,
-                                                      float s_lo) {
-  __shared__ __align__(16) float2 buf[64 * TX];
-  __shared__ float2 tw[64];
-  const ColJob jb = jobs[blockIdx.x];
+__device__ __forceinline__ void col64_body(float2 *a, const float *ht, int x0, int y, int nx, int ny,
+                                           const float2 *tw, float2 *buf, float s_hi, float s_lo) {
   const int tid = threadIdx.x;
   const int col = tid % TX, t = tid / TX;
-  if (tid < 64) tw[tid] = tw_g[tid];
   const long long plane = (long long)nx * ny;
-  const long long base = (long long)jb.y * nx + jb.x0 + col;
-  float2 *a = reinterpret_cast<float2 *>(jb.ptr);
-  const float *ht = reinterpret_cast<const float *>(jb.kern);
-  const float hx = ht[jb.x0 + col], hy = ht[nx + jb.y];
+  const long long base = (long long)y * nx + x0 + col;
+  const float hx = ht[x0 + col], hy = ht[nx + y];
   const float hxy = fmaf(-hx, hy, hx + hy);
   float2 v[8];
 #pragma unroll
@@ -344,12 +371,24 @@ __global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__
     const float hv = fmaf(-hxy, hz, hxy + hz);
     float2 u = make_float2(fmaf(v[d].x, s_hi, v[d].x * s_lo), fmaf(v[d].y, s_hi, v[d].y * s_lo));
     u = make_float2(fmaf(-hv, u.x, u.x), fmaf(-hv, u.y, u.y));
-    if (kz == 0 && jb.y == 0 && jb.x0 + col == 0) u = make_float2(0.f, 0.f);
+    if (kz == 0 && y == 0 && x0 + col == 0) u = make_float2(0.f, 0.f);
     v[d] = u;
   }
   fft64_group<+1, false>(v, t, buf + col, 8 * TX, TX, tw);
 #pragma unroll
   for (int j = 0; j < 8; j++) a[(t + 8 * j) * plane + base] = v[j];
+}
+
+template <int TX>
+__global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__ jobs,
+                                                      const float2 *__restrict__ tw_g, int nx, int ny, float s_hi,
+                                                      float s_lo) {
+  __shared__ __align__(16) float2 buf[64 * TX];
+  __shared__ float2 tw[64];
+  const ColJob jb = jobs[blockIdx.x];
+  if (threadIdx.x < 64) tw[threadIdx.x] = tw_g[threadIdx.x];
+  col64_body<TX>(reinterpret_cast<float2 *>(jb.ptr), reinterpret_cast<const float *>(jb.kern), jb.x0, jb.y, nx, ny,
+                 tw, buf, s_hi, s_lo);
 }
 
 // z pass for nz = 128, same contract as k_mix_col64: 8 threads per column,
@@ -440,6 +479,246 @@ __global__ void __launch_bounds__(8 * TX) k_mix_col128(const ColJob *__restrict_
   fft128_group<+1>(v, t, buf + col, 16 * TX, TX, tw);
 #pragma unroll
   for (int j = 0; j < 16; j++) a[(t + 8 * j) * plane + base] = v[j];
+}
+
+// ---------------------------------------------------------------------------
+// The whole sweep in one persistent launch
+// ---------------------------------------------------------------------------
+// k_mix_sweep64 runs every step of the propagator sweep of a batch of
+// 64 x 64 x 64 instances (the recurrence of code/diblock_discrete.cpp:31-85,
+// q and qdag at once) as one launch.  Its CTAs (as many as are resident at
+// once, launched cooperatively so that all of them are) take tasks in a fixed
+// order from an atomic counter:
+//   step n = 0:      plane tasks P(0, i, z)            for every active i, z
+//   step n >= 1:     z tasks P'(n, i, y), then P(n, i, z)
+// where P(n, i, z) is the plane pass of plane z (plane64_body) and Z(n, i, y)
+// the z pass of row y, all 64 columns (col64_body with 64 columns).  Active
+// instances at step n are those with N > n, a prefix of the job order.
+// Dependencies, per instance, carried by two counters of finished tasks:
+//   Z(n, i, .) needs every P(n - 1, i, .)        (plane tasks done >= 64 n)
+//   P(n, i, .) needs every Z(n, i, .)            (z tasks done >= 64 n)
+//   and, on a paired step, the plane tasks of step m2 = N - 1 - n, which
+//   wrote the stored partner plane             (plane tasks done >= 64 (m2 + 1))
+// A task depends only on tasks earlier in the order, and every CTA is
+// resident, so the task with the smallest unfinished index can always run:
+// the sweep cannot deadlock.  A finished task is published by its thread 0
+// after a block barrier with a release (fence + atomic add); a waiting task's
+// thread 0 acquires the counter before the block barrier that lets its
+// threads read.  A plane task stages its Boltzmann plane (constant during the
+// sweep) and partner plane by TMA as soon as the partner's step is published,
+// before it waits for the z pass of its own step, so the copies overlap that
+// wait.  Every wait is bounded (err[2] polls, kSpinPolls by default): one
+// that runs out sets the error word to 2 and raises the abort flag, which
+// every other waiting CTA checks, so the launch always ends; the host reports
+// SCFT_ERR_CUDA and the sweep's results are invalid.
+namespace {
+
+enum { kPlaneTask = 0, kZTask = 1 };
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];\n" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+// Orders this thread's (acquired) view of global memory before its later
+// bulk-copy (async proxy) reads.
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;\n" ::: "memory");
+}
+
+// Thread 0 of a CTA: waits until *cnt >= target.  False when the wait ran
+// out (it then records the timeout) or another CTA has aborted the sweep.
+// On success a GPU-scope fence follows the acquiring load (as after a grid
+// barrier), so that the CTA's threads, ordered after thread 0 by a block
+// barrier, read what the producing tasks wrote.
+__device__ bool wait_count(const unsigned *cnt, unsigned target, unsigned *abort_flag, int *err) {
+  const int polls = err[2];  // kSpinPolls unless lowered with scft_set_wait_limit
+  for (int k = 0; k < polls; k++) {
+    if (ld_acquire(cnt) >= target) {
+      __threadfence();
+      return true;
+    }
+    if ((k & 63) == 63 && ld_acquire(abort_flag)) return false;
+    __nanosleep(64);
+  }
+  atomicExch(err, 2);
+  atomicExch(abort_flag, 1u);
+  return false;
+}
+
+// Task t of the order above -> (kind, step n, instance ii, plane or row).
+__device__ __forceinline__ void sweep64_decode(const Sweep64Table &T, unsigned t, int &kind, int &n, int &ii,
+                                               int &row) {
+  unsigned base = 0;
+  int s0 = 0;
+  for (int a = T.ninst; a >= 1; a--) {
+    const int s1 = T.m.inst[a - 1].N;  // steps s0 .. s1 - 1 have `a` active instances
+    if (s1 <= s0) continue;
+    const unsigned per = 128u * (unsigned)a;  // tasks of a step n >= 1
+    const unsigned seg = (s0 == 0 ? 64u * a + per * (unsigned)(s1 - 1) : per * (unsigned)(s1 - s0));
+    if (t < base + seg) {
+      unsigned r = t - base;
+      if (s0 == 0 && r < 64u * a) {
+        kind = kPlaneTask;
+        n = 0;
+      } else {
+        if (s0 == 0) {
+          r -= 64u * a;
+          n = 1 + (int)(r / per);
+        } else {
+          n = s0 + (int)(r / per);
+        }
+        r %= per;
+        kind = r < 64u * a ? kZTask : kPlaneTask;
+        if (kind == kPlaneTask) r -= 64u * a;
+      }
+      ii = (int)(r >> 6);
+      row = (int)(r & 63);
+      return;
+    }
+    base += seg;
+    s0 = s1;
+  }
+  kind = -1;  // past the end (not reached: t < total)
+  n = ii = row = 0;
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(512, 2) k_mix_sweep64(const __grid_constant__ Sweep64Table T,
+                                                        const float2 *__restrict__ tw_g) {
+  extern __shared__ __align__(16) unsigned char dsm_raw[];
+  // Es, Hs: staged planes; then buf: padded plane (plane tasks) or 64 x 64
+  // z-pass tile (z tasks); formed where used, to keep registers free
+#define SWEEP64_ES reinterpret_cast<float2 *>(dsm_raw + ((1024 - (smem_u32(dsm_raw) & 1023)) & 1023))
+  __shared__ Plane64Shared S;
+  __shared__ __align__(8) uint64_t s_bar;
+  __shared__ unsigned s_task;
+  __shared__ int s_go;
+  if (threadIdx.x == 0) mbar_init(&s_bar, 1);
+  if (threadIdx.x < 64) S.tw[threadIdx.x] = tw_g[threadIdx.x];
+  __syncthreads();
+  uint32_t parity = 0;
+  for (;;) {
+    if (threadIdx.x == 0) s_task = atomicAdd(T.ctr, 1u);
+    __syncthreads();
+    const unsigned t = s_task;
+    if (t >= T.total) break;
+    int kind, n, ii, row;
+    sweep64_decode(T, t, kind, n, ii, row);
+    if (kind < 0) break;  // not reached: every t < total decodes
+    if (kind == kPlaneTask) {
+      if (threadIdx.x == 0) {
+        unsigned *abort_flag = T.ctr + 1, *done_p = T.ctr + 2, *done_z = T.ctr + 2 + T.ninst;
+        float2 *Es = SWEEP64_ES;
+        const MixInst &P = T.m.inst[ii];
+        const int m2 = P.N - 1 - n;
+        bool ok = true, issued = false;
+        if (m2 < n) ok = wait_count(done_p + ii, 64u * (unsigned)(m2 + 1), abort_flag, T.m.err);
+        if (ok) {
+          fence_proxy_async_global();
+          plane64_stage(T.m, ii, row, 64, n, Es, Es + 4096, &s_bar);
+          issued = true;
+        }
+        if (ok && n > 0) ok = wait_count(done_z + ii, 64u * (unsigned)n, abort_flag, T.m.err);
+        if (!ok && issued) mbar_wait(&s_bar, parity, kWaitPolls);  // the copies land before the CTA leaves
+        s_go = ok;
+      }
+      __syncthreads();
+      if (!s_go) break;
+      {
+        float2 *Es = SWEEP64_ES;
+        plane64_body<64, false>(T.m, ii, row, n, Es, Es + 4096, Es + 8192, S, &s_bar, parity);
+      }
+      parity ^= 1u;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(T.ctr + 2 + ii, 1u);
+      }
+    } else {
+      if (threadIdx.x == 0) s_go = wait_count(T.ctr + 2 + ii, 64u * (unsigned)n, T.ctr + 1, T.m.err);
+      __syncthreads();
+      if (!s_go) break;
+      col64_body<64>(T.m.inst[ii].work, T.ht[ii], 0, row, 64, 64, S.tw, SWEEP64_ES + 8192, T.s_hi, T.s_lo);
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(T.ctr + 2 + T.ninst + ii, 1u);
+      }
+    }
+  }
+#undef SWEEP64_ES
+}
+
+static int sweep64_smem() { return 1024 + 2 * 4096 * (int)sizeof(float2) + kPlanePad * (int)sizeof(float2); }
+
+cudaError_t sweep64_capacity(int *ctas) {
+  const int smem = sweep64_smem();
+  cudaError_t e = cudaFuncSetAttribute(k_mix_sweep64, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(k_mix_sweep64, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_mix_sweep64, 512, smem);
+  if (e != cudaSuccess) return e;
+  *ctas = per_sm * sms;
+  return per_sm < 1 ? cudaErrorInvalidConfiguration : cudaSuccess;
+}
+
+cudaError_t launch_mix_sweep64(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH,
+                               const float *const *ht, int ninst, const void *tw64, unsigned *ctr, int *err,
+                               int max_ctas, cudaStream_t st) {
+  if (ninst <= 0) return cudaSuccess;
+  if (ninst > kMix64MaxInst) return cudaErrorInvalidValue;
+  const int smem = sweep64_smem();
+  static_assert(64 * 64 * (int)sizeof(float2) <= kPlanePad * (int)sizeof(float2), "z tile fits the plane buffer");
+  int capacity = 0;
+  cudaError_t e = sweep64_capacity(&capacity);
+  if (e != cudaSuccess) return e;
+  Sweep64Table T;
+  memset(&T, 0, sizeof T);
+  unsigned total = 0;
+  for (int k = 0; k < ninst; k++) {
+    if (insts[k].N < 1 || (k > 0 && insts[k].N > insts[k - 1].N)) return cudaErrorInvalidValue;  // job order
+    T.m.inst[k] = insts[k];
+    T.m.tmE[k] = tmE[k];
+    T.m.tmH[k] = tmH[k];
+    T.ht[k] = ht[k];
+    total += 64u + 128u * (unsigned)(insts[k].N - 1);
+  }
+  T.m.err = err;
+  T.m.nz = 64;
+  T.ctr = ctr;
+  T.ninst = ninst;
+  T.total = total;
+  const double sc = 1.0 / (64.0 * 64.0 * 64.0);
+  T.s_hi = (float)sc;
+  T.s_lo = (float)(sc - (double)T.s_hi);
+  // at most 64 tasks of one instance are ready at a time
+  int grid = capacity;
+  const int useful = 128 * ninst;
+  if (grid > useful) grid = useful;
+  if (max_ctas > 0 && grid > max_ctas) grid = max_ctas;
+  e = cudaMemsetAsync(ctr, 0, sizeof(unsigned) * (size_t)sweep64_counters(ninst), st);
+  if (e != cudaSuccess) return e;
+  cudaLaunchConfig_t cfg;
+  memset(&cfg, 0, sizeof cfg);
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(512);
+  cfg.dynamicSmemBytes = (size_t)smem;
+  cfg.stream = st;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  e = cudaLaunchKernelEx(&cfg, k_mix_sweep64, T, reinterpret_cast<const float2 *>(tw64));
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
 }
 
 cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,

@@ -38,6 +38,29 @@ struct Mix64Table {
   int *err;                        // set to 1 when an mbarrier wait runs out
   int nz;                          // z planes per instance (64 x 64 xy planes)
 };
+// The whole mixed sweep of a batch of 64 x 64 x 64 instances in one
+// persistent launch (k_mix_sweep64): the kernel parameter adds to the plane
+// pass's table each instance's per-axis h table of the z pass and the task
+// counters.  Instances in job order (N non-increasing), at most
+// kMix64MaxInst.
+struct Sweep64Table {
+  Mix64Table m;
+  const float *ht[kMix64MaxInst];  // [hx | hy | hz] of each instance (z pass)
+  unsigned *ctr;   // [0] next task, [1] abort flag, [2 + i] plane tasks done and [2 + ninst + i] z tasks done of instance i
+  int ninst;
+  unsigned total;  // tasks of the sweep
+  float s_hi, s_lo;  // 1/M as a two-float pair
+};
+// Counters needed by launch_mix_sweep64 for ninst instances (unsigned ints).
+inline int sweep64_counters(int ninst) { return 2 + 2 * ninst; }
+// CTAs of k_mix_sweep64 resident at once on the current device.
+cudaError_t sweep64_capacity(int *ctas);
+// insts, tmE, tmH, ht: host arrays of the instances in job order; ctr: device
+// array of sweep64_counters(ninst) unsigned ints (cleared by the launch);
+// max_ctas: cap on the grid (0: as many CTAs as are resident at once)
+cudaError_t launch_mix_sweep64(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH,
+                               const float *const *ht, int ninst, const void *tw64, unsigned *ctr, int *err,
+                               int max_ctas, cudaStream_t st);
 // insts, tmE, tmH: host arrays of the active instances in job order (nz CTAs each)
 cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
                                int nz, const void *tw64, int n, int *err, cudaStream_t st);

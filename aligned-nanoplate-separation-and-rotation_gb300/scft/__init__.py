@@ -27,7 +27,8 @@ EXPORTS = ("scft_last_error", "scft_version", "scft_create", "scft_destroy", "sc
            "scft_calc_H", "scft_grad_geom", "scft_get_density", "scft_get_plate_density", "scft_get_smeared", "scft_diblock_density",
            "scft_homopolymer_density", "scft_fft3d", "scft_sync", "scft_get_stream", "scft_launch_count",
            "scft_profile_step", "scft_diblock_density_noalloc", "scft_set_sweep_groups", "scft_autotune",
-           "scft_set_fields_all", "scft_set_wait_limit", "scft_fp64_fma_rate")
+           "scft_set_fields_all", "scft_set_wait_limit", "scft_fp64_fma_rate",
+           "scft_set_persistent", "scft_get_schedule", "scft_profile_sweep")
 
 
 class ScftError(RuntimeError):
@@ -105,6 +106,9 @@ def load(path: str | None = None):
     lib.scft_set_sweep_groups.argtypes = [vp, ctypes.c_int, ctypes.c_int]
     lib.scft_set_wait_limit.argtypes = [vp, ctypes.c_int]
     lib.scft_fp64_fma_rate.argtypes = [ctypes.c_int, dp]
+    lib.scft_set_persistent.argtypes = [vp, ctypes.c_int]
+    lib.scft_profile_sweep.argtypes = [vp, ctypes.c_int, dp, dp]
+    lib.scft_get_schedule.argtypes = [vp] + [ctypes.POINTER(ctypes.c_int)] * 4
     lib.scft_set_fields_all.argtypes = [vp, ctypes.POINTER(ctypes.c_void_p)]
     ip = ctypes.POINTER(ctypes.c_int)
     lib.scft_autotune.argtypes = [vp, ctypes.c_int, ip, ip, ip, dp]
@@ -272,11 +276,19 @@ class Context:
     def set_wait_limit(self, polls: int):
         _check(load().scft_set_wait_limit(self._h, int(polls)))
 
+    def set_persistent(self, on: bool):
+        _check(load().scft_set_persistent(self._h, int(bool(on))))
+
+    def schedule(self) -> dict:
+        v = [ctypes.c_int() for _ in range(4)]
+        _check(load().scft_get_schedule(self._h, *[ctypes.byref(x) for x in v]))
+        return {"groups": v[0].value, "phases": v[1].value, "col_tile": v[2].value, "persistent": bool(v[3].value)}
+
     def autotune(self, reps=3) -> dict:
         g, ph, t, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
         _check(load().scft_autotune(self._h, reps, ctypes.byref(g), ctypes.byref(ph), ctypes.byref(t),
                                     ctypes.byref(ms)))
-        return {"groups": g.value, "phases": ph.value, "col_tile": t.value, "ms_per_sweep": ms.value}
+        return dict(self.schedule(), ms_per_sweep=ms.value)
 
     def stream(self) -> int:
         h = ctypes.c_void_p()
@@ -292,6 +304,11 @@ class Context:
         v = [ctypes.c_double() for _ in range(4)]
         _check(load().scft_profile_step(self._h, int(reps), *[ctypes.byref(x) for x in v]))
         return {"ms_plane": v[0].value, "bytes_plane": v[1].value, "ms_col": v[2].value, "bytes_col": v[3].value}
+
+    def profile_sweep(self, reps=5) -> dict:
+        ms, by = ctypes.c_double(), ctypes.c_double()
+        _check(load().scft_profile_sweep(self._h, int(reps), ctypes.byref(ms), ctypes.byref(by)))
+        return {"ms_sweep": ms.value, "bytes_sweep": by.value}
 
     def set_fields_all_raw(self, ptrs):
         """scft_set_fields_all from device-visible host pointers (one per instance)."""

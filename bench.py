@@ -315,6 +315,8 @@ def main():
                     help="warm-up + timed iterations only (for ncu launch lists)")
     ap.add_argument("--no-plain", action="store_true", help="skip the plain FP64 comparison run")
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch schedule")
+    ap.add_argument("--persistent", choices=["auto", "on", "off"], default="auto",
+                    help="persistent sweep of 64^3 groups: autotuned (auto) or fixed")
     ap.add_argument("--sweep-groups", type=int, default=0, help="fixed number of sweep groups (0: autotune)")
     ap.add_argument("--sweep-phases", type=int, default=1, help="sequential phases with --sweep-groups")
     ap.add_argument("--plain-max", type=int, default=None,
@@ -388,10 +390,13 @@ def main():
     ctx.calc_poly_density()
     schedule = None
     if form == "mixed":
-        if args.sweep_groups > 0:
-            ctx.set_sweep_groups(args.sweep_groups, args.sweep_phases)
-            schedule = {"groups": args.sweep_groups, "phases": args.sweep_phases, "tuned": False}
-        elif not args.no_autotune:
+        if args.sweep_groups > 0 or args.no_autotune or args.persistent != "auto":
+            if args.sweep_groups > 0:
+                ctx.set_sweep_groups(args.sweep_groups, args.sweep_phases)
+            if args.persistent != "auto":
+                ctx.set_persistent(args.persistent == "on")
+            schedule = dict(ctx.schedule(), tuned=False)
+        else:
             schedule = dict(ctx.autotune(3), tuned=True)
     config["schedule"] = schedule
     stream = torch.cuda.ExternalStream(ctx.stream())
@@ -534,22 +539,46 @@ def main():
                          f"separate context); drho = max |rho32 - rho64| / max |rho64| over rho_A, rho_B"}
 
     # ---- dominant kernel, isolated (after the timed regions)
+    hbm, peak_kind = peaks()
+    sched = ctx.schedule() if form == "mixed" else {}
+    sweep_roof = None
+    if form == "mixed":
+        sw = ctx.profile_sweep(5)
+        a_sw = sw["bytes_sweep"] / (sw["ms_sweep"] / 1e3) / 1e9
+        sweep_roof = {"ms_per_sweep": sw["ms_sweep"], "algorithmic_bytes_per_sweep": sw["bytes_sweep"],
+                      "achieved": a_sw, "frac": a_sw / hbm,
+                      "note": "whole FP32 sweep of the batch alone (no field work), current schedule"}
     prof = ctx.profile_step(20)
     nz0 = params[0].Nx[2]
     xy64 = all(p.Nx[0] == 64 and p.Nx[1] == 64 and p.Nx[2] == nz0 for p in params)
     col_fast = {64: "k_mix_col64", 128: "k_mix_col128"}.get(nz0) if xy64 else None
     kernel_names = {"mixed": ("k_mix_plane64" if xy64 else "k_mix_prop_plane", col_fast or "k_col_fft<float>"),
                     "plain": ("k_prop_plane_f64", "k_col_fft<double> (bond kernel)")}
-    hbm, peak_kind = peaks()
     dom = "plane" if prof["ms_plane"] >= prof["ms_col"] else "col"
     ms_k = prof["ms_" + dom]
     by = prof["bytes_" + dom]
     achieved = by / (ms_k / 1e3) / 1e9
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                "traffic": NCU_TRAFFIC.get((args.workload, form)) if dom == "plane" else None,
-                "kernel": kernel_names[form][0 if dom == "plane" else 1],
-                "peak_kind": peak_kind, "ms_per_launch": ms_k, "algorithmic_bytes_per_launch": by,
+    per_step = {"kernel": kernel_names[form][0 if dom == "plane" else 1], "ms_per_launch": ms_k,
+                "algorithmic_bytes_per_launch": by, "achieved": achieved, "frac": achieved / hbm,
+                "other_kernel": kernel_names[form][1 if dom == "plane" else 0],
                 "other_kernel_ms_per_launch": prof["ms_col" if dom == "plane" else "ms_plane"]}
+    if sched.get("persistent"):
+        # the sweep is one launch of k_mix_sweep64 (per group): that launch is the dominant kernel
+        roofline = {"bound": "hbm", "achieved": sweep_roof["achieved"], "peak": hbm, "unit": "GB/s",
+                    "frac": sweep_roof["frac"], "traffic": NCU_TRAFFIC.get((args.workload, "sweep64")),
+                    "kernel": "k_mix_sweep64", "peak_kind": peak_kind,
+                    "ms_per_launch": sweep_roof["ms_per_sweep"] / max(1, sched.get("groups", 1)),
+                    "algorithmic_bytes_per_launch": sweep_roof["algorithmic_bytes_per_sweep"] /
+                    max(1, sched.get("groups", 1)),
+                    "per_step_kernels_alone": per_step}
+    else:
+        roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                    "traffic": NCU_TRAFFIC.get((args.workload, form)) if dom == "plane" else None,
+                    "kernel": per_step["kernel"], "peak_kind": peak_kind, "ms_per_launch": ms_k,
+                    "algorithmic_bytes_per_launch": by,
+                    "other_kernel_ms_per_launch": per_step["other_kernel_ms_per_launch"]}
+    if sweep_roof is not None:
+        roofline["sweep"] = sweep_roof
     ctx.close()
 
     cpu = None

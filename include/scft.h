@@ -247,19 +247,38 @@ int scft_set_sweep_groups(scft_ctx *ctx, int groups, int phases);
 int scft_fp64_fma_rate(int reps, double *gflops);
 
 /* Diagnostic (no counterpart in the reference, whose loops have no waits):
- * the number of polls the first bounded mbarrier wait of each mixed
- * plane-pass CTA makes before it records a timeout in the context's error
- * word (default 4194304).  A CTA whose wait ran out still waits, bounded, for
- * its copies to land, so its results are complete and the context stays
- * usable; the next scft_calc_poly_density / scft_update_1s returns
- * SCFT_ERR_CUDA ("a TMA wait ... ran out").  polls = 0 makes every such wait
- * run out at once, which is how a test sees that path without a fault. */
+ * the number of polls a bounded wait makes before it records a timeout in
+ * the context's error word: the first mbarrier wait of each mixed plane-pass
+ * CTA (default 4194304) and each dependency wait of the persistent sweep
+ * (default 16777216); polls < 0 restores the defaults.  A plane-pass CTA
+ * whose mbarrier wait ran out still waits, bounded, for its copies to land,
+ * so its results are complete and the context stays usable; the call returns
+ * SCFT_ERR_CUDA ("a TMA wait ... ran out").  A dependency wait that runs out
+ * stops the persistent sweep (every CTA leaves within its own bounded wait):
+ * the call returns SCFT_ERR_CUDA ("a dependency wait ... ran out"), its
+ * results are invalid, and the context is usable again once the fields are
+ * set anew.  polls = 0 makes every such wait run out at once, which is how a
+ * test sees both paths without a fault. */
 int scft_set_wait_limit(scft_ctx *ctx, int polls);
+
+/* Persistent sweep (no counterpart in the reference): on = 1 runs the whole
+ * propagator sweep of each group of 64 x 64 x 64 instances as one persistent
+ * launch, whose CTAs take plane and z-column tasks of every step from a
+ * counter and wait (bounded) on per-instance task counts, instead of two
+ * launches per step.  Other grids keep the per-step launches.  Results are
+ * bit-identical either way. */
+int scft_set_persistent(scft_ctx *ctx, int on);
+
+/* The current launch schedule of the mixed sweep (any pointer may be NULL):
+ * groups, phases, z-pass columns per CTA of the 64-point kernels (0 where it
+ * does not apply) and whether the sweep is persistent. */
+int scft_get_schedule(scft_ctx *ctx, int *groups, int *phases, int *col_tile, int *persistent);
 
 /* Autotuner: times reps full propagator sweeps of the batch for every
  * candidate schedule (1-4 phases x 1-6 or 8 groups; for 64-point grids also
- * 8, 16 or 32 z-pass columns per CTA) with CUDA events and keeps the
- * fastest.  Reports the choice (col_tile 0 where it does not apply) and its
+ * 8, 16 or 32 z-pass columns per CTA, and the persistent sweep with 1-3
+ * groups x 1-2 phases) with CUDA events and keeps the fastest
+ * (scft_get_schedule reads the choice).  Reports the choice (col_tile 0 where it does not apply) and its
  * time per sweep.  FP64 contexts have a single schedule (1 group, 1 phase). */
 int scft_autotune(scft_ctx *ctx, int reps, int *groups, int *phases, int *col_tile, double *ms_per_sweep);
 
@@ -274,6 +293,16 @@ int scft_autotune(scft_ctx *ctx, int reps, int *groups, int *phases, int *col_ti
  * buffers in an undefined state; call scft_calc_poly_density afterwards. */
 int scft_profile_step(scft_ctx *ctx, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
                       double *bytes_col);
+
+/* Times `reps` FP32 propagator sweeps of the whole batch (mixed form) with
+ * the current schedule, alone (no field work), on the context stream with
+ * CUDA events; writes the mean milliseconds per sweep and the algorithmic
+ * bytes of one sweep (per point and step: the z pass's 16 B, the plane
+ * pass's working plane in and out, Boltzmann pair, history out or stored
+ * partner in, FP32 accumulators read and written).  With the persistent
+ * sweep this is one launch per group.  Leaves the densities invalid; call
+ * scft_calc_poly_density afterwards. */
+int scft_profile_sweep(scft_ctx *ctx, int reps, double *ms, double *bytes);
 
 #ifdef __cplusplus
 }

@@ -70,14 +70,18 @@ def _sweep_case(scft):
 
 
 def test_mbarrier_wait_that_runs_out_returns_err_cuda(scft):
+    """With the per-step launches (the persistent sweep's own waits are in
+    tests/test_gpu_persistent.py)."""
     ps, fields = _sweep_case(scft)
     with scft.Context(ps) as ref:
+        ref.set_persistent(False)
         for k in range(2):
             ref.set_fields(k, fields[k])
         ref.calc_poly_density()
         ref.update_1s(3)
         H_ref = ref.calc_H()[:, 0].copy()
     with scft.Context(ps) as ctx:
+        ctx.set_persistent(False)
         for k in range(2):
             ctx.set_fields(k, fields[k])
         ctx.calc_poly_density()
@@ -87,7 +91,7 @@ def test_mbarrier_wait_that_runs_out_returns_err_cuda(scft):
             ctx.update_1s(1)
         assert e.value.code == scft.ERR_CUDA
         assert "ran out" in str(e.value)
-        ctx.set_wait_limit(1 << 22)
+        ctx.set_wait_limit(-1)
         ctx.update_1s(1)
         H = ctx.calc_H()[:, 0]
     # every CTA finished its work after the timeout: the state is the same
