@@ -2,10 +2,11 @@
 //
 // Set-up follows code/initialize.cpp:45-412 (grid, smearing kernel hhat, plate
 // density and graft map, volumes and chain counts, Debye functions, bond
-// kernel).  Tables that the reference computes point by point from get_k()
-// (hhat, poly_bond_fft, gaa, gab, gbb, gc) are computed here on the host in
-// FP64 with the same expressions; the plate profile and its spectral gradient
-// are computed on the device (they need FFTs).
+// kernel).  Every per-point table is built on the device: the tables that the
+// reference computes point by point from get_k() (hhat, poly_bond_fft, gaa,
+// gab, gbb, gc) and the mixed form's update coefficients in
+// kernels_setup.cu, with the same FP64 expressions; the plate profile and its
+// spectral gradient with the library's FFTs.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -14,6 +15,7 @@
 #include <stdexcept>
 
 #include "context.h"
+#include "kernels_setup.h"
 #include "fft_core.cuh"
 #include "prop_launch.h"
 #include "grad.h"
@@ -71,28 +73,6 @@ static LaunchShape choose_shape(int E, size_t elem, size_t extra) {
     s.smem = (int)extra;
   }
   return s;
-}
-
-// ---------------------------------------------------------------------------
-// host-side tables (code/array_utils.cpp:239-272, code/initialize.cpp:97-102,
-// :401-404, code/calc_debye.cpp:5-68)
-// ---------------------------------------------------------------------------
-static double get_k(const Instance &I, long long id, double k[3]) {
-  const int *Nx = I.p.Nx;
-  const double *L = I.p.L;
-  int n[3];
-  n[2] = (int)(id / Nx[1] / Nx[0]);
-  n[1] = (int)(id / Nx[0] - (long long)n[2] * Nx[1]);
-  n[0] = (int)(id - ((long long)n[1] + (long long)n[2] * Nx[1]) * Nx[0]);
-  double kmag = 0.0;
-  for (int d = 0; d < 3; d++) {
-    if (double(n[d]) < double(Nx[d]) / 2.)
-      k[d] = 2 * kPI * double(n[d]) / L[d];
-    else
-      k[d] = 2 * kPI * double(n[d] - Nx[d]) / L[d];
-  }
-  for (int d = 0; d < 3; d++) kmag += k[d] * k[d];
-  return kmag;
 }
 
 template <class T> static T *dalloc(scft_ctx *c, size_t n) {
@@ -363,15 +343,6 @@ void validate(const scft_params &p) {
   if (p.Nx[2] > 768) throw ScftError(SCFT_ERR_UNSUPPORTED, "Nx[2] above 768 is not supported by the z pass");
 }
 
-// alpha, beta of w <- alpha w - beta F for each field and sign branch of
-// code/1s_update.cpp:58-329: semi-implicit fields (lam_pl with A and B)
-// alpha = (1 + lam B)/(1 + lam A), beta = lam/(1 + lam A); explicit fields
-// (lam_mi) alpha = 1/(1 + lam 2 rho0/chi), beta = lam/(1 + lam 2 rho0/chi).
-// phiD and phiG are those of the set-up; they are final once the plates are
-// built, so this runs again from setup_plates (mix_coefficients_final).
-void mix_coefficients(scft_ctx *c, Instance &I, const std::vector<double> &hh, const std::vector<double> &gaa,
-                      const std::vector<double> &gab, const std::vector<double> &gbb, const std::vector<double> &gc);
-
 void setup_instance(scft_ctx *c, Instance &I, int idx) {
   const scft_params &p = I.p;
   I.N = p.Nda + p.Ndb;
@@ -412,37 +383,30 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
   I.geom = (int)c->geoms.size();
   c->geoms.push_back(g);
 
-  // tables from get_k
-  std::vector<double> hh(M), pb(M), gaa(M), gab(M), gbb(M), gc(M, 0.0);
-  const double a2 = p.a_smear * p.a_smear;
-  const double fD = I.fD, Rg2 = I.Rg2;
-  const double alpha_c = (I.N > 1) ? double(p.Ng - 1) / double(I.N - 1) : 0.0;
-  for (long long i = 0; i < M; i++) {
-    double kv[3];
-    const double k2 = get_k(I, i, kv);
-    hh[i] = exp(-k2 * a2 / 2.0);
-    pb[i] = exp(-k2 / 6.0);
-    const double x = k2 * Rg2;
-    gaa[i] = 2.0 * (exp(-x * fD) + fD * x - 1.0) / x / x;
-    gbb[i] = 2.0 * (exp(-x * (1.0 - fD)) + (1.0 - fD) * x - 1.0) / x / x;
-    gab[i] = (1.0 - exp(-x * fD)) * (1.0 - exp(-x * (1.0 - fD))) / x / x;
-    if (sigma > 0) {
-      const double dm1 = k2 * Rg2 * alpha_c;
-      gc[i] = (dm1 == 0.0) ? 1.0 : 2.0 * (exp(-dm1) + dm1 - 1.0) / dm1 / dm1;
-    }
+  // k-space tables from get_k, built on the device (kernels_setup.cu)
+  I.mixed = (p.precision == SCFT_PREC_MIXED);
+  {
+    SetupTableArgs ta;
+    ta.nx = p.Nx[0];
+    ta.ny = p.Nx[1];
+    ta.nz = p.Nx[2];
+    for (int d = 0; d < 3; d++) ta.L[d] = p.L[d];
+    ta.a2 = p.a_smear * p.a_smear;
+    ta.fD = I.fD;
+    ta.Rg2 = I.Rg2;
+    ta.alpha_c = (I.N > 1) ? double(p.Ng - 1) / double(I.N - 1) : 0.0;
+    ta.graft = sigma > 0;
+    I.hhat = dalloc<double>(c, M);
+    I.pbond = dalloc<double>(c, M);
+    I.gaa = dalloc<double>(c, M);
+    I.gab = dalloc<double>(c, M);
+    I.gbb = dalloc<double>(c, M);
+    I.gc = dalloc<double>(c, M);
+    if (I.mixed) I.h32 = dalloc<float>(c, M);
+    CK(launch_setup_tables(ta, I.hhat, I.pbond, I.gaa, I.gab, I.gbb, I.gc, I.mixed ? I.h32 : nullptr, c->st));
   }
-  gaa[0] = fD * fD;
-  gbb[0] = (1.0 - fD) * (1.0 - fD);
-  gab[0] = fD * (1.0 - fD);
-  I.hhat = dupload(c, hh);
-  I.pbond = dupload(c, pb);
-  I.gaa = dupload(c, gaa);
-  I.gab = dupload(c, gab);
-  I.gbb = dupload(c, gbb);
-  I.gc = dupload(c, gc);
 
   // device arrays
-  I.mixed = (p.precision == SCFT_PREC_MIXED);
   // the seven fields in one allocation, in scft_set_fields' order: one copy per instance
   I.w[0] = dalloc<double2>(c, 7 * (size_t)M);
   for (int f = 1; f < 7; f++) I.w[f] = I.w[0] + (size_t)f * M;
@@ -484,9 +448,6 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
     I.acc32[1] = dalloc<float>(c, M);
     I.part = dalloc<double>(c, (size_t)2 * I.N * g.nz);
     I.K = dalloc<int>(c, (size_t)2 * I.N + 1);
-    std::vector<float> h32(M);
-    for (long long i = 0; i < M; i++) h32[i] = (float)(1.0 - pb[i]);
-    I.h32 = dupload(c, h32);
     // per-axis h_d = 1 - exp(-k_d^2/6) with get_k's branch
     // (code/array_utils.cpp:248-265); g(k) = prod_d (1 - h_d)
     std::vector<float> ht;
@@ -496,8 +457,7 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
                                                             : 2 * kPI * double(nn - p.Nx[d]) / p.L[d];
         ht.push_back((float)(-std::expm1(-k * k / 6.0)));
       }
-    I.htab32 = dupload(c, ht);
-    mix_coefficients(c, I, hh, gaa, gab, gbb, gc);
+    I.htab32 = dupload(c, ht);  // alpha, beta: mix_coefficients_final, once the plates fix phiD, phiG
   }
   I.qpart = dalloc<double2>(c, g.nz);
   I.scal = dalloc<double2>(c, kNumScalars);
@@ -507,101 +467,75 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
   (void)idx;
 }
 
-void mix_coefficients(scft_ctx *c, Instance &I, const std::vector<double> &hh, const std::vector<double> &gaa,
-                      const std::vector<double> &gab, const std::vector<double> &gbb, const std::vector<double> &gc) {
-  (void)c;
-  I.tab_hh = hh;
-  I.tab_gaa = gaa;
-  I.tab_gab = gab;
-  I.tab_gbb = gbb;
-  I.tab_gc = gc;
-}
-
+// alpha, beta of w <- alpha w - beta F for each field and sign branch of
+// code/1s_update.cpp:58-329 (kernels_setup.cu): semi-implicit fields (lam_pl
+// with A and B) alpha = (1 + lam B)/(1 + lam A), beta = lam/(1 + lam A);
+// explicit fields (lam_mi) alpha = 1/(1 + lam 2 rho0/chi), beta = lam/(1 +
+// lam 2 rho0/chi); with the Euler scheme (code/Euler_update.cpp:54-179)
+// alpha = 1 - lam c, beta = lam.  Runs once the plates have fixed phiD, phiG.
 void mix_coefficients_final(scft_ctx *c, Instance &I) {
-  const long long M = I.M;
   const scft_params &p = I.p;
-  const double rho0 = p.rho0, N = I.N, Ng = I.Ng, phiD = I.info.phiD, phiG = I.info.phiG;
+  const double rho0 = p.rho0;
   const double li = p.lam_pl, lr = p.lam_mi;
-  std::vector<double> a(M), b(M);
-  auto semi = [&](int f, auto Afun, double Boff) {
-    for (long long i = 0; i < M; i++) {
-      const double A = Afun(i), B = A - Boff;
-      a[i] = (1.0 + li * B) / (1.0 + li * A);
-      b[i] = li / (1.0 + li * A);
-    }
-    I.alpha[f] = dupload(c, a);
-    I.beta[f] = dupload(c, b);
+  MixCoeffArgs a;
+  memset(&a, 0, sizeof a);
+  a.rho0 = rho0;
+  a.kappa = p.kappa;
+  a.N = I.N;
+  a.Ng = I.Ng;
+  a.phiD = I.info.phiD;
+  a.phiG = I.info.phiG;
+  auto semi = [&](int f, int formula, double cc, double boff) {
+    a.f[f].kind = kCoeffSemi;
+    a.f[f].formula = formula;
+    a.f[f].lam = li;
+    a.f[f].c = cc;
+    a.f[f].boff = boff;
   };
-  auto expl = [&](int f, double chi) {
-    const double d = 1.0 + lr * 2.0 * rho0 / chi;
-    for (long long i = 0; i < M; i++) {
-      a[i] = 1.0 / d;
-      b[i] = lr / d;
-    }
-    I.alpha[f] = dupload(c, a);
-    I.beta[f] = dupload(c, b);
+  auto expl = [&](int f, double cc) {
+    a.f[f].kind = kCoeffExplicit;
+    a.f[f].lam = lr;
+    a.f[f].c = cc;
   };
+  auto eul = [&](int f, double lam, double cc) {
+    a.f[f].kind = kCoeffEuler;
+    a.f[f].lam = lam;
+    a.f[f].c = cc;
+  };
+  const double chis[3] = {I.cab, I.cbc, I.cac};
+  const int negs[3] = {I.neg_ab, I.neg_bc, I.neg_ac};
   if (p.update_scheme == SCFT_UPDATE_EULER) {
-    // explicit step w <- (1 - lam c) w - lam F (code/Euler_update.cpp:54-179)
-    auto eul = [&](int f, double lam, double cc) {
-      for (long long i = 0; i < M; i++) {
-        a[i] = 1.0 - lam * cc;
-        b[i] = lam;
-      }
-      I.alpha[f] = dupload(c, a);
-      I.beta[f] = dupload(c, b);
-    };
     eul(0, li, p.kappa > 0.0 ? rho0 / p.kappa : 0.0);
-    const double chis[3] = {I.cab, I.cbc, I.cac};
     for (int k = 0; k < 3; k++)
       if (chis[k] != 0.0) {
         eul(1 + 2 * k, li, 2.0 * rho0 / chis[k]);
         eul(2 + 2 * k, lr, 2.0 * rho0 / chis[k]);
       }
-    return;
-  }
-  const auto &hh = I.tab_hh, &gaa = I.tab_gaa, &gab = I.tab_gab, &gbb = I.tab_gbb, &gc = I.tab_gc;
-  // w+ (:67-83)
-  semi(0, [&](long long i) {
-    return rho0 / p.kappa + phiD * rho0 * N * hh[i] * hh[i] * (gaa[i] + 2.0 * gab[i] + gbb[i]) +
-           (phiG * Ng * gc[i]) * rho0 * hh[i] * hh[i];
-  }, rho0 / p.kappa);
-  if (I.cab != 0.0) {
-    const double cc = I.cab;
-    if (!I.neg_ab) {
-      semi(1, [&](long long i) { return 2.0 * rho0 / cc + phiD * rho0 * N * hh[i] * hh[i] * (gaa[i] + 2.0 * gab[i] + gbb[i]); },
-           2.0 * rho0 / cc);
-      expl(2, cc);
-    } else {
-      expl(1, cc);
-      semi(2, [&](long long i) { return 2.0 * rho0 / cc + phiD * rho0 * N * hh[i] * hh[i] * (gaa[i] - gbb[i]); },
-           2.0 * rho0 / cc);
+  } else {
+    semi(0, kAPlus, 0.0, rho0 / p.kappa);
+    const int pos[3] = {kAB, kBC, kAC}, neg[3] = {kABNeg, kBCNeg, kACNeg};
+    for (int k = 0; k < 3; k++) {
+      if (chis[k] == 0.0) continue;
+      const double cc = chis[k];
+      if (!negs[k]) {
+        semi(1 + 2 * k, pos[k], cc, 2.0 * rho0 / cc);
+        expl(2 + 2 * k, cc);
+      } else {
+        expl(1 + 2 * k, cc);
+        semi(2 + 2 * k, neg[k], cc, 2.0 * rho0 / cc);
+      }
     }
   }
-  if (I.cbc != 0.0) {
-    const double cc = I.cbc;
-    if (!I.neg_bc) {
-      semi(3, [&](long long i) { return 2.0 * rho0 / cc + phiD * rho0 * N * hh[i] * hh[i] * gbb[i] + phiG * rho0 * Ng * hh[i] * hh[i] * gc[i]; },
-           2.0 * rho0 / cc);
-      expl(4, cc);
-    } else {
-      expl(3, cc);
-      semi(4, [&](long long i) { return 2.0 * rho0 / cc + phiD * rho0 * N * hh[i] * hh[i] * gbb[i] - phiG * Ng * hh[i] * hh[i] * rho0 * gc[i]; },
-           2.0 * rho0 / cc);
+  // tables for the active fields only (a field whose chi is zero has none;
+  // the update skips it)
+  for (int f = 0; f < 7; f++)
+    if (a.f[f].kind != kCoeffNone) {
+      if (!I.alpha[f]) I.alpha[f] = dalloc<double>(c, I.M);
+      if (!I.beta[f]) I.beta[f] = dalloc<double>(c, I.M);
+      a.f[f].alpha = I.alpha[f];
+      a.f[f].beta = I.beta[f];
     }
-  }
-  if (I.cac != 0.0) {
-    const double cc = I.cac;
-    if (!I.neg_ac) {
-      semi(5, [&](long long i) { return 2.0 * rho0 / cc + phiD * rho0 * N * hh[i] * hh[i] * gaa[i] + phiG * Ng * hh[i] * hh[i] * rho0 * gc[i]; },
-           2.0 * rho0 / cc);
-      expl(6, cc);
-    } else {
-      expl(5, cc);
-      semi(6, [&](long long i) { return 2.0 * rho0 / cc + phiD * rho0 * N * hh[i] * hh[i] * gaa[i] - phiG * Ng * hh[i] * hh[i] * rho0 * gc[i]; },
-           2.0 * rho0 / cc);
-    }
-  }
+  CK(launch_mix_coeff(a, I.M, I.hhat, I.gaa, I.gab, I.gbb, I.gc, c->st));
 }
 
 // Plate profile, graft map and chain counts (code/initialize.cpp:139-386).
@@ -713,14 +647,7 @@ void setup_plates(scft_ctx *c, Instance &I) {
     I.gpart = dalloc<double>(c, (size_t)2 * p.Ng * p.Nx[2]);
     I.sm[2] = dalloc<double2>(c, M);
   }
-  if (I.mixed) {
-    mix_coefficients_final(c, I);
-    I.tab_hh.clear();
-    I.tab_gaa.clear();
-    I.tab_gab.clear();
-    I.tab_gbb.clear();
-    I.tab_gc.clear();
-  }
+  if (I.mixed) mix_coefficients_final(c, I);
   CK(cudaStreamSynchronize(c->st));
 }
 

@@ -65,7 +65,6 @@ struct Instance {
   double *shellU = nullptr;  // Lambda * shell profile on A segments (extension), real, or NULL
   float *htab32 = nullptr;  // [hx | hy | hz], h_d = 1 - exp(-k_d^2/6), FP32
   double *alpha[7] = {}, *beta[7] = {};  // tabulated 1S coefficients (mixed form)
-  std::vector<double> tab_hh, tab_gaa, tab_gab, tab_gbb, tab_gc;  // host copies, set-up only
 };
 
 struct DevBuf {
