@@ -276,6 +276,15 @@ int scft_profile_sweep(scft_ctx *c, int reps, double *ms, double *bytes) {
   return SCFT_OK;
 }
 
+int scft_get_fft_plan(scft_ctx *c, int inst, int axis, int *radix, int *nst) {
+  if (int s = check_ctx(c, inst)) return s;
+  if (axis < 0 || axis > 2 || !radix || !nst) return fail(SCFT_ERR_ARG, "axis 0..2 and output pointers needed");
+  const scft::AxisPlan &ap = c->geoms[c->inst[inst].geom].ax[axis];
+  *nst = ap.nst;
+  for (int k = 0; k < scft::kMaxStages; k++) radix[k] = k < ap.nst ? ap.radix[k] : 0;
+  return SCFT_OK;
+}
+
 int scft_get_schedule(scft_ctx *c, int *groups, int *phases, int *col_tile, int *persistent) {
   if (int s = check_ctx(c, 0)) return s;
   if (groups) *groups = c->sweep_streams;

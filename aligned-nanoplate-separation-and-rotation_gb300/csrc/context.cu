@@ -8,9 +8,11 @@
 // kernels_setup.cu, with the same FP64 expressions; the plate profile and its
 // spectral gradient with the library's FFTs.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <stdexcept>
 
@@ -49,6 +51,55 @@ static bool make_axis_plan(int n, AxisPlan &ap) {
   while (m % 3 == 0 && ap.nst < kMaxStages) { ap.radix[ap.nst++] = 3; m /= 3; }
   while (m % 5 == 0 && ap.nst < kMaxStages) { ap.radix[ap.nst++] = 5; m /= 5; }
   return m == 1;
+}
+
+// Stage orders an n-point axis can run with: radices 8, 4, 2, 3, 5 whose
+// product is n, at most one radix-2 stage and kMaxStages stages, every
+// distinct order of each such multiset; the greedy plan (make_axis_plan)
+// first, then by number of stages, at most `cap` plans.  The Stockham stages
+// (fft_core.cuh) take the radices in any order, so each is a valid plan.
+static std::vector<AxisPlan> axis_plan_candidates(int n, int cap) {
+  std::vector<std::vector<int>> sets;
+  std::vector<int> cur;
+  const int rs[5] = {8, 4, 2, 3, 5};
+  // multisets as non-increasing index sequences into rs
+  std::function<void(int, int, int)> rec = [&](int m, int from, int twos) {
+    if (m == 1) {
+      sets.push_back(cur);
+      return;
+    }
+    if ((int)cur.size() >= kMaxStages) return;
+    for (int k = from; k < 5; k++) {
+      const int r = rs[k];
+      if (m % r || (r == 2 && twos >= 1)) continue;
+      cur.push_back(r);
+      rec(m / r, k, twos + (r == 2));
+      cur.pop_back();
+    }
+  };
+  rec(n, 0, 0);
+  std::sort(sets.begin(), sets.end(), [](const std::vector<int> &a, const std::vector<int> &b) {
+    return a.size() < b.size();
+  });
+  std::vector<AxisPlan> out;
+  AxisPlan greedy;
+  if (make_axis_plan(n, greedy)) out.push_back(greedy);
+  for (auto &st : sets) {
+    std::vector<int> perm = st;
+    std::sort(perm.begin(), perm.end());
+    do {
+      AxisPlan ap;
+      ap.n = n;
+      ap.nst = (int)perm.size();
+      for (int i = 0; i < ap.nst; i++) ap.radix[i] = perm[i];
+      bool dup = false;
+      for (auto &o : out)
+        dup = dup || (o.nst == ap.nst && std::equal(o.radix, o.radix + o.nst, ap.radix));
+      if (!dup) out.push_back(ap);
+    } while (std::next_permutation(perm.begin(), perm.end()) && (int)out.size() < cap);
+    if ((int)out.size() >= cap) break;
+  }
+  return out;
 }
 
 static LaunchShape choose_shape(int E, size_t elem, size_t extra) {
@@ -180,18 +231,6 @@ __global__ void k_mul_ik_alias(double2 *a, int nx, int ny, int nz, double Lx, do
     // v * (I*kv) with (I*kv) = (0, kv)
     a[i] = make_double2(v.x * 0.0 - v.y * kv, v.x * kv + v.y * 0.0);
   }
-}
-
-__device__ double2 csqrt_d(double2 z) {
-  const double x = z.x, y = z.y;
-  if (x == 0.0 && y == 0.0) return make_double2(0.0, y);
-  const double r = hypot(x, y);
-  if (x >= 0.0) {
-    const double t = sqrt(0.5 * (r + x));
-    return make_double2(t, y / (2.0 * t));
-  }
-  const double t = sqrt(0.5 * (r - x));
-  return make_double2(fabs(y) / (2.0 * t), copysign(t, y));
 }
 
 // graft map += sqrt(gx^2 + gy^2 + gz^2) (complex), code/initialize.cpp:175-186
@@ -539,6 +578,36 @@ void mix_coefficients_final(scft_ctx *c, Instance &I) {
 }
 
 // Plate profile, graft map and chain counts (code/initialize.cpp:139-386).
+// Plate j of instance I with thickness len and radius rad, as k_plate takes it.
+PlateArgs plate_args_of(const Instance &I, int j, double len, double rad) {
+  const scft_params &p = I.p;
+  PlateArgs a;
+  a.nx = p.Nx[0]; a.ny = p.Nx[1]; a.nz = p.Nx[2];
+  double un = 0.0;
+  for (int d = 0; d < 3; d++) un += p.orient[j][d] * p.orient[j][d];
+  un = sqrt(un);
+  for (int d = 0; d < 3; d++) {
+    a.dx[d] = I.info.dx[d];
+    a.L[d] = p.L[d];
+    a.c[d] = p.center[j][d] * p.L[d];
+    a.u[d] = p.orient[j][d] / un;  // code/read_input.cpp:220-235
+  }
+  a.len = len; a.rad = rad; a.xi = p.xi_nr;
+  a.shape = p.plate_shape;
+  return a;
+}
+
+// Spectral gradient component d of a real-space FP64 array (in place):
+// forward transform, times i k_alias[d] (Nyquist killed), inverse transform
+// (code/array_utils.cpp:181-235, :565-579).
+void spectral_gradient(scft_ctx *c, const Instance &I, double2 *a, int d) {
+  const scft_params &p = I.p;
+  fft3d_arrays(c, I, {a}, -1);
+  k_mul_ik_alias<<<1024, 256, 0, c->st>>>(a, p.Nx[0], p.Nx[1], p.Nx[2], p.L[0], p.L[1], p.L[2], d);
+  CK(cudaGetLastError());
+  fft3d_arrays(c, I, {a}, +1);
+}
+
 void setup_plates(scft_ctx *c, Instance &I) {
   const scft_params &p = I.p;
   const long long M = I.M;
@@ -548,32 +617,14 @@ void setup_plates(scft_ctx *c, Instance &I) {
   double2 *gr[3] = {dalloc<double2>(c, M), dalloc<double2>(c, M), dalloc<double2>(c, M)};
   double2 *scratch = dalloc<double2>(c, kSumBlocks);
   const int blocks = 1024;
-  auto plate_args = [&](int j, double len, double rad) {
-    PlateArgs a;
-    a.nx = p.Nx[0]; a.ny = p.Nx[1]; a.nz = p.Nx[2];
-    double un = 0.0;
-    for (int d = 0; d < 3; d++) un += p.orient[j][d] * p.orient[j][d];
-    un = sqrt(un);
-    for (int d = 0; d < 3; d++) {
-      a.dx[d] = I.info.dx[d];
-      a.L[d] = p.L[d];
-      a.c[d] = p.center[j][d] * p.L[d];
-      a.u[d] = p.orient[j][d] / un;  // code/read_input.cpp:220-235
-    }
-    a.len = len; a.rad = rad; a.xi = p.xi_nr;
-    a.shape = p.plate_shape;
-    return a;
-  };
+  auto plate_args = [&](int j, double len, double rad) { return plate_args_of(I, j, len, rad); };
   // graft map from the 1.05x-enlarged plates (code/initialize.cpp:160-200)
   for (int j = 0; j < p.n_exp_nr; j++) {
     k_plate<<<blocks, 256, 0, c->st>>>(pd, plate_args(j, p.L_nr * 1.05, p.R_nr * 1.05), 0);
     CK(cudaGetLastError());
     for (int d = 0; d < 3; d++) {
       CK(cudaMemcpyAsync(gr[d], pd, sizeof(double2) * M, cudaMemcpyDeviceToDevice, c->st));
-      fft3d_arrays(c, I, {gr[d]}, -1);
-      k_mul_ik_alias<<<blocks, 256, 0, c->st>>>(gr[d], p.Nx[0], p.Nx[1], p.Nx[2], p.L[0], p.L[1], p.L[2], d);
-      CK(cudaGetLastError());
-      fft3d_arrays(c, I, {gr[d]}, +1);
+      spectral_gradient(c, I, gr[d], d);
     }
     k_grad_mag_acc<<<blocks, 256, 0, c->st>>>(I.grafts, gr[0], gr[1], gr[2], M);
     CK(cudaGetLastError());
@@ -1772,11 +1823,58 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
         bpers = pers;
       }
     }
-  cudaEventDestroy(e0);
-  cudaEventDestroy(e1);
   c->col64_tx = bt;
   c->sweep_persistent = bpers;
   ctx_set_sweep_groups(c, bg, bp);
+  // FFT stage orders of the generic transforms (field transforms; plane and
+  // z passes of the generic grids), one axis length at a time with the
+  // others fixed, timed the same way with the chosen schedule
+  std::map<int, int> lens;  // axis length -> points it is applied to
+  for (auto &I : c->inst)
+    for (int d = 0; d < 3; d++) lens[I.p.Nx[d]] += (int)std::min<long long>(I.M, 1 << 30);
+  auto time_builds = [&]() {
+    seq_mix_density(c);
+    CK(cudaEventRecord(e0, c->st));
+    for (int r = 0; r < reps; r++) seq_mix_density(c);
+    CK(cudaEventRecord(e1, c->st));
+    CK(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, e0, e1));
+    return (double)ms / reps;
+  };
+  auto apply = [&](int n, const AxisPlan &ap) {
+    for (auto &g : c->geoms)
+      for (int d = 0; d < 3; d++)
+        if (g.ax[d].n == n) {
+          const int tw = g.ax[d].tw;
+          g.ax[d] = ap;
+          g.ax[d].tw = tw;
+        }
+    CK(cudaMemcpyAsync(c->d_geoms, c->geoms.data(), sizeof(DevGeom) * c->geoms.size(), cudaMemcpyHostToDevice,
+                       c->st));
+  };
+  best = time_builds();
+  for (auto &kv : lens) {
+    const int n = kv.first;
+    const std::vector<AxisPlan> cand = axis_plan_candidates(n, 12);
+    if (cand.size() < 2) continue;
+    AxisPlan keep = cand[0];
+    for (auto &g : c->geoms)
+      for (int d = 0; d < 3; d++)
+        if (g.ax[d].n == n) keep = g.ax[d];
+    for (const AxisPlan &ap : cand) {
+      apply(n, ap);
+      const double ms = time_builds();
+      if (ms < best) {
+        best = ms;
+        keep = ap;
+      }
+    }
+    apply(n, keep);
+  }
+  CK(cudaStreamSynchronize(c->st));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
   if (c->g_update) {
     CK(cudaGraphExecDestroy(c->g_update));
     c->g_update = nullptr;
@@ -2165,6 +2263,89 @@ int error_code(const std::exception &e) {
 namespace scft {
 // dH/d(plate rotation about z) and dH/d(plate centre) at the current fields
 // (kernels_grad.cu): out[8*inst + 4*j + {0, 1, 2, 3}] for plate j.
+// Grafted plates: adds d(-n_exp_nr ng_per_np Re Qga)/dg_k of every plate j to
+// out[4 j + k] at the current fields (kernels_grad.cu gives the terms).
+// Device temporaries (about 12 arrays of the grid) are allocated here and
+// freed before returning.
+static void graft_map_derivative(scft_ctx *c, Instance &I, const GradArgs &g, double *out) {
+  const scft_params &p = I.p;
+  const long long M = I.M;
+  const int nb = 128;
+  const double dV = I.info.dx[0] * I.info.dx[1] * I.info.dx[2];
+  std::vector<void *> tmp;
+  auto get = [&](size_t bytes) {
+    void *q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      throw ScftError(SCFT_ERR_NOMEM, std::string("cudaMalloc failed: ") + cudaGetErrorString(e));
+    }
+    tmp.push_back(q);
+    return q;
+  };
+  auto sums = [&](double *part) {
+    std::vector<double> h(4 * nb);
+    CK(cudaMemcpyAsync(h.data(), part, sizeof(double) * h.size(), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    double s4[4] = {0.0, 0.0, 0.0, 0.0};
+    for (int b = 0; b < nb; b++)
+      for (int k = 0; k < 4; k++) s4[k] += h[4 * b + k];
+    return std::array<cd, 2>{cd(s4[0], s4[1]) * dV, cd(s4[2], s4[3]) * dV};
+  };
+  try {
+    const size_t ab = sizeof(double2) * (size_t)M;
+    double2 *L = static_cast<double2 *>(get(ab));
+    double *part = static_cast<double *>(get(sizeof(double) * 4 * nb));
+    if (I.mixed) {
+      int K = 0;
+      CK(cudaMemcpyAsync(&K, I.gK + (p.Ng - 1), sizeof(int), cudaMemcpyDeviceToHost, c->st));
+      CK(cudaStreamSynchronize(c->st));
+      CK(launch_graft_log(L, I.grafts, nullptr, I.ghist32 + (size_t)(p.Ng - 1) * M, K, M, c->st));
+    } else {
+      CK(launch_graft_log(L, I.grafts, static_cast<const double2 *>(I.ghist) + (size_t)(p.Ng - 1) * M, nullptr, 0,
+                          M, c->st));
+    }
+    const double len = p.L_nr * 1.05, rad = p.R_nr * 1.05;  // the graft map's enlarged plates
+    const int np = p.n_exp_nr;
+    std::vector<std::array<double2 *, 3>> gr(np);
+    cd S(0.0, 0.0);
+    for (int j = 0; j < np; j++) {
+      double2 *pd = static_cast<double2 *>(get(ab));
+      k_plate<<<1024, 256, 0, c->st>>>(pd, plate_args_of(I, j, len, rad), 0);
+      CK(cudaGetLastError());
+      for (int d = 0; d < 3; d++) {
+        gr[j][d] = static_cast<double2 *>(get(ab));
+        CK(cudaMemcpyAsync(gr[j][d], pd, ab, cudaMemcpyDeviceToDevice, c->st));
+        spectral_gradient(c, I, gr[j][d], d);
+      }
+      CK(launch_graft_dmap(gr[j].data(), nullptr, L, M, part, nb, c->st));
+      S += sums(part)[1];
+    }
+    std::vector<double2> sc(kNumScalars);
+    CK(cudaMemcpyAsync(sc.data(), I.scal, sizeof(double2) * kNumScalars, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    const cd Qga(sc[kQga].x, sc[kQga].y);
+    double2 *D = static_cast<double2 *>(get(ab));
+    double2 *gd[3] = {static_cast<double2 *>(get(ab)), static_cast<double2 *>(get(ab)), static_cast<double2 *>(get(ab))};
+    for (int j = 0; j < np; j++)
+      for (int q = 0; q < 4; q++) {
+        CK(launch_plate_deriv(D, g, j, q, len, rad, c->st));
+        for (int d = 0; d < 3; d++) {
+          CK(cudaMemcpyAsync(gd[d], D, ab, cudaMemcpyDeviceToDevice, c->st));
+          spectral_gradient(c, I, gd[d], d);
+        }
+        CK(launch_graft_dmap(gr[j].data(), gd, L, M, part, nb, c->st));
+        const auto I12 = sums(part);
+        const cd dQ = (I12[0] - I12[1] * Qga) / S;
+        out[4 * j + q] += -double(np) * I.info.ng_per_np * dQ.real();
+      }
+  } catch (...) {
+    for (void *q : tmp) cudaFree(q);
+    throw;
+  }
+  for (void *q : tmp) cudaFree(q);
+}
+
 int ctx_grad_geom(scft_ctx *c, double *out) {
   if (c->dirty_density) ctx_poly_density(c);
   const int n = (int)c->inst.size();
@@ -2184,7 +2365,7 @@ int ctx_grad_geom(scft_ctx *c, double *out) {
       for (int j = 0; j < 8; j++) out[8 * k + j] = 0.0;
       const scft_params &p = I.p;
       if (p.n_exp_nr == 0) continue;
-      if (I.graft || p.plate_shape != SCFT_PLATE_REFERENCE) {
+      if (p.plate_shape != SCFT_PLATE_REFERENCE) {
         status = SCFT_ERR_UNSUPPORTED;
         continue;
       }
@@ -2236,6 +2417,7 @@ int ctx_grad_geom(scft_ctx *c, double *out) {
           const double ts = g.shell ? p.shell_lambda * dV * (sv[3] - sv[4]) : 0.0;
           out[8 * k + 4 * j + q] = t.real() + ts;
         }
+      if (I.graft) graft_map_derivative(c, I, g, out + 8 * k);
     }
   } catch (...) {
     cudaFree(part);

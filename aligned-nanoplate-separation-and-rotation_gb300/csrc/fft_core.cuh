@@ -31,6 +31,18 @@ template <class C> __device__ __forceinline__ C cmul(C a, C b) {
   return mkc(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
 }
 template <class C, typename S> __device__ __forceinline__ C cscale(C a, S s) { return mkc(a.x * s, a.y * s); }
+// principal square root of a complex FP64 number (the branch of std::sqrt)
+__device__ __forceinline__ double2 csqrt_d(double2 z) {
+  const double x = z.x, y = z.y;
+  if (x == 0.0 && y == 0.0) return make_double2(0.0, y);
+  const double r = hypot(x, y);
+  if (x >= 0.0) {
+    const double t = sqrt(0.5 * (r + x));
+    return make_double2(t, y / (2.0 * t));
+  }
+  const double t = sqrt(0.5 * (r - x));
+  return make_double2(fabs(y) / (2.0 * t), copysign(t, y));
+}
 
 // a * w (SIGN < 0) or a * conj(w) (SIGN > 0); tables hold exp(-2*pi*i*t/n).
 template <int SIGN, class C> __device__ __forceinline__ C ctw(C a, C w) {

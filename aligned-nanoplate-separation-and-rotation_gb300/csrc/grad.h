@@ -25,4 +25,14 @@ struct GradArgs {
 cudaError_t launch_geom_grad(const GradArgs &g, const double2 *wpl, const double2 *rhoA, double *part, int blocks,
                              cudaStream_t st);
 
+// Grafted plates (kernels_grad.cu): d rho^big_j / d g_k as a complex field;
+// L = masked log q_g[Ng-1]; block sums (4 doubles per block) of the graft
+// map's derivative terms for one plate (gd == NULL: of |grad rho_j^big|).
+cudaError_t launch_plate_deriv(double2 *out, const GradArgs &g, int j, int k, double len, double rad,
+                               cudaStream_t st);
+cudaError_t launch_graft_log(double2 *L, const double2 *grafts, const double2 *q64, const float *q32, int K,
+                             long long M, cudaStream_t st);
+cudaError_t launch_graft_dmap(const double2 *const *gr, const double2 *const *gd, const double2 *L, long long M,
+                              double *part, int blocks, cudaStream_t st);
+
 }  // namespace scft

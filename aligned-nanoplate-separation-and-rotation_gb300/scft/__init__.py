@@ -28,7 +28,8 @@ EXPORTS = ("scft_last_error", "scft_version", "scft_create", "scft_destroy", "sc
            "scft_homopolymer_density", "scft_fft3d", "scft_sync", "scft_get_stream", "scft_launch_count",
            "scft_profile_step", "scft_diblock_density_noalloc", "scft_set_sweep_groups", "scft_autotune",
            "scft_set_fields_all", "scft_set_wait_limit", "scft_fp64_fma_rate",
-           "scft_set_persistent", "scft_get_schedule", "scft_profile_sweep")
+           "scft_set_persistent", "scft_get_schedule", "scft_profile_sweep",
+           "scft_get_fft_plan")
 
 
 class ScftError(RuntimeError):
@@ -108,6 +109,8 @@ def load(path: str | None = None):
     lib.scft_fp64_fma_rate.argtypes = [ctypes.c_int, dp]
     lib.scft_set_persistent.argtypes = [vp, ctypes.c_int]
     lib.scft_profile_sweep.argtypes = [vp, ctypes.c_int, dp, dp]
+    lib.scft_get_fft_plan.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                      ctypes.POINTER(ctypes.c_int)]
     lib.scft_get_schedule.argtypes = [vp] + [ctypes.POINTER(ctypes.c_int)] * 4
     lib.scft_set_fields_all.argtypes = [vp, ctypes.POINTER(ctypes.c_void_p)]
     ip = ctypes.POINTER(ctypes.c_int)
@@ -304,6 +307,13 @@ class Context:
         v = [ctypes.c_double() for _ in range(4)]
         _check(load().scft_profile_step(self._h, int(reps), *[ctypes.byref(x) for x in v]))
         return {"ms_plane": v[0].value, "bytes_plane": v[1].value, "ms_col": v[2].value, "bytes_col": v[3].value}
+
+    def fft_plan(self, inst: int, axis: int) -> list:
+        """Radices of the generic FFT stages along one axis, in order."""
+        r = (ctypes.c_int * 8)()
+        n = ctypes.c_int()
+        _check(load().scft_get_fft_plan(self._h, int(inst), int(axis), r, ctypes.byref(n)))
+        return list(r[: n.value])
 
     def profile_sweep(self, reps=5) -> dict:
         ms, by = ctypes.c_double(), ctypes.c_double()

@@ -424,6 +424,12 @@ def main():
             schedule = dict(ctx.schedule(), tuned=False)
         else:
             schedule = dict(ctx.autotune(3), tuned=True)
+    if form == "mixed":
+        plans = {}
+        for k, p in enumerate(params):
+            for d in range(3):
+                plans.setdefault(str(p.Nx[d]), ctx.fft_plan(k, d))
+        schedule["fft_plans"] = plans
     config["schedule"] = schedule
     stream = torch.cuda.ExternalStream(ctx.stream())
     ctx.update_1s(max(3, args.warmup))

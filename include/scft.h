@@ -169,8 +169,12 @@ int scft_get_density(scft_ctx *ctx, int inst, double *rhoda, double *rhodb, doub
  * dH/dd = (dH/dc_2 - dH/dc_1).e / 2.  The reference has no derivative code;
  * this replaces finite differences over its sweeps (angle-rotation/,
  * particle-separation/).  With the shell potential the derivative includes
- * shell_lambda * int rho_A d(shell)/dg.  SCFT_ERR_UNSUPPORTED for grafted
- * plates and for SCFT_PLATE_CUBOID. */
+ * shell_lambda * int rho_A d(shell)/dg; with grafted plates it includes
+ * -n_exp_nr ng_per_np Re int (dg_map/dg) log q_g[Ng-1], the graft map
+ * g_map ~ |grad rho_p(1.05 L, 1.05 R)| differentiated through its spectral
+ * gradient and normalisation (code/initialize.cpp:160-200,
+ * code/grafted_nanoparticle.cpp:82-112).  SCFT_ERR_UNSUPPORTED for
+ * SCFT_PLATE_CUBOID. */
 int scft_grad_geom(scft_ctx *ctx, double *out);
 
 /* The explicit plates' density rho_exp_nr of one instance (M real values),
@@ -274,11 +278,19 @@ int scft_set_persistent(scft_ctx *ctx, int on);
  * does not apply) and whether the sweep is persistent. */
 int scft_get_schedule(scft_ctx *ctx, int *groups, int *phases, int *col_tile, int *persistent);
 
+/* The FFT stage plan of instance inst along axis 0 (x), 1 or 2: *nst radices
+ * in application order in radix[0..7] (the rest 0).  Generic transforms
+ * only; the 64-point kernels use a fixed 8 x 8 four-step transform. */
+int scft_get_fft_plan(scft_ctx *ctx, int inst, int axis, int *radix, int *nst);
+
 /* Autotuner: times reps full propagator sweeps of the batch for every
  * candidate schedule (1-4 phases x 1-6 or 8 groups; for 64-point grids also
  * 8, 16 or 32 z-pass columns per CTA, and the persistent sweep with 1-3
  * groups x 1-2 phases) with CUDA events and keeps the fastest
- * (scft_get_schedule reads the choice).  Reports the choice (col_tile 0 where it does not apply) and its
+ * (scft_get_schedule reads the choice); then, with that schedule, the stage
+ * order of the generic FFTs for each axis length of the batch (every order of
+ * radices 8, 4, 2, 3, 5 with at most one radix-2 stage, up to 12 plans per
+ * length, one length at a time; scft_get_fft_plan reads the choice).  Reports the choice (col_tile 0 where it does not apply) and its
  * time per sweep.  FP64 contexts have a single schedule (1 group, 1 phase). */
 int scft_autotune(scft_ctx *ctx, int reps, int *groups, int *phases, int *col_tile, double *ms_per_sweep);
 

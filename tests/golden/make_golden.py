@@ -3,6 +3,7 @@ reference SCFT code itself (compiled by oracle/Makefile into
 oracle/_ref/scft_ref, Dim=3, FFT via the oracle shim).
 
     make -C oracle && python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --homopolymer | --separation
     python tests/golden/make_golden.py --large [name ...]   (configs 1, 3, 4;
                                                              about 20 min and
                                                              35 GB of host RAM)
@@ -219,6 +220,57 @@ def make_driver_fixtures(tmp):
         print(name, open(os.path.join(run, "data.dat")).read().splitlines()[-1])
 
 
+# A separation sweep converged by the reference itself: two coplanar discs
+# (normal along x, centres 0.5 -+ d/2 of L_z) on a 16 x 16 x 32 grid, N = 16,
+# chiN = 20, C = 50, from one seeded field, SEP_ITERS update_1s() each (H
+# then changes by < 1e-9 per iteration).  It checks the geometric derivative
+# dH/dd against differences of H between separations the reference converged
+# independently.
+SEP_D = (0.36, 0.40, 0.44, 0.48, 0.52)
+SEP_FD = (0.438, 0.442)
+SEP_ITERS = 4500
+
+
+def separation_params(d, precision=0):
+    sys.path.insert(0, os.path.join(ROOT, "aligned-nanoplate-separation-and-rotation_gb300"))
+    from scft.workloads import plate_params
+
+    return plate_params(0.0, N=16, grid=(16, 16, 32), box_rg=(3.2, 3.2, 6.4), precision=precision,
+                        centers=((0.5, 0.5, 0.5 - d / 2), (0.5, 0.5, 0.5 + d / 2)), thickness_rg=0.4,
+                        radius_rg=1.0, xi_rg=0.2, lam_pl=0.004, lam_mi=0.001)
+
+
+def separation_fields(p):
+    sys.path.insert(0, os.path.join(ROOT, "aligned-nanoplate-separation-and-rotation_gb300"))
+    from scft.workloads import seeded_fields
+
+    return seeded_fields(p, 1234)
+
+
+def make_separation_fixture(tmp):
+    from concurrent.futures import ThreadPoolExecutor
+
+    from ref_case import case_from_params
+
+    ds = list(SEP_D) + list(SEP_FD)
+
+    def one(d):
+        p = separation_params(d)
+        c = case_from_params(p, separation_fields(p))
+        out = run_reference(os.path.join(tmp, f"sep{d:.3f}"), c, SEP_ITERS, hist=False, timeout=6 * 3600)
+        return out["trace"]
+
+    with ThreadPoolExecutor(max_workers=min(8, len(ds))) as ex:
+        traces = list(ex.map(one, ds))
+    z = {"d": np.array(ds), "iters": SEP_ITERS,
+         "H": np.array([t[-1, 1] for t in traces]), "Qd": np.array([t[-1, 3] for t in traces]),
+         "dH_last": np.array([t[-1, 1] - t[-2, 1] for t in traces]),
+         "trace_tail": np.array([t[-50:, :4] for t in traces])}
+    np.savez_compressed(os.path.join(HERE, "separation_sweep_16x16x32_N16.npz"), **z)
+    for d, t in zip(ds, traces):
+        print(f"d={d}: H={t[-1, 1]!r} last change {t[-1, 1] - t[-2, 1]:.3e}")
+
+
 def make_homopolymer_fixture(tmp, Nh=7, nK=3.5):
     """The reference's homopolymer_discrete + integrate_homopoly_discrete
     (dead in its shipped inputs) on the smeared w_A of the tiny_plate case,
@@ -250,6 +302,9 @@ def main():
     tmp = tempfile.mkdtemp(prefix="golden_")
     if "--homopolymer" in sys.argv:
         make_homopolymer_fixture(tmp)
+        return
+    if "--separation" in sys.argv:
+        make_separation_fixture(tmp)
         return
     if "--large" in sys.argv:
         names = [a for a in sys.argv[1:] if not a.startswith("--")]

@@ -146,3 +146,58 @@ def test_autograd_function_wrapper(S):
     h = 1e-3
     fd = (PlateH.apply(torch.tensor(theta.item() + h)) - PlateH.apply(torch.tensor(theta.item() - h))) / (2 * h)
     assert abs(theta.grad.item() - fd.item()) <= 1e-5 * max(abs(fd.item()), 1e-3 * abs(H.item()))
+
+
+def grafted(S, theta_deg, prec=0, centers=((0.5, 0.5, 0.5),)):
+    """small_plate with grafted chains of Ng = 4 at sigma = 0.5 / Rg^2 (graft
+    species A-like: chi_AC = 0, chi_BC = chi_AB)."""
+    p = small_plate(S, theta_deg, prec=prec, centers=centers)
+    p.sigma = 0.5 / ((16 - 1) / 6.0)
+    p.Ng = 4
+    p.chi_bc = p.chi_ab
+    return p
+
+
+def grafted_fields(p, seed):
+    from scft.workloads import seeded_fields
+
+    f = seeded_fields(p, seed)
+    x = np.arange(24) / 24
+    f["wpl"] = 1j * 0.3 * np.cos(2 * np.pi * x)[None, None, :] * np.ones((24, 24, 24))
+    f["wbcm"] = (0.2 * np.sin(2 * np.pi * x)[None, :, None] * np.ones((24, 24, 24))).astype(np.complex128)
+    return f
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+def test_grafted_plate_derivatives_at_fixed_fields(S, prec):
+    """Grafted plates: the graft map g ~ |grad rho_p(1.05 L, 1.05 R)| moves with
+    the plate, so dH/dg gains -n_exp_nr ng_per_np Re int dg/dg_k log q_g
+    (code/grafted_nanoparticle.cpp:82-112, code/initialize.cpp:160-200).
+    Rotation and separation of two grafted plates against central
+    differences of H at fixed fields."""
+    th, h = 12.0, 1e-3
+    f = grafted_fields(grafted(S, th), 21)
+    H0, g0, _ = H_at(S, grafted(S, th, prec), f)
+    Hp, _, _ = H_at(S, grafted(S, th + math.degrees(h), prec), f)
+    Hm, _, _ = H_at(S, grafted(S, th - math.degrees(h), prec), f)
+    fd = (Hp - Hm) / (2 * h)
+    tol = 1e-5 if prec == 0 else 1e-4
+    assert abs(g0[0, 0] - fd) <= tol * max(abs(fd), 1e-3 * abs(H0)), (g0[0, 0], fd)
+
+    def two(d):
+        return grafted(S, 0.0, prec, centers=((0.5, 0.5 - d / 2, 0.5), (0.5, 0.5 + d / 2, 0.5)))
+
+    d, hd = 0.45, 1e-4
+    H0, g0, _ = H_at(S, two(d), f)
+    Hp, _, _ = H_at(S, two(d + hd), f)
+    Hm, _, _ = H_at(S, two(d - hd), f)
+    fd = (Hp - Hm) / (2 * hd)
+    an = two(d).L[1] * (g0[1, 2] - g0[0, 2]) / 2
+    assert abs(an - fd) <= tol * max(abs(fd), 1e-3 * abs(H0)), (an, fd)
+
+
+def test_grafted_gradient_mixed_matches_fp64(S):
+    f = grafted_fields(grafted(S, 25.0), 22)
+    _, g64, _ = H_at(S, grafted(S, 25.0), f, iters=3)
+    _, g32, _ = H_at(S, grafted(S, 25.0, S.PREC_MIXED), f, iters=3)
+    assert np.abs(g32[0] - g64[0]).max() <= 1e-4 * np.abs(g64[0]).max()
