@@ -562,6 +562,9 @@ def main():
                                                                                     (ms64 / 1e3)),
                  "dH_rel_max": float(dH.max()), "dH_rel_median": float(np.median(dH)),
                  "dH_abs_max": float(np.abs(Hc[:, 0] - H64[:, 0]).max()),
+                 "dH_per_volume_max": float(max(abs(a - b) / (p.L[0] * p.L[1] * p.L[2])
+                                                for a, b, p in zip(Hc[:, 0], H64[:, 0], pp))),
+                 "dH_bar_reading": "relative |dH| / |H| <= 1e-6 (dH_rel_max); absolute and per volume also given",
                  "drho_rel_max": float(max(drho)),
                  "dgrad_rel_max": float(max(dg)) if dg[0] is not None else None,
                  "per_instance": [{"grid": list(p.Nx), "N": p.Nda + p.Ndb, "dH_rel": float(d), "drho_rel": float(r),
