@@ -26,6 +26,7 @@ void ctx_set_sweep_groups(scft_ctx *c, int groups, int phases);
 void ctx_set_wait_limit(scft_ctx *c, int polls);
 void ctx_set_persistent(scft_ctx *c, int on);
 void ctx_profile_sweep(scft_ctx *c, int reps, double *ms, double *bytes);
+int ctx_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *out);
 void ctx_set_fields_all(scft_ctx *c, const double *const *w);
 void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *tx_out, double *ms_out);
 void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
@@ -267,6 +268,18 @@ int scft_set_persistent(scft_ctx *c, int on) {
   if (int s = check_ctx(c, 0)) return s;
   API_BODY(scft::ctx_set_persistent(c, on));
   return SCFT_OK;
+}
+
+int scft_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *H_out) {
+  if (int s = check_ctx(c, 0)) return s;
+  if (!w || !H_out || n_iter < 1) return fail(SCFT_ERR_ARG, "need field pointers, an output and n_iter >= 1");
+  for (size_t k = 0; k < c->inst.size(); k++)
+    if (!w[k]) return fail(SCFT_ERR_ARG, "null field pointer");
+  int st = SCFT_OK;
+  API_BODY(st = scft::ctx_step_fields(c, w, n_iter, H_out));
+  if (st == SCFT_ERR_NAN) return fail(st, "H is NaN");
+  if (st == SCFT_ERR_QNONPOS) return fail(st, "graft propagator q_g[Ng-1] <= 0 at 5 or more points");
+  return st;
 }
 
 int scft_profile_sweep(scft_ctx *c, int reps, double *ms, double *bytes) {

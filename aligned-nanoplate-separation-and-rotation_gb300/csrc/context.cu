@@ -2143,6 +2143,159 @@ static void set_fields_ks(scft_ctx *c, const std::vector<int> &ks, const double 
 
 void ctx_set_fields(scft_ctx *c, int k, const double *w) { set_fields_ks(c, {k}, &w); }
 
+int ctx_calc_H(scft_ctx *c, double *out);
+void ctx_update(scft_ctx *c, int n_iter);
+void ctx_set_fields_all(scft_ctx *c, const double *const *w);
+
+// Per-group FP64 forward-transform jobs of the fields a mixed instance uses
+// (w+ and the pair of every nonzero chi), in job order; rebuilt when the
+// groups change.
+static void build_step_jobs(scft_ctx *c) {
+  std::vector<int> sig;
+  for (auto &gr : c->groups) {
+    sig.push_back(gr.inst_begin);
+    sig.push_back(gr.inst_end);
+    sig.push_back(gr.phase);
+  }
+  if (sig == c->step_groups_sig && c->step_pj.size() == c->groups.size()) return;
+  c->step_pj.clear();
+  c->step_cj.clear();
+  c->step_npj.clear();
+  c->step_ncj.clear();
+  for (auto &gr : c->groups) {
+    std::vector<PlaneJob> pj;
+    std::vector<ColJob> cj;
+    for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) {
+      const Instance &I = c->inst[c->job_order[oi]];
+      const DevGeom &g = c->geoms[I.geom];
+      const bool active[7] = {true, I.cab != 0.0, I.cab != 0.0, I.cbc != 0.0, I.cbc != 0.0, I.cac != 0.0,
+                              I.cac != 0.0};
+      for (int f = 0; f < 7; f++) {
+        if (!active[f]) continue;
+        for (int z = 0; z < g.nz; z++) pj.push_back(PlaneJob{I.w[f], I.geom, z});
+        for (int y = 0; y < g.ny; y++)
+          for (int x0 = 0; x0 < g.nx; x0 += g.tx) cj.push_back(ColJob{I.w[f], nullptr, I.geom, x0, y});
+      }
+    }
+    c->step_pj.push_back(dupload(c, pj));
+    c->step_cj.push_back(dupload(c, cj));
+    c->step_npj.push_back((int)pj.size());
+    c->step_ncj.push_back((int)cj.size());
+  }
+  c->step_groups_sig = sig;
+}
+
+// The graph body of scft_step_fields (mixed form, no grafted chains): per
+// sweep group on its side stream, the upload of its instances' fields from
+// host memory, their realness check (results copied to pinned host memory,
+// read after the call's synchronisation), the FP64 forward transform of the
+// fields in use (the inactive pairs are zeroed: they do not enter the
+// model), then the density build and n_iter updates of the group.  One
+// group's upload runs beside another group's compute.
+static void step_body(scft_ctx *c, const double *const *w, int n_iter) {
+  cudaStream_t st = c->st;
+  const int G = (int)c->groups.size();
+  CK(cudaEventRecord(c->ev_fork, st));
+  for (int g = 0; g < G; g++) {
+    const scft_ctx::SweepGroup &gr = c->groups[g];
+    cudaStream_t sg = c->side[g];
+    CK(cudaStreamWaitEvent(sg, c->ev_fork, 0));
+    const int cnt = gr.inst_end - gr.inst_begin;
+    for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) {
+      const int k = c->job_order[oi];
+      Instance &I = c->inst[k];
+      CK(cudaMemcpyAsync(I.w[0], w[k], sizeof(double2) * 7 * (size_t)I.M, cudaMemcpyHostToDevice, sg));
+    }
+    k_real_check_all<<<dim3(kCheckBlocks, cnt), 256, 0, sg>>>(c->d_fi_ord + gr.inst_begin, nullptr,
+                                                              c->d_realout + 128 * (size_t)gr.inst_begin);
+    CK(cudaGetLastError());
+    c->launches++;
+    CK(cudaMemcpyAsync(c->h_pin + 128 * (size_t)gr.inst_begin, c->d_realout + 128 * (size_t)gr.inst_begin,
+                       sizeof(double) * 128 * (size_t)cnt, cudaMemcpyDeviceToHost, sg));
+    for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) {
+      Instance &I = c->inst[c->job_order[oi]];
+      const bool active[7] = {true, I.cab != 0.0, I.cab != 0.0, I.cbc != 0.0, I.cbc != 0.0, I.cac != 0.0,
+                              I.cac != 0.0};
+      for (int f = 0; f < 7; f++)
+        if (!active[f]) CK(cudaMemsetAsync(I.w[f], 0, sizeof(double2) * (size_t)I.M, sg));
+    }
+    if (c->step_npj[g] > 0) {
+      LK(launch_plane_fft<double>(c->shp_plane, c->step_pj[g], c->step_npj[g], c->d_geoms, c->d_tw64, -1, 0, sg));
+      LK(launch_col_fft<double>(c->shp_col, c->step_cj[g], c->step_ncj[g], c->d_geoms, c->d_tw64, 0, 1, sg));
+    }
+    mix_group_chain(c, g, sg, false);
+    for (int it = 0; it < n_iter; it++) mix_group_chain(c, g, sg, true);
+    CK(cudaEventRecord(c->ev_join[g], sg));
+    CK(cudaStreamWaitEvent(st, c->ev_join[g], 0));
+  }
+}
+
+// scft_step_fields: fields of every instance from host memory (w[inst], 7 x M
+// complex, the scft_set_fields layout; pinned memory lets the uploads overlap
+// compute), the density build of those fields, n_iter updates, H into out
+// (5 per instance, as scft_calc_H) -- one call and one synchronisation.
+// Mixed-form batches without grafted chains or complex Langevin run as one
+// captured graph (re-captured when the host pointers or n_iter change);
+// everything else runs scft_set_fields_all, scft_update_1s and scft_calc_H.
+int ctx_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *out) {
+  const int n = (int)c->inst.size();
+  bool cl = false;
+  for (auto &I : c->inst) cl = cl || I.p.do_cl;
+  if (!c->mixed || c->ngmax > 0 || cl || c->groups.empty()) {
+    ctx_set_fields_all(c, w);
+    ctx_update(c, n_iter);
+    return ctx_calc_H(c, out);
+  }
+  if (!c->h_pin || !c->d_realout) throw ScftError(SCFT_ERR_CUDA, "scft_step_fields: staging buffers missing");
+  build_step_jobs(c);
+  std::vector<const double *> ptrs(w, w + n);
+  if (c->g_step && (ptrs != c->step_ptrs || n_iter != c->step_iters)) {
+    CK(cudaGraphExecDestroy(c->g_step));
+    c->g_step = nullptr;
+  }
+  if (!c->g_step) {
+    // the first run is eager (kernel attributes get set), then capture
+    if (!c->update_runs && !c->density_runs) {
+      step_body(c, w, n_iter);
+      CK(cudaStreamSynchronize(c->st));
+      c->density_runs++;
+      c->update_runs++;
+    }
+    cudaGraph_t graph;
+    CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+    try {
+      step_body(c, w, n_iter);
+    } catch (...) {
+      cudaGraph_t g2;
+      cudaStreamEndCapture(c->st, &g2);
+      throw;
+    }
+    CK(cudaStreamEndCapture(c->st, &graph));
+    CK(cudaGraphInstantiate(&c->g_step, graph, 0));
+    cudaGraphDestroy(graph);
+    c->step_ptrs = ptrs;
+    c->step_iters = n_iter;
+  }
+  CK(cudaGraphLaunch(c->g_step, c->st));
+  c->dirty_density = 0;
+  int status = ctx_calc_H(c, out);  // queues H and synchronises
+  check_device_error(c);
+  std::string bad;
+  for (int oi = 0; oi < n; oi++) {
+    double m[9] = {};
+    for (int b = 0; b < kCheckBlocks; b++)
+      for (int q = 0; q < 9; q++) m[q] = std::max(m[q], c->h_pin[128 * (size_t)oi + 9 * b + q]);
+    if (m[0] > 1e-12 * std::max(1.0, m[1]) && bad.empty()) bad = std::to_string(c->job_order[oi]);
+  }
+  if (!bad.empty()) {
+    c->dirty_density = 1;
+    throw ScftError(SCFT_ERR_COMPLEX, "instance " + bad +
+                                          ": mixed precision needs real w_A, w_B: the mean-field phase convention "
+                                          "(the results of this call are invalid)");
+  }
+  return status;
+}
+
 void ctx_set_fields_all(scft_ctx *c, const double *const *w) {
   std::vector<int> ks(c->inst.size());
   for (size_t k = 0; k < ks.size(); k++) ks[k] = (int)k;

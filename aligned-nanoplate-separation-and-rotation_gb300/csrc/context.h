@@ -174,6 +174,16 @@ struct scft_ctx {
   int eblocks = 0;  // blocks per instance for pointwise kernels
   double2 *d_hpart = nullptr;
   int hblocks = 0;
+  // scft_step_fields: its captured graph (uploads, checks, transforms, density
+  // build, updates) for one set of host pointers and iteration count, and the
+  // per-group FP64 transform jobs of the uploaded fields (job-order groups)
+  cudaGraphExec_t g_step = nullptr;
+  std::vector<const double *> step_ptrs;
+  int step_iters = 0;
+  std::vector<scft::PlaneJob *> step_pj;
+  std::vector<scft::ColJob *> step_cj;
+  std::vector<int> step_npj, step_ncj;
+  std::vector<int> step_groups_sig;  // group boundaries the job lists were built for
   cudaGraphExec_t g_update = nullptr;
   cudaGraphExec_t g_density = nullptr;  // captured density build (after the first, eager one)
   long long launches_per_density = 0;

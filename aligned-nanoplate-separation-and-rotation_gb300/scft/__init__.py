@@ -29,7 +29,7 @@ EXPORTS = ("scft_last_error", "scft_version", "scft_create", "scft_destroy", "sc
            "scft_profile_step", "scft_diblock_density_noalloc", "scft_set_sweep_groups", "scft_autotune",
            "scft_set_fields_all", "scft_set_wait_limit", "scft_fp64_fma_rate",
            "scft_set_persistent", "scft_get_schedule", "scft_profile_sweep",
-           "scft_get_fft_plan")
+           "scft_get_fft_plan", "scft_step_fields")
 
 
 class ScftError(RuntimeError):
@@ -109,6 +109,7 @@ def load(path: str | None = None):
     lib.scft_fp64_fma_rate.argtypes = [ctypes.c_int, dp]
     lib.scft_set_persistent.argtypes = [vp, ctypes.c_int]
     lib.scft_profile_sweep.argtypes = [vp, ctypes.c_int, dp, dp]
+    lib.scft_step_fields.argtypes = [vp, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_void_p]
     lib.scft_get_fft_plan.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                       ctypes.POINTER(ctypes.c_int)]
     lib.scft_get_schedule.argtypes = [vp] + [ctypes.POINTER(ctypes.c_int)] * 4
@@ -319,6 +320,29 @@ class Context:
         ms, by = ctypes.c_double(), ctypes.c_double()
         _check(load().scft_profile_sweep(self._h, int(reps), ctypes.byref(ms), ctypes.byref(by)))
         return {"ms_sweep": ms.value, "bytes_sweep": by.value}
+
+    def step_fields_raw(self, ptrs, n_iter: int, out_ptr: int) -> int:
+        """scft_step_fields from host pointers (one per instance, 7 x M complex
+        each) into a host buffer of 5 doubles per instance; returns the status
+        (OK or ERR_NAN), raises on other errors."""
+        arr = (ctypes.c_void_p * self.n)(*ptrs)
+        code = load().scft_step_fields(self._h, arr, int(n_iter), ctypes.c_void_p(out_ptr))
+        if code not in (OK, ERR_NAN):
+            _check(code)
+        return code
+
+    def step_fields(self, fields: list, n_iter: int = 1) -> np.ndarray:
+        """step_fields_raw from a list of field dicts (as set_fields takes)."""
+        bufs = []
+        for k, f in enumerate(fields):
+            b = np.zeros((7,) + self._shape(k), np.complex128)
+            for q, name in enumerate(FIELD_NAMES):
+                if name in f:
+                    b[q] = np.asarray(f[name], np.complex128).reshape(self._shape(k))
+            bufs.append(b)
+        out = np.zeros((self.n, 5), np.float64)
+        self.last_status = self.step_fields_raw([b.ctypes.data for b in bufs], n_iter, out.ctypes.data)
+        return out
 
     def set_fields_all_raw(self, ptrs):
         """scft_set_fields_all from device-visible host pointers (one per instance)."""
