@@ -2241,7 +2241,18 @@ int ctx_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *out
   const int n = (int)c->inst.size();
   bool cl = false;
   for (auto &I : c->inst) cl = cl || I.p.do_cl;
-  if (!c->mixed || c->ngmax > 0 || cl || c->groups.empty()) {
+  // a captured upload needs page-locked (pinned or registered) host memory
+  bool pinned = true;
+  for (int k = 0; k < n && pinned; k++) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, w[k]) != cudaSuccess) {
+      cudaGetLastError();
+      pinned = false;
+    } else {
+      pinned = (a.type == cudaMemoryTypeHost);
+    }
+  }
+  if (!c->mixed || c->ngmax > 0 || cl || c->groups.empty() || !pinned) {
     ctx_set_fields_all(c, w);
     ctx_update(c, n_iter);
     return ctx_calc_H(c, out);

@@ -151,7 +151,8 @@ int scft_get_fields(scft_ctx *ctx, int inst, double *w);
  * into H_out (5 doubles per instance, as scft_calc_H), with one
  * synchronisation.  The sequence scft_set_fields_all, scft_update_1s,
  * scft_calc_H does the same; here, for mixed-form batches without grafted
- * chains or complex Langevin, each sweep group's upload, realness check,
+ * chains or complex Langevin and with page-locked host buffers (pinned or
+ * registered; others run the sequence), each sweep group's upload, realness check,
  * field transform, density build and updates run as one chain on its own
  * stream inside one captured graph (re-captured when the host pointers or
  * n_iter change), so one group's upload runs beside another group's compute,
