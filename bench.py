@@ -617,6 +617,15 @@ def main():
                     "other_kernel_ms_per_launch": per_step["other_kernel_ms_per_launch"]}
     if sweep_roof is not None:
         roofline["sweep"] = sweep_roof
+    # the whole iteration against the survey's per-iteration byte count
+    # B = M s [5 (N - 1) + 30], s = 8 B (FP32 propagators) or 16 B (FP64)
+    s_b = 8.0 if form == "mixed" else 16.0
+    b_it = sum(p.Nx[0] * p.Nx[1] * p.Nx[2] * s_b * (5 * (p.Nda + p.Ndb - 1) + 30) for p in params)
+    a_it = b_it / (ms / args.steps / 1e3) / 1e9
+    roofline["iteration"] = {"bytes_per_iteration": b_it, "ms_per_iteration": ms / args.steps, "achieved": a_it,
+                             "frac": a_it / hbm,
+                             "note": "B = M s [5(N-1) + 30] per instance and iteration (s = 8 B FP32, 16 B FP64), "
+                                     "the timed iterations with field work and launch gaps"}
     ctx.close()
 
     cpu = None
