@@ -120,6 +120,9 @@ def large_cases() -> dict:
         "config1_plate64_N100": ("plate64_N100", 0, 1001, 1, 3),
         "config3_sep030_64x64x128_N100": ("sep9_64x64x128_N100", 4, 1004, 1, 3),
         "config4_graft_128x128x256_N200": ("graft8_128x128x256_N200", 0, 1000, 3, 1),
+        # config 2's two non-64^3 grids (instances 5 and 9 of the mixed-size sweep)
+        "config2_96x64x64_N100": ("sweep15_mixed_sizes", 5, 1005, 1, 3),
+        "config2_48cubed_N100": ("sweep15_mixed_sizes", 9, 1009, 1, 3),
     }
 
 

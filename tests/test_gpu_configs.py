@@ -1,7 +1,8 @@
 """Plain FP64 method against the reference at the benchmark configurations'
-full sizes: config 1 (one plate, 64^3, N=100), config 3 (two plates at
-d = 0.30 L_z, 64 x 64 x 128, N=100) and config 4 (two grafted plates,
-128 x 128 x 256, N=200, Ng=20).
+full sizes: config 1 (one plate, 64^3, N=100), config 2's non-64^3 grids
+(96 x 64 x 64 and 48^3, N=100, from the mixed-size sweep), config 3 (two
+plates at d = 0.30 L_z, 64 x 64 x 128, N=100) and config 4 (two grafted
+plates, 128 x 128 x 256, N=200, Ng=20).
 
 The fixtures (tests/golden/config*_*.npz, make_golden.py --large) hold what
 the compiled reference wrote after set-up and after a few update_1s() calls
@@ -24,7 +25,8 @@ pytestmark = pytest.mark.gpu
 RHO_TOL = 1e-10
 H_TOL = 1e-9
 
-LARGE = ["config1_plate64_N100", "config3_sep030_64x64x128_N100", "config4_graft_128x128x256_N200"]
+LARGE = ["config1_plate64_N100", "config2_96x64x64_N100", "config2_48cubed_N100", "config3_sep030_64x64x128_N100",
+         "config4_graft_128x128x256_N200"]
 
 
 def digest_close(a, ref, tol, M):
