@@ -73,5 +73,13 @@ __device__ __forceinline__ void bulk_load_1d(void *dst, const void *src, uint32_
       : "memory");
 }
 
+// 16-byte asynchronous copy global -> shared (cp.async, L2 only), both
+// addresses 16-byte aligned; completed by cp_async_wait_all.
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
 }  // namespace
 }  // namespace scft

@@ -25,6 +25,7 @@ int ctx_grad_geom(scft_ctx *c, double *out);
 void ctx_set_sweep_groups(scft_ctx *c, int groups, int phases);
 void ctx_set_wait_limit(scft_ctx *c, int polls);
 void ctx_set_persistent(scft_ctx *c, int on);
+void ctx_set_plane_form(scft_ctx *c, int form);
 void ctx_profile_sweep(scft_ctx *c, int reps, double *ms, double *bytes);
 int ctx_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *out);
 void ctx_set_fields_all(scft_ctx *c, const double *const *w);
@@ -304,6 +305,19 @@ int scft_get_schedule(scft_ctx *c, int *groups, int *phases, int *col_tile, int 
   if (phases) *phases = c->sweep_phases;
   if (col_tile) *col_tile = (c->colfast || c->anyfast) ? c->col64_tx : 0;
   if (persistent) *persistent = c->sweep_persistent;
+  return SCFT_OK;
+}
+
+int scft_set_plane_form(scft_ctx *c, int form) {
+  if (int s = check_ctx(c, 0)) return s;
+  API_BODY(scft::ctx_set_plane_form(c, form));
+  return SCFT_OK;
+}
+
+int scft_get_plane_form(scft_ctx *c, int *form) {
+  if (int s = check_ctx(c, 0)) return s;
+  if (!form) return fail(SCFT_ERR_ARG, "null output pointer");
+  *form = c->plane64_form;
   return SCFT_OK;
 }
 

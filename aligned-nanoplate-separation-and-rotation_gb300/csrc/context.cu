@@ -1470,8 +1470,9 @@ void mix_group_sweep(scft_ctx *c, int g, cudaStream_t sg) {
         LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cc, c->d_geoms, c->d_tw32, 3, 1, sg));
     }
     if (p64)
-      LK(launch_mix_plane64(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
-                            c->tmH.data() + gr.inst_begin, act, nzi, c->d_tw32_64, s, c->d_err, sg));
+      LK((c->plane64_form ? launch_mix_plane64w : launch_mix_plane64)(
+          c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin, c->tmH.data() + gr.inst_begin, act,
+          nzi, c->d_tw32_64, s, c->d_err, sg));
     else
       LK(launch_mix_prop_plane(c->shp_mixp, c->d_prop_pj + gr.pj_begin, cnt, c->d_mi, c->d_geoms, c->d_tw32, s,
                                c->d_err, sg));
@@ -1728,6 +1729,25 @@ void ctx_set_wait_limit(scft_ctx *c, int polls) {
   CK(cudaStreamSynchronize(c->st));
 }
 
+// Form of the 64-point plane pass (0: block-barrier exchanges, 1: warp-local
+// columns); results are bit-identical, the captured graphs hold the old form.
+void ctx_set_plane_form(scft_ctx *c, int form) {
+  if (form < 0 || form > 1) throw ScftError(SCFT_ERR_ARG, "plane form must be 0 or 1");
+  c->plane64_form = form;
+  if (c->g_update) {
+    CK(cudaGraphExecDestroy(c->g_update));
+    c->g_update = nullptr;
+  }
+  if (c->g_density) {
+    CK(cudaGraphExecDestroy(c->g_density));
+    c->g_density = nullptr;
+  }
+  if (c->g_step) {
+    CK(cudaGraphExecDestroy(c->g_step));
+    c->g_step = nullptr;
+  }
+}
+
 // Persistent sweep on or off (64 x 64 x 64 groups only; others keep the
 // per-step launches).  The captured graphs hold the old launches.
 void ctx_set_persistent(scft_ctx *c, int on) {
@@ -1796,13 +1816,18 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
   // the persistent sweep applies to 64 x 64 x 64 instances
   const bool can_persist = (c->xy64 && c->inst[0].p.Nx[2] == 64) || c->anyfast;
   if (can_persist && !c->sweep64_cap) CK(sweep64_capacity(&c->sweep64_cap));
+  const bool has64 = c->xy64 || c->anyfast;
+  int bform = c->plane64_form;
+  for (int form = 0; form <= (has64 ? 1 : 0); form++)
   for (int pers = 0; pers <= (can_persist ? 1 : 0); pers++)
   for (int ph : ps)
   for (int g : gs)
     for (int tx : txs) {
       if (g * ph > n) continue;
-      // persistent: the z tasks take whole rows (tx unused); few groups, phases
-      if (pers && (tx != txs[0] || g > 3 || ph > 2)) continue;
+      // persistent: the z tasks take whole rows (tx unused); few groups, phases;
+      // its plane tasks use the first form
+      if (pers && (tx != txs[0] || g > 3 || ph > 2 || form)) continue;
+      c->plane64_form = form;
       c->sweep_persistent = pers;
       c->sweep_phases = ph;
       c->sweep_streams = g;
@@ -1821,10 +1846,12 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
         bt = tx;
         bp = ph;
         bpers = pers;
+        bform = form;
       }
     }
   c->col64_tx = bt;
   c->sweep_persistent = bpers;
+  c->plane64_form = bform;
   ctx_set_sweep_groups(c, bg, bp);
   // FFT stage orders of the generic transforms (field transforms; plane and
   // z passes of the generic grids), one axis length at a time with the
@@ -1963,7 +1990,7 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   CK(cudaEventRecord(e0, c->st));
   for (int r = 0; r < reps; r++) {
     if (c->mixed && c->xy64)
-      LK(launch_mix_plane64(c->mix64_tab.data(), c->tmE.data(), c->tmH.data(),
+      LK((c->plane64_form ? launch_mix_plane64w : launch_mix_plane64)(c->mix64_tab.data(), c->tmE.data(), c->tmH.data(),
                             c->prop_pj_count[s] / c->inst[0].p.Nx[2], c->inst[0].p.Nx[2], c->d_tw32_64, s, c->d_err,
                             c->st));
     else if (c->mixed)

@@ -114,6 +114,9 @@ struct scft_ctx {
   // (k_mix_sweep64) instead of two launches per step; its task counters
   // (sweep64_counters(kMix64MaxInst) per group) and the CTAs resident at once
   int sweep_persistent = 0;
+  // plane pass of the 64-point family: 0 = block-barrier exchanges
+  // (k_mix_plane64), 1 = warp-local columns (k_mix_plane64w); bit-identical
+  int plane64_form = 0;
   unsigned *d_sweep_ctr = nullptr;
   int sweep_ctr_groups = 0;
   int sweep64_cap = 0;

@@ -482,6 +482,263 @@ __global__ void __launch_bounds__(8 * TX) k_mix_col128(const ColJob *__restrict_
 }
 
 // ---------------------------------------------------------------------------
+// Plane pass, second form: warp-local column transforms
+// ---------------------------------------------------------------------------
+// The same step as plane64_body with fewer block barriers.  The working plane
+// arrives by cp.async (16-byte chunks, coalesced) into an unpadded shared
+// plane W laid out so that every access of the step is free of bank
+// conflicts: element (y, x) at W[y*64 + 2 s_y(x/2) + x%2] with the 16-byte
+// chunk permutation s_y(k) = (k & 24) | ((h(y%8) ^ y/8 ^ k ^ k/8) & 7),
+// h = [0,4,1,5,2,6,3,7] (a CPU emulation of every access pattern: column
+// reads and writes, the in-column exchange, row reads and writes are
+// conflict-free; the in-row exchange read, whose 16 lanes share one x
+// parity, is two-way).  The 8 threads of a column are 8 lanes of one warp
+// (warp w owns columns 4w .. 4w+3; rows 4w .. 4w+3 in the row phase), so the
+// column exchanges need only warp barriers; block barriers remain for the
+// plane's arrival, the two transposes and the plane sums (4 against 8).
+// The arithmetic and its order are those of plane64_body: results are
+// bit-identical.
+__device__ __forceinline__ int w_idx(int y, int x) {
+  const int k = x >> 1, e = y & 7;
+  const int hh = (e >> 1) | ((e & 1) << 2);
+  return y * 64 + 2 * ((k & 24) | ((hh ^ (y >> 3) ^ k ^ (k >> 3)) & 7)) + (x & 1);
+}
+
+// 64-point transform of a column x held by 8 lanes (position t) of one warp:
+// thread t holds x[t + 8a]; the exchange goes through the column's own slots
+// of W (element (b, c) of the 8 x 8 exchange at row b + 8c).
+template <int SIGN>
+__device__ __forceinline__ void fft64_col_w(float2 *v, int x, int t, float2 *W, const float2 *tw) {
+  dft8f<SIGN>(v);
+  tw64<SIGN>(v, t, tw);
+  __syncwarp();
+#pragma unroll
+  for (int c = 0; c < 8; c++) W[w_idx(t + 8 * c, x)] = v[c];
+  __syncwarp();
+#pragma unroll
+  for (int b = 0; b < 8; b++) v[b] = W[w_idx(b + 8 * t, x)];
+  __syncwarp();
+  dft8f<SIGN>(v);
+}
+
+// The same for a row (element (b, c) at x = b + 8c of the row).
+template <int SIGN>
+__device__ __forceinline__ void fft64_row_w(float2 *v, int row, int t, float2 *W, const float2 *tw) {
+  dft8f<SIGN>(v);
+  tw64<SIGN>(v, t, tw);
+  __syncwarp();
+#pragma unroll
+  for (int c = 0; c < 8; c++) W[w_idx(row, t + 8 * c)] = v[c];
+  __syncwarp();
+#pragma unroll
+  for (int b = 0; b < 8; b++) v[b] = W[w_idx(row, b + 8 * t)];
+  __syncwarp();
+  dft8f<SIGN>(v);
+}
+
+template <int NZ>
+__device__ __forceinline__ void plane64w_body(const Mix64Table &T, int ii, int zz, int n, float2 *Es, float2 *Hs,
+                                              float2 *W, Plane64Shared &S, uint64_t *bar, uint32_t parity) {
+  const int nz = NZ ? NZ : T.nz;
+  const MixInst &P = T.inst[ii];
+  const int N = P.N, Na = P.Na;
+  const long long M = 4096LL * nz;
+  const long long zoff = (long long)zz * 4096;
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  // row phase: (y = row, x = tr + 8d); column phase: (y = ct + 8d, x = cx)
+  const int row = tid >> 3, tr = tid & 7;
+  const int cx = 4 * warp + (lane >> 3), ct = lane & 7;
+  float2 v[8];
+  float2 *work = P.work + zoff;
+  if (n > 0) {
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+      const int q = tid + 512 * j, y = q >> 5, k = q & 31;
+      cp_async16(W + w_idx(y, 2 * k), work + y * 64 + 2 * k);
+    }
+    cp_async_commit();
+  }
+  const int m2 = N - 1 - n;
+  const bool pair = (m2 < n);
+  const uint64_t pol_first = l2_policy_first();
+  if (tid == 0) plane64_stage(T, ii, zz, nz, n, Es, Hs, bar);
+  const int gi = row * 64 + tr;
+  float acc1[8], acc2[8];
+  float *a1 = P.acc[n < Na ? 0 : 1] + zoff + gi;
+  float *a2 = P.acc[m2 < Na ? 0 : 1] + zoff + gi;
+  const bool same_acc = (a1 == a2);
+  if (pair) {
+#pragma unroll
+    for (int d = 0; d < 8; d++) acc1[d] = a1[8 * d];
+    if (!same_acc) {
+#pragma unroll
+      for (int d = 0; d < 8; d++) acc2[d] = a2[8 * d];
+    }
+  }
+  if (warp < 2) {
+    double a = 0.0;
+    if (n > 0) {
+      const double *pp = P.part + (long long)(warp * N + n - 1) * nz;
+      for (int z = lane; z < nz; z += 32) a += pp[z];
+    }
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) {
+      const double ma = NZ ? a * (1.0 / (double)M) : a / (double)M;
+      int ea = 0;
+      if (n > 0 && isfinite(ma) && ma > 0.0) frexp(ma, &ea);
+      S.exp[warp] = ea;
+      const float hi = (float)ma;
+      S.mh[warp] = hi;
+      S.ml[warp] = (float)(ma - (double)hi);
+    }
+  }
+  const bool useA_q = (Na > 0 && n < Na);
+  const bool useA_d = !(n <= N - Na - 1);
+  if (n > 0) cp_async_wait_all();
+  __syncthreads();  // W, means, exponents (and, on entry, the twiddles and the barrier's initialisation)
+  if (n > 0) {
+    // inverse y transform (warp-local column phase), back into the column's slots
+#pragma unroll
+    for (int a = 0; a < 8; a++) v[a] = W[w_idx(ct + 8 * a, cx)];
+    fft64_col_w<+1>(v, cx, ct, W, S.tw);
+#pragma unroll
+    for (int d = 0; d < 8; d++) W[w_idx(ct + 8 * d, cx)] = v[d];
+    __syncthreads();
+    // inverse x transform (row phase; a warp owns its four rows)
+#pragma unroll
+    for (int d = 0; d < 8; d++) v[d] = W[w_idx(row, tr + 8 * d)];
+    fft64_row_w<+1>(v, row, tr, W, S.tw);
+  }
+  if (!mbar_wait(bar, parity, T.err[1])) {
+    atomicExch(T.err, 1);
+    mbar_wait(bar, parity, kWaitPolls);
+  }
+  if (n == 0) {
+#pragma unroll
+    for (int d = 0; d < 8; d++) {
+      const float2 e = swz(Es, row, tr + 8 * d);
+      v[d] = make_float2(useA_q ? e.x : e.y, useA_d ? e.x : e.y);
+    }
+  } else {
+    const int eq = S.exp[0], ed = S.exp[1];
+    const float sq = ldexpf(1.0f, -eq), sd = ldexpf(1.0f, -ed);
+    const float mq_hi = S.mh[0], mq_lo = S.ml[0];
+    const float md_hi = S.mh[1], md_lo = S.ml[1];
+#pragma unroll
+    for (int d = 0; d < 8; d++) {
+      const float2 e = swz(Es, row, tr + 8 * d);
+      const float eq_ = useA_q ? e.x : e.y, ed_ = useA_d ? e.x : e.y;
+      const float uq = fmaf(v[d].x, eq_, fmaf(mq_hi, eq_, mq_lo * eq_));
+      const float ud = fmaf(v[d].y, ed_, fmaf(md_hi, ed_, md_lo * ed_));
+      v[d] = make_float2(uq * sq, ud * sd);
+    }
+  }
+  const int Kq = (n == 0) ? 0 : P.K[n - 1] + S.exp[0];
+  const int Kd = (n == 0) ? 0 : P.K[N + n - 1] + S.exp[1];
+  if (zz == 0 && tid == 0) {
+    P.K[n] = Kq;
+    P.K[N + n] = Kd;
+  }
+  if (n <= P.hmax) {
+    float2 *hst = P.hist + (long long)n * M + zoff + gi;
+#pragma unroll
+    for (int d = 0; d < 8; d++) st_stream(hst + 8 * d, v[d], pol_first);
+  }
+  const int n0 = N / 2;
+  if (m2 <= n) {
+    const int Kref = (n == n0) ? Kq + (m2 == n ? Kd : P.K[N + m2]) : P.K[2 * N];
+    if (n == n0 && zz == 0 && tid == 0) P.K[2 * N] = Kref;
+    if (pair) {
+      const float f1 = ldexpf(1.0f, Kq + P.K[N + m2] - Kref);
+      const float f2 = ldexpf(1.0f, P.K[m2] + Kd - Kref);
+      if (same_acc) {
+#pragma unroll
+        for (int d = 0; d < 8; d++) {
+          const float2 h = swz(Hs, row, tr + 8 * d);
+          a1[8 * d] = acc1[d] + fmaf(v[d].x * h.y, f1, (h.x * v[d].y) * f2);
+        }
+      } else {
+#pragma unroll
+        for (int d = 0; d < 8; d++) {
+          const float2 h = swz(Hs, row, tr + 8 * d);
+          a1[8 * d] = acc1[d] + (v[d].x * h.y) * f1;
+          a2[8 * d] = acc2[d] + (h.x * v[d].y) * f2;
+        }
+      }
+    } else {
+      const float f = ldexpf(1.0f, Kq + Kd - Kref);
+#pragma unroll
+      for (int d = 0; d < 8; d++) a1[8 * d] += (v[d].x * v[d].y) * f;
+    }
+  }
+  float sq_ = 0.f, cq = 0.f, sd_ = 0.f, cd = 0.f;
+#pragma unroll
+  for (int d = 0; d < 8; d++) {
+    float e;
+    two_sum(sq_, v[d].x, sq_, e);
+    cq += e;
+    two_sum(sd_, v[d].y, sd_, e);
+    cd += e;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const float s2 = __shfl_down_sync(0xffffffffu, sq_, o), c2 = __shfl_down_sync(0xffffffffu, cq, o);
+    const float t2 = __shfl_down_sync(0xffffffffu, sd_, o), d2 = __shfl_down_sync(0xffffffffu, cd, o);
+    float e;
+    two_sum(sq_, s2, sq_, e);
+    cq += c2 + e;
+    two_sum(sd_, t2, sd_, e);
+    cd += d2 + e;
+  }
+  if (lane == 0) {
+    S.red[0][warp] = (double)sq_ + (double)cq;
+    S.red[1][warp] = (double)sd_ + (double)cd;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    double aq = lane < 16 ? S.red[0][lane] : 0.0;
+    double ad = lane < 16 ? S.red[1][lane] : 0.0;
+    for (int o = 8; o > 0; o >>= 1) {
+      aq += __shfl_down_sync(0xffffffffu, aq, o);
+      ad += __shfl_down_sync(0xffffffffu, ad, o);
+    }
+    if (lane == 0) {
+      P.part[(long long)n * nz + zz] = aq;
+      P.part[(long long)(N + n) * nz + zz] = ad;
+    }
+  }
+  if (n == N - 1) return;
+  // forward x transform (row phase), back into the rows; then the columns
+  fft64_row_w<-1>(v, row, tr, W, S.tw);
+#pragma unroll
+  for (int d = 0; d < 8; d++) W[w_idx(row, tr + 8 * d)] = v[d];
+  __syncthreads();
+#pragma unroll
+  for (int a = 0; a < 8; a++) v[a] = W[w_idx(ct + 8 * a, cx)];
+  fft64_col_w<-1>(v, cx, ct, W, S.tw);
+#pragma unroll
+  for (int d = 0; d < 8; d++) work[(ct + 8 * d) * 64 + cx] = v[d];
+}
+
+template <int NZ>
+__global__ void __launch_bounds__(512, 2) k_mix_plane64w(const __grid_constant__ Mix64Table T,
+                                                         const float2 *__restrict__ tw_g, int n) {
+  extern __shared__ __align__(16) unsigned char dsm_raw[];
+  float2 *Es = reinterpret_cast<float2 *>(dsm_raw + ((1024 - (smem_u32(dsm_raw) & 1023)) & 1023));
+  float2 *Hs = Es + 4096;
+  float2 *W = Hs + 4096;
+  __shared__ Plane64Shared S;
+  __shared__ __align__(8) uint64_t s_bar;
+  const int nz = NZ ? NZ : T.nz;
+  const int ii = blockIdx.x / nz;
+  const int zz = blockIdx.x - ii * nz;
+  if (n >= T.inst[ii].N) return;
+  if (threadIdx.x == 0) mbar_init(&s_bar, 1);
+  if (threadIdx.x < 64) S.tw[threadIdx.x] = tw_g[threadIdx.x];
+  plane64w_body<NZ>(T, ii, zz, n, Es, Hs, W, S, &s_bar, 0);
+}
+
+// ---------------------------------------------------------------------------
 // The whole sweep in one persistent launch
 // ---------------------------------------------------------------------------
 // k_mix_sweep64 runs every step of the propagator sweep of a batch of
@@ -726,6 +983,33 @@ cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, con
   if (ninst <= 0) return cudaSuccess;
   const int smem = 1024 + 2 * 4096 * (int)sizeof(float2) + kPlanePad * (int)sizeof(float2);
   auto kfn = (nz == 64) ? k_mix_plane64<64> : k_mix_plane64<0>;
+  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return e;
+  for (int i0 = 0; i0 < ninst; i0 += kMix64MaxInst) {
+    const int cnt = ninst - i0 < kMix64MaxInst ? ninst - i0 : kMix64MaxInst;
+    Mix64Table T;
+    memset(&T, 0, sizeof T);
+    for (int k = 0; k < cnt; k++) {
+      T.inst[k] = insts[i0 + k];
+      T.tmE[k] = tmE[i0 + k];
+      T.tmH[k] = tmH[i0 + k];
+    }
+    T.err = err;
+    T.nz = nz;
+    kfn<<<nz * cnt, 512, smem, st>>>(T, reinterpret_cast<const float2 *>(tw64), n);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_mix_plane64w(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
+                                int nz, const void *tw64, int n, int *err, cudaStream_t st) {
+  if (ninst <= 0) return cudaSuccess;
+  const int smem = 1024 + 3 * 4096 * (int)sizeof(float2);
+  auto kfn = (nz == 64) ? k_mix_plane64w<64> : k_mix_plane64w<0>;
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);

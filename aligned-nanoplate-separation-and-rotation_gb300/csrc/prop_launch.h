@@ -64,6 +64,10 @@ cudaError_t launch_mix_sweep64(const MixInst *insts, const CUtensorMap *tmE, con
 // insts, tmE, tmH: host arrays of the active instances in job order (nz CTAs each)
 cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
                                int nz, const void *tw64, int n, int *err, cudaStream_t st);
+// The same plane pass with warp-local column transforms (k_mix_plane64w):
+// bit-identical results, a different launch shape.
+cudaError_t launch_mix_plane64w(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
+                                int nz, const void *tw64, int n, int *err, cudaStream_t st);
 // z pass of the 64 x 64-plane instances for nz = 64 or 128 (tw: the nz-point
 // twiddles); tx: x columns per CTA (8, 16 or 32); jobs built for that width
 cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw, int nx, int ny, int nz, int tx,

@@ -29,7 +29,7 @@ EXPORTS = ("scft_last_error", "scft_version", "scft_create", "scft_destroy", "sc
            "scft_profile_step", "scft_diblock_density_noalloc", "scft_set_sweep_groups", "scft_autotune",
            "scft_set_fields_all", "scft_set_wait_limit", "scft_fp64_fma_rate",
            "scft_set_persistent", "scft_get_schedule", "scft_profile_sweep",
-           "scft_get_fft_plan", "scft_step_fields")
+           "scft_get_fft_plan", "scft_step_fields", "scft_set_plane_form", "scft_get_plane_form")
 
 
 class ScftError(RuntimeError):
@@ -108,6 +108,8 @@ def load(path: str | None = None):
     lib.scft_set_wait_limit.argtypes = [vp, ctypes.c_int]
     lib.scft_fp64_fma_rate.argtypes = [ctypes.c_int, dp]
     lib.scft_set_persistent.argtypes = [vp, ctypes.c_int]
+    lib.scft_set_plane_form.argtypes = [vp, ctypes.c_int]
+    lib.scft_get_plane_form.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     lib.scft_profile_sweep.argtypes = [vp, ctypes.c_int, dp, dp]
     lib.scft_step_fields.argtypes = [vp, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_void_p]
     lib.scft_get_fft_plan.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
@@ -283,10 +285,16 @@ class Context:
     def set_persistent(self, on: bool):
         _check(load().scft_set_persistent(self._h, int(bool(on))))
 
+    def set_plane_form(self, form: int):
+        _check(load().scft_set_plane_form(self._h, int(form)))
+
     def schedule(self) -> dict:
         v = [ctypes.c_int() for _ in range(4)]
         _check(load().scft_get_schedule(self._h, *[ctypes.byref(x) for x in v]))
-        return {"groups": v[0].value, "phases": v[1].value, "col_tile": v[2].value, "persistent": bool(v[3].value)}
+        f = ctypes.c_int()
+        _check(load().scft_get_plane_form(self._h, ctypes.byref(f)))
+        return {"groups": v[0].value, "phases": v[1].value, "col_tile": v[2].value, "persistent": bool(v[3].value),
+                "plane_form": f.value}
 
     def autotune(self, reps=3) -> dict:
         g, ph, t, ms = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()

@@ -39,7 +39,7 @@ METRIC = "SCFT iters/s @64^3,N=100"
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant
 # kernel, from an ncu capture of the same workload (the paired plane-pass step;
 # profiles/mixed_kernels_sweep15_64_N100_ncu.txt).  Only valid for that workload.
-NCU_TRAFFIC = {("sweep15_64_N100", "mixed"): 125.905664e6 + 16.460032e6}
+NCU_TRAFFIC = {("sweep15_64_N100", "k_mix_plane64"): 125.905664e6 + 16.460032e6}
 UNIT = "iters/s"
 
 
@@ -341,6 +341,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true", help="keep the default launch schedule")
     ap.add_argument("--persistent", choices=["auto", "on", "off"], default="auto",
                     help="persistent sweep of 64^3 groups: autotuned (auto) or fixed")
+    ap.add_argument("--plane-form", choices=["auto", "0", "1"], default="auto",
+                    help="64-point plane pass: block-barrier (0) or warp-local (1) form, or autotuned")
     ap.add_argument("--sweep-groups", type=int, default=0, help="fixed number of sweep groups (0: autotune)")
     ap.add_argument("--sweep-phases", type=int, default=1, help="sequential phases with --sweep-groups")
     ap.add_argument("--plain-max", type=int, default=None,
@@ -417,11 +419,13 @@ def main():
     ctx.calc_poly_density()
     schedule = None
     if form == "mixed":
-        if args.sweep_groups > 0 or args.no_autotune or args.persistent != "auto":
+        if args.sweep_groups > 0 or args.no_autotune or args.persistent != "auto" or args.plane_form != "auto":
             if args.sweep_groups > 0:
                 ctx.set_sweep_groups(args.sweep_groups, args.sweep_phases)
             if args.persistent != "auto":
                 ctx.set_persistent(args.persistent == "on")
+            if args.plane_form != "auto":
+                ctx.set_plane_form(int(args.plane_form))
             schedule = dict(ctx.schedule(), tuned=False)
         else:
             schedule = dict(ctx.autotune(3), tuned=True)
@@ -590,7 +594,8 @@ def main():
     nz0 = params[0].Nx[2]
     xy64 = all(p.Nx[0] == 64 and p.Nx[1] == 64 and p.Nx[2] == nz0 for p in params)
     col_fast = {64: "k_mix_col64", 128: "k_mix_col128"}.get(nz0) if xy64 else None
-    kernel_names = {"mixed": ("k_mix_plane64" if xy64 else "k_mix_prop_plane", col_fast or "k_col_fft<float>"),
+    p64name = "k_mix_plane64w" if sched.get("plane_form") else "k_mix_plane64"
+    kernel_names = {"mixed": (p64name if xy64 else "k_mix_prop_plane", col_fast or "k_col_fft<float>"),
                     "plain": ("k_prop_plane_f64", "k_col_fft<double> (bond kernel)")}
     dom = "plane" if prof["ms_plane"] >= prof["ms_col"] else "col"
     ms_k = prof["ms_" + dom]
@@ -611,7 +616,7 @@ def main():
                     "per_step_kernels_alone": per_step}
     else:
         roofline = {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                    "traffic": NCU_TRAFFIC.get((args.workload, form)) if dom == "plane" else None,
+                    "traffic": NCU_TRAFFIC.get((args.workload, per_step["kernel"])),
                     "kernel": per_step["kernel"], "peak_kind": peak_kind, "ms_per_launch": ms_k,
                     "algorithmic_bytes_per_launch": by,
                     "other_kernel_ms_per_launch": per_step["other_kernel_ms_per_launch"]}

@@ -297,6 +297,14 @@ int scft_set_persistent(scft_ctx *ctx, int on);
  * does not apply) and whether the sweep is persistent. */
 int scft_get_schedule(scft_ctx *ctx, int *groups, int *phases, int *col_tile, int *persistent);
 
+/* Form of the mixed form's 64-point plane pass (no counterpart in the
+ * reference): 0 exchanges through a padded shared plane with block barriers
+ * (k_mix_plane64), 1 loads the working plane asynchronously into a swizzled
+ * shared plane and transforms columns inside one warp (k_mix_plane64w).
+ * Results are bit-identical; the autotuner picks one. */
+int scft_set_plane_form(scft_ctx *ctx, int form);
+int scft_get_plane_form(scft_ctx *ctx, int *form);
+
 /* The FFT stage plan of instance inst along axis 0 (x), 1 or 2: *nst radices
  * in application order in radix[0..7] (the rest 0).  Generic transforms
  * only; the 64-point kernels use a fixed 8 x 8 four-step transform. */

@@ -103,3 +103,36 @@ def test_dependency_wait_that_runs_out_stops_the_sweep(S):
         c.calc_poly_density()
         H = c.calc_H()
     np.testing.assert_array_equal(H, ref[0])
+
+
+@pytest.mark.parametrize("case", ["uneven", "nz128", "single_block"])
+def test_warp_local_plane_form_is_bit_identical(S, case):
+    """The two forms of the 64-point plane pass (block-barrier exchanges and
+    warp-local columns over the swizzled, asynchronously loaded plane) do the
+    same arithmetic in the same order."""
+    from scft.workloads import plate_params, seeded_fields
+
+    if case == "uneven":
+        ps, fields = batch(S, [14, 11, 11, 6])
+    elif case == "single_block":
+        ps, fields = batch(S, [8, 8], fA=1.0)
+    else:
+        ps = [plate_params(0.0, N=9, grid=(64, 64, 128), box_rg=(6.4, 6.4, 12.8), precision=S.PREC_MIXED,
+                           centers=((0.5, 0.5, 0.4), (0.5, 0.5, 0.6)))]
+        fields = [seeded_fields(ps[0], 71)]
+    res = []
+    for form in (0, 1):
+        with S.Context(ps) as c:
+            c.set_sweep_groups(2 if len(ps) > 1 else 1, 1)
+            c.set_persistent(False)
+            c.set_plane_form(form)
+            for k, f in enumerate(fields):
+                c.set_fields(k, f)
+            c.calc_poly_density()
+            c.update_1s(3)
+            assert c.schedule()["plane_form"] == form
+            res.append((c.calc_H().copy(), [c.density(k)[:2] for k in range(len(ps))]))
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+    for (ra, rb), (qa, qb) in zip(res[0][1], res[1][1]):
+        np.testing.assert_array_equal(ra, qa)
+        np.testing.assert_array_equal(rb, qb)
