@@ -492,7 +492,10 @@ def main():
     torch.cuda.synchronize()
     t_e2e = allmax(time.perf_counter() - t0)
     e2e = {"value": job_rate(n_inst * e2e_steps, world, t_e2e), "unit": UNIT,
-           "h2d_bytes_per_step": int(sum(7 * 16 * m for m in M)), "d2h_bytes_per_step": int(5 * 8 * n_inst)}
+           "h2d_bytes_per_step": int(sum(7 * 16 * m for m in M)),
+           # H (5 doubles per instance) and, in the mixed form, the realness
+           # check's maxima (128 doubles per instance) that the call reads back
+           "d2h_bytes_per_step": int(5 * 8 * n_inst + (128 * 8 * n_inst if form == "mixed" else 0))}
 
     # ---- the plain FP64 method on the same batch, same iteration count:
     # its rate (the metric's comparison) and the mixed form's H error
