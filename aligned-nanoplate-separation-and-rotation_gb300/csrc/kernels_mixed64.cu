@@ -96,7 +96,8 @@ struct Plane64Shared {
 // and, on a paired step n (partner step m2 = N - 1 - n < n), of the stored
 // history plane m2, into Es / Hs, completing on `bar` (E rows z*64 + y of a
 // 64 nz-row tensor; history rows (m2*nz + z)*64 + y).
-__device__ __forceinline__ void plane64_stage(const Mix64Table &T, int ii, int zz, int nz, int n, float2 *Es,
+template <class TT>
+__device__ __forceinline__ void plane64_stage(const TT &T, int ii, int zz, int nz, int n, float2 *Es,
                                               float2 *Hs, uint64_t *bar) {
   const MixInst &P = T.inst[ii];
   const int m2 = P.N - 1 - n;
@@ -117,8 +118,8 @@ __device__ __forceinline__ void plane64_stage(const Mix64Table &T, int ii, int z
 // passed a block barrier.
 // STAGE: thread 0 issues plane64_stage itself, right after its working-plane
 // loads (the one-launch-per-step kernel); otherwise the caller has issued it.
-template <int NZ, bool STAGE>
-__device__ __forceinline__ void plane64_body(const Mix64Table &T, int ii, int zz, int n, float2 *Es, float2 *Hs,
+template <int NZ, bool STAGE, class TT>
+__device__ __forceinline__ void plane64_body(const TT &T, int ii, int zz, int n, float2 *Es, float2 *Hs,
                                              float2 *buf, Plane64Shared &S, uint64_t *bar, uint32_t parity) {
   const int nz = NZ ? NZ : T.nz;
   const MixInst &P = T.inst[ii];
@@ -321,8 +322,8 @@ __device__ __forceinline__ void plane64_body(const Mix64Table &T, int ii, int zz
 // plane and history plane (32 KB each), then the padded exchange/transpose
 // plane (36.9 KB); 101 KB, two CTAs per SM.
 // NZ: nz known at compile time (64), or 0 to read it from the table.
-template <int NZ>
-__global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ Mix64Table T,
+template <int NZ, int CAP>
+__global__ void __launch_bounds__(512, 2) k_mix_plane64(const __grid_constant__ Mix64TableT<CAP> T,
                                                         const float2 *__restrict__ tw_g, int n) {
   extern __shared__ __align__(16) unsigned char dsm_raw[];
   float2 *Es = reinterpret_cast<float2 *>(dsm_raw + ((1024 - (smem_u32(dsm_raw) & 1023)) & 1023));
@@ -536,8 +537,8 @@ __device__ __forceinline__ void fft64_row_w(float2 *v, int row, int t, float2 *W
   dft8f<SIGN>(v);
 }
 
-template <int NZ>
-__device__ __forceinline__ void plane64w_body(const Mix64Table &T, int ii, int zz, int n, float2 *Es, float2 *Hs,
+template <int NZ, class TT>
+__device__ __forceinline__ void plane64w_body(const TT &T, int ii, int zz, int n, float2 *Es, float2 *Hs,
                                               float2 *W, Plane64Shared &S, uint64_t *bar, uint32_t parity) {
   const int nz = NZ ? NZ : T.nz;
   const MixInst &P = T.inst[ii];
@@ -720,8 +721,8 @@ __device__ __forceinline__ void plane64w_body(const Mix64Table &T, int ii, int z
   for (int d = 0; d < 8; d++) work[(ct + 8 * d) * 64 + cx] = v[d];
 }
 
-template <int NZ>
-__global__ void __launch_bounds__(512, 2) k_mix_plane64w(const __grid_constant__ Mix64Table T,
+template <int NZ, int CAP>
+__global__ void __launch_bounds__(512, 2) k_mix_plane64w(const __grid_constant__ Mix64TableT<CAP> T,
                                                          const float2 *__restrict__ tw_g, int n) {
   extern __shared__ __align__(16) unsigned char dsm_raw[];
   float2 *Es = reinterpret_cast<float2 *>(dsm_raw + ((1024 - (smem_u32(dsm_raw) & 1023)) & 1023));
@@ -978,18 +979,20 @@ cudaError_t launch_mix_sweep64(const MixInst *insts, const CUtensorMap *tmE, con
   return cudaGetLastError();
 }
 
-cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
-                               int nz, const void *tw64, int n, int *err, cudaStream_t st) {
-  if (ninst <= 0) return cudaSuccess;
-  const int smem = 1024 + 2 * 4096 * (int)sizeof(float2) + kPlanePad * (int)sizeof(float2);
-  auto kfn = (nz == 64) ? k_mix_plane64<64> : k_mix_plane64<0>;
+
+// One plane-pass launch per chunk of at most CAP instances, the table by value.
+template <int CAP, class K>
+static cudaError_t launch_plane64_chunks(K kfn64, K kfn0, const MixInst *insts, const CUtensorMap *tmE,
+                                         const CUtensorMap *tmH, int ninst, int nz, const void *tw64, int n, int *err,
+                                         int smem, cudaStream_t st) {
+  auto kfn = (nz == 64) ? kfn64 : kfn0;
   cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   if (e != cudaSuccess) return e;
   e = cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
   if (e != cudaSuccess) return e;
-  for (int i0 = 0; i0 < ninst; i0 += kMix64MaxInst) {
-    const int cnt = ninst - i0 < kMix64MaxInst ? ninst - i0 : kMix64MaxInst;
-    Mix64Table T;
+  for (int i0 = 0; i0 < ninst; i0 += CAP) {
+    const int cnt = ninst - i0 < CAP ? ninst - i0 : CAP;
+    Mix64TableT<CAP> T;
     memset(&T, 0, sizeof T);
     for (int k = 0; k < cnt; k++) {
       T.inst[k] = insts[i0 + k];
@@ -1009,27 +1012,28 @@ cudaError_t launch_mix_plane64w(const MixInst *insts, const CUtensorMap *tmE, co
                                 int nz, const void *tw64, int n, int *err, cudaStream_t st) {
   if (ninst <= 0) return cudaSuccess;
   const int smem = 1024 + 3 * 4096 * (int)sizeof(float2);
-  auto kfn = (nz == 64) ? k_mix_plane64w<64> : k_mix_plane64w<0>;
-  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  if (e != cudaSuccess) return e;
-  e = cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-  if (e != cudaSuccess) return e;
-  for (int i0 = 0; i0 < ninst; i0 += kMix64MaxInst) {
-    const int cnt = ninst - i0 < kMix64MaxInst ? ninst - i0 : kMix64MaxInst;
-    Mix64Table T;
-    memset(&T, 0, sizeof T);
-    for (int k = 0; k < cnt; k++) {
-      T.inst[k] = insts[i0 + k];
-      T.tmE[k] = tmE[i0 + k];
-      T.tmH[k] = tmH[i0 + k];
-    }
-    T.err = err;
-    T.nz = nz;
-    kfn<<<nz * cnt, 512, smem, st>>>(T, reinterpret_cast<const float2 *>(tw64), n);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) return e;
-  }
-  return cudaSuccess;
+  if (ninst <= 4)
+    return launch_plane64_chunks<4>(k_mix_plane64w<64, 4>, k_mix_plane64w<0, 4>, insts, tmE, tmH, ninst, nz, tw64, n,
+                                    err, smem, st);
+  if (ninst <= 16)
+    return launch_plane64_chunks<16>(k_mix_plane64w<64, 16>, k_mix_plane64w<0, 16>, insts, tmE, tmH, ninst, nz, tw64,
+                                     n, err, smem, st);
+  return launch_plane64_chunks<kMix64MaxInst>(k_mix_plane64w<64, kMix64MaxInst>, k_mix_plane64w<0, kMix64MaxInst>,
+                                              insts, tmE, tmH, ninst, nz, tw64, n, err, smem, st);
+}
+
+cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
+                               int nz, const void *tw64, int n, int *err, cudaStream_t st) {
+  if (ninst <= 0) return cudaSuccess;
+  const int smem = 1024 + 2 * 4096 * (int)sizeof(float2) + kPlanePad * (int)sizeof(float2);
+  if (ninst <= 4)
+    return launch_plane64_chunks<4>(k_mix_plane64<64, 4>, k_mix_plane64<0, 4>, insts, tmE, tmH, ninst, nz, tw64, n,
+                                    err, smem, st);
+  if (ninst <= 16)
+    return launch_plane64_chunks<16>(k_mix_plane64<64, 16>, k_mix_plane64<0, 16>, insts, tmE, tmH, ninst, nz, tw64, n,
+                                     err, smem, st);
+  return launch_plane64_chunks<kMix64MaxInst>(k_mix_plane64<64, kMix64MaxInst>, k_mix_plane64<0, kMix64MaxInst>,
+                                              insts, tmE, tmH, ninst, nz, tw64, n, err, smem, st);
 }
 
 cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw, int nx, int ny, int nz, int tx,

@@ -30,14 +30,19 @@ cudaError_t launch_mix_prop_plane(const LaunchShape &ls, const PropJob *jobs, in
 // parameter (15.4 KB: TMA descriptors of each instance's Boltzmann and
 // history arrays, the instance views, the error word); larger batches are
 // launched in chunks.
+// The per-step launchers pass the smallest table that holds the launch's
+// instances (CAP 4, 16 or 48): a kernel's parameter block is copied to the
+// GPU with every launch, and the 48-instance table (15.4 KB) cost as much
+// launch time as the kernel itself.
 constexpr int kMix64MaxInst = 48;
-struct Mix64Table {
-  CUtensorMap tmE[kMix64MaxInst];  // E32 as 4096 rows x 128 floats, boxes of 64 rows x 32 floats, 128B swizzle
-  CUtensorMap tmH[kMix64MaxInst];  // hist32 as 4096 (hmax + 1) rows x 128 floats, same boxes
-  MixInst inst[kMix64MaxInst];
-  int *err;                        // set to 1 when an mbarrier wait runs out
-  int nz;                          // z planes per instance (64 x 64 xy planes)
+template <int CAP> struct Mix64TableT {
+  CUtensorMap tmE[CAP];  // E32 as 4096 rows x 128 floats, boxes of 64 rows x 32 floats, 128B swizzle
+  CUtensorMap tmH[CAP];  // hist32 as 4096 (hmax + 1) rows x 128 floats, same boxes
+  MixInst inst[CAP];
+  int *err;              // set to 1 when an mbarrier wait runs out
+  int nz;                // z planes per instance (64 x 64 xy planes)
 };
+typedef Mix64TableT<kMix64MaxInst> Mix64Table;
 // The whole mixed sweep of a batch of 64 x 64 x 64 instances in one
 // persistent launch (k_mix_sweep64): the kernel parameter adds to the plane
 // pass's table each instance's per-axis h table of the z pass and the task
