@@ -220,7 +220,6 @@ int scft_grad_geom(scft_ctx *c, double *out) {
   if (!out) return fail(SCFT_ERR_ARG, "null output");
   int st = SCFT_OK;
   API_BODY(st = scft::ctx_grad_geom(c, out));
-  if (st == SCFT_ERR_UNSUPPORTED) return fail(st, "geometric derivatives are built for bare plates of the reference shape");
   return st;
 }
 
@@ -303,7 +302,7 @@ int scft_get_schedule(scft_ctx *c, int *groups, int *phases, int *col_tile, int 
   if (int s = check_ctx(c, 0)) return s;
   if (groups) *groups = c->sweep_streams;
   if (phases) *phases = c->sweep_phases;
-  if (col_tile) *col_tile = (c->colfast || c->anyfast) ? c->col64_tx : 0;
+  if (col_tile) *col_tile = (c->colfast || c->anyfast || c->xy128) ? c->col64_tx : 0;
   if (persistent) *persistent = c->sweep_persistent;
   return SCFT_OK;
 }

@@ -21,6 +21,7 @@
 #include "fft_core.cuh"
 #include "prop_launch.h"
 #include "grad.h"
+#include "plate_profile.cuh"
 
 namespace scft {
 
@@ -155,7 +156,8 @@ struct PlateArgs {
   int shape;
 };
 
-// code/initialize.cpp:578-612 (explicit_nanorod), code/array_utils.cpp:588-646
+// code/initialize.cpp:578-612 (explicit_nanorod), code/array_utils.cpp:588-646;
+// the profile of either shape is plate_value (plate_profile.cuh)
 __global__ void k_plate(double2 *out, PlateArgs a, int accumulate) {
   const long long M = (long long)a.nx * a.ny * a.nz;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < M; i += (long long)gridDim.x * blockDim.x) {
@@ -171,38 +173,7 @@ __global__ void k_plate(double2 *out, PlateArgs a, int accumulate) {
       else if (r < -0.5 * a.L[d]) r += a.L[d];
       dr[d] = r;
     }
-    double v;
-    if (a.shape == SCFT_PLATE_CUBOID) {
-      // slab of thickness len along u, square of side 2*rad in the plane:
-      // in-plane axes e1 = normalised (u x z) (or u x y when u is along z), e2 = u x e1
-      double e1[3];
-      if (fabs(a.u[2]) < 0.9) {
-        e1[0] = a.u[1]; e1[1] = -a.u[0]; e1[2] = 0.0;
-      } else {
-        e1[0] = 0.0; e1[1] = a.u[2]; e1[2] = -a.u[1];
-      }
-      const double n1 = sqrt(e1[0] * e1[0] + e1[1] * e1[1] + e1[2] * e1[2]);
-      for (int d = 0; d < 3; d++) e1[d] /= n1;
-      const double e2[3] = {a.u[1] * e1[2] - a.u[2] * e1[1], a.u[2] * e1[0] - a.u[0] * e1[2],
-                            a.u[0] * e1[1] - a.u[1] * e1[0]};
-      const double p0 = a.u[0] * dr[0] + a.u[1] * dr[1] + a.u[2] * dr[2];
-      const double p1 = e1[0] * dr[0] + e1[1] * dr[1] + e1[2] * dr[2];
-      const double p2 = e2[0] * dr[0] + e2[1] * dr[1] + e2[2] * dr[2];
-      v = 0.125 * erfc((fabs(p0) - 0.5 * a.len) / a.xi) * erfc((fabs(p1) - a.rad) / a.xi) *
-          erfc((fabs(p2) - a.rad) / a.xi);
-    } else {
-      double udr = 0.0;
-      for (int d = 0; d < 3; d++) udr += a.u[d] * dr[d];
-      double mag = 0.0, dum;
-      dum = a.u[1] * dr[2] - a.u[2] * dr[1];
-      mag += dum * dum;
-      dum = a.u[2] * dr[0] - a.u[0] * dr[2];
-      mag += dum * dum;
-      dum = a.u[0] * dr[1] - a.u[1] * dr[0];
-      mag += dum * dum;
-      const double ucr = sqrt(mag);
-      v = 0.25 * erfc((fabs(udr) - 0.5 * a.len) / a.xi) * erfc((fabs(ucr) - a.rad) / a.xi);
-    }
+    const double v = plate_value(a.shape, dr, a.u, a.len, a.rad, a.xi);
     if (accumulate) out[i] = make_double2(out[i].x + v, out[i].y);
     else out[i] = make_double2(v, 0.0);
   }
@@ -382,6 +353,23 @@ void validate(const scft_params &p) {
   if (p.Nx[2] > 768) throw ScftError(SCFT_ERR_UNSUPPORTED, "Nx[2] above 768 is not supported by the z pass");
 }
 
+// Per-axis h_d = 1 - exp(-k_d^2/6) with get_k's branch
+// (code/array_utils.cpp:248-265), g(k) = prod_d (1 - h_d), as [hx | hy | hz]
+// for the specialised z passes.  parity_xy: x and y in the parity-major order
+// of the 128 x 128 plane pass (wavenumber k at position (k % 2) n/2 + k / 2).
+std::vector<float> axis_h_table(const scft_params &p, bool parity_xy) {
+  std::vector<float> ht;
+  for (int d = 0; d < 3; d++)
+    for (int pos = 0; pos < p.Nx[d]; pos++) {
+      const int h = p.Nx[d] / 2;
+      const int nn = (parity_xy && d < 2) ? 2 * (pos % h) + pos / h : pos;
+      const double k = (double(nn) < double(p.Nx[d]) / 2.) ? 2 * kPI * double(nn) / p.L[d]
+                                                          : 2 * kPI * double(nn - p.Nx[d]) / p.L[d];
+      ht.push_back((float)(-std::expm1(-k * k / 6.0)));
+    }
+  return ht;
+}
+
 void setup_instance(scft_ctx *c, Instance &I, int idx) {
   const scft_params &p = I.p;
   I.N = p.Nda + p.Ndb;
@@ -487,16 +475,7 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
     I.acc32[1] = dalloc<float>(c, M);
     I.part = dalloc<double>(c, (size_t)2 * I.N * g.nz);
     I.K = dalloc<int>(c, (size_t)2 * I.N + 1);
-    // per-axis h_d = 1 - exp(-k_d^2/6) with get_k's branch
-    // (code/array_utils.cpp:248-265); g(k) = prod_d (1 - h_d)
-    std::vector<float> ht;
-    for (int d = 0; d < 3; d++)
-      for (int nn = 0; nn < p.Nx[d]; nn++) {
-        const double k = (double(nn) < double(p.Nx[d]) / 2.) ? 2 * kPI * double(nn) / p.L[d]
-                                                            : 2 * kPI * double(nn - p.Nx[d]) / p.L[d];
-        ht.push_back((float)(-std::expm1(-k * k / 6.0)));
-      }
-    I.htab32 = dupload(c, ht);  // alpha, beta: mix_coefficients_final, once the plates fix phiD, phiG
+    I.htab32 = dupload(c, axis_h_table(p, false));  // alpha, beta: mix_coefficients_final, once the plates fix phiD, phiG
   }
   I.qpart = dalloc<double2>(c, g.nz);
   I.scal = dalloc<double2>(c, kNumScalars);
@@ -705,7 +684,7 @@ void setup_plates(scft_ctx *c, Instance &I) {
 // TMA descriptor of a float2 array seen as `rows` rows of 64 float2 (128
 // floats), boxes of 64 rows x 32 floats with the 128-byte swizzle; the entry
 // point comes from the driver (cuTensorMapEncodeTiled) through the runtime.
-CUtensorMap tensor_map_rows(const float2 *base, unsigned long long rows) {
+CUtensorMap tensor_map_rows(const float2 *base, unsigned long long rows, unsigned row_floats) {
   typedef CUresult (*EncodeFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -719,8 +698,8 @@ CUtensorMap tensor_map_rows(const float2 *base, unsigned long long rows) {
     encode = reinterpret_cast<EncodeFn>(fn);
   }
   CUtensorMap m;
-  const cuuint64_t dims[2] = {128, rows};
-  const cuuint64_t strides[1] = {128 * sizeof(float)};
+  const cuuint64_t dims[2] = {row_floats, rows};
+  const cuuint64_t strides[1] = {row_floats * sizeof(float)};
   const cuuint32_t box[2] = {32, 64};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = encode(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2 *>(base), dims, strides, box, estr,
@@ -756,6 +735,7 @@ void check_device_error(scft_ctx *c) {
 }
 
 ColJob *col64_jobs(scft_ctx *c) { return c->d_mix64_cj_tx[c->col64_tx == 8 ? 0 : (c->col64_tx == 16 ? 1 : 2)]; }
+ColJob *col128_jobs(scft_ctx *c) { return c->d_mix128_cj_tx[c->col64_tx == 8 ? 0 : (c->col64_tx == 16 ? 1 : 2)]; }
 
 // Sweep groups: the job order is cut into `sweep_phases` contiguous phases and
 // each phase into `sweep_streams` contiguous groups, all of about equal N * M.
@@ -1084,6 +1064,12 @@ void build_jobs(scft_ctx *c) {
     for (auto &I : c->inst)
       if (I.p.Nx[0] != 64 || I.p.Nx[1] != 64 || I.p.Nx[2] != c->inst[0].p.Nx[2]) c->xy64 = 0;
     c->colfast = c->xy64 && (c->inst[0].p.Nx[2] == 64 || c->inst[0].p.Nx[2] == 128);
+    {
+      const int nz0 = c->inst[0].p.Nx[2];
+      c->xy128 = (nz0 == 64 || nz0 == 128 || nz0 == 256) && c->d_tw32_64 && c->d_tw32_128 && c->d_tw32_z;
+      for (auto &I : c->inst)
+        if (I.p.Nx[0] != 128 || I.p.Nx[1] != 128 || I.p.Nx[2] != nz0) c->xy128 = 0;
+    }
     auto is64 = [&](int k) {
       const int *X = c->inst[k].p.Nx;
       return X[0] == 64 && X[1] == 64 && X[2] == 64;
@@ -1171,6 +1157,34 @@ void build_jobs(scft_ctx *c) {
         c->d_mix64_cj_tx[t] = dupload(c, cj64);
       }
     }
+    if (c->xy128) {
+      // parity-major factor tables, z-pass jobs (128 x (128 / tx) per instance),
+      // instance views and tensor maps of rows of 128 float2
+      c->mix64_tab.clear();
+      c->tmE.clear();
+      c->tmH.clear();
+      for (int t = 0; t < 3; t++) {
+        const int tx = 8 << t;
+        std::vector<ColJob> cj;
+        for (int oi = 0; oi < n; oi++) {
+          Instance &I = c->inst[order[oi]];
+          for (int y = 0; y < 128; y++)
+            for (int x0 = 0; x0 < 128; x0 += tx) cj.push_back(ColJob{I.work32, I.htab32, I.geom, x0, y});
+        }
+        c->d_mix128_cj_tx[t] = dupload(c, cj);
+      }
+      for (int oi = 0; oi < n; oi++) {
+        Instance &I = c->inst[order[oi]];
+        const std::vector<float> ht = axis_h_table(I.p, true);
+        CK(cudaMemcpyAsync(I.htab32, ht.data(), sizeof(float) * ht.size(), cudaMemcpyHostToDevice, c->st));
+        c->mix64_tab.push_back(c->h_mi[order[oi]]);
+        const unsigned long long rows = 128ULL * (unsigned long long)I.p.Nx[2];
+        c->tmE.push_back(tensor_map_rows(I.E32, rows, 256));
+        c->tmH.push_back(tensor_map_rows(I.hist32, rows * (unsigned long long)(I.hmax + 1), 256));
+      }
+      CK(cudaStreamSynchronize(c->st));  // the host tables are released
+      ensure_err(c);
+    }
     if (c->xy64 || c->anyfast) {
       c->mix64_tab.clear();
       c->tmE.clear();
@@ -1180,8 +1194,8 @@ void build_jobs(scft_ctx *c) {
         Instance &I = c->inst[order[oi]];
         if (c->xy64 || c->fast64[oi]) {
           const unsigned long long rows = 64ULL * (unsigned long long)I.p.Nx[2];
-          c->tmE.push_back(tensor_map_rows(I.E32, rows));
-          c->tmH.push_back(tensor_map_rows(I.hist32, rows * (unsigned long long)(I.hmax + 1)));
+          c->tmE.push_back(tensor_map_rows(I.E32, rows, 128));
+          c->tmH.push_back(tensor_map_rows(I.hist32, rows * (unsigned long long)(I.hmax + 1), 128));
         } else {
           c->tmE.push_back(CUtensorMap{});
           c->tmH.push_back(CUtensorMap{});
@@ -1453,6 +1467,7 @@ void mix_group_sweep(scft_ctx *c, int g, cudaStream_t sg) {
     return;
   }
   const int per = 64 * (64 / c->col64_tx);  // z-pass jobs per instance of the 64-point kernels
+  const int per128 = 128 * (128 / c->col64_tx);  // and of the 128 x 128 kernels
   for (int s = 0; s < c->nmax; s++) {
     // instances of the group still active at step s: a prefix (decreasing N)
     int act = 0;
@@ -1463,13 +1478,19 @@ void mix_group_sweep(scft_ctx *c, int g, cudaStream_t sg) {
     const int cnt = c->inst_pj_end[last] - gr.pj_begin;
     const int cc = c->inst_cj_end[last] - gr.cj_begin;
     if (s > 0) {
-      if (z64)
+      if (c->xy128)
+        LK(launch_mix_col64(col128_jobs(c) + (size_t)gr.inst_begin * per128, act * per128, c->d_tw32_z, 128, 128,
+                            nzi, c->col64_tx, sg));
+      else if (z64)
         LK(launch_mix_col64(col64_jobs(c) + (size_t)gr.inst_begin * per, act * per, twz, 64, 64, nzi, c->col64_tx,
                             sg));
       else
         LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cc, c->d_geoms, c->d_tw32, 3, 1, sg));
     }
-    if (p64)
+    if (c->xy128)
+      LK(launch_mix_plane128(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
+                             c->tmH.data() + gr.inst_begin, act, nzi, c->d_tw32_64, c->d_tw32_128, s, c->d_err, sg));
+    else if (p64)
       LK((c->plane64_form ? launch_mix_plane64w : launch_mix_plane64)(
           c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin, c->tmH.data() + gr.inst_begin, act,
           nzi, c->d_tw32_64, s, c->d_err, sg));
@@ -1608,11 +1629,22 @@ void ctx_create(scft_ctx *c, const scft_params *params, int n_inst) {
       g.ax[d].tw = off[nn];
     }
   }
+  // the 64- and 128-point tables of the 128 x 128 plane pass
+  for (int nn : {64, 128})
+    if (!off.count(nn)) {
+      off[nn] = (int)tw.size();
+      const long double two_pi = 6.283185307179586476925286766559005768L;
+      for (int t = 0; t < nn; t++) {
+        const long double a = two_pi * (long double)t / (long double)nn;
+        tw.push_back(make_double2((double)cosl(a), (double)-sinl(a)));
+      }
+    }
   c->d_tw64 = dupload(c, tw);
   std::vector<float2> tw32(tw.size());
   for (size_t t = 0; t < tw.size(); t++) tw32[t] = make_float2((float)tw[t].x, (float)tw[t].y);
   c->d_tw32 = dupload(c, tw32);
-  if (off.count(64)) c->d_tw32_64 = static_cast<float2 *>(c->d_tw32) + off[64];
+  c->d_tw32_64 = static_cast<float2 *>(c->d_tw32) + off[64];
+  c->d_tw32_128 = static_cast<float2 *>(c->d_tw32) + off[128];
   {
     const int nz0 = c->inst.empty() ? 0 : c->inst[0].p.Nx[2];
     if (off.count(nz0)) c->d_tw32_z = static_cast<float2 *>(c->d_tw32) + off[nz0];
@@ -1801,7 +1833,9 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
   std::vector<int> gs, txs;
   for (int g : {1, 2, 3, 4, 5, 6, 8})
     if (g <= n) gs.push_back(g);
-  if (c->colfast || c->anyfast)
+  if (c->xy128 && c->inst[0].p.Nx[2] == 256)
+    txs = {8, 16};  // the 256-point z pass takes at most 16 columns per CTA
+  else if (c->colfast || c->anyfast || c->xy128)
     txs = {8, 16, 32};
   else
     txs = {c->col64_tx};
@@ -1912,7 +1946,7 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
   }
   *groups_out = bg;
   *phases_out = bp;
-  *tx_out = (c->colfast || c->anyfast) ? bt : 0;
+  *tx_out = (c->colfast || c->anyfast || c->xy128) ? bt : 0;
   *ms_out = best;
 }
 
@@ -1989,7 +2023,11 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   CK(cudaEventCreate(&e2));
   CK(cudaEventRecord(e0, c->st));
   for (int r = 0; r < reps; r++) {
-    if (c->mixed && c->xy64)
+    if (c->mixed && c->xy128)
+      LK(launch_mix_plane128(c->mix64_tab.data(), c->tmE.data(), c->tmH.data(),
+                             c->prop_pj_count[s] / c->inst[0].p.Nx[2], c->inst[0].p.Nx[2], c->d_tw32_64,
+                             c->d_tw32_128, s, c->d_err, c->st));
+    else if (c->mixed && c->xy64)
       LK((c->plane64_form ? launch_mix_plane64w : launch_mix_plane64)(c->mix64_tab.data(), c->tmE.data(), c->tmH.data(),
                             c->prop_pj_count[s] / c->inst[0].p.Nx[2], c->inst[0].p.Nx[2], c->d_tw32_64, s, c->d_err,
                             c->st));
@@ -2003,7 +2041,10 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   }
   CK(cudaEventRecord(e1, c->st));
   for (int r = 0; r < reps; r++) {
-    if (c->mixed && c->colfast)
+    if (c->mixed && c->xy128)
+      LK(launch_mix_col64(col128_jobs(c), (c->prop_pj_count[s] / c->inst[0].p.Nx[2]) * 128 * (128 / c->col64_tx),
+                          c->d_tw32_z, 128, 128, c->inst[0].p.Nx[2], c->col64_tx, c->st));
+    else if (c->mixed && c->colfast)
       LK(launch_mix_col64(col64_jobs(c), (c->prop_pj_count[s] / c->inst[0].p.Nx[2]) * 64 * (64 / c->col64_tx),
                           c->d_tw32_z, 64, 64, c->inst[0].p.Nx[2], c->col64_tx, c->st));
     else if (c->mixed)
@@ -2028,7 +2069,7 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
       // the FP32 accumulators A and B (2 x 8 B); column: read + write z, plus
       // the h table in the generic pass (the 64-point pass forms h on the fly)
       bp += I.M * (4.0 * sizeof(float2) + 4.0 * sizeof(float));
-      bc += I.M * (2.0 * sizeof(float2) + (c->colfast ? 0.0 : sizeof(float)));
+      bc += I.M * (2.0 * sizeof(float2) + ((c->colfast || c->xy128) ? 0.0 : sizeof(float)));
     } else {
       const double props = I.single ? 1.0 : 2.0;
       bp += props * I.M * 6.0 * sizeof(double2);
@@ -2556,10 +2597,6 @@ int ctx_grad_geom(scft_ctx *c, double *out) {
       for (int j = 0; j < 8; j++) out[8 * k + j] = 0.0;
       const scft_params &p = I.p;
       if (p.n_exp_nr == 0) continue;
-      if (p.plate_shape != SCFT_PLATE_REFERENCE) {
-        status = SCFT_ERR_UNSUPPORTED;
-        continue;
-      }
       const double2 *wpl = I.w[0];
       if (I.mixed) {  // fields are held as transforms
         CK(cudaMemcpyAsync(I.rho[2], I.w[0], sizeof(double2) * I.M, cudaMemcpyDeviceToDevice, c->st));
@@ -2587,6 +2624,7 @@ int ctx_grad_geom(scft_ctx *c, double *out) {
       g.len = p.L_nr;
       g.rad = p.R_nr;
       g.xi = p.xi_nr;
+      g.shape = p.plate_shape;
       g.shell = I.shellU != nullptr;
       g.len_big = p.L_nr + 2.0 * p.shell_width;
       g.rad_big = p.R_nr + p.shell_width;

@@ -105,6 +105,12 @@ struct scft_ctx {
   int mixed = 0;
   int xy64 = 0;          // every instance has 64 x 64 xy planes and the same nz: specialised plane pass
   int colfast = 0;       // xy64 with nz = 64 or 128: specialised z pass
+  // every instance has 128 x 128 xy planes and the same nz (64, 128 or 256):
+  // the four-CTA cluster plane pass with parity-major k-space planes and the
+  // specialised z pass (kernels_mixed128.cu)
+  int xy128 = 0;
+  void *d_tw32_128 = nullptr;           // the 128-point twiddle table inside d_tw32
+  scft::ColJob *d_mix128_cj_tx[3] = {};  // z-pass jobs of the 128 x 128 kernels for 8, 16, 32 columns per CTA
   void *d_tw32_z = nullptr;  // twiddles of that nz
   void *d_tw32_64 = nullptr;  // the 64-point twiddle table inside d_tw32
   void *d_tw32 = nullptr;

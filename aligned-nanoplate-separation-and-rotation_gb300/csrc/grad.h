@@ -18,6 +18,7 @@ struct GradArgs {
   double c[2][3];  // absolute centres
   double u[2][3];  // unit axes
   double len, rad, xi;
+  int shape;              // SCFT_PLATE_REFERENCE or SCFT_PLATE_CUBOID
   int shell;              // shell potential present
   double len_big, rad_big;  // enlarged plate of the shell
 };

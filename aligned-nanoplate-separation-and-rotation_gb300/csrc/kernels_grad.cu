@@ -1,8 +1,8 @@
 // kernels_grad.cu -- geometric derivatives of H with respect to the plates.
 //
-// The plate core density (code/initialize.cpp:578-612)
-//   rho_p(r) = 1/4 erfc(a) erfc(b),  a = (|u.dr| - L/2)/xi,  b = (|u x dr| - R)/xi,
-// dr = r - c (minimum image), enters H at fixed fields through
+// The plate core density rho_p (code/initialize.cpp:578-612, or the cuboid
+// extension; plate_profile.cuh), a function of dr = r - c (minimum image),
+// enters H at fixed fields through
 //   -i rho0 int (1 - rho_p) w+           (code/calc_h.cpp:66-87)
 //   -nD log Qd with nD = rho0 (Vf - V_exp - phiG Vf)/N, V_exp = int rho_p
 //                                          (code/initialize.cpp:251-351),
@@ -16,37 +16,9 @@
 // terms (FP64); the host assembles dH/dg.
 #include "fft_core.cuh"
 #include "grad.h"
+#include "plate_profile.cuh"
 
 namespace scft {
-
-__device__ __forceinline__ double derfc(double x) {
-  // d/dx erfc(x) = -2/sqrt(pi) exp(-x^2)
-  return -1.1283791670955125738961589031215452 * exp(-x * x);
-}
-
-// d rho_p/dg for g = (theta_z, c_x, c_y, c_z) of a plate of thickness len and
-// radius rad at minimum-image offset dr from its centre, axis u.
-__device__ __forceinline__ void plate_derivs(const double dr[3], const double *u, double len, double rad, double xi,
-                                             double dg[4]) {
-  const double ud = u[0] * dr[0] + u[1] * dr[1] + u[2] * dr[2];
-  const double cx = u[1] * dr[2] - u[2] * dr[1], cy = u[2] * dr[0] - u[0] * dr[2], cz = u[0] * dr[1] - u[1] * dr[0];
-  const double uc = sqrt(cx * cx + cy * cy + cz * cz);
-  const double a = (fabs(ud) - 0.5 * len) / xi, b = (uc - rad) / xi;
-  const double Ea = erfc(a), Eb = erfc(b);
-  const double dEa = derfc(a) / xi, dEb = derfc(b) / xi;  // d/d|u.dr|, d/d|u x dr|
-  const double sg = ud > 0.0 ? 1.0 : (ud < 0.0 ? -1.0 : 0.0);
-  // rotation about z: du = (-u_y, u_x, 0) dtheta
-  const double dudr = -u[1] * dr[0] + u[0] * dr[1];
-  const double dud_dth = sg * dudr;
-  const double duc_dth = uc > 1e-300 ? -ud * dudr / uc : 0.0;
-  dg[0] = 0.25 * (dEa * dud_dth * Eb + Ea * dEb * duc_dth);
-  // centre: d dr / d c_k = -e_k
-  for (int k = 0; k < 3; k++) {
-    const double dud_dc = -sg * u[k];
-    const double duc_dc = uc > 1e-300 ? -(dr[k] - ud * u[k]) / uc : 0.0;
-    dg[1 + k] = 0.25 * (dEa * dud_dc * Eb + Ea * dEb * duc_dc);
-  }
-}
 
 __global__ void k_geom_grad(GradArgs g, const double2 *__restrict__ wpl, const double2 *__restrict__ rhoA,
                             double *__restrict__ part) {
@@ -67,8 +39,8 @@ __global__ void k_geom_grad(GradArgs g, const double2 *__restrict__ wpl, const d
         dr[d] = r;
       }
       double dg[4], db[4];
-      plate_derivs(dr, g.u[j], g.len, g.rad, g.xi, dg);
-      if (g.shell) plate_derivs(dr, g.u[j], g.len_big, g.rad_big, g.xi, db);
+      plate_derivs(g.shape, dr, g.u[j], g.len, g.rad, g.xi, dg);
+      if (g.shell) plate_derivs(g.shape, dr, g.u[j], g.len_big, g.rad_big, g.xi, db);
       for (int k = 0; k < 4; k++) {
         double *a = acc + j * kGradPerPlate + kGradTerms * k;
         a[0] += dg[k] * w.x;
@@ -122,7 +94,7 @@ __global__ void k_plate_deriv(double2 *out, GradArgs g, int j, int k, double len
       dr[d] = r;
     }
     double dg[4];
-    plate_derivs(dr, g.u[j], len, rad, g.xi, dg);
+    plate_derivs(g.shape, dr, g.u[j], len, rad, g.xi, dg);
     out[i] = make_double2(dg[k], 0.0);
   }
 }

@@ -25,64 +25,15 @@
 // Plane sums are formed with error-free FP32 two-sums per thread and across
 // the warp (FP64 only for the 16 warp results): GB300 issues FP64 at a small
 // fraction of its FP32 rate.
-#include "async_copy.cuh"
-#include "fft_core.cuh"
 #include "inst.h"
 #include "launch.h"
+#include "mix_core.cuh"
 #include "prop_launch.h"
 
 #include <string.h>
 
 namespace scft {
 
-namespace {
-
-constexpr int kRowPad = 72;              // padded row stride (float2) of a 64 x 64 plane
-constexpr int kPlanePad = 64 * kRowPad;  // float2 per padded plane
-
-template <int SIGN> __device__ __forceinline__ void dft8f(float2 *v) { Dft<8, SIGN, float2>::run(v); }
-
-template <int SIGN> __device__ __forceinline__ void tw64(float2 *v, int t, const float2 *tw) {
-#pragma unroll
-  for (int c = 1; c < 8; c++) v[c] = ctw<SIGN>(v[c], tw[t * c]);
-}
-
-// 64-point transform of a group of 8 threads (see above).  Element (b, c) of
-// the exchange lives at xch[b * sb + c * sc].  WARP: the 8 threads and their
-// exchange area belong to one warp, so a warp barrier suffices.
-template <int SIGN, bool WARP>
-__device__ __forceinline__ void fft64_group(float2 *v, int t, float2 *xch, int sb, int sc, const float2 *tw) {
-  dft8f<SIGN>(v);
-  tw64<SIGN>(v, t, tw);
-#pragma unroll
-  for (int c = 0; c < 8; c++) xch[t * sb + c * sc] = v[c];
-  if (WARP) __syncwarp(); else __syncthreads();
-#pragma unroll
-  for (int b = 0; b < 8; b++) v[b] = xch[b * sb + t * sc];
-  if (WARP) __syncwarp(); else __syncthreads();
-  dft8f<SIGN>(v);
-}
-
-__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-
-// The per-step arrays (propagator, factors, accumulators) stay in L2 while
-// the history streams past with evict-first (async_copy.cuh).
-__device__ __forceinline__ void st_stream(float2 *g, float2 v, uint64_t pol) {
-  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;\n" ::"l"(g), "f"(v.x), "f"(v.y), "l"(pol)
-               : "memory");
-}
-
-// Element (row, x) of a plane staged by four 64 x 128 B boxes with the
-// 128-byte swizzle: box x / 16, 16-byte chunk ((x % 16) / 2) ^ (row % 8).
-__device__ __forceinline__ float2 swz(const float2 *plane, int row, int x) {
-  return plane[(x >> 4) * 1024 + row * 16 + ((((x & 15) >> 1) ^ (row & 7)) << 1) + (x & 1)];
-}
-
-}  // namespace
 
 // Static shared scratch of one plane task.
 struct Plane64Shared {
@@ -400,28 +351,6 @@ __global__ void __launch_bounds__(8 * TX) k_mix_col64(const ColJob *__restrict__
 //   X[c + 16 d] = sum_b Y[b][c] w8^(b d)          (two DFT8)
 // which returns X[t + 8m] in v[m], the input order, so the same routine runs
 // both directions.
-template <int SIGN> __device__ __forceinline__ void dft16f(float2 *v, const float2 *tw128) {
-  // n = a + 4b, k = c + 4d: DFT4 over b, twiddle w16^(a c) = w128^(8 a c), DFT4 over a
-  float2 z[4][4];
-#pragma unroll
-  for (int a = 0; a < 4; a++) {
-#pragma unroll
-    for (int b = 0; b < 4; b++) z[a][b] = v[a + 4 * b];
-    Dft<4, SIGN, float2>::run(z[a]);
-  }
-#pragma unroll
-  for (int a = 1; a < 4; a++)
-#pragma unroll
-    for (int c = 1; c < 4; c++) z[a][c] = ctw<SIGN>(z[a][c], tw128[8 * a * c]);
-#pragma unroll
-  for (int c = 0; c < 4; c++) {
-    float2 u[4] = {z[0][c], z[1][c], z[2][c], z[3][c]};
-    Dft<4, SIGN, float2>::run(u);
-#pragma unroll
-    for (int d = 0; d < 4; d++) v[c + 4 * d] = u[d];
-  }
-}
-
 template <int SIGN>
 __device__ __forceinline__ void fft128_group(float2 *v, int t, float2 *xch, int sb, int sc, const float2 *tw) {
   dft16f<SIGN>(v, tw);
@@ -1042,6 +971,7 @@ cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw, int 
   const double s = 1.0 / ((double)nx * ny * nz);
   const float s_hi = (float)s, s_lo = (float)(s - (double)s_hi);
   const float2 *t2 = reinterpret_cast<const float2 *>(tw);
+  if (nz == 256) return launch_mix_col256(jobs, njobs, tw, nx, ny, tx, st);
   if (nz == 128) {
     switch (tx) {
       case 8: k_mix_col128<8><<<njobs, 64, 0, st>>>(jobs, t2, nx, ny, s_hi, s_lo); break;

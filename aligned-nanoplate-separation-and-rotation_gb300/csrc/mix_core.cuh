@@ -1,0 +1,93 @@
+// mix_core.cuh -- building blocks of the specialised mixed-form propagator
+// kernels (kernels_mixed64.cu, kernels_mixed128.cu): the 64-point transform of
+// a group of 8 threads, the 16-point transform in registers, error-free FP32
+// sums, cache-hinted stores and the swizzled staging layout.
+//
+// A 64-point transform is done by a group of 8 threads, thread t holding the
+// 8 values x[t + 8a], a = 0..7 ("four-step", 64 = 8 x 8):
+//   Y[t][c]  = sum_a x[8a + t] w8^(a c)          (DFT8 in registers)
+//   Y[t][c] *= w64^(t c)                          (twiddle)
+//   exchange through shared memory so that thread t holds Y[b][t], b = 0..7
+//   X[t + 8d] = sum_b Y[b][t] w8^(b d)            (DFT8 in registers)
+// so the output comes back in the same "t + 8j" order as the input.
+#pragma once
+
+#include "async_copy.cuh"
+#include "fft_core.cuh"
+
+namespace scft {
+
+namespace {
+
+constexpr int kRowPad = 72;              // padded row stride (float2) of a 64 x 64 plane
+constexpr int kPlanePad = 64 * kRowPad;  // float2 per padded plane
+
+template <int SIGN> __device__ __forceinline__ void dft8f(float2 *v) { Dft<8, SIGN, float2>::run(v); }
+
+template <int SIGN> __device__ __forceinline__ void tw64(float2 *v, int t, const float2 *tw) {
+#pragma unroll
+  for (int c = 1; c < 8; c++) v[c] = ctw<SIGN>(v[c], tw[t * c]);
+}
+
+// 64-point transform of a group of 8 threads (see above).  Element (b, c) of
+// the exchange lives at xch[b * sb + c * sc].  WARP: the 8 threads and their
+// exchange area belong to one warp, so a warp barrier suffices.
+template <int SIGN, bool WARP>
+__device__ __forceinline__ void fft64_group(float2 *v, int t, float2 *xch, int sb, int sc, const float2 *tw) {
+  dft8f<SIGN>(v);
+  tw64<SIGN>(v, t, tw);
+#pragma unroll
+  for (int c = 0; c < 8; c++) xch[t * sb + c * sc] = v[c];
+  if (WARP) __syncwarp(); else __syncthreads();
+#pragma unroll
+  for (int b = 0; b < 8; b++) v[b] = xch[b * sb + t * sc];
+  if (WARP) __syncwarp(); else __syncthreads();
+  dft8f<SIGN>(v);
+}
+
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+
+// The per-step arrays (propagator, factors, accumulators) stay in L2 while
+// the history streams past with evict-first (async_copy.cuh).
+__device__ __forceinline__ void st_stream(float2 *g, float2 v, uint64_t pol) {
+  asm volatile("st.global.L2::cache_hint.v2.f32 [%0], {%1, %2}, %3;\n" ::"l"(g), "f"(v.x), "f"(v.y), "l"(pol)
+               : "memory");
+}
+
+// Element (row, x) of a plane staged by four 64 x 128 B boxes with the
+// 128-byte swizzle: box x / 16, 16-byte chunk ((x % 16) / 2) ^ (row % 8).
+__device__ __forceinline__ float2 swz(const float2 *plane, int row, int x) {
+  return plane[(x >> 4) * 1024 + row * 16 + ((((x & 15) >> 1) ^ (row & 7)) << 1) + (x & 1)];
+}
+
+}  // namespace
+
+// 16-point transform in registers, n = a + 4b, k = c + 4d: DFT4 over b,
+// twiddle w16^(a c) = tw[S a c] (tw: the 16 S-point twiddles), DFT4 over a;
+// the output is in natural order.
+template <int SIGN, int S = 8> __device__ __forceinline__ void dft16f(float2 *v, const float2 *tw) {
+  float2 z[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; a++) {
+#pragma unroll
+    for (int b = 0; b < 4; b++) z[a][b] = v[a + 4 * b];
+    Dft<4, SIGN, float2>::run(z[a]);
+  }
+#pragma unroll
+  for (int a = 1; a < 4; a++)
+#pragma unroll
+    for (int c = 1; c < 4; c++) z[a][c] = ctw<SIGN>(z[a][c], tw[S * a * c]);
+#pragma unroll
+  for (int c = 0; c < 4; c++) {
+    float2 u[4] = {z[0][c], z[1][c], z[2][c], z[3][c]};
+    Dft<4, SIGN, float2>::run(u);
+#pragma unroll
+    for (int d = 0; d < 4; d++) v[c + 4 * d] = u[d];
+  }
+}
+
+}  // namespace scft

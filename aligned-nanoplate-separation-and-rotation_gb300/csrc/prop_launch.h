@@ -73,10 +73,17 @@ cudaError_t launch_mix_plane64(const MixInst *insts, const CUtensorMap *tmE, con
 // bit-identical results, a different launch shape.
 cudaError_t launch_mix_plane64w(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
                                 int nz, const void *tw64, int n, int *err, cudaStream_t st);
-// z pass of the 64 x 64-plane instances for nz = 64 or 128 (tw: the nz-point
-// twiddles); tx: x columns per CTA (8, 16 or 32); jobs built for that width
+// z pass of the specialised instances for nz = 64, 128 or 256 (tw: the
+// nz-point twiddles; jb.kern: the [hx | hy | hz] table); tx: x columns per
+// CTA (8, 16 or 32); jobs built for that width
 cudaError_t launch_mix_col64(const ColJob *jobs, int njobs, const void *tw, int nx, int ny, int nz, int tx,
                              cudaStream_t st);
+cudaError_t launch_mix_col256(const ColJob *jobs, int njobs, const void *tw, int nx, int ny, int tx, cudaStream_t st);
+// Plane pass of step n for 128 x 128 xy planes (kernels_mixed128.cu): four
+// CTAs per plane; insts, tmE, tmH as for launch_mix_plane64 with tensor maps
+// of rows of 128 float2; tw64, tw128: the 64- and 128-point twiddles.
+cudaError_t launch_mix_plane128(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
+                                int nz, const void *tw64, const void *tw128, int n, int *err, cudaStream_t st);
 cudaError_t launch_mix_graft_plane(const LaunchShape &ls, const PropJob *jobs, int njobs, const GraftMixInst *insts,
                                    const DevGeom *geoms, const void *tw, int sweep, int n, cudaStream_t st);
 cudaError_t launch_mix_graft_finalize(const FieldInst *fi, int ninst, int blocks, double2 *part, cudaStream_t st);

@@ -250,6 +250,12 @@ class Context:
                                        _ptr(g.view(np.float64))))
         return a, b, g
 
+    def plate_density(self, inst) -> np.ndarray:
+        """The explicit plates' core density rho_exp_nr of one instance (real)."""
+        out = np.zeros(self._shape(inst), np.float64)
+        _check(load().scft_get_plate_density(self._h, inst, _ptr(out)))
+        return out
+
     def smeared(self, inst):
         sh = self._shape(inst)
         a, b, g = (np.zeros(sh, np.complex128) for _ in range(3))

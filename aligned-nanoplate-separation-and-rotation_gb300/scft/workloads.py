@@ -16,7 +16,7 @@ import math
 
 import numpy as np
 
-from . import PREC_FP64, PREC_MIXED, make_params
+from . import PLATE_CUBOID, PLATE_REFERENCE, PREC_FP64, PREC_MIXED, make_params
 
 SWEEP_ANGLES = (0, 1, 2, 3, 4, 5, 6, 7, 8, 9, 10, 20, 30, 45, 90)
 
@@ -28,9 +28,12 @@ def rg(N: int) -> float:
 def plate_params(theta_deg: float, N: int = 100, fA: float = 0.5, chiN: float = 20.0, C: float = 50.0,
                  grid=(64, 64, 64), box_rg=(6.4, 6.4, 6.4), precision=PREC_FP64, lam_pl=0.002, lam_mi=0.0005,
                  centers=((0.5, 0.5, 0.5),), thickness_rg=0.2, radius_rg=0.8, xi_rg=0.1, sigma=0.0, Ng=0,
-                 shell=False):
+                 shell=False, shape=PLATE_REFERENCE):
     """Config 1 geometry: plate(s) rotated by theta about z, normal along x at 0.
-    shell=True adds the A-attractive shell Lambda = -1/N in a 0.1 Rg shell."""
+    shell=True adds the A-attractive shell Lambda = -1/N in a 0.1 Rg shell;
+    shape=PLATE_CUBOID makes each plate a cuboid (thickness along the normal,
+    a 2 radius_rg x 2 radius_rg square in the plane) instead of the
+    reference's disc."""
     R = rg(N)
     Nda = int(round(fA * N))
     th = math.radians(theta_deg)
@@ -40,7 +43,8 @@ def plate_params(theta_deg: float, N: int = 100, fA: float = 0.5, chiN: float = 
                        Nx=grid, L=tuple(b * R for b in box_rg), lam_pl=lam_pl, lam_mi=lam_mi,
                        n_exp_nr=len(centers), L_nr=thickness_rg * R, R_nr=radius_rg * R, xi_nr=xi_rg * R,
                        center=cs, orient=(u, u), precision=precision, sigma=sigma, Ng=Ng,
-                       shell_lambda=(-1.0 / N if shell else 0.0), shell_width=(0.1 * R if shell else 0.0))
+                       shell_lambda=(-1.0 / N if shell else 0.0), shell_width=(0.1 * R if shell else 0.0),
+                       plate_shape=shape)
 
 
 def seeded_fields(p, seed: int, periods: int = 1) -> dict:
@@ -109,6 +113,9 @@ def large_grafted8(precision=PREC_MIXED):
 WORKLOADS = {
     "plate64_N100": lambda prec: [plate_params(10.0, precision=prec)],
     "plate64_N100_shell": lambda prec: [plate_params(10.0, precision=prec, shell=True)],
+    # config 1 as written: a 1.6 x 1.6 x 0.2 Rg cuboid with a 0.1 Rg interface,
+    # rotated by 10 degrees, with the A-attractive shell
+    "plate64_N100_cuboid_shell": lambda prec: [plate_params(10.0, precision=prec, shell=True, shape=PLATE_CUBOID)],
     "sweep15_64_N100_shell": lambda prec: [plate_params(t, precision=prec, shell=True) for t in SWEEP_ANGLES],
     "sweep15_64_N100": lambda prec: sweep15(precision=prec),
     "sweep15_mixed_sizes": lambda prec: sweep15_mixed_sizes(precision=prec),

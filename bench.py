@@ -252,12 +252,18 @@ def converge_study(args):
     1. Mixed form from the seeded start (seed 1000, the same field for every
        angle): the iteration at which each instance meets the reference's
        stop rule (error_tol --tol), then on to --tol-tight (or --itmax), so
-       that the converged H is precise enough for a central difference.
+       that the converged H is precise enough for a central difference.  Then
+       10 - 0.5, 10 and 10 + 0.5 degrees start again from the converged 10
+       degree fields (continuation, so that all three lie in the same basin:
+       from the seeded start, nearby angles can settle into different
+       lamellar states) and relax alike; the derivative is read there.
     2. FP64 method from the mixed form's converged fields to the stop rule
        (it starts next to its own saddle point).
     3. |dH| between the two converged states (absolute, per volume as the
        stop rule measures, relative); dH/dtheta at 10 degrees from each
        form's adjoint against central differences of each form's converged H.
+    --converge-plate picks the plate: the reference's disc, or the cuboid with
+    the A-attractive shell of the single-plate configuration as written.
     """
     import math
 
@@ -268,23 +274,19 @@ def converge_study(args):
     from scft.workloads import plate_params, seeded_fields
 
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    # the reference's disc, or the single-plate configuration as written (a
+    # 1.6 x 1.6 x 0.2 Rg cuboid with the A-attractive shell)
+    plate_kw = {"disc": {}, "cuboid_shell": {"shell": True, "shape": scft.PLATE_CUBOID}}[args.converge_plate]
     hdeg = 0.5
     thetas = [0.0, 10.0, 45.0, 90.0, 10.0 - hdeg, 10.0 + hdeg]
     n = 4
     t0 = time.time()
-    res = {}
-    fields = None
-    for form, prec, tol, itmax in (("mixed", scft.PREC_MIXED, args.tol_tight, args.itmax),
-                                   ("fp64", scft.PREC_FP64, args.tol, args.itmax_fp64)):
-        ps = [plate_params(t, precision=prec) for t in thetas]
+
+    def converge(prec, ths, start, tol, itmax):
+        ps = [plate_params(t, precision=prec, **plate_kw) for t in ths]
         with scft.Context(ps) as ctx:
-            if fields is None:
-                f0 = seeded_fields(ps[0], 1000)
-                for k in range(len(ps)):
-                    ctx.set_fields(k, f0)
-            else:
-                for k in range(len(ps)):
-                    ctx.set_fields(k, fields[k])
+            for k in range(len(ps)):
+                ctx.set_fields(k, start[k])
             ctx.calc_poly_density()
             V = [ctx.info(k)["V"] for k in range(len(ps))]
             ts = time.time()
@@ -293,27 +295,39 @@ def converge_study(args):
             while its < itmax and float(np.max(err)) > tol:
                 d2, err, more = converge_to_stop_rule(ctx, len(ps), V, tol, min(2000, itmax - its))
                 its += more
-            H = ctx.calc_H()[:, 0].copy()
-            g = ctx.grad_geom()
-            fields = [ctx.get_fields(k) for k in range(len(ps))]
-            res[form] = {"H": H, "g": g, "done": done, "err": err, "its": its, "V": V, "seconds": time.time() - ts}
-            print(f"{form}: stop rule met at {done}; {its} iterations, last err {list(err)}, "
-                  f"{time.time() - ts:.1f} s", file=sys.stderr, flush=True)
-    m, d = res["mixed"], res["fp64"]
+            r = {"H": ctx.calc_H()[:, 0].copy(), "g": ctx.grad_geom(), "done": done, "err": list(err), "its": its,
+                 "V": V, "seconds": time.time() - ts, "fields": [ctx.get_fields(k) for k in range(len(ps))]}
+        print(f"{len(ths)} instances: stop rule met at {done}; {its} iterations, last err {list(err)}, "
+              f"{r['seconds']:.1f} s", file=sys.stderr, flush=True)
+        return r
+
+    f0 = seeded_fields(plate_params(0.0, **plate_kw), 1000)
+    a = converge(scft.PREC_MIXED, thetas[:n], [f0] * n, args.tol_tight, args.itmax)
+    # 10 - h, 10, 10 + h from the converged 10 degree fields, relaxed alike
+    b = converge(scft.PREC_MIXED, [thetas[4], 10.0, thetas[5]], [a["fields"][1]] * 3, args.tol_tight, args.itmax)
+    m = {"H": np.concatenate([a["H"], b["H"]]), "g": np.concatenate([a["g"], b["g"]]),
+         "done": a["done"] + b["done"], "err": a["err"] + b["err"], "its": [a["its"], b["its"]],
+         "seconds": a["seconds"] + b["seconds"]}
+    d = converge(scft.PREC_FP64, thetas[:n] + [thetas[4], 10.0, thetas[5]], a["fields"] + b["fields"], args.tol,
+                 args.itmax_fp64)
     dH = np.abs(m["H"][:n] - d["H"][:n])
-    k10 = thetas.index(10.0)
+    k10 = n + 1  # the 10 degree instance relaxed beside its neighbours
     two_h = math.radians(2 * hdeg)
-    fd_m = (m["H"][5] - m["H"][4]) / two_h
-    fd_d = (d["H"][5] - d["H"][4]) / two_h
+    fd_m = (m["H"][n + 2] - m["H"][n]) / two_h
+    fd_d = (d["H"][n + 2] - d["H"][n]) / two_h
     g_m, g_d = float(m["g"][k10, 0, 0]), float(d["g"][k10, 0, 0])
-    line = {"study": "converged accuracy, mixed vs FP64", "grid": [64, 64, 64], "N": 100, "angles": thetas[:n],
+    line = {"study": "converged accuracy, mixed vs FP64", "plate": args.converge_plate, "grid": [64, 64, 64],
+            "N": 100, "angles": thetas[:n],
             "stop_rule": {"error_tol": args.tol, "print_freq": 25, "reference": "code/simulate.cpp:97-155"},
-            "mixed": {"from": "seeded start (seed 1000)", "iterations_to_stop_rule": m["done"],
+            "mixed": {"from": "seeded start (seed 1000); 10 - 0.5, 10, 10 + 0.5 degrees again from the converged "
+                              "10 degree fields",
+                      "iterations_to_stop_rule": m["done"],
                       "iterations": m["its"], "then_to_error": args.tol_tight,
                       "last_err": [float(x) for x in m["err"]], "seconds": m["seconds"]},
             "fp64": {"from": "the mixed form's converged fields", "iterations_to_stop_rule": d["done"],
                      "iterations": d["its"], "last_err": [float(x) for x in d["err"]], "seconds": d["seconds"]},
-            "H": {"mixed": [float(x) for x in m["H"][:n]], "fp64": [float(x) for x in d["H"][:n]]},
+            "H": {"angles": thetas[:n] + [thetas[4], 10.0, thetas[5]], "mixed": [float(x) for x in m["H"]],
+                  "fp64": [float(x) for x in d["H"]]},
             "dH_abs": [float(x) for x in dH], "dH_per_volume": [float(x / v) for x, v in zip(dH, d["V"][:n])],
             "dH_rel": [float(x / abs(h)) for x, h in zip(dH, d["H"][:n])],
             "dHdtheta_10deg": {"mixed_adjoint": g_m, "fp64_adjoint": g_d,
@@ -355,6 +369,8 @@ def main():
                     help="convergence study instead of the timing: angles 0, 10, 45, 90 (and 10 +- 0.5 for the "
                          "FP64 finite difference) at 64^3, N=100, both forms from the same seeded start to the "
                          "reference's stop rule; prints one JSON line")
+    ap.add_argument("--converge-plate", choices=["disc", "cuboid_shell"], default="disc",
+                    help="plate of the --converge study")
     ap.add_argument("--tol", type=float, default=1e-8, help="error_tol of the stop rule (--converge)")
     ap.add_argument("--tol-tight", type=float, default=1e-11,
                     help="error the mixed form continues to after the stop rule (--converge)")
@@ -596,9 +612,12 @@ def main():
     prof = ctx.profile_step(20)
     nz0 = params[0].Nx[2]
     xy64 = all(p.Nx[0] == 64 and p.Nx[1] == 64 and p.Nx[2] == nz0 for p in params)
-    col_fast = {64: "k_mix_col64", 128: "k_mix_col128"}.get(nz0) if xy64 else None
+    xy128 = (not xy64 and nz0 in (64, 128, 256) and
+             all(p.Nx[0] == 128 and p.Nx[1] == 128 and p.Nx[2] == nz0 for p in params))
+    col_fast = {64: "k_mix_col64", 128: "k_mix_col128", 256: "k_mix_col256"}.get(nz0) if (xy64 or xy128) else None
     p64name = "k_mix_plane64w" if sched.get("plane_form") else "k_mix_plane64"
-    kernel_names = {"mixed": (p64name if xy64 else "k_mix_prop_plane", col_fast or "k_col_fft<float>"),
+    pname = p64name if xy64 else ("k_mix_plane128" if xy128 else "k_mix_prop_plane")
+    kernel_names = {"mixed": (pname, col_fast or "k_col_fft<float>"),
                     "plain": ("k_prop_plane_f64", "k_col_fft<double> (bond kernel)")}
     dom = "plane" if prof["ms_plane"] >= prof["ms_col"] else "col"
     ms_k = prof["ms_" + dom]

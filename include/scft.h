@@ -192,8 +192,8 @@ int scft_get_density(scft_ctx *ctx, int inst, double *rhoda, double *rhodb, doub
  * -n_exp_nr ng_per_np Re int (dg_map/dg) log q_g[Ng-1], the graft map
  * g_map ~ |grad rho_p(1.05 L, 1.05 R)| differentiated through its spectral
  * gradient and normalisation (code/initialize.cpp:160-200,
- * code/grafted_nanoparticle.cpp:82-112).  SCFT_ERR_UNSUPPORTED for
- * SCFT_PLATE_CUBOID. */
+ * code/grafted_nanoparticle.cpp:82-112).  Both plate shapes are covered;
+ * for SCFT_PLATE_CUBOID the in-plane axes turn with u. */
 int scft_grad_geom(scft_ctx *ctx, double *out);
 
 /* The explicit plates' density rho_exp_nr of one instance (M real values),

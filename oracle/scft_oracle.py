@@ -176,6 +176,35 @@ def explicit_nanorod(g: Grid, length, rad, xi, rel_center, u):
         np.complex128)
 
 
+def cuboid_frame(u):
+    """In-plane axes of the cuboid plate (project extension, no reference
+    counterpart): e1 = u x z normalised when |u_z| < 0.9, else u x x
+    normalised; e2 = u x e1."""
+    u = np.asarray(u, float)
+    t = np.cross(u, (0.0, 0.0, 1.0)) if abs(u[2]) < 0.9 else np.cross(u, (1.0, 0.0, 0.0))
+    e1 = t / np.linalg.norm(t)
+    return e1, np.cross(u, e1)
+
+
+def cuboid_plate(g: Grid, length, rad, xi, rel_center, u):
+    """Project extension without a reference counterpart (SCFT_PLATE_CUBOID):
+    a slab of thickness len along u and a 2 rad x 2 rad square in the plane,
+    1/8 erfc((|u.r|-len/2)/xi) erfc((|e1.r|-rad)/xi) erfc((|e2.r|-rad)/xi),
+    r the minimum-image vector from the centre as in explicit_nanorod."""
+    center = [rel_center[d] * g.L[d] for d in range(3)]
+    comps = []
+    for d in range(3):
+        dr = g.dx[d] * np.arange(g.Nx[d], dtype=np.float64) - center[d]
+        comps.append(np.where(dr >= 0.5 * g.L[d], dr - g.L[d], np.where(dr < -0.5 * g.L[d], dr + g.L[d], dr)))
+    DZ, DY, DX = np.meshgrid(comps[2], comps[1], comps[0], indexing="ij")
+    e1, e2 = cuboid_frame(u)
+    out = 0.125 * np.ones(DX.shape)
+    for e, half in ((np.asarray(u, float), 0.5 * length), (e1, rad), (e2, rad)):
+        p = e[0] * DX + e[1] * DY + e[2] * DZ
+        out = out * erfc((np.abs(p) - half) / xi)
+    return out.astype(np.complex128)
+
+
 def field_gradient(g: Grid, a, d):
     """code/array_utils.cpp:565-579: spectral derivative with get_k_alias."""
     K = g.k_alias_components()[d]
@@ -215,6 +244,8 @@ class System:
     # segments in the shell between the plate and the plate enlarged by w
     shell_lambda: float = 0.0
     shell_width: float = 0.0
+    # project extension: 0 = the reference's disc, 1 = cuboid_plate
+    plate_shape: int = 0
     update_scheme: int = 1  # bcp.input numbering: 0 = Euler, otherwise 1S (code/simulate.cpp:86-89)
     tables: dict = field(default_factory=dict)
 
@@ -240,6 +271,10 @@ class System:
                    xi_nr=c.xi_nr, centers=c.centers, orients=c.orients,
                    update_scheme=getattr(c, "update_scheme", 1))
 
+    def plate(self, length, rad, i):
+        shape = cuboid_plate if self.plate_shape == 1 else explicit_nanorod
+        return shape(self.g, length, rad, self.xi_nr, self.centers[i], self.orients[i])
+
     def initialize(self):
         g = self.g
         self.N = self.Nda + self.Ndb  # code/initialize.cpp:53
@@ -254,23 +289,21 @@ class System:
             raise NotImplementedError("only np_type=2 (nanorod/plate) explicit particles")
         # code/initialize.cpp:160-200: graft map = |grad rho_p(1.05 L, 1.05 R)|, normalised
         for i in range(self.n_exp_nr):
-            pd = explicit_nanorod(g, self.L_nr * 1.05, self.R_nr * 1.05, self.xi_nr, self.centers[i],
-                                  self.orients[i])
+            pd = self.plate(self.L_nr * 1.05, self.R_nr * 1.05, i)
             grad2 = sum(field_gradient(g, pd, d) ** 2 for d in range(3))
             expl_grafts = expl_grafts + np.sqrt(grad2)
         if self.n_exp_nr > 0:
             expl_grafts = expl_grafts / integ_trapPBC(g, expl_grafts)
         # code/initialize.cpp:210-239: core density
         for i in range(self.n_exp_nr):
-            rho_exp_nr = rho_exp_nr + explicit_nanorod(g, self.L_nr, self.R_nr, self.xi_nr,
-                                                       self.centers[i], self.orients[i])
+            rho_exp_nr = rho_exp_nr + self.plate(self.L_nr, self.R_nr, i)
         t["rho_exp_nr"] = rho_exp_nr
         t["exp_nrH"] = fft_fwd(g, rho_exp_nr)
         # extension: U_A = lam * sum_j [rho_p(L + 2w, R + w) - rho_p(L, R)]
         shellU = np.zeros(g.shape)
         if self.shell_lambda != 0.0:
-            big = sum(explicit_nanorod(g, self.L_nr + 2 * self.shell_width, self.R_nr + self.shell_width,
-                                       self.xi_nr, self.centers[i], self.orients[i]) for i in range(self.n_exp_nr))
+            big = sum(self.plate(self.L_nr + 2 * self.shell_width, self.R_nr + self.shell_width, i)
+                      for i in range(self.n_exp_nr))
             shellU = self.shell_lambda * (big.real - rho_exp_nr.real)
         t["shellU"] = shellU
         # code/initialize.cpp:249-386: volumes and chain counts (no film, no field NPs)

@@ -1,0 +1,128 @@
+"""The 128 x 128 plane family of the mixed form: the four-CTA cluster plane
+pass (k_mix_plane128, parity-major k-space planes) and the specialised z
+passes (k_mix_col64 / k_mix_col128 / k_mix_col256 on 128 x 128 planes).
+
+A batch runs this family when every instance has 128 x 128 xy planes and
+the same nz in {64, 128, 256}; otherwise the generic kernels.  The family's
+transforms differ from the generic ones only in FP32 rounding, so
+* against the FP64 method over the same iterations from the same fields it
+  meets the mixed form's bar (H 2e-5 relative, densities 2e-5 of the
+  largest), for uneven chain lengths in one launch, nz = 64 and 256, and
+  grafted plates;
+* against the generic mixed kernels on the same instance (a batch that
+  mixes two nz falls back to them) Q, H and the densities agree within the
+  same bar (two FP32 paths with different transform orders);
+* the autotuner's z-pass tile choice keeps the results within the bar.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+BAR = 2e-5
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.fixture(scope="module")
+def S():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.fail("gpu tests need a CUDA device")
+    import scft
+
+    scft.load()
+    return scft
+
+
+def plate(S, theta, N, nz, prec, graft=False):
+    from scft.workloads import plate_params, rg
+
+    p = plate_params(theta, N=N, grid=(128, 128, nz), box_rg=(8.0, 8.0, 8.0 * nz / 128), precision=prec,
+                     lam_pl=0.002, lam_mi=0.001, thickness_rg=0.4, radius_rg=1.2, xi_rg=0.2,
+                     sigma=(0.5 / rg(N) ** 2 if graft else 0.0), Ng=(4 if graft else 0))
+    if graft:
+        p.chi_bc = p.chi_ab
+    return p
+
+
+def run(S, ps, fields, iters=3, tune=False):
+    with S.Context(ps) as c:
+        for k, f in enumerate(fields):
+            c.set_fields(k, f)
+        if tune:
+            c.autotune(2)
+        c.calc_poly_density()
+        H0 = c.calc_H().copy()
+        c.update_1s(iters)
+        H = c.calc_H().copy()
+        rho = [c.density(k)[:2] for k in range(len(ps))]
+        sched = c.schedule()
+    return H0, H, rho, sched
+
+
+def compare(a, b, tol):
+    assert np.abs(a[0][:, 0] - b[0][:, 0]).max() <= tol * np.abs(b[0][:, 0]).max(), (a[0][:, 0], b[0][:, 0])
+    assert np.abs(a[1][:, 0] - b[1][:, 0]).max() <= tol * np.abs(b[1][:, 0]).max(), (a[1][:, 0], b[1][:, 0])
+    for (ra, rb), (qa, qb) in zip(a[2], b[2]):
+        assert rel(ra, qa) <= tol
+        assert rel(rb, qb) <= tol
+
+
+@pytest.mark.parametrize("nz,Ns", [(64, [10, 7, 7, 4]), (256, [6, 5])])
+def test_cluster_plane_pass_matches_fp64(S, nz, Ns):
+    from scft.workloads import seeded_fields
+
+    thetas = [7.0 * k for k in range(len(Ns))]
+    p64 = [plate(S, t, N, nz, S.PREC_FP64) for t, N in zip(thetas, Ns)]
+    p32 = [plate(S, t, N, nz, S.PREC_MIXED) for t, N in zip(thetas, Ns)]
+    fields = [seeded_fields(p, 90 + k) for k, p in enumerate(p64)]
+    a = run(S, p32, fields)
+    b = run(S, p64, fields)
+    assert a[3]["col_tile"] in (8, 16, 32)  # the specialised z pass
+    compare(a, b, BAR)
+
+
+def test_cluster_plane_pass_matches_generic_kernels(S):
+    """The same instance alone (128 family) and beside one with another nz
+    (generic kernels)."""
+    from scft.workloads import seeded_fields
+
+    pa = plate(S, 12.0, 9, 64, S.PREC_MIXED)
+    pb = plate(S, 30.0, 9, 128, S.PREC_MIXED)
+    fa, fb = seeded_fields(pa, 95), seeded_fields(pb, 96)
+    a = run(S, [pa], [fa])
+    g = run(S, [pa, pb], [fa, fb])
+    assert a[3]["col_tile"] and not g[3]["col_tile"]
+    # Qd at the start and after the updates, H after the updates (at the
+    # seeded start H is a near cancellation, -156 against -nD log Qd terms
+    # of ~1e4, and both FP32 paths sit ~1e-4 of it away from the FP64 value)
+    for r in (0, 1):
+        assert abs(a[r][0, 2] - g[r][0, 2]) <= BAR * abs(g[r][0, 2])
+    assert abs(a[1][0, 0] - g[1][0, 0]) <= BAR * abs(g[1][0, 0])
+    assert rel(a[2][0][0], g[2][0][0]) <= BAR
+    assert rel(a[2][0][1], g[2][0][1]) <= BAR
+
+
+def test_grafted_plates_match_fp64(S):
+    from scft.workloads import seeded_fields
+
+    p64 = [plate(S, 20.0, 10, 64, S.PREC_FP64, graft=True)]
+    p32 = [plate(S, 20.0, 10, 64, S.PREC_MIXED, graft=True)]
+    fields = [seeded_fields(p64[0], 97, periods=2)]
+    compare(run(S, p32, fields), run(S, p64, fields), BAR)
+
+
+def test_autotuned_tile_stays_within_the_bar(S):
+    from scft.workloads import seeded_fields
+
+    Ns = [6, 6, 4]
+    p64 = [plate(S, 5.0 * k, N, 256, S.PREC_FP64) for k, N in enumerate(Ns)]
+    p32 = [plate(S, 5.0 * k, N, 256, S.PREC_MIXED) for k, N in enumerate(Ns)]
+    fields = [seeded_fields(p, 98 + k) for k, p in enumerate(p64)]
+    a = run(S, p32, fields, tune=True)
+    assert a[3]["col_tile"] in (8, 16)  # the 256-point z pass takes 8 or 16 columns
+    compare(a, run(S, p64, fields), BAR)
