@@ -970,6 +970,7 @@ void build_jobs(scft_ctx *c) {
       X.grafts = I.grafts;
     }
     c->d_gmi = dupload(c, gmi);
+    c->h_gmi = gmi;
   }
 
   // field transform job lists
@@ -1277,6 +1278,20 @@ void build_jobs(scft_ctx *c) {
     c->d_graft_pj = dupload(c, gpj);
     c->d_graft_cj = dupload(c, gcj);
   }
+  if (c->mixed && c->xy128 && !gorder.empty()) {
+    c->gmi128.clear();
+    for (int k : gorder) c->gmi128.push_back(c->h_gmi[k]);
+    for (int t = 0; t < 3; t++) {
+      const int tx = 8 << t;
+      std::vector<ColJob> cj;
+      for (int k : gorder) {
+        Instance &I = c->inst[k];
+        for (int y = 0; y < 128; y++)
+          for (int x0 = 0; x0 < 128; x0 += tx) cj.push_back(ColJob{I.gwork32, I.htab32, I.geom, x0, y});
+      }
+      c->d_mix128_gcj_tx[t] = dupload(c, cj);
+    }
+  }
   c->gblocks = 64;
   c->d_gpart = dalloc<double2>(c, (size_t)n * c->gblocks * 2);
   long long mmax = 0;
@@ -1575,6 +1590,19 @@ void seq_mix(scft_ctx *c, bool update) {
   if (c->ngmax > 0) {
     for (auto &I : c->inst)
       if (I.graft) CK(cudaMemsetAsync(I.gacc32, 0, sizeof(float) * I.M, st));
+    if (c->xy128) {
+      // the cluster plane pass and the specialised z pass (parity-major planes)
+      const int nz0 = c->inst[0].p.Nx[2];
+      const int per128 = 128 * (128 / c->col64_tx);
+      ColJob *gcj = c->d_mix128_gcj_tx[c->col64_tx == 8 ? 0 : (c->col64_tx == 16 ? 1 : 2)];
+      for (int sweep = 0; sweep < 2; sweep++)
+        for (int s = 0; s < c->ngmax; s++) {
+          const int act = c->graft_pj_count[s] / nz0;  // grafted instances with Ng > s (a prefix)
+          if (s > 0)
+            LK(launch_mix_col64(gcj, act * per128, c->d_tw32_z, 128, 128, nz0, c->col64_tx, st));
+          LK(launch_mix_graft_plane128(c->gmi128.data(), act, nz0, c->d_tw32_64, c->d_tw32_128, sweep, s, st));
+        }
+    } else
     for (int sweep = 0; sweep < 2; sweep++) {
       LK(launch_mix_graft_plane(c->shp_mixg, c->d_graft_pj, c->graft_pj_count[0], c->d_gmi, c->d_geoms, c->d_tw32,
                                 sweep, 0, st));

@@ -111,6 +111,10 @@ struct scft_ctx {
   int xy128 = 0;
   void *d_tw32_128 = nullptr;           // the 128-point twiddle table inside d_tw32
   scft::ColJob *d_mix128_cj_tx[3] = {};  // z-pass jobs of the 128 x 128 kernels for 8, 16, 32 columns per CTA
+  // graft sweep of the 128 x 128 family: views of the grafted instances in
+  // sweep order (Ng non-increasing) and their z-pass jobs
+  std::vector<scft::GraftMixInst> gmi128;
+  scft::ColJob *d_mix128_gcj_tx[3] = {};
   void *d_tw32_z = nullptr;  // twiddles of that nz
   void *d_tw32_64 = nullptr;  // the 64-point twiddle table inside d_tw32
   void *d_tw32 = nullptr;
@@ -129,6 +133,7 @@ struct scft_ctx {
   scft::MixInst *d_mi = nullptr;
   scft::GraftMixInst *d_gmi = nullptr;  // per instance (zero for instances without grafts)
   std::vector<scft::MixInst> h_mi;       // host copy of d_mi
+  std::vector<scft::GraftMixInst> h_gmi;  // host copy of d_gmi
   std::vector<scft::MixInst> mix64_tab;  // instances in job order (64^3 plane pass)
   std::vector<CUtensorMap> tmE, tmH;      // their TMA descriptors (Boltzmann, history)
   // d_err[0]: error word of the plane passes (1: an mbarrier wait ran out;

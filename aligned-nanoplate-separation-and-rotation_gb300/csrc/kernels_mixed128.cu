@@ -166,6 +166,107 @@ struct Plane128Shared {
   int exp[2];          // power-of-two exponents of the step
 };
 
+// Thread roles in a quadrant task (512 threads): row phase (y = row,
+// x = tr + 8d), column phase (y = tc + 8d, x = col); q = rx + 2 ry the CTA's
+// rank in the cluster.
+struct Quad {
+  int q, rx, ry, row, tr, col, tc;
+};
+
+__device__ __forceinline__ Quad quad_roles() {
+  Quad Z;
+  Z.q = (int)cl_rank();
+  Z.rx = Z.q & 1;
+  Z.ry = Z.q >> 1;
+  const int tid = threadIdx.x;
+  Z.row = tid >> 3;
+  Z.tr = tid & 7;
+  Z.col = tid & 63;
+  Z.tc = tid >> 6;
+  return Z;
+}
+
+// Inverse transform of a plane: on entry v holds the CTA's k-space quadrant
+// in column ownership (jy = tc + 8a, jx = col); on return the real-space
+// quadrant in row ownership (x = tr + 8d of row `row`).  Two cluster
+// barriers plus one split one; buf is free for the caller afterwards, but a
+// partner may read it until it passes its next cluster barrier.
+__device__ __forceinline__ void quad_inverse(float2 *v, float2 *buf, const Plane128Shared &S, const Quad &Z) {
+  fft64_group<+1, false>(v, Z.tc, buf + Z.col, 8 * 64, 64, S.tw);
+#pragma unroll
+  for (int d = 0; d < 8; d++) buf[(Z.tc + 8 * d) * kRowPad + Z.col] = v[d];
+  cl_sync();
+  {
+    const uint32_t rb = cl_map(buf + Z.row * kRowPad + Z.tr, (uint32_t)(Z.q ^ 2));
+    const float2 w = S.w128[Z.row];
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+      const float2 own = buf[Z.row * kRowPad + Z.tr + 8 * a];
+      const float2 oth = ld_cl(rb + 8u * (uint32_t)(8 * a));
+      v[a] = Z.ry == 0 ? cadd(own, ctw<+1>(oth, w)) : csub(oth, ctw<+1>(own, w));
+    }
+  }
+  cl_arrive();  // done reading the partner's buffer
+  cl_wait();    // and every partner done reading this one: buf may be overwritten
+  fft64_group<+1, true>(v, Z.tr, buf + Z.row * kRowPad, 9, 1, S.tw);
+#pragma unroll
+  for (int d = 0; d < 8; d++) buf[Z.row * kRowPad + Z.tr + 8 * d] = v[d];
+  cl_sync();
+  {
+    const uint32_t rb = cl_map(buf + Z.row * kRowPad + Z.tr, (uint32_t)(Z.q ^ 1));
+#pragma unroll
+    for (int d = 0; d < 8; d++) {
+      const float2 oth = ld_cl(rb + 8u * (uint32_t)(8 * d));
+      const float2 w = S.w128[Z.tr + 8 * d];
+      v[d] = Z.rx == 0 ? cadd(v[d], ctw<+1>(oth, w)) : csub(oth, ctw<+1>(v[d], w));
+    }
+  }
+}
+
+// First half of the forward transform: the real-space quadrant v (row
+// ownership) into X (swizzled 64 x 64), for the x partner.  X must be free
+// in this CTA; the caller then passes a cluster barrier (cl_sync) before
+// quad_forward.
+__device__ __forceinline__ void quad_forward_publish(const float2 *v, float2 *X, const Quad &Z) {
+#pragma unroll
+  for (int d = 0; d < 8; d++) X[swz_idx(Z.row, Z.tr + 8 * d)] = v[d];
+}
+
+// Rest of the forward transform after that barrier: x radix-2 with the x
+// partner's X, DFT64 over x, y radix-2 through Y (free in this CTA) with the
+// y partner, DFT64 over y; on return v holds the k-space quadrant in column
+// ownership.  Ends with a cluster arrive: the caller stores v and then calls
+// cl_wait() before leaving, so that no CTA leaves while a partner may still
+// read its X or Y.
+__device__ __forceinline__ void quad_forward(float2 *v, const float2 *X, float2 *Y, float2 *buf,
+                                             const Plane128Shared &S, const Quad &Z) {
+  {
+    const uint32_t rb = cl_map(X, (uint32_t)(Z.q ^ 1));
+#pragma unroll
+    for (int d = 0; d < 8; d++) {
+      const int x = Z.tr + 8 * d;
+      const float2 oth = ld_cl(rb + 8u * (uint32_t)swz_idx(Z.row, x));
+      v[d] = Z.rx == 0 ? cadd(v[d], oth) : ctw<-1>(csub(oth, v[d]), S.w128[x]);
+    }
+  }
+  fft64_group<-1, true>(v, Z.tr, buf + Z.row * kRowPad, 9, 1, S.tw);
+#pragma unroll
+  for (int d = 0; d < 8; d++) Y[swz_idx(Z.row, Z.tr + 8 * d)] = v[d];
+  cl_sync();
+  {
+    const uint32_t rb = cl_map(Y, (uint32_t)(Z.q ^ 2));
+#pragma unroll
+    for (int a = 0; a < 8; a++) {
+      const int m = Z.tc + 8 * a;
+      const float2 own = Y[swz_idx(m, Z.col)];
+      const float2 oth = ld_cl(rb + 8u * (uint32_t)swz_idx(m, Z.col));
+      v[a] = Z.ry == 0 ? cadd(own, oth) : ctw<-1>(csub(oth, own), S.w128[m]);
+    }
+  }
+  cl_arrive();  // done reading the partners' buffers
+  fft64_group<-1, false>(v, Z.tc, buf + Z.col, 8 * 64, 64, S.tw);
+}
+
 // Plane pass of step n for 128 x 128 xy planes (any nz, the same for every
 // instance of the launch): 512 threads per CTA, clusters of four CTAs, one
 // cluster per (instance, z plane): cluster b works on plane b % nz of
@@ -186,8 +287,8 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
   __shared__ Plane128Shared S;
   __shared__ __align__(8) uint64_t s_bar;
   const int nz = T.nz;
-  const int q = (int)cl_rank();
-  const int rx = q & 1, ry = q >> 1;
+  const Quad Z = quad_roles();
+  const int q = Z.q, rx = Z.rx, ry = Z.ry;
   const int task = blockIdx.x >> 2;
   const int ii = task / nz;
   const int zz = task - ii * nz;
@@ -198,9 +299,7 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
   const int lane = tid & 31, warp = tid >> 5;
   const long long M = 16384LL * nz;
   const long long qoff = (long long)zz * 16384 + (64 * ry) * 128 + 64 * rx;  // quadrant origin
-  // row-phase ownership: (y = row, x = tr + 8d); column phase: (y = tc + 8d, x = col)
-  const int row = tid >> 3, tr = tid & 7;
-  const int col = tid & 63, tc = tid >> 6;
+  const int row = Z.row, tr = Z.tr, col = Z.col, tc = Z.tc;
   if (tid == 0) mbar_init(&s_bar, 1);
   if (tid < 64) {
     S.tw[tid] = tw64_g[tid];
@@ -259,40 +358,8 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
   const bool useA_q = (Na > 0 && n < Na);
   const bool useA_d = !(n <= N - Na - 1);
   __syncthreads();  // means, exponents, twiddles
-  if (n > 0) {
-    // inverse y over the quadrant's jy, then the radix-2 step with the y partner
-    fft64_group<+1, false>(v, tc, buf + col, 8 * 64, 64, S.tw);
-#pragma unroll
-    for (int d = 0; d < 8; d++) buf[(tc + 8 * d) * kRowPad + col] = v[d];
-    cl_sync();
-    {
-      const uint32_t rb = cl_map(buf + row * kRowPad + tr, (uint32_t)(q ^ 2));
-      const float2 w = S.w128[row];
-#pragma unroll
-      for (int a = 0; a < 8; a++) {
-        const float2 own = buf[row * kRowPad + tr + 8 * a];
-        const float2 oth = ld_cl(rb + 8u * (uint32_t)(8 * a));
-        v[a] = ry == 0 ? cadd(own, ctw<+1>(oth, w)) : csub(oth, ctw<+1>(own, w));
-      }
-    }
-    cl_arrive();  // done reading the partner's buffer
-    cl_wait();    // and every partner done reading this one: buf may be overwritten
-    // inverse x over jx (row phase, inside one warp), then the x partner
-    fft64_group<+1, true>(v, tr, buf + row * kRowPad, 9, 1, S.tw);
-#pragma unroll
-    for (int d = 0; d < 8; d++) buf[row * kRowPad + tr + 8 * d] = v[d];
-    cl_sync();
-    {
-      const uint32_t rb = cl_map(buf + row * kRowPad + tr, (uint32_t)(q ^ 1));
-#pragma unroll
-      for (int d = 0; d < 8; d++) {
-        const float2 oth = ld_cl(rb + 8u * (uint32_t)(8 * d));
-        const float2 w = S.w128[tr + 8 * d];
-        v[d] = rx == 0 ? cadd(v[d], ctw<+1>(oth, w)) : csub(oth, ctw<+1>(v[d], w));
-      }
-    }
-    // the partners' reads of buf end before they arrive at the next barrier
-  }
+  if (n > 0) quad_inverse(v, buf, S, Z);
+  // (the partners' reads of buf end before they arrive at the next barrier)
   if (!mbar_wait(&s_bar, 0, T.err[1])) {
     atomicExch(T.err, 1);
     mbar_wait(&s_bar, 0, kWaitPolls);  // let copies in flight land before the CTA moves on
@@ -393,11 +460,8 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
   }
   const bool last = (n == N - 1);
   // forward x (decimation in frequency): the x partner's real-space values
-  // through Es
-  if (!last) {
-#pragma unroll
-    for (int d = 0; d < 8; d++) Es[swz_idx(row, tr + 8 * d)] = v[d];
-  }
+  // through Es (its staged factors are consumed)
+  if (!last) quad_forward_publish(v, Es, Z);
   cl_sync();  // quadrant sums and the exchange values visible in the cluster
   if (q == 0 && tid == 0) {
     // plane sums over the four quadrants, in rank order
@@ -413,35 +477,172 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
     cl_sync();  // CTA 0 has read every quadrant sum
     return;
   }
-  {
-    const uint32_t rb = cl_map(Es, (uint32_t)(q ^ 1));
-#pragma unroll
-    for (int d = 0; d < 8; d++) {
-      const int x = tr + 8 * d;
-      const float2 oth = ld_cl(rb + 8u * (uint32_t)swz_idx(row, x));
-      v[d] = rx == 0 ? cadd(v[d], oth) : ctw<-1>(csub(oth, v[d]), S.w128[x]);
-    }
-  }
-  fft64_group<-1, true>(v, tr, buf + row * kRowPad, 9, 1, S.tw);
-  // forward y: the y partner's values through Hs, read in column ownership
-#pragma unroll
-  for (int d = 0; d < 8; d++) Hs[swz_idx(row, tr + 8 * d)] = v[d];
-  cl_sync();
-  {
-    const uint32_t rb = cl_map(Hs, (uint32_t)(q ^ 2));
-#pragma unroll
-    for (int a = 0; a < 8; a++) {
-      const int m = tc + 8 * a;
-      const float2 own = Hs[swz_idx(m, col)];
-      const float2 oth = ld_cl(rb + 8u * (uint32_t)swz_idx(m, col));
-      v[a] = ry == 0 ? cadd(own, oth) : ctw<-1>(csub(oth, own), S.w128[m]);
-    }
-  }
-  cl_arrive();  // done reading the partners' buffers
-  fft64_group<-1, false>(v, tc, buf + col, 8 * 64, 64, S.tw);
+  quad_forward(v, Es, Hs, buf, S, Z);
 #pragma unroll
   for (int d = 0; d < 8; d++) work[(tc + 8 * d) * 128 + col] = v[d];
   cl_wait();  // no CTA leaves while a partner may still read its buffers
+}
+
+// Graft sweep plane pass of step n for 128 x 128 xy planes (sweep 0: q_g from
+// the free end, stored; sweep 1: qdag_g from the grafting surface, paired
+// with the stored steps into the graft density), the contract of
+// k_mix_graft_plane (kernels_mixed.cu) with the k-space layout of
+// k_mix_plane128.  The field is real: it rides in the real part of the
+// complex transform.  Cluster b works on plane b % nz of T.inst[b / nz].
+// Dynamic shared memory: two 32 KB exchange quadrants and the padded
+// exchange/transpose quadrant, as k_mix_plane128.
+template <int CAP>
+__global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
+    k_mix_graft_plane128(const __grid_constant__ Graft128TableT<CAP> T, const float2 *__restrict__ tw64_g,
+                         const float2 *__restrict__ tw128_g, int sweep, int n) {
+  extern __shared__ __align__(16) unsigned char dsm_raw[];
+  float2 *Xs = reinterpret_cast<float2 *>(dsm_raw + ((1024 - (smem_u32(dsm_raw) & 1023)) & 1023));
+  float2 *Ys = Xs + 4096;
+  float2 *buf = Ys + 4096;
+  __shared__ Plane128Shared S;
+  const int nz = T.nz;
+  const Quad Z = quad_roles();
+  const int task = blockIdx.x >> 2;
+  const int ii = task / nz;
+  const int zz = task - ii * nz;
+  const GraftMixInst &P = T.inst[ii];
+  const int Ng = P.Ng;
+  if (n >= Ng) return;  // the whole cluster (same instance)
+  const int tid = threadIdx.x;
+  const int lane = tid & 31, warp = tid >> 5;
+  const long long M = 16384LL * nz;
+  const long long qoff = (long long)zz * 16384 + (64 * Z.ry) * 128 + 64 * Z.rx;  // quadrant origin
+  const int gi = Z.row * 128 + Z.tr;  // quadrant index of element d = 0 (row phase)
+  if (tid < 64) {
+    S.tw[tid] = tw64_g[tid];
+    S.w128[tid] = tw128_g[tid];
+  }
+  double *part = P.part + (long long)sweep * Ng * nz;
+  int *K = P.K + sweep * Ng;
+  float2 v[8];
+  float2 *work = P.work + qoff;
+  if (n > 0) {
+#pragma unroll
+    for (int a = 0; a < 8; a++) v[a] = work[(Z.tc + 8 * a) * 128 + Z.col];
+  }
+  float eg[8];
+  const float *Eg = P.Eg + qoff + gi;
+#pragma unroll
+  for (int d = 0; d < 8; d++) eg[d] = Eg[8 * d];
+  if (warp == 0) {
+    double a = 0.0;
+    if (n > 0)
+      for (int z = lane; z < nz; z += 32) a += part[(long long)(n - 1) * nz + z];
+    for (int o = 16; o > 0; o >>= 1) a += __shfl_down_sync(0xffffffffu, a, o);
+    if (lane == 0) {
+      const double ma = a / (double)M;
+      int ea = 0;
+      if (n > 0 && isfinite(ma) && ma > 0.0) frexp(ma, &ea);
+      S.exp[0] = ea;
+      const float hi = (float)ma;
+      S.mh[0] = hi;
+      S.ml[0] = (float)(ma - (double)hi);
+    }
+  }
+  __syncthreads();  // mean, exponent, twiddles
+  if (n > 0) quad_inverse(v, buf, S, Z);
+  const int ex = S.exp[0];
+  const int Kn = (n > 0) ? K[n - 1] + ex : (sweep == 0 ? 0 : -P.K[Ng - 1]);
+  if (n == 0) {
+    if (sweep == 0) {
+#pragma unroll
+      for (int d = 0; d < 8; d++) v[d] = make_float2(eg[d], 0.f);
+    } else {
+      const float *last = P.hist + (long long)(Ng - 1) * M + qoff + gi;
+      const double2 *gr = P.grafts + qoff + gi;
+#pragma unroll
+      for (int d = 0; d < 8; d++) v[d] = make_float2((float)gr[8 * d].x * eg[d] / last[8 * d], 0.f);
+    }
+  } else {
+    const float sc = ldexpf(1.0f, -ex);
+    const float m_hi = S.mh[0], m_lo = S.ml[0];
+#pragma unroll
+    for (int d = 0; d < 8; d++) v[d] = make_float2(fmaf(v[d].x, eg[d], fmaf(m_hi, eg[d], m_lo * eg[d])) * sc, 0.f);
+  }
+  if (zz == 0 && Z.q == 0 && tid == 0) K[n] = Kn;
+  if (sweep == 0) {
+    float *h = P.hist + (long long)n * M + qoff + gi;
+#pragma unroll
+    for (int d = 0; d < 8; d++) h[8 * d] = v[d].x;
+  } else {
+    const float *o = P.hist + (long long)(Ng - 1 - n) * M + qoff + gi;
+    const float f = ldexpf(1.0f, Kn + P.K[Ng - 1 - n]);
+    float *acc = P.acc + qoff + gi;
+#pragma unroll
+    for (int d = 0; d < 8; d++) acc[8 * d] += (v[d].x * o[8 * d]) * f;
+  }
+  // quadrant sum: error-free FP32 two-sums within the thread and the warp
+  float sa = 0.f, ca = 0.f;
+#pragma unroll
+  for (int d = 0; d < 8; d++) {
+    float e;
+    two_sum(sa, v[d].x, sa, e);
+    ca += e;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const float s2 = __shfl_down_sync(0xffffffffu, sa, o), c2 = __shfl_down_sync(0xffffffffu, ca, o);
+    float e;
+    two_sum(sa, s2, sa, e);
+    ca += c2 + e;
+  }
+  if (lane == 0) S.red[0][warp] = (double)sa + (double)ca;
+  __syncthreads();
+  if (warp == 0) {
+    double aq = lane < 16 ? S.red[0][lane] : 0.0;
+    for (int o = 8; o > 0; o >>= 1) aq += __shfl_down_sync(0xffffffffu, aq, o);
+    if (lane == 0) S.qs[0] = aq;
+  }
+  const bool last = (n == Ng - 1);
+  if (!last) quad_forward_publish(v, Xs, Z);
+  cl_sync();  // quadrant sums and the exchange values visible in the cluster
+  if (Z.q == 0 && tid == 0) {
+    double sv = 0.0;
+    for (int r = 0; r < 4; r++) sv += ld_cl_d(cl_map(&S.qs[0], (uint32_t)r));
+    part[(long long)n * nz + zz] = sv;
+  }
+  if (last) {
+    cl_sync();  // CTA 0 has read every quadrant sum
+    return;
+  }
+  quad_forward(v, Xs, Ys, buf, S, Z);
+#pragma unroll
+  for (int d = 0; d < 8; d++) work[(Z.tc + 8 * d) * 128 + Z.col] = v[d];
+  cl_wait();  // no CTA leaves while a partner may still read its buffers
+}
+
+template <int CAP>
+static cudaError_t launch_graft128_chunks(const GraftMixInst *insts, int ninst, int nz, const void *tw64,
+                                          const void *tw128, int sweep, int n, cudaStream_t st) {
+  const int smem = 1024 + 2 * 4096 * (int)sizeof(float2) + kPlanePad * (int)sizeof(float2);
+  auto kfn = k_mix_graft_plane128<CAP>;
+  cudaError_t e = cudaFuncSetAttribute(kfn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  e = cudaFuncSetAttribute(kfn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+  if (e != cudaSuccess) return e;
+  for (int i0 = 0; i0 < ninst; i0 += CAP) {
+    const int cnt = ninst - i0 < CAP ? ninst - i0 : CAP;
+    Graft128TableT<CAP> T;
+    memset(&T, 0, sizeof T);
+    for (int k = 0; k < cnt; k++) T.inst[k] = insts[i0 + k];
+    T.nz = nz;
+    kfn<<<4 * nz * cnt, 512, smem, st>>>(T, reinterpret_cast<const float2 *>(tw64),
+                                          reinterpret_cast<const float2 *>(tw128), sweep, n);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
+cudaError_t launch_mix_graft_plane128(const GraftMixInst *insts, int ninst, int nz, const void *tw64,
+                                      const void *tw128, int sweep, int n, cudaStream_t st) {
+  if (ninst <= 0) return cudaSuccess;
+  if (ninst <= 4) return launch_graft128_chunks<4>(insts, ninst, nz, tw64, tw128, sweep, n, st);
+  return launch_graft128_chunks<16>(insts, ninst, nz, tw64, tw128, sweep, n, st);
 }
 
 // One plane-pass launch per chunk of at most CAP instances (4 CTAs per plane).

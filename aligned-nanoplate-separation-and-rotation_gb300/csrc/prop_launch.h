@@ -84,6 +84,14 @@ cudaError_t launch_mix_col256(const ColJob *jobs, int njobs, const void *tw, int
 // of rows of 128 float2; tw64, tw128: the 64- and 128-point twiddles.
 cudaError_t launch_mix_plane128(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
                                 int nz, const void *tw64, const void *tw128, int n, int *err, cudaStream_t st);
+// Graft sweep plane pass of the same family (four CTAs per plane): the
+// grafted instances' views in sweep order (Ng non-increasing), by value.
+template <int CAP> struct Graft128TableT {
+  GraftMixInst inst[CAP];
+  int nz;
+};
+cudaError_t launch_mix_graft_plane128(const GraftMixInst *insts, int ninst, int nz, const void *tw64,
+                                      const void *tw128, int sweep, int n, cudaStream_t st);
 cudaError_t launch_mix_graft_plane(const LaunchShape &ls, const PropJob *jobs, int njobs, const GraftMixInst *insts,
                                    const DevGeom *geoms, const void *tw, int sweep, int n, cudaStream_t st);
 cudaError_t launch_mix_graft_finalize(const FieldInst *fi, int ninst, int blocks, double2 *part, cudaStream_t st);

@@ -121,6 +121,9 @@ WORKLOADS = {
     "sweep15_mixed_sizes": lambda prec: sweep15_mixed_sizes(precision=prec),
     "sep9_64x64x128_N100": lambda prec: separation9(precision=prec),
     "graft8_128x128x256_N200": lambda prec: large_grafted8(precision=prec),
+    # a small case of the 128 x 128 plane family (profiling captures)
+    "sweep4_128x128x64_N50": lambda prec: [plate_params(t, N=50, grid=(128, 128, 64), box_rg=(12.8, 12.8, 6.4),
+                                                        precision=prec) for t in (0, 10, 20, 30)],
 }
 
 # per-workload defaults of the bench: relaxation iterations, how many

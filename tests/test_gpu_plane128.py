@@ -10,8 +10,8 @@ transforms differ from the generic ones only in FP32 rounding, so
   largest), for uneven chain lengths in one launch, nz = 64 and 256, and
   grafted plates;
 * against the generic mixed kernels on the same instance (a batch that
-  mixes two nz falls back to them) Q, H and the densities agree within the
-  same bar (two FP32 paths with different transform orders);
+  mixes two nz falls back to them) Q, H and the densities agree within
+  twice that bar (two FP32 paths with different transform orders);
 * the autotuner's z-pass tile choice keeps the results within the bar.
 """
 import numpy as np
@@ -100,20 +100,35 @@ def test_cluster_plane_pass_matches_generic_kernels(S):
     # Qd at the start and after the updates, H after the updates (at the
     # seeded start H is a near cancellation, -156 against -nD log Qd terms
     # of ~1e4, and both FP32 paths sit ~1e-4 of it away from the FP64 value)
+    # each within the bar of the FP64 result, so within twice it of each other
     for r in (0, 1):
-        assert abs(a[r][0, 2] - g[r][0, 2]) <= BAR * abs(g[r][0, 2])
-    assert abs(a[1][0, 0] - g[1][0, 0]) <= BAR * abs(g[1][0, 0])
-    assert rel(a[2][0][0], g[2][0][0]) <= BAR
-    assert rel(a[2][0][1], g[2][0][1]) <= BAR
+        assert abs(a[r][0, 2] - g[r][0, 2]) <= 2 * BAR * abs(g[r][0, 2])
+    assert abs(a[1][0, 0] - g[1][0, 0]) <= 2 * BAR * abs(g[1][0, 0])
+    assert rel(a[2][0][0], g[2][0][0]) <= 2 * BAR
+    assert rel(a[2][0][1], g[2][0][1]) <= 2 * BAR
 
 
 def test_grafted_plates_match_fp64(S):
+    """The graft sweep runs the cluster form too (k_mix_graft_plane128);
+    Qga and the geometric derivatives (graft-map term included) follow."""
     from scft.workloads import seeded_fields
 
-    p64 = [plate(S, 20.0, 10, 64, S.PREC_FP64, graft=True)]
-    p32 = [plate(S, 20.0, 10, 64, S.PREC_MIXED, graft=True)]
-    fields = [seeded_fields(p64[0], 97, periods=2)]
-    compare(run(S, p32, fields), run(S, p64, fields), BAR)
+    p64 = [plate(S, 20.0, 10, 64, S.PREC_FP64, graft=True), plate(S, 35.0, 8, 64, S.PREC_FP64, graft=True)]
+    p64[1].Ng = 3  # uneven graft chains in one launch
+    p32 = [plate(S, 20.0, 10, 64, S.PREC_MIXED, graft=True), plate(S, 35.0, 8, 64, S.PREC_MIXED, graft=True)]
+    p32[1].Ng = 3
+    fields = [seeded_fields(p, 97 + k, periods=2) for k, p in enumerate(p64)]
+    a, b = run(S, p32, fields), run(S, p64, fields)
+    compare(a, b, BAR)
+    assert np.abs(a[1][:, 4] - b[1][:, 4]).max() <= BAR * np.abs(b[1][:, 4]).max()  # Qga
+    g = {}
+    for prec, ps in ((0, p64), (1, p32)):
+        with S.Context(ps) as c:
+            for k, f in enumerate(fields):
+                c.set_fields(k, f)
+            c.calc_poly_density()
+            g[prec] = c.grad_geom()
+    assert np.abs(g[1] - g[0]).max() <= 1e-4 * np.abs(g[0]).max()
 
 
 def test_autotuned_tile_stays_within_the_bar(S):
