@@ -80,10 +80,12 @@ __device__ __forceinline__ double ld_cl_d(uint32_t a) {
   return v;
 }
 
-// index of element (row, x) of a 64 x 64 plane in the 128-byte swizzled layout (swz)
-__device__ __forceinline__ int swz_idx(int row, int x) {
-  return (x >> 4) * 1024 + row * 16 + ((((x & 15) >> 1) ^ (row & 7)) << 1) + (x & 1);
-}
+// Element (row, x) of a 64 x 64 exchange quadrant: rows of 64 float2 with
+// bit 3 of x flipped on odd rows.  Each half-warp's access is then free of
+// bank conflicts in both phases: two rows x 8 consecutive x (row phase) take
+// the two 8-slot halves of the 16 eight-byte slots, and 16 consecutive x of
+// one row (column phase) take all 16.
+__device__ __forceinline__ int xl_idx(int row, int x) { return row * 64 + (x ^ ((row & 1) << 3)); }
 
 __device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
@@ -224,12 +226,12 @@ __device__ __forceinline__ void quad_inverse(float2 *v, float2 *buf, const Plane
 }
 
 // First half of the forward transform: the real-space quadrant v (row
-// ownership) into X (swizzled 64 x 64), for the x partner.  X must be free
+// ownership) into X (xl_idx layout), for the x partner.  X must be free
 // in this CTA; the caller then passes a cluster barrier (cl_sync) before
 // quad_forward.
 __device__ __forceinline__ void quad_forward_publish(const float2 *v, float2 *X, const Quad &Z) {
 #pragma unroll
-  for (int d = 0; d < 8; d++) X[swz_idx(Z.row, Z.tr + 8 * d)] = v[d];
+  for (int d = 0; d < 8; d++) X[xl_idx(Z.row, Z.tr + 8 * d)] = v[d];
 }
 
 // Rest of the forward transform after that barrier: x radix-2 with the x
@@ -245,21 +247,21 @@ __device__ __forceinline__ void quad_forward(float2 *v, const float2 *X, float2 
 #pragma unroll
     for (int d = 0; d < 8; d++) {
       const int x = Z.tr + 8 * d;
-      const float2 oth = ld_cl(rb + 8u * (uint32_t)swz_idx(Z.row, x));
+      const float2 oth = ld_cl(rb + 8u * (uint32_t)xl_idx(Z.row, x));
       v[d] = Z.rx == 0 ? cadd(v[d], oth) : ctw<-1>(csub(oth, v[d]), S.w128[x]);
     }
   }
   fft64_group<-1, true>(v, Z.tr, buf + Z.row * kRowPad, 9, 1, S.tw);
 #pragma unroll
-  for (int d = 0; d < 8; d++) Y[swz_idx(Z.row, Z.tr + 8 * d)] = v[d];
+  for (int d = 0; d < 8; d++) Y[xl_idx(Z.row, Z.tr + 8 * d)] = v[d];
   cl_sync();
   {
     const uint32_t rb = cl_map(Y, (uint32_t)(Z.q ^ 2));
 #pragma unroll
     for (int a = 0; a < 8; a++) {
       const int m = Z.tc + 8 * a;
-      const float2 own = Y[swz_idx(m, Z.col)];
-      const float2 oth = ld_cl(rb + 8u * (uint32_t)swz_idx(m, Z.col));
+      const float2 own = Y[xl_idx(m, Z.col)];
+      const float2 oth = ld_cl(rb + 8u * (uint32_t)xl_idx(m, Z.col));
       v[a] = Z.ry == 0 ? cadd(own, oth) : ctw<-1>(csub(oth, own), S.w128[m]);
     }
   }
@@ -390,36 +392,27 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
     P.K[n] = Kq;
     P.K[N + n] = Kd;
   }
-  if (n <= P.hmax) {
-    float2 *hst = P.hist + (long long)n * M + qoff + gi;
-#pragma unroll
-    for (int d = 0; d < 8; d++) st_stream(hst + 8 * d, v[d], pol_first);
-  }
+  // density terms of a paired step into the accumulator registers (stored
+  // after the cluster arrive below)
   const int n0 = N / 2;
-  if (m2 <= n) {
-    const int Kref = (n == n0) ? Kq + (m2 == n ? Kd : P.K[N + m2]) : P.K[2 * N];
-    if (n == n0 && zz == 0 && q == 0 && tid == 0) P.K[2 * N] = Kref;
-    if (pair) {
-      const float f1 = ldexpf(1.0f, Kq + P.K[N + m2] - Kref);
-      const float f2 = ldexpf(1.0f, P.K[m2] + Kd - Kref);
-      if (same_acc) {
+  const int Kref = (m2 <= n) ? ((n == n0) ? Kq + (m2 == n ? Kd : P.K[N + m2]) : P.K[2 * N]) : 0;
+  if (m2 <= n && n == n0 && zz == 0 && q == 0 && tid == 0) P.K[2 * N] = Kref;
+  if (pair) {
+    const float f1 = ldexpf(1.0f, Kq + P.K[N + m2] - Kref);
+    const float f2 = ldexpf(1.0f, P.K[m2] + Kd - Kref);
+    if (same_acc) {
 #pragma unroll
-        for (int d = 0; d < 8; d++) {
-          const float2 h = swz(Hs, row, tr + 8 * d);
-          a1[8 * d] = acc1[d] + fmaf(v[d].x * h.y, f1, (h.x * v[d].y) * f2);
-        }
-      } else {
-#pragma unroll
-        for (int d = 0; d < 8; d++) {
-          const float2 h = swz(Hs, row, tr + 8 * d);
-          a1[8 * d] = acc1[d] + (v[d].x * h.y) * f1;
-          a2[8 * d] = acc2[d] + (h.x * v[d].y) * f2;
-        }
+      for (int d = 0; d < 8; d++) {
+        const float2 h = swz(Hs, row, tr + 8 * d);
+        acc1[d] = acc1[d] + fmaf(v[d].x * h.y, f1, (h.x * v[d].y) * f2);
       }
     } else {
-      const float f = ldexpf(1.0f, Kq + Kd - Kref);
 #pragma unroll
-      for (int d = 0; d < 8; d++) a1[8 * d] += (v[d].x * v[d].y) * f;
+      for (int d = 0; d < 8; d++) {
+        const float2 h = swz(Hs, row, tr + 8 * d);
+        acc1[d] = acc1[d] + (v[d].x * h.y) * f1;
+        acc2[d] = acc2[d] + (h.x * v[d].y) * f2;
+      }
     }
   }
   // quadrant sums: error-free FP32 two-sums within the thread and the warp
@@ -462,7 +455,28 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
   // forward x (decimation in frequency): the x partner's real-space values
   // through Es (its staged factors are consumed)
   if (!last) quad_forward_publish(v, Es, Z);
-  cl_sync();  // quadrant sums and the exchange values visible in the cluster
+  cl_arrive();  // quadrant sums and the exchange values released to the cluster
+  // this step's global writes, issued after the arrive so that its release
+  // does not wait for them (the new accumulator values were formed above,
+  // while the staged partner plane Hs was still this CTA's)
+  if (n <= P.hmax) {
+    float2 *hst = P.hist + (long long)n * M + qoff + gi;
+#pragma unroll
+    for (int d = 0; d < 8; d++) st_stream(hst + 8 * d, v[d], pol_first);
+  }
+  if (pair) {
+#pragma unroll
+    for (int d = 0; d < 8; d++) a1[8 * d] = acc1[d];
+    if (!same_acc) {
+#pragma unroll
+      for (int d = 0; d < 8; d++) a2[8 * d] = acc2[d];
+    }
+  } else if (m2 == n) {
+    const float f = ldexpf(1.0f, Kq + Kd - Kref);
+#pragma unroll
+    for (int d = 0; d < 8; d++) a1[8 * d] += (v[d].x * v[d].y) * f;
+  }
+  cl_wait();
   if (q == 0 && tid == 0) {
     // plane sums over the four quadrants, in rank order
     double sqv = 0.0, sdv = 0.0;
@@ -565,17 +579,6 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
     for (int d = 0; d < 8; d++) v[d] = make_float2(fmaf(v[d].x, eg[d], fmaf(m_hi, eg[d], m_lo * eg[d])) * sc, 0.f);
   }
   if (zz == 0 && Z.q == 0 && tid == 0) K[n] = Kn;
-  if (sweep == 0) {
-    float *h = P.hist + (long long)n * M + qoff + gi;
-#pragma unroll
-    for (int d = 0; d < 8; d++) h[8 * d] = v[d].x;
-  } else {
-    const float *o = P.hist + (long long)(Ng - 1 - n) * M + qoff + gi;
-    const float f = ldexpf(1.0f, Kn + P.K[Ng - 1 - n]);
-    float *acc = P.acc + qoff + gi;
-#pragma unroll
-    for (int d = 0; d < 8; d++) acc[8 * d] += (v[d].x * o[8 * d]) * f;
-  }
   // quadrant sum: error-free FP32 two-sums within the thread and the warp
   float sa = 0.f, ca = 0.f;
 #pragma unroll
@@ -599,7 +602,20 @@ __global__ void __cluster_dims__(4, 1, 1) __launch_bounds__(512, 2)
   }
   const bool last = (n == Ng - 1);
   if (!last) quad_forward_publish(v, Xs, Z);
-  cl_sync();  // quadrant sums and the exchange values visible in the cluster
+  cl_arrive();  // quadrant sums and the exchange values released to the cluster
+  // this step's global writes after the arrive (its release does not wait for them)
+  if (sweep == 0) {
+    float *h = P.hist + (long long)n * M + qoff + gi;
+#pragma unroll
+    for (int d = 0; d < 8; d++) h[8 * d] = v[d].x;
+  } else {
+    const float *o = P.hist + (long long)(Ng - 1 - n) * M + qoff + gi;
+    const float f = ldexpf(1.0f, Kn + P.K[Ng - 1 - n]);
+    float *acc = P.acc + qoff + gi;
+#pragma unroll
+    for (int d = 0; d < 8; d++) acc[8 * d] += (v[d].x * o[8 * d]) * f;
+  }
+  cl_wait();
   if (Z.q == 0 && tid == 0) {
     double sv = 0.0;
     for (int r = 0; r < 4; r++) sv += ld_cl_d(cl_map(&S.qs[0], (uint32_t)r));
