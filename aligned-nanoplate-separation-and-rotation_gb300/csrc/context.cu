@@ -2282,11 +2282,11 @@ static void build_step_jobs(scft_ctx *c) {
 }
 
 // The graph body of scft_step_fields (mixed form, no grafted chains): per
-// sweep group on its side stream, the upload of its instances' fields from
-// host memory, their realness check (results copied to pinned host memory,
-// read after the call's synchronisation), the FP64 forward transform of the
-// fields in use (the inactive pairs are zeroed: they do not enter the
-// model), then the density build and n_iter updates of the group.  One
+// sweep group on its side stream, the upload of its instances' fields in use
+// from host memory (the inactive pairs are zeroed: they do not enter the
+// model), their realness check (results copied to pinned host memory, read
+// after the call's synchronisation), the FP64 forward transform of the
+// fields in use, then the density build and n_iter updates of the group.  One
 // group's upload runs beside another group's compute.
 static void step_body(scft_ctx *c, const double *const *w, int n_iter) {
   cudaStream_t st = c->st;
@@ -2297,10 +2297,23 @@ static void step_body(scft_ctx *c, const double *const *w, int n_iter) {
     cudaStream_t sg = c->side[g];
     CK(cudaStreamWaitEvent(sg, c->ev_fork, 0));
     const int cnt = gr.inst_end - gr.inst_begin;
+    // the fields in use come from the host (one copy per run of adjacent
+    // fields in use); the pairs whose chi is 0 are set to zero instead
     for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) {
       const int k = c->job_order[oi];
       Instance &I = c->inst[k];
-      CK(cudaMemcpyAsync(I.w[0], w[k], sizeof(double2) * 7 * (size_t)I.M, cudaMemcpyHostToDevice, sg));
+      const bool active[7] = {true, I.cab != 0.0, I.cab != 0.0, I.cbc != 0.0, I.cbc != 0.0, I.cac != 0.0,
+                              I.cac != 0.0};
+      const size_t fb = sizeof(double2) * (size_t)I.M;  // bytes per field
+      for (int f = 0; f < 7;) {
+        int f1 = f + 1;
+        while (f1 < 7 && active[f1] == active[f]) f1++;
+        if (active[f])
+          CK(cudaMemcpyAsync(I.w[f], w[k] + 2 * (size_t)I.M * f, fb * (f1 - f), cudaMemcpyHostToDevice, sg));
+        else
+          CK(cudaMemsetAsync(I.w[f], 0, fb * (f1 - f), sg));
+        f = f1;
+      }
     }
     k_real_check_all<<<dim3(kCheckBlocks, cnt), 256, 0, sg>>>(c->d_fi_ord + gr.inst_begin, nullptr,
                                                               c->d_realout + 128 * (size_t)gr.inst_begin);
@@ -2308,13 +2321,6 @@ static void step_body(scft_ctx *c, const double *const *w, int n_iter) {
     c->launches++;
     CK(cudaMemcpyAsync(c->h_pin + 128 * (size_t)gr.inst_begin, c->d_realout + 128 * (size_t)gr.inst_begin,
                        sizeof(double) * 128 * (size_t)cnt, cudaMemcpyDeviceToHost, sg));
-    for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) {
-      Instance &I = c->inst[c->job_order[oi]];
-      const bool active[7] = {true, I.cab != 0.0, I.cab != 0.0, I.cbc != 0.0, I.cbc != 0.0, I.cac != 0.0,
-                              I.cac != 0.0};
-      for (int f = 0; f < 7; f++)
-        if (!active[f]) CK(cudaMemsetAsync(I.w[f], 0, sizeof(double2) * (size_t)I.M, sg));
-    }
     if (c->step_npj[g] > 0) {
       LK(launch_plane_fft<double>(c->shp_plane, c->step_pj[g], c->step_npj[g], c->d_geoms, c->d_tw64, -1, 0, sg));
       LK(launch_col_fft<double>(c->shp_col, c->step_cj[g], c->step_ncj[g], c->d_geoms, c->d_tw64, 0, 1, sg));

@@ -39,7 +39,10 @@ METRIC = "SCFT iters/s @64^3,N=100"
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant
 # kernel, from an ncu capture of the same workload (the paired plane-pass step;
 # profiles/mixed_kernels_sweep15_64_N100_ncu.txt).  Only valid for that workload.
-NCU_TRAFFIC = {("sweep15_64_N100", "k_mix_plane64"): 125.905664e6 + 16.460032e6}
+NCU_TRAFFIC = {("sweep15_64_N100", "k_mix_plane64"): 125.905664e6 + 16.460032e6,
+               # captured on sweep4_128x128x64_N50 (2,097,152 points of a paired step),
+               # scaled by points to the 33,554,432 of one launch of this workload
+               ("graft8_128x128x256_N200", "k_mix_plane128"): (67.17568e6 + 0.783104e6) * 16}
 UNIT = "iters/s"
 
 
@@ -213,6 +216,15 @@ def job_rate(units_per_rank: float, world: int, seconds_max: float) -> float:
     """Whole-job rate: the units every rank processed (the same batch on each
     rank, weak scaling) over the slowest rank's time."""
     return units_per_rank * world / seconds_max
+
+
+def fields_in_use(p, form):
+    """Fields scft_step_fields copies from the host for one instance: all 7
+    in the FP64 method (it runs set_fields), w+ and the pairs of nonzero chi
+    in the mixed form."""
+    if form != "mixed" or p.Ng > 0 or p.do_cl:
+        return 7
+    return 1 + 2 * sum(1 for chi in (p.chi_ab, p.chi_bc, p.chi_ac) if chi != 0.0)
 
 
 def converge_to_stop_rule(ctx, n, V, tol, itmax, print_freq=25):
@@ -508,7 +520,9 @@ def main():
     torch.cuda.synchronize()
     t_e2e = allmax(time.perf_counter() - t0)
     e2e = {"value": job_rate(n_inst * e2e_steps, world, t_e2e), "unit": UNIT,
-           "h2d_bytes_per_step": int(sum(7 * 16 * m for m in M)),
+           # the fields in use (w+ and the pairs of nonzero chi; the mixed
+           # form's step sets the others to zero instead of copying them)
+           "h2d_bytes_per_step": int(sum(fields_in_use(p, form) * 16 * m for p, m in zip(params, M))),
            # H (5 doubles per instance) and, in the mixed form, the realness
            # check's maxima (128 doubles per instance) that the call reads back
            "d2h_bytes_per_step": int(5 * 8 * n_inst + (128 * 8 * n_inst if form == "mixed" else 0))}

@@ -144,9 +144,9 @@ int scft_set_fields_all(scft_ctx *ctx, const double *const *w);
 int scft_set_fields(scft_ctx *ctx, int inst, const double *w);
 int scft_get_fields(scft_ctx *ctx, int inst, double *w);
 
-/* One call for "iterate from these fields": uploads the seven fields of
- * every instance from host memory (w[inst], each as for scft_set_fields;
- * pinned memory lets the uploads overlap compute), builds the densities of
+/* One call for "iterate from these fields": uploads the fields of every
+ * instance from host memory (w[inst], each as for scft_set_fields; pinned
+ * memory lets the uploads overlap compute), builds the densities of
  * those fields, runs n_iter field updates (as scft_update_1s) and writes H
  * into H_out (5 doubles per instance, as scft_calc_H), with one
  * synchronisation.  The sequence scft_set_fields_all, scft_update_1s,
@@ -155,9 +155,10 @@ int scft_get_fields(scft_ctx *ctx, int inst, double *w);
  * registered; others run the sequence), each sweep group's upload, realness check,
  * field transform, density build and updates run as one chain on its own
  * stream inside one captured graph (re-captured when the host pointers or
- * n_iter change), so one group's upload runs beside another group's compute,
- * and the fields of pairs whose chi is 0 are set to zero (they do not enter
- * the model).  The realness check of the mixed form is read after the work:
+ * n_iter change), so one group's upload runs beside another group's compute;
+ * only w+ and the pairs of nonzero chi are copied, and the fields of pairs
+ * whose chi is 0 are set to zero (they do not enter the model).  The
+ * realness check of the mixed form is read after the work:
  * SCFT_ERR_COMPLEX then means this call's results are invalid.  Returns
  * SCFT_ERR_NAN / SCFT_ERR_QNONPOS like scft_calc_H.  No counterpart in the
  * reference (its driver keeps the fields in host memory throughout). */

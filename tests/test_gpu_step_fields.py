@@ -88,3 +88,26 @@ def test_step_fields_rejects_complex_fields_in_the_mixed_form(S):
         with pytest.raises(S.ScftError) as e:
             c.step_fields_raw([b.ctypes.data for b in bufs], 1, out.ctypes.data)
         assert e.value.code == S.ERR_COMPLEX and "instance 1" in str(e.value)
+
+
+def test_step_fields_ignores_the_pairs_whose_chi_is_zero(S):
+    """Only w+ and the pairs of nonzero chi are read from the host: values in
+    the others (here chi_bc = chi_ac = 0) change nothing."""
+    ps, fields = batch(S, S.PREC_MIXED)
+    rng = np.random.default_rng(5)
+    noisy = []
+    for p, f in zip(ps, fields):
+        g = dict(f)
+        sh = (p.Nx[2], p.Nx[1], p.Nx[0])
+        for name in ("wbcp", "wbcm", "wacp", "wacm"):
+            g[name] = rng.standard_normal(sh) + 0j
+        noisy.append(g)
+    clean, dirty = host_buffers(S, ps, fields), host_buffers(S, ps, noisy)
+    res = []
+    for bufs in (clean, dirty):
+        with S.Context(ps) as c:
+            c.set_sweep_groups(2)
+            out = np.zeros((len(ps), 5))
+            assert c.step_fields_raw([b.ctypes.data for b in bufs], 1, out.ctypes.data) == S.OK
+            res.append(out.copy())
+    np.testing.assert_array_equal(res[0], res[1])
