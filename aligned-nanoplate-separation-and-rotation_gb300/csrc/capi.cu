@@ -302,7 +302,8 @@ int scft_get_schedule(scft_ctx *c, int *groups, int *phases, int *col_tile, int 
   if (int s = check_ctx(c, 0)) return s;
   if (groups) *groups = c->sweep_streams;
   if (phases) *phases = c->sweep_phases;
-  if (col_tile) *col_tile = (c->colfast || c->anyfast || c->xy128) ? c->col64_tx : 0;
+  if (col_tile)
+    *col_tile = ((c->colfast || c->anyfast || c->xy128 || c->any96) && c->plane64_form != 2) ? c->col64_tx : 0;
   if (persistent) *persistent = c->sweep_persistent;
   return SCFT_OK;
 }

@@ -355,14 +355,17 @@ void validate(const scft_params &p) {
 
 // Per-axis h_d = 1 - exp(-k_d^2/6) with get_k's branch
 // (code/array_utils.cpp:248-265), g(k) = prod_d (1 - h_d), as [hx | hy | hz]
-// for the specialised z passes.  parity_xy: x and y in the parity-major order
-// of the 128 x 128 plane pass (wavenumber k at position (k % 2) n/2 + k / 2).
-std::vector<float> axis_h_table(const scft_params &p, bool parity_xy) {
+// for the specialised z passes.  order 2: x and y in the parity-major order
+// of the 128 x 128 plane pass (wavenumber k at position (k % 2) n/2 + k / 2);
+// order 3: x in the residue-major order of the 96 x 64 plane pass (k at
+// (k % 3) n/3 + k / 3); 0: natural order.
+std::vector<float> axis_h_table(const scft_params &p, int order) {
   std::vector<float> ht;
   for (int d = 0; d < 3; d++)
     for (int pos = 0; pos < p.Nx[d]; pos++) {
-      const int h = p.Nx[d] / 2;
-      const int nn = (parity_xy && d < 2) ? 2 * (pos % h) + pos / h : pos;
+      const int r = (order == 2 && d < 2) ? 2 : ((order == 3 && d == 0) ? 3 : 1);
+      const int h = p.Nx[d] / r;
+      const int nn = r * (pos % h) + pos / h;
       const double k = (double(nn) < double(p.Nx[d]) / 2.) ? 2 * kPI * double(nn) / p.L[d]
                                                           : 2 * kPI * double(nn - p.Nx[d]) / p.L[d];
       ht.push_back((float)(-std::expm1(-k * k / 6.0)));
@@ -475,7 +478,7 @@ void setup_instance(scft_ctx *c, Instance &I, int idx) {
     I.acc32[1] = dalloc<float>(c, M);
     I.part = dalloc<double>(c, (size_t)2 * I.N * g.nz);
     I.K = dalloc<int>(c, (size_t)2 * I.N + 1);
-    I.htab32 = dupload(c, axis_h_table(p, false));  // alpha, beta: mix_coefficients_final, once the plates fix phiD, phiG
+    I.htab32 = dupload(c, axis_h_table(p, 0));  // alpha, beta: mix_coefficients_final, once the plates fix phiD, phiG
   }
   I.qpart = dalloc<double2>(c, g.nz);
   I.scal = dalloc<double2>(c, kNumScalars);
@@ -736,6 +739,7 @@ void check_device_error(scft_ctx *c) {
 
 ColJob *col64_jobs(scft_ctx *c) { return c->d_mix64_cj_tx[c->col64_tx == 8 ? 0 : (c->col64_tx == 16 ? 1 : 2)]; }
 ColJob *col128_jobs(scft_ctx *c) { return c->d_mix128_cj_tx[c->col64_tx == 8 ? 0 : (c->col64_tx == 16 ? 1 : 2)]; }
+ColJob *col96_jobs(scft_ctx *c) { return c->d_mix96_cj_tx[c->col64_tx == 8 ? 0 : (c->col64_tx == 16 ? 1 : 2)]; }
 
 // Sweep groups: the job order is cut into `sweep_phases` contiguous phases and
 // each phase into `sweep_streams` contiguous groups, all of about equal N * M.
@@ -774,11 +778,11 @@ void build_groups(scft_ctx *c) {
     const int G = std::max(1, std::min(c->sweep_streams, pe - p0));
     int i0 = p0;
     for (int i1 : cut(p0, pe, G)) {
-      // a group never straddles the 64^3 instances and the others of a
-      // batch of mixed grids: split at that boundary
+      // a group never straddles the kernel classes of a batch of mixed grids
+      // (64^3, 96 x 64 x 64, the rest): split at those boundaries
       for (int a = i0; a < i1;) {
         int b = a + 1;
-        while (b < i1 && (c->fast64.empty() || c->fast64[b] == c->fast64[a])) b++;
+        while (b < i1 && (c->fast64.empty() || (c->fast64[b] == c->fast64[a] && c->fast96[b] == c->fast96[a]))) b++;
         scft_ctx::SweepGroup gr;
         gr.inst_begin = a;
         gr.inst_end = b;
@@ -788,6 +792,7 @@ void build_groups(scft_ctx *c) {
         gr.cj_end = c->inst_cj_end[b - 1];
         gr.phase = ph;
         gr.fast = c->fast64.empty() ? 0 : c->fast64[a];
+        gr.fast96 = c->fast96.empty() ? 0 : c->fast96[a];
         c->groups.push_back(gr);
         a = b;
       }
@@ -1075,13 +1080,24 @@ void build_jobs(scft_ctx *c) {
       const int *X = c->inst[k].p.Nx;
       return X[0] == 64 && X[1] == 64 && X[2] == 64;
     };
+    auto is96 = [&](int k) {
+      const int *X = c->inst[k].p.Nx;
+      return X[0] == 96 && X[1] == 64 && X[2] == 64;
+    };
     c->fast64.assign(n, 0);
+    c->fast96.assign(n, 0);
     c->anyfast = 0;
+    c->any96 = 0;
     if (!c->xy64) {
-      std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return is64(a) && !is64(b); });
+      // 64^3 instances first, then 96 x 64 x 64, then the rest
+      auto cls = [&](int k) { return is64(k) ? 0 : (is96(k) ? 1 : 2); };
+      std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cls(a) < cls(b); });
       for (int oi = 0; oi < n; oi++) {
         c->fast64[oi] = is64(order[oi]) ? 1 : 0;
+        c->fast96[oi] = is96(order[oi]) ? 1 : 0;
         c->anyfast = c->anyfast || c->fast64[oi];
+        if (c->fast96[oi] && !c->any96) c->first96 = oi;
+        c->any96 = c->any96 || c->fast96[oi];
       }
     }
     // one plane job per z (q and qdag packed), FP32 column jobs
@@ -1176,7 +1192,7 @@ void build_jobs(scft_ctx *c) {
       }
       for (int oi = 0; oi < n; oi++) {
         Instance &I = c->inst[order[oi]];
-        const std::vector<float> ht = axis_h_table(I.p, true);
+        const std::vector<float> ht = axis_h_table(I.p, 2);
         CK(cudaMemcpyAsync(I.htab32, ht.data(), sizeof(float) * ht.size(), cudaMemcpyHostToDevice, c->st));
         c->mix64_tab.push_back(c->h_mi[order[oi]]);
         const unsigned long long rows = 128ULL * (unsigned long long)I.p.Nx[2];
@@ -1186,7 +1202,29 @@ void build_jobs(scft_ctx *c) {
       CK(cudaStreamSynchronize(c->st));  // the host tables are released
       ensure_err(c);
     }
-    if (c->xy64 || c->anyfast) {
+    if (c->any96) {
+      // residue-major x factor tables and z-pass jobs (64 x (96 / tx) per
+      // instance) of the 96 x 64 x 64 instances, contiguous in job order
+      for (int t = 0; t < 3; t++) {
+        const int tx = 8 << t;
+        std::vector<ColJob> cj;
+        for (int oi = 0; oi < n; oi++) {
+          if (!c->fast96[oi]) continue;
+          Instance &I = c->inst[order[oi]];
+          for (int y = 0; y < 64; y++)
+            for (int x0 = 0; x0 < 96; x0 += tx) cj.push_back(ColJob{I.work32, I.htab32, I.geom, x0, y});
+        }
+        c->d_mix96_cj_tx[t] = dupload(c, cj);
+      }
+      for (int oi = 0; oi < n; oi++) {
+        if (!c->fast96[oi]) continue;
+        Instance &I = c->inst[order[oi]];
+        const std::vector<float> ht = axis_h_table(I.p, 3);
+        CK(cudaMemcpyAsync(I.htab32, ht.data(), sizeof(float) * ht.size(), cudaMemcpyHostToDevice, c->st));
+      }
+      CK(cudaStreamSynchronize(c->st));  // the host tables are released
+    }
+    if (c->xy64 || c->anyfast || c->any96) {
       c->mix64_tab.clear();
       c->tmE.clear();
       c->tmH.clear();
@@ -1197,6 +1235,10 @@ void build_jobs(scft_ctx *c) {
           const unsigned long long rows = 64ULL * (unsigned long long)I.p.Nx[2];
           c->tmE.push_back(tensor_map_rows(I.E32, rows, 128));
           c->tmH.push_back(tensor_map_rows(I.hist32, rows * (unsigned long long)(I.hmax + 1), 128));
+        } else if (c->fast96[oi]) {  // rows of 96 float2
+          const unsigned long long rows = 64ULL * (unsigned long long)I.p.Nx[2];
+          c->tmE.push_back(tensor_map_rows(I.E32, rows, 192));
+          c->tmH.push_back(tensor_map_rows(I.hist32, rows * (unsigned long long)(I.hmax + 1), 192));
         } else {
           c->tmE.push_back(CUtensorMap{});
           c->tmH.push_back(CUtensorMap{});
@@ -1442,7 +1484,7 @@ void seq_update_1s(scft_ctx *c) {
 // The group's sweep runs as one persistent launch: the context asks for it,
 // and the group's instances are 64 x 64 x 64 grids, at most kMix64MaxInst.
 bool persistent_group(const scft_ctx *c, const scft_ctx::SweepGroup &gr) {
-  if (!c->sweep_persistent) return false;
+  if (!c->sweep_persistent || c->plane64_form == 2) return false;
   const bool p64 = c->xy64 || gr.fast, z64 = c->colfast || gr.fast;
   const int nzi = gr.fast ? 64 : c->inst[0].p.Nx[2];
   return p64 && z64 && nzi == 64 && gr.inst_end - gr.inst_begin <= kMix64MaxInst;
@@ -1460,7 +1502,11 @@ void mix_group_sweep(scft_ctx *c, int g, cudaStream_t sg) {
     CK(cudaMemsetAsync(I.acc32[0], 0, sizeof(float) * I.M, sg));
     CK(cudaMemsetAsync(I.acc32[1], 0, sizeof(float) * I.M, sg));
   }
-  const bool p64 = c->xy64 || gr.fast, z64 = c->colfast || gr.fast;
+  // plane form 2: the generic kernels for every group (the reference the
+  // specialised classes are checked against)
+  const bool spec = c->plane64_form != 2;
+  const bool p64 = spec && (c->xy64 || gr.fast), z64 = spec && (c->colfast || gr.fast);
+  const bool c96 = spec && gr.fast96, c128 = spec && c->xy128;
   const int nzi = gr.fast ? 64 : c->inst[0].p.Nx[2];
   const void *twz = gr.fast ? c->d_tw32_64 : c->d_tw32_z;
   if (persistent_group(c, gr)) {
@@ -1483,6 +1529,7 @@ void mix_group_sweep(scft_ctx *c, int g, cudaStream_t sg) {
   }
   const int per = 64 * (64 / c->col64_tx);  // z-pass jobs per instance of the 64-point kernels
   const int per128 = 128 * (128 / c->col64_tx);  // and of the 128 x 128 kernels
+  const int per96 = 64 * (96 / c->col64_tx);     // and of the 96 x 64 x 64 instances
   for (int s = 0; s < c->nmax; s++) {
     // instances of the group still active at step s: a prefix (decreasing N)
     int act = 0;
@@ -1493,7 +1540,10 @@ void mix_group_sweep(scft_ctx *c, int g, cudaStream_t sg) {
     const int cnt = c->inst_pj_end[last] - gr.pj_begin;
     const int cc = c->inst_cj_end[last] - gr.cj_begin;
     if (s > 0) {
-      if (c->xy128)
+      if (c96)
+        LK(launch_mix_col64(col96_jobs(c) + (size_t)(gr.inst_begin - c->first96) * per96, act * per96, c->d_tw32_64,
+                            96, 64, 64, c->col64_tx, sg));
+      else if (c128)
         LK(launch_mix_col64(col128_jobs(c) + (size_t)gr.inst_begin * per128, act * per128, c->d_tw32_z, 128, 128,
                             nzi, c->col64_tx, sg));
       else if (z64)
@@ -1502,7 +1552,11 @@ void mix_group_sweep(scft_ctx *c, int g, cudaStream_t sg) {
       else
         LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cc, c->d_geoms, c->d_tw32, 3, 1, sg));
     }
-    if (c->xy128)
+    if (c96)
+      LK(launch_mix_plane96(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
+                            c->tmH.data() + gr.inst_begin, act, 64, c->d_tw32_64, c->d_tw32_32, c->d_tw32_96, s,
+                            c->d_err, sg));
+    else if (c128)
       LK(launch_mix_plane128(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
                              c->tmH.data() + gr.inst_begin, act, nzi, c->d_tw32_64, c->d_tw32_128, s, c->d_err, sg));
     else if (p64)
@@ -1590,7 +1644,7 @@ void seq_mix(scft_ctx *c, bool update) {
   if (c->ngmax > 0) {
     for (auto &I : c->inst)
       if (I.graft) CK(cudaMemsetAsync(I.gacc32, 0, sizeof(float) * I.M, st));
-    if (c->xy128) {
+    if (c->xy128 && c->plane64_form != 2) {
       // the cluster plane pass and the specialised z pass (parity-major planes)
       const int nz0 = c->inst[0].p.Nx[2];
       const int per128 = 128 * (128 / c->col64_tx);
@@ -1657,8 +1711,8 @@ void ctx_create(scft_ctx *c, const scft_params *params, int n_inst) {
       g.ax[d].tw = off[nn];
     }
   }
-  // the 64- and 128-point tables of the 128 x 128 plane pass
-  for (int nn : {64, 128})
+  // the 32-, 64-, 96- and 128-point tables of the cluster plane passes
+  for (int nn : {32, 64, 96, 128})
     if (!off.count(nn)) {
       off[nn] = (int)tw.size();
       const long double two_pi = 6.283185307179586476925286766559005768L;
@@ -1673,6 +1727,8 @@ void ctx_create(scft_ctx *c, const scft_params *params, int n_inst) {
   c->d_tw32 = dupload(c, tw32);
   c->d_tw32_64 = static_cast<float2 *>(c->d_tw32) + off[64];
   c->d_tw32_128 = static_cast<float2 *>(c->d_tw32) + off[128];
+  c->d_tw32_32 = static_cast<float2 *>(c->d_tw32) + off[32];
+  c->d_tw32_96 = static_cast<float2 *>(c->d_tw32) + off[96];
   {
     const int nz0 = c->inst.empty() ? 0 : c->inst[0].p.Nx[2];
     if (off.count(nz0)) c->d_tw32_z = static_cast<float2 *>(c->d_tw32) + off[nz0];
@@ -1792,7 +1848,7 @@ void ctx_set_wait_limit(scft_ctx *c, int polls) {
 // Form of the 64-point plane pass (0: block-barrier exchanges, 1: warp-local
 // columns); results are bit-identical, the captured graphs hold the old form.
 void ctx_set_plane_form(scft_ctx *c, int form) {
-  if (form < 0 || form > 1) throw ScftError(SCFT_ERR_ARG, "plane form must be 0 or 1");
+  if (form < 0 || form > 2) throw ScftError(SCFT_ERR_ARG, "plane form must be 0, 1 or 2");
   c->plane64_form = form;
   if (c->g_update) {
     CK(cudaGraphExecDestroy(c->g_update));
@@ -1863,7 +1919,7 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
     if (g <= n) gs.push_back(g);
   if (c->xy128 && c->inst[0].p.Nx[2] == 256)
     txs = {8, 16};  // the 256-point z pass takes at most 16 columns per CTA
-  else if (c->colfast || c->anyfast || c->xy128)
+  else if (c->colfast || c->anyfast || c->xy128 || c->any96)
     txs = {8, 16, 32};
   else
     txs = {c->col64_tx};
@@ -1974,7 +2030,7 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
   }
   *groups_out = bg;
   *phases_out = bp;
-  *tx_out = (c->colfast || c->anyfast || c->xy128) ? bt : 0;
+  *tx_out = (c->colfast || c->anyfast || c->xy128 || c->any96) ? bt : 0;
   *ms_out = best;
 }
 
@@ -2051,11 +2107,11 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   CK(cudaEventCreate(&e2));
   CK(cudaEventRecord(e0, c->st));
   for (int r = 0; r < reps; r++) {
-    if (c->mixed && c->xy128)
+    if (c->mixed && c->xy128 && c->plane64_form != 2)
       LK(launch_mix_plane128(c->mix64_tab.data(), c->tmE.data(), c->tmH.data(),
                              c->prop_pj_count[s] / c->inst[0].p.Nx[2], c->inst[0].p.Nx[2], c->d_tw32_64,
                              c->d_tw32_128, s, c->d_err, c->st));
-    else if (c->mixed && c->xy64)
+    else if (c->mixed && c->xy64 && c->plane64_form != 2)
       LK((c->plane64_form ? launch_mix_plane64w : launch_mix_plane64)(c->mix64_tab.data(), c->tmE.data(), c->tmH.data(),
                             c->prop_pj_count[s] / c->inst[0].p.Nx[2], c->inst[0].p.Nx[2], c->d_tw32_64, s, c->d_err,
                             c->st));
@@ -2069,10 +2125,10 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   }
   CK(cudaEventRecord(e1, c->st));
   for (int r = 0; r < reps; r++) {
-    if (c->mixed && c->xy128)
+    if (c->mixed && c->xy128 && c->plane64_form != 2)
       LK(launch_mix_col64(col128_jobs(c), (c->prop_pj_count[s] / c->inst[0].p.Nx[2]) * 128 * (128 / c->col64_tx),
                           c->d_tw32_z, 128, 128, c->inst[0].p.Nx[2], c->col64_tx, c->st));
-    else if (c->mixed && c->colfast)
+    else if (c->mixed && c->colfast && c->plane64_form != 2)
       LK(launch_mix_col64(col64_jobs(c), (c->prop_pj_count[s] / c->inst[0].p.Nx[2]) * 64 * (64 / c->col64_tx),
                           c->d_tw32_z, 64, 64, c->inst[0].p.Nx[2], c->col64_tx, c->st));
     else if (c->mixed)

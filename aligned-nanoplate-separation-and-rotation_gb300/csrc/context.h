@@ -159,7 +159,7 @@ struct scft_ctx {
   // run on the 64-point plane and z kernels (a batch of 64 x 64 planes only
   // uses them throughout: xy64)
   struct SweepGroup {
-    int inst_begin, inst_end, pj_begin, pj_end, cj_begin, cj_end, phase, fast;
+    int inst_begin, inst_end, pj_begin, pj_end, cj_begin, cj_end, phase, fast, fast96;
   };
   std::vector<SweepGroup> groups;
   int sweep_phases = 1;  // requested number of sequential phases
@@ -168,6 +168,14 @@ struct scft_ctx {
   // position oi), which come first in job order; anyfast = some instance is one
   std::vector<char> fast64;
   int anyfast = 0;
+  // batch with 96 x 64 x 64 instances: fast96[oi] = 1 for those (after the
+  // 64^3 ones in job order), run by the three-CTA cluster plane pass
+  // (kernels_mixed96.cu) and the 64-point z pass; first96 = job-order
+  // position of the first of them
+  std::vector<char> fast96;
+  int any96 = 0, first96 = 0;
+  void *d_tw32_32 = nullptr, *d_tw32_96 = nullptr;  // 32- and 96-point twiddle tables inside d_tw32
+  scft::ColJob *d_mix96_cj_tx[3] = {};               // their z-pass jobs for 8, 16, 32 columns per CTA
   // mixed field-level data in job order: FieldInst table, the FP32 transform
   // jobs of z32 and the FP64 ones of zg (grafted instances); fld_end[4 oi + k]
   // = end of instance oi's jobs in list k (z32 plane, z32 column, zg plane,

@@ -52,43 +52,12 @@ namespace scft {
 
 namespace {
 
-__device__ __forceinline__ uint32_t cl_rank() {
-  uint32_t r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arrive.release;\n" ::: "memory"); }
-__device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.acquire;\n" ::: "memory"); }
-__device__ __forceinline__ void cl_sync() {
-  cl_arrive();
-  cl_wait();
-}
-// address of this CTA's shared object p in the shared memory of CTA `rank` of the cluster
-__device__ __forceinline__ uint32_t cl_map(const void *p, uint32_t rank) {
-  uint32_t r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
-  return r;
-}
-__device__ __forceinline__ float2 ld_cl(uint32_t a) {
-  float2 v;
-  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];\n" : "=f"(v.x), "=f"(v.y) : "r"(a) : "memory");
-  return v;
-}
-__device__ __forceinline__ double ld_cl_d(uint32_t a) {
-  double v;
-  asm volatile("ld.shared::cluster.f64 %0, [%1];\n" : "=d"(v) : "r"(a) : "memory");
-  return v;
-}
-
 // Element (row, x) of a 64 x 64 exchange quadrant: rows of 64 float2 with
 // bit 3 of x flipped on odd rows.  Each half-warp's access is then free of
 // bank conflicts in both phases: two rows x 8 consecutive x (row phase) take
 // the two 8-slot halves of the 16 eight-byte slots, and 16 consecutive x of
 // one row (column phase) take all 16.
 __device__ __forceinline__ int xl_idx(int row, int x) { return row * 64 + (x ^ ((row & 1) << 3)); }
-
-__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
-__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 
 template <int SIGN>
 __device__ __forceinline__ void fft256_group(float2 *v, int t, float2 *xch, int sb, int sc, const float2 *tw) {

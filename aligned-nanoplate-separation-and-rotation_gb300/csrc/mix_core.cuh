@@ -64,6 +64,73 @@ __device__ __forceinline__ float2 swz(const float2 *plane, int row, int x) {
   return plane[(x >> 4) * 1024 + row * 16 + ((((x & 15) >> 1) ^ (row & 7)) << 1) + (x & 1)];
 }
 
+
+// Thread-block clusters: rank in the cluster, barrier (arrive with release,
+// wait with acquire), and loads from a partner CTA's shared memory.
+__device__ __forceinline__ uint32_t cl_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;\n" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cl_arrive() { asm volatile("barrier.cluster.arrive.release;\n" ::: "memory"); }
+__device__ __forceinline__ void cl_wait() { asm volatile("barrier.cluster.wait.acquire;\n" ::: "memory"); }
+__device__ __forceinline__ void cl_sync() {
+  cl_arrive();
+  cl_wait();
+}
+// address of this CTA's shared object p in the shared memory of CTA `rank` of the cluster
+__device__ __forceinline__ uint32_t cl_map(const void *p, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;\n" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ float2 ld_cl(uint32_t a) {
+  float2 v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];\n" : "=f"(v.x), "=f"(v.y) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ double ld_cl_d(uint32_t a) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];\n" : "=d"(v) : "r"(a) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+
+// 32-point transform of a group of 4 threads, thread t holding the 8 values
+// x[t + 4a] (32 = 8 x 4):
+//   Y[t][c]  = sum_a x[t + 4a] w8^(a c)          (DFT8 in registers)
+//   Y[t][c] *= w32^(t c)
+//   exchange: thread t takes c = t and c = t + 4
+//   X[c + 8d] = sum_b Y[b][c] w4^(b d)            (two DFT4)
+// so X[t + 4j] returns in v[j], the input order.  Element (b, c) of the
+// exchange lives at xch[b * sb + c * sc]; WARP: the 4 threads and their
+// exchange area belong to one warp.
+template <int SIGN, bool WARP>
+__device__ __forceinline__ void fft32_group(float2 *v, int t, float2 *xch, int sb, int sc, const float2 *tw32) {
+  dft8f<SIGN>(v);
+#pragma unroll
+  for (int c = 1; c < 8; c++) v[c] = ctw<SIGN>(v[c], tw32[t * c]);
+#pragma unroll
+  for (int c = 0; c < 8; c++) xch[t * sb + c * sc] = v[c];
+  if (WARP) __syncwarp(); else __syncthreads();
+  float2 p[4], q[4];
+#pragma unroll
+  for (int b = 0; b < 4; b++) {
+    p[b] = xch[b * sb + t * sc];
+    q[b] = xch[b * sb + (t + 4) * sc];
+  }
+  if (WARP) __syncwarp(); else __syncthreads();
+  Dft<4, SIGN, float2>::run(p);
+  Dft<4, SIGN, float2>::run(q);
+#pragma unroll
+  for (int d = 0; d < 4; d++) {
+    v[2 * d] = p[d];
+    v[2 * d + 1] = q[d];
+  }
+}
+
 }  // namespace
 
 // 16-point transform in registers, n = a + 4b, k = c + 4d: DFT4 over b,

@@ -84,6 +84,12 @@ cudaError_t launch_mix_col256(const ColJob *jobs, int njobs, const void *tw, int
 // of rows of 128 float2; tw64, tw128: the 64- and 128-point twiddles.
 cudaError_t launch_mix_plane128(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
                                 int nz, const void *tw64, const void *tw128, int n, int *err, cudaStream_t st);
+// Plane pass of step n for 96 x 64 xy planes (kernels_mixed96.cu): three
+// CTAs per plane; tensor maps of rows of 96 float2; tw64, tw32, tw96: the
+// 64-, 32- and 96-point twiddles.
+cudaError_t launch_mix_plane96(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
+                               int nz, const void *tw64, const void *tw32, const void *tw96, int n, int *err,
+                               cudaStream_t st);
 // Graft sweep plane pass of the same family (four CTAs per plane): the
 // grafted instances' views in sweep order (Ng non-increasing), by value.
 template <int CAP> struct Graft128TableT {

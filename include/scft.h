@@ -298,11 +298,15 @@ int scft_set_persistent(scft_ctx *ctx, int on);
  * does not apply) and whether the sweep is persistent. */
 int scft_get_schedule(scft_ctx *ctx, int *groups, int *phases, int *col_tile, int *persistent);
 
-/* Form of the mixed form's 64-point plane pass (no counterpart in the
- * reference): 0 exchanges through a padded shared plane with block barriers
- * (k_mix_plane64), 1 loads the working plane asynchronously into a swizzled
- * shared plane and transforms columns inside one warp (k_mix_plane64w).
- * Results are bit-identical; the autotuner picks one. */
+/* Form of the mixed form's plane pass (no counterpart in the reference):
+ * 0 (default) the specialised kernels of each grid class, with the 64-point
+ * plane pass exchanging through a padded shared plane with block barriers
+ * (k_mix_plane64); 1 the same with the 64-point pass loading the working
+ * plane asynchronously into a swizzled shared plane and transforming
+ * columns inside one warp (k_mix_plane64w; bit-identical, the autotuner
+ * picks 0 or 1); 2 the generic plane and z passes for every instance, the
+ * reference the specialised classes (64 x 64, 96 x 64 x 64 and 128 x 128
+ * planes) are checked against. */
 int scft_set_plane_form(scft_ctx *ctx, int form);
 int scft_get_plane_form(scft_ctx *ctx, int *form);
 
