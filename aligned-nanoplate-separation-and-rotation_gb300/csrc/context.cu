@@ -687,7 +687,7 @@ void setup_plates(scft_ctx *c, Instance &I) {
 // TMA descriptor of a float2 array seen as `rows` rows of 64 float2 (128
 // floats), boxes of 64 rows x 32 floats with the 128-byte swizzle; the entry
 // point comes from the driver (cuTensorMapEncodeTiled) through the runtime.
-CUtensorMap tensor_map_rows(const float2 *base, unsigned long long rows, unsigned row_floats) {
+CUtensorMap tensor_map_rows(const float2 *base, unsigned long long rows, unsigned row_floats, unsigned box_rows = 64) {
   typedef CUresult (*EncodeFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
                                const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -703,7 +703,7 @@ CUtensorMap tensor_map_rows(const float2 *base, unsigned long long rows, unsigne
   CUtensorMap m;
   const cuuint64_t dims[2] = {row_floats, rows};
   const cuuint64_t strides[1] = {row_floats * sizeof(float)};
-  const cuuint32_t box[2] = {32, 64};
+  const cuuint32_t box[2] = {32, box_rows};
   const cuuint32_t estr[2] = {1, 1};
   const CUresult r = encode(&m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float2 *>(base), dims, strides, box, estr,
                             CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
@@ -779,10 +779,12 @@ void build_groups(scft_ctx *c) {
     int i0 = p0;
     for (int i1 : cut(p0, pe, G)) {
       // a group never straddles the kernel classes of a batch of mixed grids
-      // (64^3, 96 x 64 x 64, the rest): split at those boundaries
+      // (64^3, 96 x 64 x 64, 48^3, the rest): split at those boundaries
       for (int a = i0; a < i1;) {
         int b = a + 1;
-        while (b < i1 && (c->fast64.empty() || (c->fast64[b] == c->fast64[a] && c->fast96[b] == c->fast96[a]))) b++;
+        while (b < i1 && (c->fast64.empty() || (c->fast64[b] == c->fast64[a] && c->fast96[b] == c->fast96[a] &&
+                                                c->fast48[b] == c->fast48[a])))
+          b++;
         scft_ctx::SweepGroup gr;
         gr.inst_begin = a;
         gr.inst_end = b;
@@ -793,6 +795,7 @@ void build_groups(scft_ctx *c) {
         gr.phase = ph;
         gr.fast = c->fast64.empty() ? 0 : c->fast64[a];
         gr.fast96 = c->fast96.empty() ? 0 : c->fast96[a];
+        gr.fast48 = c->fast48.empty() ? 0 : c->fast48[a];
         c->groups.push_back(gr);
         a = b;
       }
@@ -1084,20 +1087,29 @@ void build_jobs(scft_ctx *c) {
       const int *X = c->inst[k].p.Nx;
       return X[0] == 96 && X[1] == 64 && X[2] == 64;
     };
+    auto is48 = [&](int k) {
+      const int *X = c->inst[k].p.Nx;
+      return X[0] == 48 && X[1] == 48 && X[2] == 48;
+    };
     c->fast64.assign(n, 0);
     c->fast96.assign(n, 0);
+    c->fast48.assign(n, 0);
     c->anyfast = 0;
     c->any96 = 0;
+    c->any48 = 0;
     if (!c->xy64) {
-      // 64^3 instances first, then 96 x 64 x 64, then the rest
-      auto cls = [&](int k) { return is64(k) ? 0 : (is96(k) ? 1 : 2); };
+      // 64^3 instances first, then 96 x 64 x 64, then 48^3, then the rest
+      auto cls = [&](int k) { return is64(k) ? 0 : (is96(k) ? 1 : (is48(k) ? 2 : 3)); };
       std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cls(a) < cls(b); });
       for (int oi = 0; oi < n; oi++) {
         c->fast64[oi] = is64(order[oi]) ? 1 : 0;
         c->fast96[oi] = is96(order[oi]) ? 1 : 0;
+        c->fast48[oi] = is48(order[oi]) ? 1 : 0;
         c->anyfast = c->anyfast || c->fast64[oi];
         if (c->fast96[oi] && !c->any96) c->first96 = oi;
         c->any96 = c->any96 || c->fast96[oi];
+        if (c->fast48[oi] && !c->any48) c->first48 = oi;
+        c->any48 = c->any48 || c->fast48[oi];
       }
     }
     // one plane job per z (q and qdag packed), FP32 column jobs
@@ -1224,7 +1236,19 @@ void build_jobs(scft_ctx *c) {
       }
       CK(cudaStreamSynchronize(c->st));  // the host tables are released
     }
-    if (c->xy64 || c->anyfast || c->any96) {
+    if (c->any48) {
+      // z-pass jobs of the 48^3 instances (48 x 3 tiles of 16 columns each),
+      // contiguous in job order
+      std::vector<ColJob> cj;
+      for (int oi = 0; oi < n; oi++) {
+        if (!c->fast48[oi]) continue;
+        Instance &I = c->inst[order[oi]];
+        for (int y = 0; y < 48; y++)
+          for (int x0 = 0; x0 < 48; x0 += 16) cj.push_back(ColJob{I.work32, I.htab32, I.geom, x0, y});
+      }
+      c->d_mix48_cj = dupload(c, cj);
+    }
+    if (c->xy64 || c->anyfast || c->any96 || c->any48) {
       c->mix64_tab.clear();
       c->tmE.clear();
       c->tmH.clear();
@@ -1239,6 +1263,10 @@ void build_jobs(scft_ctx *c) {
           const unsigned long long rows = 64ULL * (unsigned long long)I.p.Nx[2];
           c->tmE.push_back(tensor_map_rows(I.E32, rows, 192));
           c->tmH.push_back(tensor_map_rows(I.hist32, rows * (unsigned long long)(I.hmax + 1), 192));
+        } else if (c->fast48[oi]) {  // rows of 48 float2, boxes of 48 rows
+          const unsigned long long rows = 48ULL * (unsigned long long)I.p.Nx[2];
+          c->tmE.push_back(tensor_map_rows(I.E32, rows, 96, 48));
+          c->tmH.push_back(tensor_map_rows(I.hist32, rows * (unsigned long long)(I.hmax + 1), 96, 48));
         } else {
           c->tmE.push_back(CUtensorMap{});
           c->tmH.push_back(CUtensorMap{});
@@ -1490,6 +1518,67 @@ bool persistent_group(const scft_ctx *c, const scft_ctx::SweepGroup &gr) {
   return p64 && z64 && nzi == 64 && gr.inst_end - gr.inst_begin <= kMix64MaxInst;
 }
 
+// One pass of propagator step s for sweep group g as the sweep launches it,
+// on stream sg: the z pass (z = true; steps s > 0) or the plane pass, by the
+// group's kernel class.  Returns false when no instance of the group is
+// active at step s.
+bool mix_group_step_pass(scft_ctx *c, int g, int s, bool z, cudaStream_t sg) {
+  const scft_ctx::SweepGroup &gr = c->groups[g];
+  // plane form 2: the generic kernels for every group (the reference the
+  // specialised classes are checked against)
+  const bool spec = c->plane64_form != 2;
+  const bool p64 = spec && (c->xy64 || gr.fast), z64 = spec && (c->colfast || gr.fast);
+  const bool c96 = spec && gr.fast96, c128 = spec && c->xy128, c48 = spec && gr.fast48;
+  const int nzi = gr.fast ? 64 : c->inst[0].p.Nx[2];
+  const void *twz = gr.fast ? c->d_tw32_64 : c->d_tw32_z;
+  const int per = 64 * (64 / c->col64_tx);       // z-pass jobs per instance of the 64-point kernels
+  const int per128 = 128 * (128 / c->col64_tx);  // and of the 128 x 128 kernels
+  const int per96 = 64 * (96 / c->col64_tx);     // and of the 96 x 64 x 64 instances
+  // instances of the group still active at step s: a prefix (decreasing N)
+  int act = 0;
+  for (int oi = gr.inst_begin; oi < gr.inst_end; oi++)
+    if (c->inst[c->job_order[oi]].N > s) act = oi + 1 - gr.inst_begin;
+  if (act == 0) return false;
+  const int last = gr.inst_begin + act - 1;
+  const int cnt = c->inst_pj_end[last] - gr.pj_begin;
+  const int cc = c->inst_cj_end[last] - gr.cj_begin;
+  if (z) {
+    if (s == 0) return true;
+    if (c48)
+      LK(launch_mix_col48(c->d_mix48_cj + (size_t)(gr.inst_begin - c->first48) * 144, act * 144, c->d_tw32_48, 48, 48,
+                          sg));
+    else if (c96)
+      LK(launch_mix_col64(col96_jobs(c) + (size_t)(gr.inst_begin - c->first96) * per96, act * per96, c->d_tw32_64, 96,
+                          64, 64, c->col64_tx, sg));
+    else if (c128)
+      LK(launch_mix_col64(col128_jobs(c) + (size_t)gr.inst_begin * per128, act * per128, c->d_tw32_z, 128, 128, nzi,
+                          c->col64_tx, sg));
+    else if (z64)
+      LK(launch_mix_col64(col64_jobs(c) + (size_t)gr.inst_begin * per, act * per, twz, 64, 64, nzi, c->col64_tx, sg));
+    else
+      LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cc, c->d_geoms, c->d_tw32, 3, 1, sg));
+    return true;
+  }
+  if (c48)
+    LK(launch_mix_plane48(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
+                          c->tmH.data() + gr.inst_begin, act, 48, c->d_tw32_48, s, c->d_err, sg));
+  else if (c96)
+    LK(launch_mix_plane96(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
+                          c->tmH.data() + gr.inst_begin, act, 64, c->d_tw32_64, c->d_tw32_32, c->d_tw32_96, s, c->d_err,
+                          sg));
+  else if (c128)
+    LK(launch_mix_plane128(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
+                           c->tmH.data() + gr.inst_begin, act, nzi, c->d_tw32_64, c->d_tw32_128, s, c->d_err, sg));
+  else if (p64)
+    LK((c->plane64_form ? launch_mix_plane64w : launch_mix_plane64)(
+        c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin, c->tmH.data() + gr.inst_begin, act, nzi,
+        c->d_tw32_64, s, c->d_err, sg));
+  else
+    LK(launch_mix_prop_plane(c->shp_mixp, c->d_prop_pj + gr.pj_begin, cnt, c->d_mi, c->d_geoms, c->d_tw32, s, c->d_err,
+                             sg));
+  return true;
+}
+
 // The FP32 propagator sweep of group g on stream sg (accumulators cleared,
 // then every step), from the Boltzmann factors to the plane sums and the
 // density accumulators: one persistent launch (persistent_group) or a z pass
@@ -1502,13 +1591,6 @@ void mix_group_sweep(scft_ctx *c, int g, cudaStream_t sg) {
     CK(cudaMemsetAsync(I.acc32[0], 0, sizeof(float) * I.M, sg));
     CK(cudaMemsetAsync(I.acc32[1], 0, sizeof(float) * I.M, sg));
   }
-  // plane form 2: the generic kernels for every group (the reference the
-  // specialised classes are checked against)
-  const bool spec = c->plane64_form != 2;
-  const bool p64 = spec && (c->xy64 || gr.fast), z64 = spec && (c->colfast || gr.fast);
-  const bool c96 = spec && gr.fast96, c128 = spec && c->xy128;
-  const int nzi = gr.fast ? 64 : c->inst[0].p.Nx[2];
-  const void *twz = gr.fast ? c->d_tw32_64 : c->d_tw32_z;
   if (persistent_group(c, gr)) {
     // the whole sweep of the group in one launch; concurrent groups share the
     // GPU's resident CTAs in proportion to their instances
@@ -1527,45 +1609,9 @@ void mix_group_sweep(scft_ctx *c, int g, cudaStream_t sg) {
                           c->d_sweep_ctr + (size_t)g * sweep64_counters(kMix64MaxInst), c->d_err, cap, sg));
     return;
   }
-  const int per = 64 * (64 / c->col64_tx);  // z-pass jobs per instance of the 64-point kernels
-  const int per128 = 128 * (128 / c->col64_tx);  // and of the 128 x 128 kernels
-  const int per96 = 64 * (96 / c->col64_tx);     // and of the 96 x 64 x 64 instances
   for (int s = 0; s < c->nmax; s++) {
-    // instances of the group still active at step s: a prefix (decreasing N)
-    int act = 0;
-    for (int oi = gr.inst_begin; oi < gr.inst_end; oi++)
-      if (c->inst[c->job_order[oi]].N > s) act = oi + 1 - gr.inst_begin;
-    if (act == 0) break;
-    const int last = gr.inst_begin + act - 1;
-    const int cnt = c->inst_pj_end[last] - gr.pj_begin;
-    const int cc = c->inst_cj_end[last] - gr.cj_begin;
-    if (s > 0) {
-      if (c96)
-        LK(launch_mix_col64(col96_jobs(c) + (size_t)(gr.inst_begin - c->first96) * per96, act * per96, c->d_tw32_64,
-                            96, 64, 64, c->col64_tx, sg));
-      else if (c128)
-        LK(launch_mix_col64(col128_jobs(c) + (size_t)gr.inst_begin * per128, act * per128, c->d_tw32_z, 128, 128,
-                            nzi, c->col64_tx, sg));
-      else if (z64)
-        LK(launch_mix_col64(col64_jobs(c) + (size_t)gr.inst_begin * per, act * per, twz, 64, 64, nzi, c->col64_tx,
-                            sg));
-      else
-        LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj + gr.cj_begin, cc, c->d_geoms, c->d_tw32, 3, 1, sg));
-    }
-    if (c96)
-      LK(launch_mix_plane96(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
-                            c->tmH.data() + gr.inst_begin, act, 64, c->d_tw32_64, c->d_tw32_32, c->d_tw32_96, s,
-                            c->d_err, sg));
-    else if (c128)
-      LK(launch_mix_plane128(c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin,
-                             c->tmH.data() + gr.inst_begin, act, nzi, c->d_tw32_64, c->d_tw32_128, s, c->d_err, sg));
-    else if (p64)
-      LK((c->plane64_form ? launch_mix_plane64w : launch_mix_plane64)(
-          c->mix64_tab.data() + gr.inst_begin, c->tmE.data() + gr.inst_begin, c->tmH.data() + gr.inst_begin, act,
-          nzi, c->d_tw32_64, s, c->d_err, sg));
-    else
-      LK(launch_mix_prop_plane(c->shp_mixp, c->d_prop_pj + gr.pj_begin, cnt, c->d_mi, c->d_geoms, c->d_tw32, s,
-                               c->d_err, sg));
+    if (!mix_group_step_pass(c, g, s, true, sg)) break;
+    mix_group_step_pass(c, g, s, false, sg);
   }
 }
 
@@ -1711,8 +1757,8 @@ void ctx_create(scft_ctx *c, const scft_params *params, int n_inst) {
       g.ax[d].tw = off[nn];
     }
   }
-  // the 32-, 64-, 96- and 128-point tables of the cluster plane passes
-  for (int nn : {32, 64, 96, 128})
+  // the 32-, 48-, 64-, 96- and 128-point tables of the specialised passes
+  for (int nn : {32, 48, 64, 96, 128})
     if (!off.count(nn)) {
       off[nn] = (int)tw.size();
       const long double two_pi = 6.283185307179586476925286766559005768L;
@@ -1729,6 +1775,7 @@ void ctx_create(scft_ctx *c, const scft_params *params, int n_inst) {
   c->d_tw32_128 = static_cast<float2 *>(c->d_tw32) + off[128];
   c->d_tw32_32 = static_cast<float2 *>(c->d_tw32) + off[32];
   c->d_tw32_96 = static_cast<float2 *>(c->d_tw32) + off[96];
+  c->d_tw32_48 = static_cast<float2 *>(c->d_tw32) + off[48];
   {
     const int nz0 = c->inst.empty() ? 0 : c->inst[0].p.Nx[2];
     if (off.count(nz0)) c->d_tw32_z = static_cast<float2 *>(c->d_tw32) + off[nz0];
@@ -2107,32 +2154,16 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   CK(cudaEventCreate(&e2));
   CK(cudaEventRecord(e0, c->st));
   for (int r = 0; r < reps; r++) {
-    if (c->mixed && c->xy128 && c->plane64_form != 2)
-      LK(launch_mix_plane128(c->mix64_tab.data(), c->tmE.data(), c->tmH.data(),
-                             c->prop_pj_count[s] / c->inst[0].p.Nx[2], c->inst[0].p.Nx[2], c->d_tw32_64,
-                             c->d_tw32_128, s, c->d_err, c->st));
-    else if (c->mixed && c->xy64 && c->plane64_form != 2)
-      LK((c->plane64_form ? launch_mix_plane64w : launch_mix_plane64)(c->mix64_tab.data(), c->tmE.data(), c->tmH.data(),
-                            c->prop_pj_count[s] / c->inst[0].p.Nx[2], c->inst[0].p.Nx[2], c->d_tw32_64, s, c->d_err,
-                            c->st));
-    else if (c->mixed)
-      LK(launch_mix_prop_plane(c->shp_mixp, c->d_prop_pj, c->prop_pj_count[s], c->d_mi, c->d_geoms, c->d_tw32, s,
-                               c->d_err,
-                               c->st));
+    if (c->mixed)  // every group's plane pass, as the sweep launches it
+      for (int g = 0; g < (int)c->groups.size(); g++) mix_group_step_pass(c, g, s, false, c->st);
     else
       LK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[s], c->d_pi, c->d_geoms, c->d_tw64, s,
                                c->st));
   }
   CK(cudaEventRecord(e1, c->st));
   for (int r = 0; r < reps; r++) {
-    if (c->mixed && c->xy128 && c->plane64_form != 2)
-      LK(launch_mix_col64(col128_jobs(c), (c->prop_pj_count[s] / c->inst[0].p.Nx[2]) * 128 * (128 / c->col64_tx),
-                          c->d_tw32_z, 128, 128, c->inst[0].p.Nx[2], c->col64_tx, c->st));
-    else if (c->mixed && c->colfast && c->plane64_form != 2)
-      LK(launch_mix_col64(col64_jobs(c), (c->prop_pj_count[s] / c->inst[0].p.Nx[2]) * 64 * (64 / c->col64_tx),
-                          c->d_tw32_z, 64, 64, c->inst[0].p.Nx[2], c->col64_tx, c->st));
-    else if (c->mixed)
-      LK(launch_col_fft<float>(c->shp_col32, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw32, 3, 1, c->st));
+    if (c->mixed)  // every group's z pass, as the sweep launches it
+      for (int g = 0; g < (int)c->groups.size(); g++) mix_group_step_pass(c, g, s, true, c->st);
     else
       LK(launch_col_fft<double>(c->shp_col, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw64, 2, 1,
                                 c->st));
@@ -2153,7 +2184,7 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
       // the FP32 accumulators A and B (2 x 8 B); column: read + write z, plus
       // the h table in the generic pass (the 64-point pass forms h on the fly)
       bp += I.M * (4.0 * sizeof(float2) + 4.0 * sizeof(float));
-      bc += I.M * (2.0 * sizeof(float2) + ((c->colfast || c->xy128) ? 0.0 : sizeof(float)));
+      bc += I.M * 2.0 * sizeof(float2);  // (the generic z pass also reads its h table, 4 B per point)
     } else {
       const double props = I.single ? 1.0 : 2.0;
       bp += props * I.M * 6.0 * sizeof(double2);

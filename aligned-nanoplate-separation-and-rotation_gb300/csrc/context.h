@@ -159,7 +159,7 @@ struct scft_ctx {
   // run on the 64-point plane and z kernels (a batch of 64 x 64 planes only
   // uses them throughout: xy64)
   struct SweepGroup {
-    int inst_begin, inst_end, pj_begin, pj_end, cj_begin, cj_end, phase, fast, fast96;
+    int inst_begin, inst_end, pj_begin, pj_end, cj_begin, cj_end, phase, fast, fast96, fast48;
   };
   std::vector<SweepGroup> groups;
   int sweep_phases = 1;  // requested number of sequential phases
@@ -174,6 +174,12 @@ struct scft_ctx {
   // position of the first of them
   std::vector<char> fast96;
   int any96 = 0, first96 = 0;
+  // the same for 48 x 48 x 48 instances (after the 96 x 64 x 64 ones), run
+  // by the 48-point plane and z passes (kernels_mixed48.cu)
+  std::vector<char> fast48;
+  int any48 = 0, first48 = 0;
+  void *d_tw32_48 = nullptr;           // the 48-point twiddle table inside d_tw32
+  scft::ColJob *d_mix48_cj = nullptr;  // their z-pass jobs (16 columns per CTA)
   void *d_tw32_32 = nullptr, *d_tw32_96 = nullptr;  // 32- and 96-point twiddle tables inside d_tw32
   scft::ColJob *d_mix96_cj_tx[3] = {};               // their z-pass jobs for 8, 16, 32 columns per CTA
   // mixed field-level data in job order: FieldInst table, the FP32 transform

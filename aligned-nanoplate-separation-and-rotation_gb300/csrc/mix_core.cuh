@@ -131,6 +131,62 @@ __device__ __forceinline__ void fft32_group(float2 *v, int t, float2 *xch, int s
   }
 }
 
+
+// 12-point transform in registers (a = n1 + 3 n2, c = k2 + 4 k1): DFT4 over
+// n2, twiddle w12^(n1 k2) = tw48[4 n1 k2], DFT3 over n1; output in natural
+// order (tw48: the 48-point twiddles).
+template <int SIGN> __device__ __forceinline__ void dft12f(float2 *v, const float2 *tw48) {
+  float2 u[3][4];
+#pragma unroll
+  for (int n1 = 0; n1 < 3; n1++) {
+#pragma unroll
+    for (int n2 = 0; n2 < 4; n2++) u[n1][n2] = v[n1 + 3 * n2];
+    Dft<4, SIGN, float2>::run(u[n1]);
+  }
+#pragma unroll
+  for (int n1 = 1; n1 < 3; n1++)
+#pragma unroll
+    for (int k2 = 1; k2 < 4; k2++) u[n1][k2] = ctw<SIGN>(u[n1][k2], tw48[4 * n1 * k2]);
+#pragma unroll
+  for (int k2 = 0; k2 < 4; k2++) {
+    float2 w[3] = {u[0][k2], u[1][k2], u[2][k2]};
+    Dft<3, SIGN, float2>::run(w);
+#pragma unroll
+    for (int k1 = 0; k1 < 3; k1++) v[k2 + 4 * k1] = w[k1];
+  }
+}
+
+// 48-point transform of a group of 4 threads, thread t holding the 12
+// values x[t + 4a] (48 = 12 x 4):
+//   Y[t][c]  = sum_a x[t + 4a] w12^(a c)          (DFT12 in registers)
+//   Y[t][c] *= w48^(t c)
+//   exchange: thread t takes c = t, t + 4, t + 8
+//   X[c + 12d] = sum_b Y[b][c] w4^(b d)            (three DFT4)
+// so X[t + 4j] returns in v[j], the input order.  Element (b, c) of the
+// exchange lives at xch[b * sb + c * sc]; WARP: the 4 threads and their
+// exchange area belong to one warp.
+template <int SIGN, bool WARP>
+__device__ __forceinline__ void fft48_group(float2 *v, int t, float2 *xch, int sb, int sc, const float2 *tw48) {
+  dft12f<SIGN>(v, tw48);
+#pragma unroll
+  for (int c = 1; c < 12; c++) v[c] = ctw<SIGN>(v[c], tw48[t * c]);
+#pragma unroll
+  for (int c = 0; c < 12; c++) xch[t * sb + c * sc] = v[c];
+  if (WARP) __syncwarp(); else __syncthreads();
+  float2 p[3][4];
+#pragma unroll
+  for (int e = 0; e < 3; e++)
+#pragma unroll
+    for (int b = 0; b < 4; b++) p[e][b] = xch[b * sb + (t + 4 * e) * sc];
+  if (WARP) __syncwarp(); else __syncthreads();
+#pragma unroll
+  for (int e = 0; e < 3; e++) {
+    Dft<4, SIGN, float2>::run(p[e]);
+#pragma unroll
+    for (int d = 0; d < 4; d++) v[e + 3 * d] = p[e][d];
+  }
+}
+
 }  // namespace
 
 // 16-point transform in registers, n = a + 4b, k = c + 4d: DFT4 over b,

@@ -90,6 +90,12 @@ cudaError_t launch_mix_plane128(const MixInst *insts, const CUtensorMap *tmE, co
 cudaError_t launch_mix_plane96(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
                                int nz, const void *tw64, const void *tw32, const void *tw96, int n, int *err,
                                cudaStream_t st);
+// Plane and z passes for 48 x 48 x 48 instances (kernels_mixed48.cu): one
+// 192-thread CTA per plane; tensor maps of rows of 48 float2 with 48-row
+// boxes; tw48: the 48-point twiddles; z-pass jobs of 16 columns.
+cudaError_t launch_mix_plane48(const MixInst *insts, const CUtensorMap *tmE, const CUtensorMap *tmH, int ninst,
+                               int nz, const void *tw48, int n, int *err, cudaStream_t st);
+cudaError_t launch_mix_col48(const ColJob *jobs, int njobs, const void *tw48, int nx, int ny, cudaStream_t st);
 // Graft sweep plane pass of the same family (four CTAs per plane): the
 // grafted instances' views in sweep order (Ng non-increasing), by value.
 template <int CAP> struct Graft128TableT {

@@ -628,10 +628,22 @@ def main():
     xy64 = all(p.Nx[0] == 64 and p.Nx[1] == 64 and p.Nx[2] == nz0 for p in params)
     xy128 = (not xy64 and nz0 in (64, 128, 256) and
              all(p.Nx[0] == 128 and p.Nx[1] == 128 and p.Nx[2] == nz0 for p in params))
-    col_fast = {64: "k_mix_col64", 128: "k_mix_col128", 256: "k_mix_col256"}.get(nz0) if (xy64 or xy128) else None
     p64name = "k_mix_plane64w" if sched.get("plane_form") else "k_mix_plane64"
-    pname = p64name if xy64 else ("k_mix_plane128" if xy128 else "k_mix_prop_plane")
-    kernel_names = {"mixed": (pname, col_fast or "k_col_fft<float>"),
+
+    def class_kernels(p):
+        """The plane and z kernels the sweep runs for one instance."""
+        X = tuple(p.Nx)
+        if xy64:
+            return p64name, {64: "k_mix_col64", 128: "k_mix_col128"}.get(nz0, "k_col_fft<float>")
+        if xy128:
+            return "k_mix_plane128", {64: "k_mix_col64", 128: "k_mix_col128", 256: "k_mix_col256"}[nz0]
+        return {(64, 64, 64): (p64name, "k_mix_col64"), (96, 64, 64): ("k_mix_plane96", "k_mix_col64"),
+                (48, 48, 48): ("k_mix_plane48", "k_mix_col48")}.get(X, ("k_mix_prop_plane", "k_col_fft<float>"))
+
+    kinds = sorted(set(class_kernels(p) for p in params))
+    pname = " + ".join(sorted(set(k[0] for k in kinds)))
+    zname = " + ".join(sorted(set(k[1] for k in kinds)))
+    kernel_names = {"mixed": (pname, zname),
                     "plain": ("k_prop_plane_f64", "k_col_fft<double> (bond kernel)")}
     dom = "plane" if prof["ms_plane"] >= prof["ms_col"] else "col"
     ms_k = prof["ms_" + dom]

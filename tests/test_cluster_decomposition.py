@@ -74,3 +74,31 @@ def test_factor_table_orders():
         ks = [r * (pos % h) + pos // h for pos in range(n)]
         assert sorted(ks) == list(range(n))
         assert all((k % r) * h + k // r == pos for pos, k in enumerate(ks))
+
+
+def test_fft48_of_four_threads():
+    """fft48_group (mix_core.cuh): a DFT12 in registers (DFT4, twiddle
+    w12^(n1 k2), DFT3), twiddle w48^(t c), exchange, three DFT4 per thread;
+    thread t holds x[t + 4a] before and X[t + 4j] after."""
+    tw48 = np.exp(-2j * np.pi * np.arange(48) / 48)
+
+    def dft12(v):
+        u = [np.fft.fft([v[n1 + 3 * n2] for n2 in range(4)]) for n1 in range(3)]
+        for n1 in (1, 2):
+            for k2 in (1, 2, 3):
+                u[n1][k2] *= tw48[4 * n1 * k2]
+        out = np.zeros(12, complex)
+        for k2 in range(4):
+            out[k2 + 4 * np.arange(3)] = np.fft.fft([u[0][k2], u[1][k2], u[2][k2]])
+        return out
+
+    x = rng.standard_normal(48) + 1j * rng.standard_normal(48)
+    Y = np.array([dft12(x[t::4]) * tw48[(t * np.arange(12)) % 48] for t in range(4)])
+    out = np.zeros(48, complex)
+    for t in range(4):
+        v = np.zeros(12, complex)
+        for e in range(3):
+            p = np.fft.fft(Y[:, t + 4 * e])
+            v[e + 3 * np.arange(4)] = p
+        out[t + 4 * np.arange(12)] = v
+    np.testing.assert_allclose(out, np.fft.fft(x), atol=1e-12)

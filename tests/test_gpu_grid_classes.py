@@ -1,16 +1,19 @@
-"""The 96 x 64 plane family of the mixed form: the three-CTA cluster plane
-pass (k_mix_plane96, residue-major x in k-space) with the 64-point z pass,
-which a batch runs for its 96 x 64 x 64 instances (the mixed-size sweep's
-largest grids).  Its transforms differ from the generic kernels' only in
-FP32 rounding, so against the FP64 method over the same iterations from the
-same fields it meets the mixed form's bar (H, Q and densities 2e-5) or is
-no worse than twice the generic FP32 kernels on the same batch
-(scft_set_plane_form 2): on these short chains (N 5 to 12, chi = 20/N) the
-seeded field spreads q so widely that the generic kernels already sit at
-3e-5 in the densities of a 96 x 64 x 64 grid.  Cases: uneven chain lengths
-in one launch, a batch of mixed grids in which the 64^3, 96 x 64 x 64 and
-48^3 instances run three kernel classes side by side, and the autotuned
-z-pass tile.
+"""The grid classes of the mixed form's batches beyond 64 x 64 planes:
+96 x 64 x 64 instances run the three-CTA cluster plane pass (k_mix_plane96,
+residue-major x in k-space) with the 64-point z pass, and 48 x 48 x 48
+instances the 48-point plane and z passes (k_mix_plane48, k_mix_col48: four
+threads per line, twelve values each); a batch of mixed grids runs each of
+its instances in its class, side by side.
+
+Their transforms differ from the generic kernels' only in FP32 rounding, so
+against the FP64 method over the same iterations from the same fields each
+meets the mixed form's bar (H, Q and densities 2e-5) or is no worse than
+twice the generic FP32 kernels on the same batch (scft_set_plane_form 2):
+on these short chains (N 5 to 12, chi = 20/N) the seeded field spreads q so
+widely that the generic kernels already sit at 3e-5 in the densities of a
+96 x 64 x 64 grid.  Cases: uneven chain lengths in one launch for each
+class, a batch of mixed grids in which the 64^3, 96 x 64 x 64 and 48^3
+instances run side by side, and the autotuned z-pass tile.
 """
 import numpy as np
 import pytest
@@ -99,6 +102,11 @@ def test_cluster_plane_pass_matches_fp64(S):
     p64, p32, fields = batch(S, [(12, (96, 64, 64)), (9, (96, 64, 64)), (9, (96, 64, 64)), (5, (96, 64, 64))])
     a = compare(S, p32, p64, fields, groups=2)
     assert a[3]["col_tile"] in (8, 16, 32)  # the specialised z pass
+
+
+def test_48_point_passes_match_fp64(S):
+    p64, p32, fields = batch(S, [(12, (48, 48, 48)), (9, (48, 48, 48)), (9, (48, 48, 48)), (5, (48, 48, 48))])
+    compare(S, p32, p64, fields, groups=2)
 
 
 def test_three_kernel_classes_in_one_batch(S):
