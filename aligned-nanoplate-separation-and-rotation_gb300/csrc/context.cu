@@ -1518,12 +1518,11 @@ bool persistent_group(const scft_ctx *c, const scft_ctx::SweepGroup &gr) {
   return p64 && z64 && nzi == 64 && gr.inst_end - gr.inst_begin <= kMix64MaxInst;
 }
 
-// One pass of propagator step s for sweep group g as the sweep launches it,
-// on stream sg: the z pass (z = true; steps s > 0) or the plane pass, by the
-// group's kernel class.  Returns false when no instance of the group is
-// active at step s.
-bool mix_group_step_pass(scft_ctx *c, int g, int s, bool z, cudaStream_t sg) {
-  const scft_ctx::SweepGroup &gr = c->groups[g];
+// One pass of propagator step s for the instances of sweep group gr as the
+// sweep launches it, on stream sg: the z pass (z = true; steps s > 0) or the
+// plane pass, by the group's kernel class.  Returns false when no instance
+// of the group is active at step s.
+bool mix_group_step_pass(scft_ctx *c, const scft_ctx::SweepGroup &gr, int s, bool z, cudaStream_t sg) {
   // plane form 2: the generic kernels for every group (the reference the
   // specialised classes are checked against)
   const bool spec = c->plane64_form != 2;
@@ -1610,8 +1609,8 @@ void mix_group_sweep(scft_ctx *c, int g, cudaStream_t sg) {
     return;
   }
   for (int s = 0; s < c->nmax; s++) {
-    if (!mix_group_step_pass(c, g, s, true, sg)) break;
-    mix_group_step_pass(c, g, s, false, sg);
+    if (!mix_group_step_pass(c, gr, s, true, sg)) break;
+    mix_group_step_pass(c, gr, s, false, sg);
   }
 }
 
@@ -2153,17 +2152,42 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
   CK(cudaEventCreate(&e1));
   CK(cudaEventCreate(&e2));
   CK(cudaEventRecord(e0, c->st));
+  // the mixed form's passes one launch per kernel class (a run of the job
+  // order with one class), as a single sweep group would launch them
+  std::vector<scft_ctx::SweepGroup> runs;
+  if (c->mixed) {
+    const int n = (int)c->inst.size();
+    for (int a = 0; a < n;) {
+      int b = a + 1;
+      while (b < n && (c->fast64.empty() || (c->fast64[b] == c->fast64[a] && c->fast96[b] == c->fast96[a] &&
+                                             c->fast48[b] == c->fast48[a])))
+        b++;
+      scft_ctx::SweepGroup gr;
+      gr.inst_begin = a;
+      gr.inst_end = b;
+      gr.pj_begin = a ? c->inst_pj_end[a - 1] : 0;
+      gr.pj_end = c->inst_pj_end[b - 1];
+      gr.cj_begin = a ? c->inst_cj_end[a - 1] : 0;
+      gr.cj_end = c->inst_cj_end[b - 1];
+      gr.phase = 0;
+      gr.fast = c->fast64.empty() ? 0 : c->fast64[a];
+      gr.fast96 = c->fast96.empty() ? 0 : c->fast96[a];
+      gr.fast48 = c->fast48.empty() ? 0 : c->fast48[a];
+      runs.push_back(gr);
+      a = b;
+    }
+  }
   for (int r = 0; r < reps; r++) {
-    if (c->mixed)  // every group's plane pass, as the sweep launches it
-      for (int g = 0; g < (int)c->groups.size(); g++) mix_group_step_pass(c, g, s, false, c->st);
+    if (c->mixed)
+      for (auto &gr : runs) mix_group_step_pass(c, gr, s, false, c->st);
     else
       LK(launch_prop_plane_f64(c->shp_prop, c->d_prop_pj, c->prop_pj_count[s], c->d_pi, c->d_geoms, c->d_tw64, s,
                                c->st));
   }
   CK(cudaEventRecord(e1, c->st));
   for (int r = 0; r < reps; r++) {
-    if (c->mixed)  // every group's z pass, as the sweep launches it
-      for (int g = 0; g < (int)c->groups.size(); g++) mix_group_step_pass(c, g, s, true, c->st);
+    if (c->mixed)
+      for (auto &gr : runs) mix_group_step_pass(c, gr, s, true, c->st);
     else
       LK(launch_col_fft<double>(c->shp_col, c->d_prop_cj, c->prop_cj_count[s], c->d_geoms, c->d_tw64, 2, 1,
                                 c->st));
