@@ -121,3 +121,24 @@ def test_autotuned_tile_stays_within_the_bar(S):
     p64, p32, fields = batch(S, [(8, (96, 64, 64)), (8, (96, 64, 64)), (6, (64, 64, 64))])
     a = compare(S, p32, p64, fields, tune=True)
     assert a[3]["col_tile"] in (8, 16, 32)
+
+
+def test_grafted_instances_of_each_class(S):
+    """Grafted plates on 96 x 64 x 64 and 48^3 grids: the diblock sweep runs
+    the class kernels, the graft sweep the generic ones (natural k-space
+    order); Qga follows."""
+    from scft.workloads import plate_params, rg, seeded_fields
+
+    def gp(theta, N, grid, prec):
+        p = plate_params(theta, N=N, grid=grid, box_rg=tuple(6.4 * g / 64 for g in grid), precision=prec,
+                         lam_pl=0.002, lam_mi=0.001, sigma=0.5 / rg(N) ** 2, Ng=4)
+        p.chi_bc = p.chi_ab
+        return p
+
+    specs = [(10, (96, 64, 64)), (8, (48, 48, 48)), (8, (64, 64, 64))]
+    p64 = [gp(7.0 * k, N, g, S.PREC_FP64) for k, (N, g) in enumerate(specs)]
+    p32 = [gp(7.0 * k, N, g, S.PREC_MIXED) for k, (N, g) in enumerate(specs)]
+    fields = [seeded_fields(p, 140 + k) for k, p in enumerate(p64)]
+    a = compare(S, p32, p64, fields, groups=3)
+    b = run(S, p64, fields)
+    assert np.abs(a[1][:, 4] - b[1][:, 4]).max() <= 1e-4 * np.abs(b[1][:, 4]).max()  # Qga
