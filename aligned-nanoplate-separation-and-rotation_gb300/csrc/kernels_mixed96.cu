@@ -171,7 +171,9 @@ __global__ void __cluster_dims__(3, 1, 1) __launch_bounds__(256, 4)
         v[j] = cadd(own, cadd(ta, tb));
       }
     }
-    cl_arrive();  // done reading the partners' buffers (the wait comes before buf is rewritten)
+    // no barrier here: buf is next rewritten by the forward transform, after
+    // the cluster barrier that follows the slab sums, before which every
+    // partner has finished these reads
   }
   if (!mbar_wait(&s_bar, 0, T.err[1])) {
     atomicExch(T.err, 1);
@@ -262,7 +264,6 @@ __global__ void __cluster_dims__(3, 1, 1) __launch_bounds__(256, 4)
       S.qs[1] = ad;
     }
   }
-  if (n > 0) cl_wait();  // every partner has read this CTA's buf
   const bool last = (n == N - 1);
   // forward x, radix-3 step first: the real-space slab through Es
   if (!last) {
