@@ -1731,6 +1731,7 @@ void seq_mix_update(scft_ctx *c) { seq_mix(c, true); }
 namespace scft {
 
 void ctx_create(scft_ctx *c, const scft_params *params, int n_inst) {
+  NvtxRange nvtx_range("scft_create");
   CK(cudaGetDevice(&c->device));
   CK(cudaStreamCreateWithFlags(&c->st, cudaStreamNonBlocking));
   c->inst.resize(n_inst);
@@ -1804,6 +1805,7 @@ void ctx_destroy(scft_ctx *c) {
 // attributes get set); later builds replay a captured graph, as update_1s
 // does: a batch's density build is over a thousand launches.
 void ctx_poly_density(scft_ctx *c) {
+  NvtxRange nvtx_range("scft_calc_poly_density");
   auto body = [c]() {
     if (c->mixed)
       seq_mix_density(c);
@@ -1841,6 +1843,7 @@ void ctx_poly_density(scft_ctx *c) {
 }
 
 void ctx_update(scft_ctx *c, int n_iter) {
+  NvtxRange nvtx_range("scft_update_1s");
   if (n_iter <= 0) return;
   if (c->dirty_density) ctx_poly_density(c);
   int k = 0;
@@ -1953,6 +1956,7 @@ void ctx_set_sweep_groups(scft_ctx *c, int groups, int phases) {
 // recompute the current densities from the current fields, so the state is
 // unchanged.
 void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *tx_out, double *ms_out) {
+  NvtxRange nvtx_range("scft_autotune");
   *groups_out = 1;
   *phases_out = 1;
   *tx_out = 0;
@@ -2224,6 +2228,7 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
 
 // calc_H (code/calc_h.cpp:9-64); out per instance: Re H, Im H, Re Qd, Im Qd, Re Qga
 int ctx_calc_H(scft_ctx *c, double *out) {
+  NvtxRange nvtx_range("scft_calc_H");
   if (c->dirty_density) ctx_poly_density(c);
   const int n = (int)c->inst.size();
   if (c->mixed)
@@ -2451,6 +2456,7 @@ static void step_body(scft_ctx *c, const double *const *w, int n_iter) {
 // captured graph (re-captured when the host pointers or n_iter change);
 // everything else runs scft_set_fields_all, scft_update_1s and scft_calc_H.
 int ctx_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *out) {
+  NvtxRange nvtx_range("scft_step_fields");
   const int n = (int)c->inst.size();
   bool cl = false;
   for (auto &I : c->inst) cl = cl || I.p.do_cl;
@@ -2521,6 +2527,7 @@ int ctx_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *out
 }
 
 void ctx_set_fields_all(scft_ctx *c, const double *const *w) {
+  NvtxRange nvtx_range("scft_set_fields_all");
   std::vector<int> ks(c->inst.size());
   for (size_t k = 0; k < ks.size(); k++) ks[k] = (int)k;
   set_fields_ks(c, ks, w);
@@ -2724,6 +2731,7 @@ static void graft_map_derivative(scft_ctx *c, Instance &I, const GradArgs &g, do
 }
 
 int ctx_grad_geom(scft_ctx *c, double *out) {
+  NvtxRange nvtx_range("scft_grad_geom");
   if (c->dirty_density) ctx_poly_density(c);
   const int n = (int)c->inst.size();
   const int blocks = 128;

@@ -13,6 +13,18 @@
 #include "launch.h"
 #include "refrng.h"
 
+#include <nvtx3/nvToolsExt.h>
+
+// A named NVTX range for the lifetime of the object (no cost without a
+// profiler attached): the library's phases show up as ranges in profiler
+// timelines and can filter ncu captures (ncu --nvtx --nvtx-include).
+struct NvtxRange {
+  explicit NvtxRange(const char *name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange &) = delete;
+  NvtxRange &operator=(const NvtxRange &) = delete;
+};
+
 namespace scft {
 
 typedef std::complex<double> cd;
