@@ -670,8 +670,11 @@ def main():
                     "other_kernel_ms_per_launch": per_step["other_kernel_ms_per_launch"]}
     if sweep_roof is not None:
         roofline["sweep"] = sweep_roof
-    # the whole iteration against the survey's per-iteration byte count
-    # B = M s [5 (N - 1) + 30], s = 8 B (FP32 propagators) or 16 B (FP64)
+    # the whole iteration against a per-iteration byte count of
+    # B = M s [5 (N - 1) + 30]: five propagator-sized streams per step
+    # (read and write of the working array in each of the two passes, one
+    # history access) plus about 30 array passes of field work, s = 8 B
+    # (FP32 propagators) or 16 B (FP64)
     s_b = 8.0 if form == "mixed" else 16.0
     b_it = sum(p.Nx[0] * p.Nx[1] * p.Nx[2] * s_b * (5 * (p.Nda + p.Ndb - 1) + 30) for p in params)
     a_it = b_it / (ms / args.steps / 1e3) / 1e9
