@@ -142,3 +142,11 @@ def test_grafted_instances_of_each_class(S):
     a = compare(S, p32, p64, fields, groups=3)
     b = run(S, p64, fields)
     assert np.abs(a[1][:, 4] - b[1][:, 4]).max() <= 1e-4 * np.abs(b[1][:, 4]).max()  # Qga
+
+
+@pytest.mark.parametrize("grid", [(96, 64, 64), (48, 48, 48), (128, 128, 64)])
+def test_shortest_chains_of_each_class(S, grid):
+    """N = 2 and 3 in one launch: the first step is also the last but one or
+    the last, and N = 2 pairs its only stored step at once."""
+    p64, p32, fields = batch(S, [(3, grid), (2, grid)])
+    compare(S, p32, p64, fields, groups=1)
