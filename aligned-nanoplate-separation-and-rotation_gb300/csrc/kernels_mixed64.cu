@@ -132,7 +132,7 @@ __device__ __forceinline__ void plane64_body(const TT &T, int ii, int zz, int n,
   __syncthreads();  // means, exponents (and, on entry, the twiddles and the barrier's initialisation)
   if (n > 0) {
     // inverse y transform (column phase)
-    fft64_group<+1, false>(v, tc, buf + col, 8 * 64, 64, S.tw);
+    fft64_colhalf<+1, 1>(v, tc, buf + col, S.tw);
 #pragma unroll
     for (int d = 0; d < 8; d++) buf[(tc + 8 * d) * kRowPad + col] = v[d];
     __syncthreads();
@@ -258,7 +258,7 @@ __device__ __forceinline__ void plane64_body(const TT &T, int ii, int zz, int n,
 #pragma unroll
   for (int a = 0; a < 8; a++) v[a] = buf[(tc + 8 * a) * kRowPad + col];
   __syncthreads();
-  fft64_group<-1, false>(v, tc, buf + col, 8 * 64, 64, S.tw);
+  fft64_colhalf<-1, 0>(v, tc, buf + col, S.tw);
 #pragma unroll
   for (int d = 0; d < 8; d++) work[(tc + 8 * d) * 64 + col] = v[d];
 }

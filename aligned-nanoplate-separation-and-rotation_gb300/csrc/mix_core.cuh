@@ -45,6 +45,28 @@ __device__ __forceinline__ void fft64_group(float2 *v, int t, float2 *xch, int s
   dft8f<SIGN>(v);
 }
 
+// The same transform for the column phase of a 512-thread, 64 x 64 plane
+// task (thread tid holds column tid % 64): the 8 threads of a column lie in
+// the even warps (columns 0-31) or the odd ones (32-63), so the exchange's
+// write-to-read barrier is a named barrier over those 8 warps only.  AFTER:
+// 1 ends with a block barrier (the caller reuses the exchange area), 0 with
+// none (the caller leaves the area untouched until its own next barrier).
+template <int SIGN, int AFTER>
+__device__ __forceinline__ void fft64_colhalf(float2 *v, int t, float2 *xch, const float2 *tw) {
+  dft8f<SIGN>(v);
+  tw64<SIGN>(v, t, tw);
+#pragma unroll
+  for (int c = 0; c < 8; c++) xch[t * 512 + c * 64] = v[c];
+  if (threadIdx.x & 32)  // odd warps: columns 32-63
+    asm volatile("bar.sync 2, 256;\n" ::: "memory");
+  else
+    asm volatile("bar.sync 1, 256;\n" ::: "memory");
+#pragma unroll
+  for (int b = 0; b < 8; b++) v[b] = xch[b * 512 + t * 64];
+  if (AFTER) __syncthreads();
+  dft8f<SIGN>(v);
+}
+
 __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
   s = a + b;
   const float bb = s - a;
