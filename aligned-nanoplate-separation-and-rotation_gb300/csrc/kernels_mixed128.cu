@@ -163,7 +163,7 @@ __device__ __forceinline__ Quad quad_roles() {
 // barriers plus one split one; buf is free for the caller afterwards, but a
 // partner may read it until it passes its next cluster barrier.
 __device__ __forceinline__ void quad_inverse(float2 *v, float2 *buf, const Plane128Shared &S, const Quad &Z) {
-  fft64_group<+1, false>(v, Z.tc, buf + Z.col, 8 * 64, 64, S.tw);
+  fft64_colhalf<+1, 1>(v, Z.tc, buf + Z.col, S.tw);
 #pragma unroll
   for (int d = 0; d < 8; d++) buf[(Z.tc + 8 * d) * kRowPad + Z.col] = v[d];
   cl_sync();
@@ -235,7 +235,7 @@ __device__ __forceinline__ void quad_forward(float2 *v, const float2 *X, float2 
     }
   }
   cl_arrive();  // done reading the partners' buffers
-  fft64_group<-1, false>(v, Z.tc, buf + Z.col, 8 * 64, 64, S.tw);
+  fft64_colhalf<-1, 0>(v, Z.tc, buf + Z.col, S.tw);
 }
 
 // Plane pass of step n for 128 x 128 xy planes (any nz, the same for every
