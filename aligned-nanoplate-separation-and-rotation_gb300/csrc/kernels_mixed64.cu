@@ -257,8 +257,12 @@ __device__ __forceinline__ void plane64_body(const TT &T, int ii, int zz, int n,
   __syncthreads();
 #pragma unroll
   for (int a = 0; a < 8; a++) v[a] = buf[(tc + 8 * a) * kRowPad + col];
-  __syncthreads();
-  fft64_colhalf<-1, 0>(v, tc, buf + col, S.tw);
+  // the one-launch-per-step kernel exchanges through the consumed Boltzmann
+  // plane Es, so no barrier is needed between the transposed reads of buf
+  // and the exchange; the persistent sweep keeps buf (Es is a bulk-copy
+  // destination of its next task)
+  if (!STAGE) __syncthreads();
+  fft64_colhalf<-1, 0>(v, tc, (STAGE ? Es : buf) + col, S.tw);
 #pragma unroll
   for (int d = 0; d < 8; d++) work[(tc + 8 * d) * 64 + col] = v[d];
 }
