@@ -236,7 +236,17 @@ __device__ __forceinline__ void plane64_body(const TT &T, int ii, int zz, int n,
     S.red[0][warp] = (double)sq_ + (double)cq;
     S.red[1][warp] = (double)sd_ + (double)cd;
   }
-  __syncthreads();
+  // warp 0 sums the 16 warp results after the next block barrier: the
+  // forward transpose's, or on the last step a barrier of its own
+  const bool last = (n == N - 1);
+  if (!last) {
+    // forward x transform (row phase; a warp's own rows of buf), then the
+    // transpose to the column phase
+    fft64_group<-1, true>(v, tr, buf + row * kRowPad, 9, 1, S.tw);
+#pragma unroll
+    for (int d = 0; d < 8; d++) buf[row * kRowPad + tr + 8 * d] = v[d];
+  }
+  __syncthreads();  // also: every read of Es, Hs and every write of S.red is done
   if (warp == 0) {
     double aq = lane < 16 ? S.red[0][lane] : 0.0;
     double ad = lane < 16 ? S.red[1][lane] : 0.0;
@@ -249,12 +259,7 @@ __device__ __forceinline__ void plane64_body(const TT &T, int ii, int zz, int n,
       P.part[(long long)(N + n) * nz + zz] = ad;
     }
   }
-  if (n == N - 1) return;
-  // forward x transform (row phase), then to the column phase, forward y
-  fft64_group<-1, true>(v, tr, buf + row * kRowPad, 9, 1, S.tw);
-#pragma unroll
-  for (int d = 0; d < 8; d++) buf[row * kRowPad + tr + 8 * d] = v[d];
-  __syncthreads();
+  if (last) return;
 #pragma unroll
   for (int a = 0; a < 8; a++) v[a] = buf[(tc + 8 * a) * kRowPad + col];
   // the one-launch-per-step kernel exchanges through the consumed Boltzmann
