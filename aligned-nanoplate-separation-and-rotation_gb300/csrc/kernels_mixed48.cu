@@ -210,7 +210,16 @@ __global__ void __launch_bounds__(192, 3) k_mix_plane48(const __grid_constant__ 
     S.red[0][warp] = (double)sq_ + (double)cq;
     S.red[1][warp] = (double)sd_ + (double)cd;
   }
-  __syncthreads();
+  // warp 0 sums the warp results after the next block barrier: the forward
+  // transpose's (the forward row transform only touches the warp's own rows
+  // of buf), or on the last step a barrier of its own
+  const bool last = (n == N - 1);
+  if (!last) {
+    fft48_group<-1, true>(v, tr, buf + row * kRP48, 13, 1, S.tw);
+#pragma unroll
+    for (int a = 0; a < 12; a++) buf[row * kRP48 + tr + 4 * a] = v[a];
+  }
+  __syncthreads();  // also: every read of Es, Hs and every write of S.red is done
   if (warp == 0) {
     double aq = lane < 6 ? S.red[0][lane] : 0.0;
     double ad = lane < 6 ? S.red[1][lane] : 0.0;
@@ -223,16 +232,12 @@ __global__ void __launch_bounds__(192, 3) k_mix_plane48(const __grid_constant__ 
       P.part[(long long)(N + n) * nz + zz] = ad;
     }
   }
-  if (n == N - 1) return;
-  // forward x (row phase), then to the column phase, forward y
-  fft48_group<-1, true>(v, tr, buf + row * kRP48, 13, 1, S.tw);
-#pragma unroll
-  for (int a = 0; a < 12; a++) buf[row * kRP48 + tr + 4 * a] = v[a];
-  __syncthreads();
+  if (last) return;
+  // to the column phase, forward y (the exchange goes through the consumed
+  // Boltzmann plane Es, so no barrier between the transposed reads and it)
 #pragma unroll
   for (int a = 0; a < 12; a++) v[a] = buf[(tc + 4 * a) * kRP48 + col];
-  __syncthreads();
-  fft48_group<-1, false>(v, tc, buf + col, 12 * 48, 48, S.tw);
+  fft48_group<-1, false>(v, tc, Es + col, 12 * 48, 48, S.tw);
 #pragma unroll
   for (int d = 0; d < 12; d++) work[(tc + 4 * d) * 48 + col] = v[d];
 }
