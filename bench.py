@@ -39,7 +39,7 @@ METRIC = "SCFT iters/s @64^3,N=100"
 # dram__bytes_read.sum + dram__bytes_write.sum of one launch of the dominant
 # kernel, from an ncu capture of the same workload (the paired plane-pass step;
 # profiles/mixed_kernels_sweep15_64_N100_ncu.txt).  Only valid for that workload.
-NCU_TRAFFIC = {("sweep15_64_N100", "k_mix_plane64"): 125.905664e6 + 16.460032e6,
+NCU_TRAFFIC = {("sweep15_64_N100", "k_mix_plane64"): 125.904896e6 + 15.698944e6,
                # captured on sweep4_128x128x64_N50 (2,097,152 points of a paired step),
                # scaled by points to the 33,554,432 of one launch of this workload
                ("graft8_128x128x256_N200", "k_mix_plane128"): (67.17568e6 + 0.783104e6) * 16}
