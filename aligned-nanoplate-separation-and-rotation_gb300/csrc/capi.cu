@@ -28,6 +28,7 @@ void ctx_set_persistent(scft_ctx *c, int on);
 void ctx_set_plane_form(scft_ctx *c, int form);
 void ctx_profile_sweep(scft_ctx *c, int reps, double *ms, double *bytes);
 int ctx_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *out);
+int ctx_iterate_fields(scft_ctx *c, const double *const *w, double *const *w_out, double *out);
 void ctx_set_fields_all(scft_ctx *c, const double *const *w);
 void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *tx_out, double *ms_out);
 void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_plane, double *ms_col,
@@ -277,6 +278,18 @@ int scft_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *H_
     if (!w[k]) return fail(SCFT_ERR_ARG, "null field pointer");
   int st = SCFT_OK;
   API_BODY(st = scft::ctx_step_fields(c, w, n_iter, H_out));
+  if (st == SCFT_ERR_NAN) return fail(st, "H is NaN");
+  if (st == SCFT_ERR_QNONPOS) return fail(st, "graft propagator q_g[Ng-1] <= 0 at 5 or more points");
+  return st;
+}
+
+int scft_iterate_fields(scft_ctx *c, const double *const *w, double *const *w_out, double *H_out) {
+  if (int s = check_ctx(c, 0)) return s;
+  if (!w || !H_out) return fail(SCFT_ERR_ARG, "need field pointers and an output");
+  for (size_t k = 0; k < c->inst.size(); k++)
+    if (!w[k] || (w_out && !w_out[k])) return fail(SCFT_ERR_ARG, "null field pointer");
+  int st = SCFT_OK;
+  API_BODY(st = scft::ctx_iterate_fields(c, w, w_out, H_out));
   if (st == SCFT_ERR_NAN) return fail(st, "H is NaN");
   if (st == SCFT_ERR_QNONPOS) return fail(st, "graft propagator q_g[Ng-1] <= 0 at 5 or more points");
   return st;

@@ -812,6 +812,8 @@ void build_groups(scft_ctx *c) {
     cudaEvent_t ev;
     CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
     c->ev_join.push_back(ev);
+    CK(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    c->ev_up.push_back(ev);
   }
   if (!c->ev_fork) CK(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
   if (c->sweep_persistent && c->sweep_ctr_groups < ng) {
@@ -1614,11 +1616,49 @@ void mix_group_sweep(scft_ctx *c, int g, cudaStream_t sg) {
   }
 }
 
+// Job ranges of sweep group g in the per-kind transform job lists (job
+// order): FP32 plane and z jobs of the packed pair, FP64 plane and z jobs of
+// the graft field.
+struct GroupJobs {
+  int pb, pm, cb, cm, gpb, gpm, gcb, gcm;
+};
+static GroupJobs group_jobs(const scft_ctx *c, const scft_ctx::SweepGroup &gr) {
+  GroupJobs j;
+  const int i0 = gr.inst_begin;
+  auto range = [&](int kind, int &b0, int &n0) {
+    b0 = i0 ? c->fld_end[4 * (i0 - 1) + kind] : 0;
+    n0 = c->fld_end[4 * (gr.inst_end - 1) + kind] - b0;
+  };
+  range(0, j.pb, j.pm);
+  range(1, j.cb, j.cm);
+  range(2, j.gpb, j.gpm);
+  range(3, j.gcb, j.gcm);
+  return j;
+}
+
+// The k-space half of an update_1s for group g on stream sg: density pack ->
+// forward FP32 transform (FP64 for the graft density) -> k-space update
+// (which also forms the smeared pair).  The fields are then new and the
+// densities those of the old fields.
+static void mix_group_kspace_update(scft_ctx *c, int g, cudaStream_t sg) {
+  const scft_ctx::SweepGroup &gr = c->groups[g];
+  const int cnt_i = gr.inst_end - gr.inst_begin;
+  const FieldInst *fi = c->d_fi_ord + gr.inst_begin;
+  const GroupJobs j = group_jobs(c, gr);
+  LK(launch_mix_rho_pack(fi, cnt_i, c->eblocks, 0, sg));
+  LK(launch_plane_fft<float>(c->shp_plane32, c->d_zpj_ord + j.pb, j.pm, c->d_geoms, c->d_tw32, -1, 0, sg));
+  LK(launch_col_fft<float>(c->shp_col32, c->d_zcj_ord + j.cb, j.cm, c->d_geoms, c->d_tw32, 0, 1, sg));
+  if (j.gpm > 0) {
+    LK(launch_plane_fft<double>(c->shp_plane, c->d_gpj_ord + j.gpb, j.gpm, c->d_geoms, c->d_tw64, -1, 0, sg));
+    LK(launch_col_fft<double>(c->shp_col, c->d_gcj_ord + j.gcb, j.gcm, c->d_geoms, c->d_tw64, 0, 1, sg));
+  }
+  LK(launch_mix_update(fi, cnt_i, c->eblocks, sg));
+}
+
 // Mixed form, one sweep group on stream sg: the work of one update_1s (or of
 // calc_poly_density when `update` is false) for the group's instances, from
 // the densities of the last sweep to the densities of this one:
-//   update:  density pack -> forward FP32 transform (FP64 for the graft
-//            density) -> k-space update (which also forms the smeared pair) ->
+//   update:  the k-space half above ->
 //   density: (smeared pair from the fields) ->
 //   both:    inverse FP32 transform (FP64 for the graft field) -> Boltzmann
 //            factors -> FP32 sweep -> Q.
@@ -1629,34 +1669,18 @@ void mix_group_sweep(scft_ctx *c, int g, cudaStream_t sg) {
 // another group's bandwidth-bound sweep.
 void mix_group_chain(scft_ctx *c, int g, cudaStream_t sg, bool update) {
   const scft_ctx::SweepGroup &gr = c->groups[g];
-  const int i0 = gr.inst_begin, cnt_i = gr.inst_end - gr.inst_begin;
-  const FieldInst *fi = c->d_fi_ord + i0;
-  int pb, pm, cb, cm, gpb, gpm, gcb, gcm;
-  auto range = [&](int kind, int &b0, int &n0) {
-    b0 = i0 ? c->fld_end[4 * (i0 - 1) + kind] : 0;
-    n0 = c->fld_end[4 * (gr.inst_end - 1) + kind] - b0;
-  };
-  range(0, pb, pm);
-  range(1, cb, cm);
-  range(2, gpb, gpm);
-  range(3, gcb, gcm);
-  if (update) {
-    LK(launch_mix_rho_pack(fi, cnt_i, c->eblocks, 0, sg));
-    LK(launch_plane_fft<float>(c->shp_plane32, c->d_zpj_ord + pb, pm, c->d_geoms, c->d_tw32, -1, 0, sg));
-    LK(launch_col_fft<float>(c->shp_col32, c->d_zcj_ord + cb, cm, c->d_geoms, c->d_tw32, 0, 1, sg));
-    if (gpm > 0) {
-      LK(launch_plane_fft<double>(c->shp_plane, c->d_gpj_ord + gpb, gpm, c->d_geoms, c->d_tw64, -1, 0, sg));
-      LK(launch_col_fft<double>(c->shp_col, c->d_gcj_ord + gcb, gcm, c->d_geoms, c->d_tw64, 0, 1, sg));
-    }
-    LK(launch_mix_update(fi, cnt_i, c->eblocks, sg));
-  } else {
+  const int cnt_i = gr.inst_end - gr.inst_begin;
+  const FieldInst *fi = c->d_fi_ord + gr.inst_begin;
+  const GroupJobs j = group_jobs(c, gr);
+  if (update)
+    mix_group_kspace_update(c, g, sg);
+  else
     LK(launch_mix_smear(fi, cnt_i, c->eblocks, sg));
-  }
-  LK(launch_col_fft<float>(c->shp_col32, c->d_zcj_ord + cb, cm, c->d_geoms, c->d_tw32, 1, 0, sg));
-  LK(launch_plane_fft<float>(c->shp_plane32, c->d_zpj_ord + pb, pm, c->d_geoms, c->d_tw32, +1, 0, sg));
-  if (gpm > 0) {
-    LK(launch_col_fft<double>(c->shp_col, c->d_gcj_ord + gcb, gcm, c->d_geoms, c->d_tw64, 1, 0, sg));
-    LK(launch_plane_fft<double>(c->shp_plane, c->d_gpj_ord + gpb, gpm, c->d_geoms, c->d_tw64, +1, 0, sg));
+  LK(launch_col_fft<float>(c->shp_col32, c->d_zcj_ord + j.cb, j.cm, c->d_geoms, c->d_tw32, 1, 0, sg));
+  LK(launch_plane_fft<float>(c->shp_plane32, c->d_zpj_ord + j.pb, j.pm, c->d_geoms, c->d_tw32, +1, 0, sg));
+  if (j.gpm > 0) {
+    LK(launch_col_fft<double>(c->shp_col, c->d_gcj_ord + j.gcb, j.gcm, c->d_geoms, c->d_tw64, 1, 0, sg));
+    LK(launch_plane_fft<double>(c->shp_plane, c->d_gpj_ord + j.gpb, j.gpm, c->d_geoms, c->d_tw64, +1, 0, sg));
   }
   LK(launch_mix_boltzmann(fi, cnt_i, c->eblocks, sg));
   mix_group_sweep(c, g, sg);
@@ -1786,9 +1810,22 @@ void ctx_create(scft_ctx *c, const scft_params *params, int n_inst) {
   CK(cudaStreamSynchronize(c->st));
 }
 
+// The captured graphs (update iteration, density build, host-field steps)
+// hold launches of one schedule; any change of schedule or kernel form drops
+// them, and the next call captures anew.
+static void drop_graphs(scft_ctx *c) {
+  cudaGraphExec_t *gs[3] = {&c->g_update, &c->g_density, &c->g_step};
+  for (cudaGraphExec_t *g : gs)
+    if (*g) {
+      CK(cudaGraphExecDestroy(*g));
+      *g = nullptr;
+    }
+}
+
 void ctx_destroy(scft_ctx *c) {
   if (c->g_update) cudaGraphExecDestroy(c->g_update);
   if (c->g_density) cudaGraphExecDestroy(c->g_density);
+  if (c->g_step) cudaGraphExecDestroy(c->g_step);
   for (void *p : c->allocs) cudaFree(p);
   for (cudaStream_t sst : c->side) cudaStreamDestroy(sst);
   for (auto &I : c->inst)
@@ -1797,6 +1834,8 @@ void ctx_destroy(scft_ctx *c) {
   if (c->h_jobs) cudaFreeHost(c->h_jobs);
   if (c->h_skip) cudaFreeHost(c->h_skip);
   for (cudaEvent_t ev : c->ev_join) cudaEventDestroy(ev);
+  for (cudaEvent_t ev : c->ev_up) cudaEventDestroy(ev);
+  if (c->h_hsum) cudaFreeHost(c->h_hsum);
   if (c->ev_fork) cudaEventDestroy(c->ev_fork);
   if (c->st) cudaStreamDestroy(c->st);
 }
@@ -1899,18 +1938,7 @@ void ctx_set_wait_limit(scft_ctx *c, int polls) {
 void ctx_set_plane_form(scft_ctx *c, int form) {
   if (form < 0 || form > 2) throw ScftError(SCFT_ERR_ARG, "plane form must be 0, 1 or 2");
   c->plane64_form = form;
-  if (c->g_update) {
-    CK(cudaGraphExecDestroy(c->g_update));
-    c->g_update = nullptr;
-  }
-  if (c->g_density) {
-    CK(cudaGraphExecDestroy(c->g_density));
-    c->g_density = nullptr;
-  }
-  if (c->g_step) {
-    CK(cudaGraphExecDestroy(c->g_step));
-    c->g_step = nullptr;
-  }
+  drop_graphs(c);
 }
 
 // Persistent sweep on or off (64 x 64 x 64 groups only; others keep the
@@ -1920,14 +1948,7 @@ void ctx_set_persistent(scft_ctx *c, int on) {
   c->sweep_persistent = on ? 1 : 0;
   if (!c->mixed) return;
   build_groups(c);
-  if (c->g_update) {
-    CK(cudaGraphExecDestroy(c->g_update));
-    c->g_update = nullptr;
-  }
-  if (c->g_density) {
-    CK(cudaGraphExecDestroy(c->g_density));
-    c->g_density = nullptr;
-  }
+  drop_graphs(c);
 }
 
 // Number of independent launch chains of the mixed sweep (1 = one chain).
@@ -1937,14 +1958,7 @@ void ctx_set_sweep_groups(scft_ctx *c, int groups, int phases) {
   c->sweep_phases = phases;
   if (!c->mixed) return;
   build_groups(c);
-  if (c->g_update) {  // the captured iteration holds the old launch chains
-    CK(cudaGraphExecDestroy(c->g_update));
-    c->g_update = nullptr;
-  }
-  if (c->g_density) {
-    CK(cudaGraphExecDestroy(c->g_density));
-    c->g_density = nullptr;
-  }
+  drop_graphs(c);  // the captured graphs hold the old launch chains
 }
 
 // Autotuner of the mixed form's launch schedule: for every candidate
@@ -2070,14 +2084,7 @@ void ctx_autotune(scft_ctx *c, int reps, int *groups_out, int *phases_out, int *
   CK(cudaStreamSynchronize(c->st));
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  if (c->g_update) {
-    CK(cudaGraphExecDestroy(c->g_update));
-    c->g_update = nullptr;
-  }
-  if (c->g_density) {
-    CK(cudaGraphExecDestroy(c->g_density));
-    c->g_density = nullptr;
-  }
+  drop_graphs(c);
   *groups_out = bg;
   *phases_out = bp;
   *tx_out = (c->colfast || c->anyfast || c->xy128 || c->any96) ? bt : 0;
@@ -2227,6 +2234,9 @@ void ctx_profile_step(scft_ctx *c, int reps, double *ms_plane, double *bytes_pla
 }
 
 // calc_H (code/calc_h.cpp:9-64); out per instance: Re H, Im H, Re Qd, Im Qd, Re Qga
+static int h_collect(scft_ctx *c, double *out);
+static int h_reduce(scft_ctx *c, double *out, const double2 *hp, const double2 *sc, const std::vector<int> *rows);
+
 int ctx_calc_H(scft_ctx *c, double *out) {
   NvtxRange nvtx_range("scft_calc_H");
   if (c->dirty_density) ctx_poly_density(c);
@@ -2235,6 +2245,13 @@ int ctx_calc_H(scft_ctx *c, double *out) {
     CK(launch_mix_h_partials(c->d_fi, n, c->hblocks, c->d_hpart, c->st));
   else
     CK(launch_h_partials(c->d_fi, n, c->hblocks, c->d_hpart, c->st));
+  return h_collect(c, out);
+}
+
+// calc_H's host part: the partial sums and scalars of every instance,
+// copied after the work queued so far, reduced per instance into out.
+static int h_collect(scft_ctx *c, double *out) {
+  const int n = (int)c->inst.size();
   std::vector<double2> hp((size_t)n * 4 * c->hblocks);
   CK(cudaMemcpyAsync(hp.data(), c->d_hpart, sizeof(double2) * hp.size(), cudaMemcpyDeviceToHost, c->st));
   std::vector<double2> sc((size_t)n * kNumScalars);
@@ -2242,6 +2259,14 @@ int ctx_calc_H(scft_ctx *c, double *out) {
     CK(cudaMemcpyAsync(&sc[(size_t)k * kNumScalars], c->inst[k].scal, sizeof(double2) * kNumScalars,
                        cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
+  return h_reduce(c, out, hp.data(), sc.data(), nullptr);
+}
+
+// calc_H's reduction: the partial sums hp (instance k's at row (*rows)[k],
+// or row k) and the scalars sc (kNumScalars per instance, instance order)
+// into out, 5 per instance.
+static int h_reduce(scft_ctx *c, double *out, const double2 *hp, const double2 *sc, const std::vector<int> *rows) {
+  const int n = (int)c->inst.size();
   int status = SCFT_OK;
   for (int k = 0; k < n; k++) {
     const Instance &I = c->inst[k];
@@ -2249,7 +2274,7 @@ int ctx_calc_H(scft_ctx *c, double *out) {
     for (int j = 0; j < 4; j++) {
       cd s(0.0, 0.0);
       for (int b = 0; b < c->hblocks; b++) {
-        const double2 v = hp[((size_t)k * 4 + j) * c->hblocks + b];
+        const double2 v = hp[((size_t)(rows ? (*rows)[k] : k) * 4 + j) * c->hblocks + b];
         s += cd(v.x, v.y);
       }
       if (I.mixed)
@@ -2278,13 +2303,24 @@ int ctx_calc_H(scft_ctx *c, double *out) {
   return status;
 }
 
+// The fields an update changes: w+ and the pair of every nonzero chi (ab:
+// w[1], w[2]; bc: w[3], w[4]; ac: w[5], w[6]).  The reference updates a pair
+// only for nonzero chi (code/1s_update.cpp:42,168,339) and initialises the
+// others to zero (code/initialize.cpp:430-431); the mixed form holds them at
+// zero (its update assembles w_A, w_B without them).
+static void fields_in_use(const Instance &I, bool active[7]) {
+  const bool on[7] = {true, I.cab != 0.0, I.cab != 0.0, I.cbc != 0.0, I.cbc != 0.0, I.cac != 0.0, I.cac != 0.0};
+  for (int f = 0; f < 7; f++) active[f] = on[f];
+}
+
 // scft_set_fields of one instance or of all: one copy per instance (the seven
 // fields are contiguous on both sides), one realness check launch over the
 // instances, one synchronisation (the caller may reuse its buffers, the check
 // result is on the host), then one batched forward transform of the nonzero
 // fields (zero fields are transforms of themselves), left to run on the
-// stream.  SCFT_ERR_COMPLEX leaves the instance's fields undefined until its
-// next successful call.
+// stream.  Mixed-form instances set the pairs whose chi is 0 to zero.
+// SCFT_ERR_COMPLEX leaves the instance's fields undefined until its next
+// successful call.
 static constexpr int kCheckBlocks = 14;
 
 static void set_fields_ks(scft_ctx *c, const std::vector<int> &ks, const double *const *w) {
@@ -2294,6 +2330,12 @@ static void set_fields_ks(scft_ctx *c, const std::vector<int> &ks, const double 
   for (size_t q = 0; q < ks.size(); q++) {
     Instance &I = c->inst[ks[q]];
     CK(cudaMemcpyAsync(I.w[0], w[q], sizeof(double2) * 7 * (size_t)I.M, cudaMemcpyHostToDevice, c->st));
+    if (I.mixed) {
+      bool active[7];
+      fields_in_use(I, active);
+      for (int f = 1; f < 7; f += 2)
+        if (!active[f]) CK(cudaMemsetAsync(I.w[f], 0, sizeof(double2) * 2 * (size_t)I.M, c->st));
+    }
     mixed = mixed || I.mixed;
   }
   if (!mixed) {
@@ -2358,10 +2400,13 @@ void ctx_set_fields(scft_ctx *c, int k, const double *w) { set_fields_ks(c, {k},
 int ctx_calc_H(scft_ctx *c, double *out);
 void ctx_update(scft_ctx *c, int n_iter);
 void ctx_set_fields_all(scft_ctx *c, const double *const *w);
+void ctx_get_fields(scft_ctx *c, int k, double *w);
 
-// Per-group FP64 forward-transform jobs of the fields a mixed instance uses
-// (w+ and the pair of every nonzero chi), in job order; rebuilt when the
-// groups change.
+// Per-group FP64 transform jobs, in job order, rebuilt when the groups
+// change: the forward transforms of the uploaded fields (those an update
+// changes) and, per round of three such fields, the inverse transforms of
+// the updated fields to download (the q-th field of an instance goes
+// through rho[q % 3] in round q / 3).
 static void build_step_jobs(scft_ctx *c) {
   std::vector<int> sig;
   for (auto &gr : c->groups) {
@@ -2374,37 +2419,59 @@ static void build_step_jobs(scft_ctx *c) {
   c->step_cj.clear();
   c->step_npj.clear();
   c->step_ncj.clear();
+  c->out_pj.clear();
+  c->out_cj.clear();
+  c->out_npj.clear();
+  c->out_ncj.clear();
+  auto add = [&](std::vector<PlaneJob> &pj, std::vector<ColJob> &cj, const Instance &I, double2 *a) {
+    const DevGeom &g = c->geoms[I.geom];
+    for (int z = 0; z < g.nz; z++) pj.push_back(PlaneJob{a, I.geom, z});
+    for (int y = 0; y < g.ny; y++)
+      for (int x0 = 0; x0 < g.nx; x0 += g.tx) cj.push_back(ColJob{a, nullptr, I.geom, x0, y});
+  };
   for (auto &gr : c->groups) {
     std::vector<PlaneJob> pj;
     std::vector<ColJob> cj;
+    std::vector<PlaneJob> opj[3];
+    std::vector<ColJob> ocj[3];
     for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) {
       const Instance &I = c->inst[c->job_order[oi]];
-      const DevGeom &g = c->geoms[I.geom];
-      const bool active[7] = {true, I.cab != 0.0, I.cab != 0.0, I.cbc != 0.0, I.cbc != 0.0, I.cac != 0.0,
-                              I.cac != 0.0};
-      for (int f = 0; f < 7; f++) {
+      bool active[7];
+      fields_in_use(I, active);
+      for (int f = 0, q = 0; f < 7; f++) {
         if (!active[f]) continue;
-        for (int z = 0; z < g.nz; z++) pj.push_back(PlaneJob{I.w[f], I.geom, z});
-        for (int y = 0; y < g.ny; y++)
-          for (int x0 = 0; x0 < g.nx; x0 += g.tx) cj.push_back(ColJob{I.w[f], nullptr, I.geom, x0, y});
+        add(pj, cj, I, I.w[f]);
+        add(opj[q / 3], ocj[q / 3], I, I.rho[q % 3]);
+        q++;
       }
     }
     c->step_pj.push_back(dupload(c, pj));
     c->step_cj.push_back(dupload(c, cj));
     c->step_npj.push_back((int)pj.size());
     c->step_ncj.push_back((int)cj.size());
+    for (int r = 0; r < 3; r++) {
+      c->out_pj.push_back(opj[r].empty() ? nullptr : dupload(c, opj[r]));
+      c->out_cj.push_back(ocj[r].empty() ? nullptr : dupload(c, ocj[r]));
+      c->out_npj.push_back((int)opj[r].size());
+      c->out_ncj.push_back((int)ocj[r].size());
+    }
   }
   c->step_groups_sig = sig;
 }
 
-// The graph body of scft_step_fields (mixed form, no grafted chains): per
-// sweep group on its side stream, the upload of its instances' fields in use
-// from host memory (the inactive pairs are zeroed: they do not enter the
-// model), their realness check (results copied to pinned host memory, read
-// after the call's synchronisation), the FP64 forward transform of the
-// fields in use, then the density build and n_iter updates of the group.  One
-// group's upload runs beside another group's compute.
-static void step_body(scft_ctx *c, const double *const *w, int n_iter) {
+// The graph body of scft_step_fields and scft_iterate_fields (mixed form, no
+// grafted chains): per sweep group on its side stream, the upload of its
+// instances' fields (w+ and the pairs of nonzero chi; the others are set to
+// zero), their realness check (results copied to pinned host memory, read
+// after the call's synchronisation), their FP64 forward transform, then
+//   step_fields (iterate false): the density build and n_iter updates;
+//   iterate_fields: the density build, calc_H's partial sums of the uploaded
+//     fields, the k-space half of one update (no density build after it)
+//     and, with w_out, the download of the updated fields in use (inverse
+//     FP64 transforms with the instances' rho[0..2] as scratch, three
+//     fields a round).
+// One group's copies run beside another group's compute.
+static void step_body(scft_ctx *c, const double *const *w, int n_iter, bool iterate, double *const *w_out) {
   cudaStream_t st = c->st;
   const int G = (int)c->groups.size();
   CK(cudaEventRecord(c->ev_fork, st));
@@ -2412,14 +2479,18 @@ static void step_body(scft_ctx *c, const double *const *w, int n_iter) {
     const scft_ctx::SweepGroup &gr = c->groups[g];
     cudaStream_t sg = c->side[g];
     CK(cudaStreamWaitEvent(sg, c->ev_fork, 0));
+    // the groups' uploads run one after another, so that the first group
+    // computes while the others' fields are still coming in
+    if (g > 0) CK(cudaStreamWaitEvent(sg, c->ev_up[g - 1], 0));
     const int cnt = gr.inst_end - gr.inst_begin;
-    // the fields in use come from the host (one copy per run of adjacent
-    // fields in use); the pairs whose chi is 0 are set to zero instead
+    // the fields an update changes come from the host (one copy per run of
+    // adjacent ones); the pairs whose chi is 0 are held at zero in the mixed
+    // form (its update treats them as zero) and are not read
     for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) {
       const int k = c->job_order[oi];
       Instance &I = c->inst[k];
-      const bool active[7] = {true, I.cab != 0.0, I.cab != 0.0, I.cbc != 0.0, I.cbc != 0.0, I.cac != 0.0,
-                              I.cac != 0.0};
+      bool active[7];
+      fields_in_use(I, active);
       const size_t fb = sizeof(double2) * (size_t)I.M;  // bytes per field
       for (int f = 0; f < 7;) {
         int f1 = f + 1;
@@ -2431,6 +2502,7 @@ static void step_body(scft_ctx *c, const double *const *w, int n_iter) {
         f = f1;
       }
     }
+    CK(cudaEventRecord(c->ev_up[g], sg));
     k_real_check_all<<<dim3(kCheckBlocks, cnt), 256, 0, sg>>>(c->d_fi_ord + gr.inst_begin, nullptr,
                                                               c->d_realout + 128 * (size_t)gr.inst_begin);
     CK(cudaGetLastError());
@@ -2442,51 +2514,96 @@ static void step_body(scft_ctx *c, const double *const *w, int n_iter) {
       LK(launch_col_fft<double>(c->shp_col, c->step_cj[g], c->step_ncj[g], c->d_geoms, c->d_tw64, 0, 1, sg));
     }
     mix_group_chain(c, g, sg, false);
-    for (int it = 0; it < n_iter; it++) mix_group_chain(c, g, sg, true);
+    if (!iterate) {
+      for (int it = 0; it < n_iter; it++) mix_group_chain(c, g, sg, true);
+    } else {
+      // H needs the fields (Parseval sums) and Qd only: its partial sums are
+      // taken before the update changes the fields
+      const size_t hrow = (size_t)4 * c->hblocks;
+      LK(launch_mix_h_partials(c->d_fi_ord + gr.inst_begin, cnt, c->hblocks, c->d_hpart + hrow * gr.inst_begin, sg));
+      CK(cudaMemcpyAsync(c->h_hsum + hrow * gr.inst_begin, c->d_hpart + hrow * gr.inst_begin,
+                         sizeof(double2) * hrow * cnt, cudaMemcpyDeviceToHost, sg));
+      for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) {
+        const int k = c->job_order[oi];
+        CK(cudaMemcpyAsync(c->h_hsum + hrow * c->inst.size() + (size_t)k * kNumScalars, c->inst[k].scal,
+                           sizeof(double2) * kNumScalars, cudaMemcpyDeviceToHost, sg));
+      }
+      mix_group_kspace_update(c, g, sg);
+      for (int r = 0; w_out && r < 3; r++) {
+        const int jr = 3 * g + r;
+        if (!c->out_npj[jr]) continue;
+        auto each = [&](bool to_host) {
+          for (int oi = gr.inst_begin; oi < gr.inst_end; oi++) {
+            const int k = c->job_order[oi];
+            Instance &I = c->inst[k];
+            bool active[7];
+            fields_in_use(I, active);
+            const size_t fb = sizeof(double2) * (size_t)I.M;
+            for (int f = 0, q = 0; f < 7; f++) {
+              if (!active[f]) continue;
+              if (q / 3 == r) {
+                if (to_host)
+                  CK(cudaMemcpyAsync(w_out[k] + 2 * (size_t)I.M * f, I.rho[q % 3], fb, cudaMemcpyDeviceToHost, sg));
+                else
+                  CK(cudaMemcpyAsync(I.rho[q % 3], I.w[f], fb, cudaMemcpyDeviceToDevice, sg));
+              }
+              q++;
+            }
+          }
+        };
+        each(false);
+        LK(launch_col_fft<double>(c->shp_col, c->out_cj[jr], c->out_ncj[jr], c->d_geoms, c->d_tw64, 1, 0, sg));
+        LK(launch_plane_fft<double>(c->shp_plane, c->out_pj[jr], c->out_npj[jr], c->d_geoms, c->d_tw64, +1, 0, sg));
+        each(true);
+      }
+    }
     CK(cudaEventRecord(c->ev_join[g], sg));
     CK(cudaStreamWaitEvent(st, c->ev_join[g], 0));
   }
 }
 
-// scft_step_fields: fields of every instance from host memory (w[inst], 7 x M
-// complex, the scft_set_fields layout; pinned memory lets the uploads overlap
-// compute), the density build of those fields, n_iter updates, H into out
-// (5 per instance, as scft_calc_H) -- one call and one synchronisation.
-// Mixed-form batches without grafted chains or complex Langevin run as one
-// captured graph (re-captured when the host pointers or n_iter change);
-// everything else runs scft_set_fields_all, scft_update_1s and scft_calc_H.
-int ctx_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *out) {
-  NvtxRange nvtx_range("scft_step_fields");
-  const int n = (int)c->inst.size();
+// Whether a host-field call runs as a captured graph: mixed-form batches
+// without grafted chains or complex Langevin, with page-locked (pinned or
+// registered) host buffers; a captured copy needs page-locked memory.
+static bool step_graph_ok(scft_ctx *c, const double *const *w, const double *const *w_out) {
   bool cl = false;
   for (auto &I : c->inst) cl = cl || I.p.do_cl;
-  // a captured upload needs page-locked (pinned or registered) host memory
-  bool pinned = true;
-  for (int k = 0; k < n && pinned; k++) {
+  if (!c->mixed || c->ngmax > 0 || cl || c->groups.empty()) return false;
+  auto locked = [](const void *p) {
     cudaPointerAttributes a;
-    if (cudaPointerGetAttributes(&a, w[k]) != cudaSuccess) {
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
       cudaGetLastError();
-      pinned = false;
-    } else {
-      pinned = (a.type == cudaMemoryTypeHost);
+      return false;
     }
-  }
-  if (!c->mixed || c->ngmax > 0 || cl || c->groups.empty() || !pinned) {
-    ctx_set_fields_all(c, w);
-    ctx_update(c, n_iter);
-    return ctx_calc_H(c, out);
-  }
-  if (!c->h_pin || !c->d_realout) throw ScftError(SCFT_ERR_CUDA, "scft_step_fields: staging buffers missing");
+    return a.type == cudaMemoryTypeHost;
+  };
+  const int n = (int)c->inst.size();
+  for (int k = 0; k < n; k++)
+    if (!locked(w[k]) || (w_out && !locked(w_out[k]))) return false;
+  return true;
+}
+
+// Runs the host-field graph of (call, host pointers, n_iter), capturing it
+// first when the key differs from the last one's.  A first run ever is eager
+// (kernel attributes get set), without the download, so that w stays the
+// input of the captured run even when w_out aliases it.
+static void run_step_graph(scft_ctx *c, const double *const *w, int n_iter, bool iterate, double *const *w_out) {
+  if (!c->h_pin || !c->d_realout) throw ScftError(SCFT_ERR_CUDA, "host-field step: staging buffers missing");
+  const int n = (int)c->inst.size();
   build_step_jobs(c);
-  std::vector<const double *> ptrs(w, w + n);
-  if (c->g_step && (ptrs != c->step_ptrs || n_iter != c->step_iters)) {
+  // pinned memory for the H sums the graph copies out
+  if (!c->h_hsum)
+    CK(cudaMallocHost(&c->h_hsum, sizeof(double2) * (size_t)n * (4 * (size_t)c->hblocks + kNumScalars)));
+  std::vector<const void *> key(w, w + n);
+  key.push_back(iterate ? c : nullptr);
+  for (int k = 0; k < n; k++) key.push_back(w_out ? w_out[k] : nullptr);
+  if (c->g_step && (key != c->step_ptrs || n_iter != c->step_iters)) {
     CK(cudaGraphExecDestroy(c->g_step));
     c->g_step = nullptr;
   }
   if (!c->g_step) {
-    // the first run is eager (kernel attributes get set), then capture
     if (!c->update_runs && !c->density_runs) {
-      step_body(c, w, n_iter);
+      step_body(c, w, n_iter, iterate, nullptr);
       CK(cudaStreamSynchronize(c->st));
       c->density_runs++;
       c->update_runs++;
@@ -2494,7 +2611,7 @@ int ctx_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *out
     cudaGraph_t graph;
     CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
     try {
-      step_body(c, w, n_iter);
+      step_body(c, w, n_iter, iterate, w_out);
     } catch (...) {
       cudaGraph_t g2;
       cudaStreamEndCapture(c->st, &g2);
@@ -2503,13 +2620,16 @@ int ctx_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *out
     CK(cudaStreamEndCapture(c->st, &graph));
     CK(cudaGraphInstantiate(&c->g_step, graph, 0));
     cudaGraphDestroy(graph);
-    c->step_ptrs = ptrs;
+    c->step_ptrs = key;
     c->step_iters = n_iter;
   }
   CK(cudaGraphLaunch(c->g_step, c->st));
-  c->dirty_density = 0;
-  int status = ctx_calc_H(c, out);  // queues H and synchronises
-  check_device_error(c);
+}
+
+// The realness check of the uploaded fields, read after the call's
+// synchronisation (maxima per check block in h_pin, job order).
+static void check_step_realness(scft_ctx *c) {
+  const int n = (int)c->inst.size();
   std::string bad;
   for (int oi = 0; oi < n; oi++) {
     double m[9] = {};
@@ -2523,6 +2643,71 @@ int ctx_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *out
                                           ": mixed precision needs real w_A, w_B: the mean-field phase convention "
                                           "(the results of this call are invalid)");
   }
+}
+
+// scft_step_fields: fields of every instance from host memory (w[inst], 7 x M
+// complex, the scft_set_fields layout; pinned memory lets the uploads overlap
+// compute), the density build of those fields, n_iter updates, H into out
+// (5 per instance, as scft_calc_H) -- one call and one synchronisation.
+// Mixed-form batches without grafted chains or complex Langevin run as one
+// captured graph (re-captured when the host pointers or n_iter change);
+// everything else runs scft_set_fields_all, scft_update_1s and scft_calc_H.
+int ctx_step_fields(scft_ctx *c, const double *const *w, int n_iter, double *out) {
+  NvtxRange nvtx_range("scft_step_fields");
+  if (!step_graph_ok(c, w, nullptr)) {
+    ctx_set_fields_all(c, w);
+    ctx_update(c, n_iter);
+    return ctx_calc_H(c, out);
+  }
+  run_step_graph(c, w, n_iter, false, nullptr);
+  c->dirty_density = 0;
+  int status = ctx_calc_H(c, out);  // queues H and synchronises
+  check_device_error(c);
+  check_step_realness(c);
+  return status;
+}
+
+// scft_iterate_fields: one iteration of the reference's main loop per
+// instance, from and to host memory, in the order calc_poly_density, calc_H,
+// update: the fields of every instance from w[inst], their density build, H
+// of those fields into out, one field update; with w_out, the updated fields
+// into w_out[inst] (the mixed form writes the fields the update changes;
+// w_out may be w).
+// The densities are then those of the uploaded fields (stale: the next call
+// that needs the updated fields' densities rebuilds them).  Mixed-form
+// batches without grafted chains or complex Langevin, with page-locked
+// buffers, run as one captured graph (one density build per iteration);
+// everything else runs scft_set_fields_all, scft_calc_H, scft_update_1s and
+// scft_get_fields.
+int ctx_iterate_fields(scft_ctx *c, const double *const *w, double *const *w_out, double *out) {
+  NvtxRange nvtx_range("scft_iterate_fields");
+  const int n = (int)c->inst.size();
+  if (!step_graph_ok(c, w, w_out)) {
+    ctx_set_fields_all(c, w);
+    const int status = ctx_calc_H(c, out);
+    ctx_update(c, 1);
+    if (w_out)
+      for (int k = 0; k < n; k++) {
+        const Instance &I = c->inst[k];
+        const size_t per = 2 * (size_t)I.M;  // doubles per field
+        std::vector<double> all(7 * per);
+        ctx_get_fields(c, k, all.data());
+        bool active[7];
+        fields_in_use(I, active);
+        for (int f = 0; f < 7; f++)
+          if (active[f] || !I.mixed) std::copy(all.begin() + f * per, all.begin() + (f + 1) * per, w_out[k] + f * per);
+      }
+    return status;
+  }
+  run_step_graph(c, w, 1, true, w_out);
+  c->dirty_density = 1;
+  std::vector<int> rows(n);
+  for (int oi = 0; oi < n; oi++) rows[c->job_order[oi]] = oi;
+  CK(cudaStreamSynchronize(c->st));
+  const double2 *hp = c->h_hsum;  // the graph copied the H sums here
+  const int status = h_reduce(c, out, hp, hp + (size_t)4 * c->hblocks * n, &rows);
+  check_device_error(c);
+  check_step_realness(c);
   return status;
 }
 

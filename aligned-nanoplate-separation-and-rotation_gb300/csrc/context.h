@@ -206,6 +206,8 @@ struct scft_ctx {
   int sweep_streams = 2;  // requested number of groups (1 = a single chain)
   std::vector<cudaStream_t> side;
   std::vector<cudaEvent_t> ev_join;
+  std::vector<cudaEvent_t> ev_up;  // host-field calls: end of a group's uploads
+  double2 *h_hsum = nullptr;  // host-field calls: pinned H partial sums (job order), then scalars (instance order)
   cudaEvent_t ev_fork = nullptr;
   scft::LaunchShape shp_mix{}, shp_col32{}, shp_plane32{};
   scft::LaunchShape shp_mixg{};  // mixed plane passes in place (shp_mix; 1024 threads for the largest planes)
@@ -214,15 +216,21 @@ struct scft_ctx {
   int eblocks = 0;  // blocks per instance for pointwise kernels
   double2 *d_hpart = nullptr;
   int hblocks = 0;
-  // scft_step_fields: its captured graph (uploads, checks, transforms, density
-  // build, updates) for one set of host pointers and iteration count, and the
+  // scft_step_fields / scft_iterate_fields: the captured graph of the last
+  // such call (uploads, checks, transforms, density builds, updates,
+  // downloads), keyed by the call, its host pointers and iteration count; the
   // per-group FP64 transform jobs of the uploaded fields (job-order groups)
+  // and, per group and round of three fields, the inverse transform jobs of
+  // the downloaded fields (on the instances' rho[0..2] as scratch)
   cudaGraphExec_t g_step = nullptr;
-  std::vector<const double *> step_ptrs;
+  std::vector<const void *> step_ptrs;
   int step_iters = 0;
   std::vector<scft::PlaneJob *> step_pj;
   std::vector<scft::ColJob *> step_cj;
   std::vector<int> step_npj, step_ncj;
+  std::vector<scft::PlaneJob *> out_pj;  // [3 * group + round]
+  std::vector<scft::ColJob *> out_cj;
+  std::vector<int> out_npj, out_ncj;
   std::vector<int> step_groups_sig;  // group boundaries the job lists were built for
   cudaGraphExec_t g_update = nullptr;
   cudaGraphExec_t g_density = nullptr;  // captured density build (after the first, eager one)

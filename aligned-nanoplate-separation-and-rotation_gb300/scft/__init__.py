@@ -29,7 +29,8 @@ EXPORTS = ("scft_last_error", "scft_version", "scft_create", "scft_destroy", "sc
            "scft_profile_step", "scft_diblock_density_noalloc", "scft_set_sweep_groups", "scft_autotune",
            "scft_set_fields_all", "scft_set_wait_limit", "scft_fp64_fma_rate",
            "scft_set_persistent", "scft_get_schedule", "scft_profile_sweep",
-           "scft_get_fft_plan", "scft_step_fields", "scft_set_plane_form", "scft_get_plane_form")
+           "scft_get_fft_plan", "scft_step_fields", "scft_set_plane_form", "scft_get_plane_form",
+           "scft_iterate_fields")
 
 
 class ScftError(RuntimeError):
@@ -112,6 +113,8 @@ def load(path: str | None = None):
     lib.scft_get_plane_form.argtypes = [vp, ctypes.POINTER(ctypes.c_int)]
     lib.scft_profile_sweep.argtypes = [vp, ctypes.c_int, dp, dp]
     lib.scft_step_fields.argtypes = [vp, ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_void_p]
+    lib.scft_iterate_fields.argtypes = [vp, ctypes.POINTER(ctypes.c_void_p), ctypes.POINTER(ctypes.c_void_p),
+                                        ctypes.c_void_p]
     lib.scft_get_fft_plan.argtypes = [vp, ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                       ctypes.POINTER(ctypes.c_int)]
     lib.scft_get_schedule.argtypes = [vp] + [ctypes.POINTER(ctypes.c_int)] * 4
@@ -356,6 +359,31 @@ class Context:
             bufs.append(b)
         out = np.zeros((self.n, 5), np.float64)
         self.last_status = self.step_fields_raw([b.ctypes.data for b in bufs], n_iter, out.ctypes.data)
+        return out
+
+    def iterate_fields_raw(self, ptrs, out_ptrs, h_ptr: int) -> int:
+        """scft_iterate_fields from host pointers (one per instance, 7 x M
+        complex each) into out_ptrs (None: no download; may equal ptrs) and a
+        host buffer of 5 doubles per instance; returns the status (OK or
+        ERR_NAN), raises on other errors."""
+        arr = (ctypes.c_void_p * self.n)(*ptrs)
+        oarr = (ctypes.c_void_p * self.n)(*out_ptrs) if out_ptrs is not None else None
+        code = load().scft_iterate_fields(self._h, arr, oarr, ctypes.c_void_p(h_ptr))
+        if code not in (OK, ERR_NAN):
+            _check(code)
+        return code
+
+    def iterate_fields(self, bufs: list, download: bool = True) -> np.ndarray:
+        """iterate_fields_raw on complex128 arrays of shape (7,) + grid, one
+        per instance, updated in place when `download`; returns H (n x 5) of
+        the fields passed in."""
+        for k, b in enumerate(bufs):
+            if b.dtype != np.complex128 or b.shape != (7,) + self._shape(k) or not b.flags.c_contiguous:
+                raise ValueError("instance %d: need a C-contiguous complex128 array of shape %s"
+                                 % (k, (7,) + self._shape(k)))
+        out = np.zeros((self.n, 5), np.float64)
+        ptrs = [b.ctypes.data for b in bufs]
+        self.last_status = self.iterate_fields_raw(ptrs, ptrs if download else None, out.ctypes.data)
         return out
 
     def set_fields_all_raw(self, ptrs):

@@ -8,9 +8,10 @@ A step is one update_1s iteration (k-space field update, smearing, both
 propagator sweeps, densities) of every instance of the batch.  `value` is
 timed with CUDA events on the library's own stream with the fields resident in
 HBM; `e2e` is the same metric through the C ABI with host buffers: each step
-is one scft_step_fields call, which copies every instance's seven fields from
-pinned host memory, builds their densities, runs the iteration and reads H
-back.  The working set of one step (propagator history,
+is one scft_iterate_fields call on pinned host buffers, which copies every
+instance's fields (w+ and the pairs of nonzero chi) from host memory, builds their densities, reads H
+of those fields back, runs the field update and writes the updated fields
+back into the same host buffers (the next step's input).  The working set of one step (propagator history,
 fields, tables: >1 GB for the 15-instance batch) is larger than L2, so no
 explicit L2 flush is done.
 
@@ -218,11 +219,20 @@ def job_rate(units_per_rank: float, world: int, seconds_max: float) -> float:
     return units_per_rank * world / seconds_max
 
 
-def fields_in_use(p, form):
-    """Fields scft_step_fields copies from the host for one instance: all 7
-    in the FP64 method (it runs set_fields), w+ and the pairs of nonzero chi
-    in the mixed form."""
+def fields_uploaded(p, form):
+    """Fields scft_iterate_fields copies from the host for one instance: all
+    7 in the FP64 method and with grafted chains or complex Langevin (it runs
+    set_fields), w+ and the pairs of nonzero chi in the mixed form's graph."""
     if form != "mixed" or p.Ng > 0 or p.do_cl:
+        return 7
+    return fields_updated(p, form)
+
+
+def fields_updated(p, form):
+    """Fields scft_iterate_fields writes back for one instance: w+ and the
+    pairs of nonzero chi in the mixed form (a pair whose chi is 0 is never
+    updated), all 7 in the FP64 method."""
+    if form != "mixed":
         return 7
     return 1 + 2 * sum(1 for chi in (p.chi_ab, p.chi_bc, p.chi_ac) if chi != 0.0)
 
@@ -508,24 +518,29 @@ def main():
     host_out = torch.zeros(5 * n_inst, dtype=torch.float64, pin_memory=True)
     e2e_steps = max(1, min(args.steps, 10))
     ptrs = [t.data_ptr() for t in host_in]
-    # one call per step (scft_step_fields): upload of every instance's fields,
-    # their density build, one update, H read back; one untimed call first
-    # (it captures the call's graph for these host buffers)
-    ctx.step_fields_raw(ptrs, 1, host_out.data_ptr())
+    # one call per step (scft_iterate_fields, in place): upload of every
+    # instance's fields from the host, their density build, H of those
+    # fields read back, one update, the updated fields written back to the
+    # same host buffers -- the host-held iteration continues the relaxed
+    # state step by step; one untimed call first (it captures the call's
+    # graph for these host buffers)
+    ctx.iterate_fields_raw(ptrs, ptrs, host_out.data_ptr())
     barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
-        ctx.step_fields_raw(ptrs, 1, host_out.data_ptr())
+        ctx.iterate_fields_raw(ptrs, ptrs, host_out.data_ptr())
     torch.cuda.synchronize()
     t_e2e = allmax(time.perf_counter() - t0)
+    # up: the fields the call reads; down: the updated fields it writes
+    # back, H (5 doubles per instance) and, in the mixed form, the realness
+    # check's maxima (128 doubles per instance)
+    up = int(sum(fields_uploaded(p, form) * 16 * m for p, m in zip(params, M)))
+    down = int(sum(fields_updated(p, form) * 16 * m for p, m in zip(params, M)))
     e2e = {"value": job_rate(n_inst * e2e_steps, world, t_e2e), "unit": UNIT,
-           # the fields in use (w+ and the pairs of nonzero chi; the mixed
-           # form's step sets the others to zero instead of copying them)
-           "h2d_bytes_per_step": int(sum(fields_in_use(p, form) * 16 * m for p, m in zip(params, M))),
-           # H (5 doubles per instance) and, in the mixed form, the realness
-           # check's maxima (128 doubles per instance) that the call reads back
-           "d2h_bytes_per_step": int(5 * 8 * n_inst + (128 * 8 * n_inst if form == "mixed" else 0))}
+           "call": "scft_iterate_fields",
+           "h2d_bytes_per_step": up,
+           "d2h_bytes_per_step": down + int(5 * 8 * n_inst + (128 * 8 * n_inst if form == "mixed" else 0))}
 
     # ---- the plain FP64 method on the same batch, same iteration count:
     # its rate (the metric's comparison) and the mixed form's H error

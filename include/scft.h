@@ -140,7 +140,10 @@ int scft_set_fields_all(scft_ctx *ctx, const double *const *w);
 
 /* Sets/gets the seven fields of one instance: w[f*2*M + 2*i + {0,1}]
  * (read_resume_files(), code/io_utils.cpp:183-240; the get side feeds the
- * field files of write_outputs(), code/io_utils.cpp:11-105). */
+ * field files of write_outputs(), code/io_utils.cpp:11-105).  Mixed-form
+ * instances hold the pairs whose chi is 0 at zero, as the reference
+ * initialises them (code/initialize.cpp:430-431; its update never changes
+ * them): values given there are not kept. */
 int scft_set_fields(scft_ctx *ctx, int inst, const double *w);
 int scft_get_fields(scft_ctx *ctx, int inst, double *w);
 
@@ -155,14 +158,38 @@ int scft_get_fields(scft_ctx *ctx, int inst, double *w);
  * registered; others run the sequence), each sweep group's upload, realness check,
  * field transform, density build and updates run as one chain on its own
  * stream inside one captured graph (re-captured when the host pointers or
- * n_iter change), so one group's upload runs beside another group's compute;
- * only w+ and the pairs of nonzero chi are copied, and the fields of pairs
- * whose chi is 0 are set to zero (they do not enter the model).  The
- * realness check of the mixed form is read after the work:
+ * n_iter change), so one group's upload runs beside another group's
+ * compute; only w+ and the pairs of nonzero chi are read (the others are held
+ * at zero, as scft_set_fields does).  The realness check of the mixed form
+ * is read after the work:
  * SCFT_ERR_COMPLEX then means this call's results are invalid.  Returns
  * SCFT_ERR_NAN / SCFT_ERR_QNONPOS like scft_calc_H.  No counterpart in the
  * reference (its driver keeps the fields in host memory throughout). */
 int scft_step_fields(scft_ctx *ctx, const double *const *w, int n_iter, double *H_out);
+
+/* One iteration of the reference's main loop per instance from and to host
+ * memory, in the order calc_poly_density, calc_H, update_1s (the set-up
+ * code/simulate.cpp:36,74 and the main loop :85-157, whose update_1s ends in
+ * the next calc_poly_density, code/1s_update.cpp:351): uploads the fields of every
+ * instance from w[inst] (as scft_set_fields), builds their densities, writes
+ * H of those fields into H_out (5 doubles per instance, as scft_calc_H), runs
+ * one field update (update_1s, or update_Euler per instance) and, when w_out
+ * is not NULL, writes the updated fields into w_out[inst] (same layout; w_out
+ * may be w, which makes repeated calls a host-driven iteration).  Mixed-form
+ * instances write the fields an update changes (w+ and the pairs of nonzero
+ * chi; a pair whose chi is 0 is never updated) and leave the others as they
+ * are; FP64 instances write all seven.  The
+ * densities are not rebuilt for the updated fields: a call that needs them
+ * (scft_get_density, scft_calc_H, scft_update_1s) rebuilds them first.  For
+ * mixed-form batches without grafted chains or complex Langevin and with
+ * page-locked buffers (pinned or registered), the uploads, density builds,
+ * H sums, k-space updates and downloads of each sweep group run as one chain
+ * on its own stream inside one captured graph (re-captured when the host
+ * pointers change), so an iteration costs one density build; the others run
+ * scft_set_fields_all, scft_calc_H, scft_update_1s and scft_get_fields.
+ * Returns and realness check as scft_step_fields (SCFT_ERR_COMPLEX: this
+ * call's results, w_out included, are invalid). */
+int scft_iterate_fields(scft_ctx *ctx, const double *const *w, double *const *w_out, double *H_out);
 
 /* calc_poly_density() for every instance. */
 int scft_calc_poly_density(scft_ctx *ctx);
