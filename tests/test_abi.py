@@ -49,6 +49,8 @@ def test_null_arguments_are_rejected_without_gpu(lib):
     assert lib.scft_calc_poly_density(None) == scft.ERR_ARG
     assert lib.scft_update_1s(None, 1) == scft.ERR_ARG
     assert lib.scft_sync(None) == scft.ERR_ARG
+    assert lib.scft_step_fields(None, None, 1, None) == scft.ERR_ARG
+    assert lib.scft_iterate_fields(None, None, None, None) == scft.ERR_ARG
     out = ctypes.c_void_p()
     p = scft.make_params()
     assert lib.scft_create(ctypes.byref(p), 0, ctypes.byref(out)) == scft.ERR_ARG
