@@ -26,6 +26,11 @@
 namespace scft {
 
 constexpr double kPI = 3.14159265358979323846263383;  // code/globals.h:31
+// Realness check of the mixed form's fields: blocks per instance and the
+// per-instance stride of its per-block maxima (9 per block)
+constexpr int kCheckBlocks = 112;
+constexpr int kCheckStride = 1024;
+static_assert(9 * kCheckBlocks <= kCheckStride, "check maxima overlap");
 
 struct ScftError : std::runtime_error {
   int code;
@@ -926,7 +931,7 @@ void build_jobs(scft_ctx *c) {
   if (c->inst[0].mixed) {  // (c->mixed is set further down)
     // scft_set_fields: check results, instance mask, job staging for the
     // forward transforms of up to all seven fields of every instance
-    c->d_realout = dalloc<double>(c, 128 * (size_t)n);
+    c->d_realout = dalloc<double>(c, kCheckStride * (size_t)n);
     c->d_skip = dalloc<int>(c, n);
     size_t jobs = 0;
     for (auto &I : c->inst) {
@@ -938,7 +943,7 @@ void build_jobs(scft_ctx *c) {
     CK(cudaMallocHost(&c->h_jobs, c->jobs_cap));
     CK(cudaMallocHost(&c->h_skip, sizeof(int) * (size_t)n));
   }
-  if (!c->h_pin) CK(cudaMallocHost(&c->h_pin, 128 * sizeof(double) * (size_t)std::max(1, n)));
+  if (!c->h_pin) CK(cudaMallocHost(&c->h_pin, kCheckStride * sizeof(double) * (size_t)std::max(1, n)));
   c->d_pi = dupload(c, pi);
   c->mixed = c->inst[0].mixed;
   for (auto &I : c->inst)
@@ -1369,7 +1374,9 @@ void build_jobs(scft_ctx *c) {
   long long mmax = 0;
   for (auto &I : c->inst) mmax = std::max(mmax, I.M);
   c->eblocks = (int)std::min<long long>(2048, (mmax + 255) / 256);
-  c->hblocks = 64;
+  // calc_H's partial sums: 256 blocks per instance (its FP64 products and
+  // the index arithmetic of -k need a full grid)
+  c->hblocks = 256;
   c->d_hpart = dalloc<double2>(c, (size_t)n * 4 * c->hblocks);
 }
 
@@ -1377,8 +1384,10 @@ void build_jobs(scft_ctx *c) {
 // Realness check of the mixed form's fields of every instance (blockIdx.y),
 // from its FieldInst (code/calc_poly_density.cpp:45-54): per block, out[9 b] =
 // max |Im w_A|, |Im w_B| (and |Im w_G| with grafts), out[9 b + 1] = the
-// largest real part, out[9 b + 2 + f] = max |w_f|; out advances by 128 per
-// instance.  Instances with skip[inst] = 0 are checked.
+// largest real part, out[9 b + 2 + f] = max |w_f|; out advances by
+// kCheckStride per instance.  Instances with skip[inst] = 0 are checked.
+// kCheckBlocks blocks per instance (the check reads all seven fields, 112
+// bytes per point, and needs a full grid to run at memory speed).
 __global__ void k_real_check_all(const FieldInst *__restrict__ fi, const int *__restrict__ skip, double *out) {
   const FieldInst &F = fi[blockIdx.y];
   if (skip && skip[blockIdx.y]) return;
@@ -1415,7 +1424,7 @@ __global__ void k_real_check_all(const FieldInst *__restrict__ fi, const int *__
     for (int k = 0; k < 9; k++) {
       double v = l < (int)(blockDim.x >> 5) ? red[k][l] : 0.0;
       for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
-      if (l == 0) out[128 * (size_t)blockIdx.y + 9 * blockIdx.x + k] = v;
+      if (l == 0) out[kCheckStride * (size_t)blockIdx.y + 9 * blockIdx.x + k] = v;
     }
   }
 }
@@ -2321,7 +2330,6 @@ static void fields_in_use(const Instance &I, bool active[7]) {
 // stream.  Mixed-form instances set the pairs whose chi is 0 to zero.
 // SCFT_ERR_COMPLEX leaves the instance's fields undefined until its next
 // successful call.
-static constexpr int kCheckBlocks = 14;
 
 static void set_fields_ks(scft_ctx *c, const std::vector<int> &ks, const double *const *w) {
   const int n = (int)c->inst.size();
@@ -2351,7 +2359,8 @@ static void set_fields_ks(scft_ctx *c, const std::vector<int> &ks, const double 
   k_real_check_all<<<dim3(kCheckBlocks, n), 256, 0, c->st>>>(c->d_fi, c->d_skip, c->d_realout);
   CK(cudaGetLastError());
   for (int k : ks)
-    CK(cudaMemcpyAsync(c->h_pin + 128 * (size_t)k, c->d_realout + 128 * (size_t)k, sizeof(double) * 9 * kCheckBlocks,
+    CK(cudaMemcpyAsync(c->h_pin + kCheckStride * (size_t)k, c->d_realout + kCheckStride * (size_t)k,
+                       sizeof(double) * 9 * kCheckBlocks,
                        cudaMemcpyDeviceToHost, c->st));
   CK(cudaStreamSynchronize(c->st));
   std::vector<PlaneJob> pj;
@@ -2361,7 +2370,7 @@ static void set_fields_ks(scft_ctx *c, const std::vector<int> &ks, const double 
     Instance &I = c->inst[k];
     double m[9] = {};
     for (int b = 0; b < kCheckBlocks; b++)
-      for (int q = 0; q < 9; q++) m[q] = std::max(m[q], c->h_pin[128 * (size_t)k + 9 * b + q]);
+      for (int q = 0; q < 9; q++) m[q] = std::max(m[q], c->h_pin[kCheckStride * (size_t)k + 9 * b + q]);
     if (m[0] > 1e-12 * std::max(1.0, m[1])) {
       if (bad.empty()) bad = std::to_string(k);
       continue;
@@ -2504,11 +2513,11 @@ static void step_body(scft_ctx *c, const double *const *w, int n_iter, bool iter
     }
     CK(cudaEventRecord(c->ev_up[g], sg));
     k_real_check_all<<<dim3(kCheckBlocks, cnt), 256, 0, sg>>>(c->d_fi_ord + gr.inst_begin, nullptr,
-                                                              c->d_realout + 128 * (size_t)gr.inst_begin);
+                                                              c->d_realout + kCheckStride * (size_t)gr.inst_begin);
     CK(cudaGetLastError());
     c->launches++;
-    CK(cudaMemcpyAsync(c->h_pin + 128 * (size_t)gr.inst_begin, c->d_realout + 128 * (size_t)gr.inst_begin,
-                       sizeof(double) * 128 * (size_t)cnt, cudaMemcpyDeviceToHost, sg));
+    CK(cudaMemcpyAsync(c->h_pin + kCheckStride * (size_t)gr.inst_begin, c->d_realout + kCheckStride * (size_t)gr.inst_begin,
+                       sizeof(double) * kCheckStride * (size_t)cnt, cudaMemcpyDeviceToHost, sg));
     if (c->step_npj[g] > 0) {
       LK(launch_plane_fft<double>(c->shp_plane, c->step_pj[g], c->step_npj[g], c->d_geoms, c->d_tw64, -1, 0, sg));
       LK(launch_col_fft<double>(c->shp_col, c->step_cj[g], c->step_ncj[g], c->d_geoms, c->d_tw64, 0, 1, sg));
@@ -2634,7 +2643,7 @@ static void check_step_realness(scft_ctx *c) {
   for (int oi = 0; oi < n; oi++) {
     double m[9] = {};
     for (int b = 0; b < kCheckBlocks; b++)
-      for (int q = 0; q < 9; q++) m[q] = std::max(m[q], c->h_pin[128 * (size_t)oi + 9 * b + q]);
+      for (int q = 0; q < 9; q++) m[q] = std::max(m[q], c->h_pin[kCheckStride * (size_t)oi + 9 * b + q]);
     if (m[0] > 1e-12 * std::max(1.0, m[1]) && bad.empty()) bad = std::to_string(c->job_order[oi]);
   }
   if (!bad.empty()) {
